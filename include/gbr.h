@@ -1,0 +1,207 @@
+/*
+ * gbr.h — C ABI of the GB300-native triangle pipeline.
+ *
+ * One shared library (libgbr.so, built from openclrenderer_gb300/csrc) replaces
+ * the OpenCL triangle path of OpenCLRenderer: the object_context upload, the
+ * light build, the texture atlas build, engine::generate_realtime_shadowing and
+ * render_tris (prearrange -> kernel1 -> kernel2 -> kernel3).  Plain pointers and
+ * sizes only; every call returns a gbr_status and never exits the process.
+ *
+ * Struct layouts are byte-identical to the reference's host mirrors, so a
+ * std::vector<triangle> or std::vector<obj_g_descriptor> built for the
+ * reference uploads unchanged.
+ */
+#ifndef GBR_H
+#define GBR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Replaces lg::log-and-continue and exit(n) of the reference
+ * dispatch (engine.hpp:574-618, ocl.h:250,346,368,396). */
+typedef enum gbr_status {
+  GBR_OK = 0,
+  GBR_INVALID_ARG = 1,        /* bad handle, size, pointer or resolution */
+  GBR_OOM = 2,                /* device allocation failed */
+  GBR_BIN_OVERFLOW_RETRY = 3, /* tile bins overflowed a fixed capacity (no-alloc entry) */
+  GBR_DEVICE_TIMEOUT = 4,     /* a bounded device wait gave up */
+  GBR_INTERNAL = 5,
+  GBR_CUDA_ERROR = 6,         /* a CUDA runtime call failed; see gbr_last_error_string */
+  GBR_ADMISSION_REJECTED = 7  /* serving: request exceeds the HBM budget */
+} gbr_status;
+
+/* struct vertex (cl2.cl:131-138; host vertex.hpp:33-63): 48 bytes.
+ * object_id of vertices[0] is the object descriptor index (object_context.cpp:424). */
+typedef struct gbr_vertex {
+  float pos[4];
+  float normal[4];
+  float vt[2];
+  uint32_t object_id;
+  uint32_t vertex_col; /* R<<24 | G<<16 | B<<8 | A; 0 = use the texture */
+} gbr_vertex;
+
+/* struct triangle (cl2.cl:148-151): 144 bytes. */
+typedef struct gbr_triangle {
+  gbr_vertex vertices[3];
+} gbr_triangle;
+
+/* struct obj_g_descriptor (cl2.cl:99-124; host obj_g_descriptor.hpp:146-173): 144 bytes. */
+typedef struct gbr_obj_g_descriptor {
+  float world_pos[4];
+  float world_rot_quat[4];
+  float old_world_pos_1[4];
+  float old_world_pos_2[4];
+  float old_world_rot_quat_1[4];
+  float old_world_rot_quat_2[4];
+  float scale;
+  uint32_t tid;  /* texture gpu id (position in the texture order) */
+  uint32_t rid;
+  uint32_t ssid;
+  uint32_t has_bump;
+  float specular;
+  float spec_mult;
+  float diffuse;
+  int32_t buffer_offset;
+  int32_t feature_flag; /* 2 two-sided, 4 outline, 8 static, 16 no dynamic shadows */
+  uint32_t pad_[2];
+} gbr_obj_g_descriptor;
+
+/* struct light (cl2.cl:77-87; host light.hpp): 64 bytes. */
+typedef struct gbr_light {
+  float pos[4];
+  float col[4];
+  uint32_t shadow;
+  float brightness;
+  float radius;
+  float diffuse;
+  float godray_intensity;
+  int32_t is_static;
+  uint32_t pad_[2];
+} gbr_light;
+
+/* Camera: position and extrinsic XYZ Euler angles (radians), as the
+ * reference's engine::c_pos / c_rot (render_tris arguments, engine.cpp:1794). */
+typedef struct gbr_camera {
+  float pos[4];
+  float rot[4];
+} gbr_camera;
+
+/* Per-view parameters.  In the reference these are compile-time -D defines
+ * (SCREENWIDTH, SCREENHEIGHT, FOV_CONST; engine.cpp:474-477, ocl.h:227) plus
+ * object_context_data::g_clear_col / use_linear_rendering. */
+typedef struct gbr_view {
+  int32_t width;       /* 1 .. 3840 */
+  int32_t height;      /* 1 .. 2160 */
+  float fov_const;     /* FOV_CONST; <= 0 derives it from hfov_deg */
+  float hfov_deg;      /* horizontal FOV in degrees, used when fov_const <= 0 */
+  float clear_col[4];  /* RGBA written where nothing is drawn */
+  uint32_t use_linear; /* TEST_LINEAR sRGB approximations on (reference default 1) */
+  uint32_t reserved;
+} gbr_view;
+
+/* Device output buffers of one view, row-major W*H.  Any may be NULL. */
+typedef struct gbr_outputs {
+  uint32_t* depth;   /* u32 depth, UINT_MAX where empty (kernel1) */
+  uint32_t* id;      /* canonical id 2*triangle+clip_sub, 0xFFFFFFFF where empty (kernel2) */
+  uint8_t* rgba;     /* RGBA8 = round(clamp(c,0,1)*255) (kernel3 screen) */
+  uint16_t* normals; /* encode_normal ushort2 (kernel3 screen_normals_optional) */
+} gbr_outputs;
+
+/* Per-call counters (host-readable after a render). */
+typedef struct gbr_stats {
+  uint64_t view_records;    /* clipped, visible screen triangles */
+  uint64_t view_bin_entries;
+  uint64_t shadow_records;
+  uint64_t shadow_bin_entries;
+  uint64_t fragments_ref;   /* sum of ceil(bboxArea/500): the reference's kernel1 work items */
+  uint64_t retries;         /* workspace grow-and-retry events */
+} gbr_stats;
+
+typedef struct gbr_scene gbr_scene;
+
+/* Last error message of the calling thread ("" if none). */
+const char* gbr_last_error_string(void);
+
+/* FOV_CONST the reference derives from a horizontal FOV
+ * (engine.cpp:119-133, then std::to_string round trip at engine.cpp:474-477). */
+float gbr_fov_const_from_hfov(float hfov_deg, int32_t width);
+
+/* Scene handle on the current CUDA device (object_context + light_gpu +
+ * texture_context_data of the reference). */
+gbr_status gbr_scene_create(gbr_scene** out);
+gbr_status gbr_scene_destroy(gbr_scene* scene);
+
+/* object_context alloc_gpu triangle upload (object_context.cpp:346-458).
+ * Host array of n triangles, copied. */
+gbr_status gbr_scene_set_triangles(gbr_scene* scene, const gbr_triangle* tris, uint32_t n);
+
+/* alloc_object_descriptors (object_context.cpp:460-484). Host array, copied. */
+gbr_status gbr_scene_set_descriptors(gbr_scene* scene, const gbr_obj_g_descriptor* descs,
+                                     uint32_t n);
+
+/* light::build (light.cpp:145-276): active lights and the shadow cubemaps
+ * (6 * 1024^2 u32 per shadow-casting light, dynamic and static). Host array. */
+gbr_status gbr_scene_set_lights(gbr_scene* scene, const gbr_light* lights, uint32_t n);
+
+/* texture_context::alloc_gpu (texture_context.cpp:350-517): pack n square RGBA8
+ * textures (edge sizes[i], pixels rgba[i], in gpu-id order) into 2048^2 pages,
+ * upload them with update_gpu_tex (row flip as the reference) and generate the
+ * 4 mip levels (generate_mips / generate_mip_mips). */
+gbr_status gbr_scene_set_textures(gbr_scene* scene, uint32_t n, const int32_t* sizes,
+                                  const uint8_t* const* rgba);
+
+/* Texture descriptors after gbr_scene_set_textures: nums (slice<<16|which),
+ * page sizes and mipmap_start.  Capacities in, counts out. */
+gbr_status gbr_scene_texture_layout(gbr_scene* scene, uint32_t* nums, uint32_t* n_nums,
+                                    uint32_t* sizes, uint32_t* n_sizes,
+                                    uint32_t* mipmap_start);
+
+/* Device pointers of scene-owned buffers for inspection (atlas bytes, shadow
+ * cubemaps).  which: 0 atlas (u8), 1 dynamic cubemaps (u32), 2 static cubemaps (u32). */
+gbr_status gbr_scene_buffer(gbr_scene* scene, int32_t which, const void** dev_ptr,
+                            size_t* bytes);
+
+/* Copy `bytes` bytes at `offset` of a scene buffer (see gbr_scene_buffer) to
+ * dst, which may be host or device memory.  Synchronous. */
+gbr_status gbr_scene_read_buffer(gbr_scene* scene, int32_t which, void* dst, size_t offset,
+                                 size_t bytes);
+
+/* Host-only texture page packing of texture_context (texture_context.cpp:94-261):
+ * for n textures of edge sizes[i] (powers of two, 16..2048), writes the 5*n slot
+ * descriptors (n base textures, then 4 mips per texture) to nums and the page
+ * edge sizes to page_sizes.  Capacities in, counts out.  Needs no GPU. */
+gbr_status gbr_texture_pack(uint32_t n, const int32_t* sizes, uint32_t* nums, uint32_t* n_nums,
+                            uint32_t* page_sizes, uint32_t* n_pages);
+
+/* engine::generate_realtime_shadowing (engine.cpp:1601-1790): render the
+ * cubemap of every shadow-casting light (prearrange_realtime_shadowing +
+ * kernel1_realtime_shadowing).  stream: cudaStream_t or NULL. */
+gbr_status gbr_shadow_pass(gbr_scene* scene, void* stream);
+
+/* render_tris (engine.cpp:1794-2034): prearrange -> kernel1 -> kernel2 -> kernel3
+ * for one view into device outputs.  Shadow cubemaps come from the last
+ * gbr_shadow_pass.  Synchronises the stream once to check workspace bounds. */
+gbr_status gbr_render_view(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
+                           const gbr_outputs* out, void* stream);
+
+/* Same, with HOST output buffers (copied back before returning). */
+gbr_status gbr_render_view_host(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
+                                uint32_t* depth, uint32_t* id, uint8_t* rgba, void* stream);
+
+/* Many views of uneven resolution rendered by one launch per stage
+ * (batched form).  Arrays of n cameras, views and outputs. */
+gbr_status gbr_render_batch(gbr_scene* scene, uint32_t n, const gbr_camera* cams,
+                            const gbr_view* views, const gbr_outputs* outs, void* stream);
+
+/* Counters of the last render / shadow pass on this scene. */
+gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBR_H */

@@ -1,0 +1,659 @@
+// gbr_api.cu — C ABI of the pipeline: scene ownership, texture atlas build,
+// workspace management and the pass drivers (render_tris /
+// generate_realtime_shadowing of the reference engine).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/gbr.h"
+#include "gbr_internal.h"
+
+static_assert(sizeof(gbr_vertex) == 48, "vertex layout");
+static_assert(sizeof(gbr_triangle) == 144, "triangle layout");
+static_assert(sizeof(gbr_obj_g_descriptor) == 144, "obj_g_descriptor layout");
+static_assert(sizeof(gbr_light) == 64, "light layout");
+static_assert(offsetof(gbr_vertex, object_id) == 40, "vertex.object_id offset");
+static_assert(offsetof(gbr_obj_g_descriptor, scale) == 96, "descriptor.scale offset");
+static_assert(offsetof(gbr_obj_g_descriptor, feature_flag) == 132, "descriptor.feature_flag offset");
+static_assert(offsetof(gbr_light, shadow) == 32, "light.shadow offset");
+static_assert(sizeof(gbr::RasterRec) == 64, "raster record");
+static_assert(sizeof(gbr::ShadeRec) == 48, "shade record");
+
+using namespace gbr;
+
+namespace {
+
+thread_local std::string g_err;
+
+gbr_status fail(gbr_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return s;
+}
+
+#define CU(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? GBR_OOM : GBR_CUDA_ERROR, "%s: %s (%s:%d)", \
+                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                      \
+  } while (0)
+
+#define TRY(expr)                        \
+  do {                                   \
+    gbr_status s_ = (expr);              \
+    if (s_ != GBR_OK) return s_;         \
+  } while (0)
+
+// Device buffer that only grows.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  gbr_status reserve(size_t n) {
+    if (n <= cap && p) return GBR_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t m = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, m * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(GBR_OOM, "cudaMalloc of %zu bytes failed: %s", m * sizeof(T), cudaGetErrorString(e));
+    }
+    cap = m;
+    return GBR_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Pinned host staging buffer that only grows.
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  gbr_status reserve(size_t n) {
+    if (n <= bytes && p) return GBR_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(n, 64));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(GBR_OOM, "cudaMallocHost of %zu bytes failed", n);
+    }
+    bytes = std::max<size_t>(n, 64);
+    return GBR_OK;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+// Scratch memory of one pass (records, bins, tile counters, per-pixel record
+// indices of the views).
+struct WorkMem {
+  DevBuf<RasterRec> rec;
+  DevBuf<ShadeRec> srec;
+  DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins;
+  DevBuf<Counters> ctr;
+  DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
+  DevBuf<uint8_t> pix_rgba;
+  DevBuf<Surface> surf;
+  DevBuf<ViewParams> views;
+  DevBuf<ShadowJob> jobs;
+  uint32_t rec_target = 0, bin_target = 0;
+  void release() {
+    rec.release(); srec.release(); fine_count.release(); fine_off.release();
+    coarse_count.release(); coarse_off.release(); bins.release(); ctr.release();
+    pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
+    surf.release(); views.release(); jobs.release();
+  }
+};
+
+void euler_cs(const float ang[3], float c[3], float s[3]) {
+  for (int i = 0; i < 3; i++) {
+    c[i] = (float)cos((double)ang[i]);
+    s[i] = (float)sin((double)ang[i]);
+  }
+}
+
+}  // namespace
+
+struct gbr_scene {
+  int device = 0;
+  DevBuf<gbr_triangle> tris;
+  uint32_t ntris = 0;
+  DevBuf<gbr_obj_g_descriptor> descs;
+  uint32_t ndescs = 0;
+  DevBuf<gbr_light> lights;
+  std::vector<gbr_light> host_lights;
+  DevBuf<uchar4> atlas;
+  DevBuf<uint32_t> nums, sizes;
+  std::vector<uint32_t> host_nums, host_sizes;
+  uint32_t mipmap_start = 0;
+  uint32_t npages = 0;
+  DevBuf<uint32_t> shadow_dyn, shadow_static;
+  uint32_t n_dyn = 0, n_static = 0;
+  uint32_t max_object_id = 0, max_tid = 0;
+  bool static_dirty = true;
+  WorkMem ws;
+  HostBuf staging;     // surfaces / views / jobs / counters
+  gbr_stats stats{};
+  float face_cos[6][3], face_sin[6][3];
+
+  SceneDev dev() const {
+    SceneDev d{};
+    d.tris = tris.p;
+    d.ntris = ntris;
+    d.descs = descs.p;
+    d.ndescs = ndescs;
+    d.lights = lights.p;
+    d.nlights = (uint32_t)host_lights.size();
+    d.atlas = atlas.p;
+    d.nums = nums.p;
+    d.sizes = sizes.p;
+    d.mipmap_start = mipmap_start;
+    d.shadow_dyn = shadow_dyn.p;
+    d.shadow_static = shadow_static.p;
+    memcpy(d.face_cos, face_cos, sizeof face_cos);
+    memcpy(d.face_sin, face_sin, sizeof face_sin);
+    return d;
+  }
+};
+
+namespace {
+
+gbr_status check_scene(gbr_scene* s) {
+  if (!s) return fail(GBR_INVALID_ARG, "null scene");
+  CU(cudaSetDevice(s->device));
+  return GBR_OK;
+}
+
+// Every index the kernels follow must stay inside its table.
+gbr_status check_indices(gbr_scene* s, bool shading) {
+  if (s->ntris && s->max_object_id >= s->ndescs)
+    return fail(GBR_INVALID_ARG, "triangle object_id %u but only %u descriptors", s->max_object_id, s->ndescs);
+  if (shading && s->ntris && s->max_tid >= s->mipmap_start)
+    return fail(GBR_INVALID_ARG, "descriptor tid %u but only %u textures", s->max_tid, s->mipmap_start);
+  return GBR_OK;
+}
+
+// Reserve pass scratch: records, bins and tile counters for the given surfaces.
+gbr_status reserve_pass(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view, size_t npix) {
+  WorkMem& w = s->ws;
+  TRY(w.rec.reserve(w.rec_target));
+  if (view) TRY(w.srec.reserve(w.rec_target));
+  TRY(w.bins.reserve(w.bin_target));
+  TRY(w.fine_count.reserve(nfine));
+  TRY(w.fine_off.reserve(nfine));
+  TRY(w.coarse_count.reserve(ncoarse));
+  TRY(w.coarse_off.reserve(ncoarse));
+  TRY(w.ctr.reserve(1));
+  if (view) TRY(w.pix_rec.reserve(npix));
+  return GBR_OK;
+}
+
+Workspace make_ws(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view) {
+  WorkMem& w = s->ws;
+  Workspace ws{};
+  ws.rec = w.rec.p;
+  ws.srec = view ? w.srec.p : nullptr;
+  ws.rec_cap = (uint32_t)std::min<size_t>(w.rec.cap, 0xFFFFFFF0u);
+  ws.fine_count = w.fine_count.p;
+  ws.fine_off = w.fine_off.p;
+  ws.nfine = nfine;
+  ws.coarse_count = w.coarse_count.p;
+  ws.coarse_off = w.coarse_off.p;
+  ws.ncoarse = ncoarse;
+  ws.bins = w.bins.p;
+  ws.bin_cap = (uint32_t)std::min<size_t>(w.bins.cap, 0xFFFFFFF0u);
+  ws.ctr = w.ctr.p;
+  return ws;
+}
+
+void tile_layout(Surface& S, uint32_t& tile_base, uint32_t& ctile_base) {
+  S.tiles_x = (S.width + kTile - 1) / kTile;
+  S.tiles_y = (S.height + kTile - 1) / kTile;
+  S.ctiles_x = (S.width + kCoarse - 1) / kCoarse;
+  S.ctiles_y = (S.height + kCoarse - 1) / kCoarse;
+  S.tile_base = tile_base;
+  S.ctile_base = ctile_base;
+  tile_base += (uint32_t)(S.tiles_x * S.tiles_y);
+  ctile_base += (uint32_t)(S.ctiles_x * S.ctiles_y);
+}
+
+gbr_status validate_view(const gbr_view* v) {
+  if (!v) return fail(GBR_INVALID_ARG, "null view");
+  if (v->width < 1 || v->height < 1 || v->width > kMaxWalkWidth || v->height > kMaxWalkHeight)
+    return fail(GBR_INVALID_ARG, "view %dx%d outside 1..%d x 1..%d", v->width, v->height, kMaxWalkWidth,
+                kMaxWalkHeight);
+  float fov = v->fov_const > 0 ? v->fov_const : gbr_fov_const_from_hfov(v->hfov_deg, v->width);
+  if (!(fov > 0) || !std::isfinite(fov)) return fail(GBR_INVALID_ARG, "bad fov (hfov %g)", (double)v->hfov_deg);
+  return GBR_OK;
+}
+
+// Run one pass (views or shadow jobs) with grow-and-retry on scratch overflow.
+// The caller has filled s->ws.surf / views / jobs on the device.
+gbr_status run_pass(gbr_scene* s, bool view, uint32_t nitems, uint32_t nsurf, uint32_t nfine,
+                    uint32_t ncoarse, size_t npix, cudaStream_t st) {
+  const SceneDev sd = s->dev();
+  for (int attempt = 0; attempt < 6; attempt++) {
+    TRY(reserve_pass(s, nfine, ncoarse, view, npix));
+    Workspace ws = make_ws(s, nfine, ncoarse, view);
+    CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
+    CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(nfine, 1), st));
+    CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(ncoarse, 1), st));
+    if (view)
+      CU(launch_setup_views(sd, s->ws.views.p, nitems, s->ws.surf.p, ws, st));
+    else
+      CU(launch_setup_shadow(sd, s->ws.jobs.p, nitems, s->ws.surf.p, ws, st));
+    CU(launch_scan(ws, st));
+    CU(launch_fill(ws, s->ws.surf.p, st));
+    CU(launch_raster(ws, s->ws.surf.p, nsurf, nfine, view, st));
+    if (view) CU(launch_shade(sd, s->ws.views.p, nitems, s->ws.surf.p, nfine, ws.srec, st));
+    Counters* hc = reinterpret_cast<Counters*>(s->staging.p);
+    CU(cudaMemcpyAsync(hc, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    Counters c = *hc;
+    if (!c.overflow) {
+      if (view) {
+        s->stats.view_records = c.nrec;
+        s->stats.view_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
+        s->stats.fragments_ref = c.frag_ref;
+      } else {
+        s->stats.shadow_records = c.nrec;
+        s->stats.shadow_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
+      }
+      return GBR_OK;
+    }
+    s->stats.retries++;
+    if (c.overflow & 1u) s->ws.rec_target = (uint32_t)std::min<uint64_t>((uint64_t)c.nrec * 5 / 4 + 1024, 0xFFFFFFF0u);
+    uint64_t need_bins = (uint64_t)c.fine_total + c.coarse_total;
+    if (c.overflow & 1u) need_bins = std::max<uint64_t>(need_bins, (uint64_t)s->ws.rec_target * 4);
+    s->ws.bin_target = (uint32_t)std::min<uint64_t>(need_bins * 5 / 4 + 4096, 0xFFFFFFF0u);
+  }
+  return fail(GBR_INTERNAL, "scratch kept overflowing after 6 attempts");
+}
+
+// texture_context.cpp:94-261: page list and slot descriptors.
+gbr_status pack_textures(uint32_t n, const int32_t* sz, std::vector<uint32_t>& nums,
+                         std::vector<uint32_t>& pages) {
+  std::map<int, int> count;
+  for (uint32_t i = 0; i < n; i++) {
+    if (sz[i] < 16 || sz[i] > kTexPage || (sz[i] & (sz[i] - 1)))
+      return fail(GBR_INVALID_ARG, "texture %u size %d: need a power of two in 16..2048", i, sz[i]);
+    count[sz[i]]++;
+    for (int j = 0; j < kMipLevels; j++) count[sz[i] >> (j + 1)]++;
+  }
+  struct Page { int size, num; };
+  std::vector<Page> pl;
+  for (auto& kv : count) {
+    int per = (kTexPage / kv.first) * (kTexPage / kv.first);
+    int rem = kv.second;
+    while (rem >= per) { pl.push_back({kv.first, per}); rem -= per; }
+    if (rem > 0) pl.push_back({kv.first, rem});
+  }
+  std::vector<Page> free_pl = pl;
+  auto take = [&](int size, uint32_t* out) {
+    for (size_t p = 0; p < free_pl.size(); p++)
+      if (free_pl[p].size == size && free_pl[p].num > 0) {
+        free_pl[p].num--;
+        *out = (uint32_t)(p << 16) | (uint32_t)free_pl[p].num;
+        return true;
+      }
+    return false;
+  };
+  nums.assign(n * (1 + kMipLevels), 0);
+  for (uint32_t i = 0; i < n; i++)
+    if (!take(sz[i], &nums[i])) return fail(GBR_INTERNAL, "no free texture page");
+  for (uint32_t i = 0; i < n; i++)
+    for (int j = 0; j < kMipLevels; j++)
+      if (!take(sz[i] >> (j + 1), &nums[n + i * kMipLevels + j])) return fail(GBR_INTERNAL, "no free mip page");
+  pages.clear();
+  for (auto& p : pl) pages.push_back((uint32_t)p.size);
+  return GBR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* gbr_last_error_string(void) { return g_err.c_str(); }
+
+float gbr_fov_const_from_hfov(float hfov_deg, int32_t width) {
+  float fov_radians = (float)((double)((hfov_deg / 360.f) * 2) * 3.14159265358979323846);
+  float half = fov_radians / 2;
+  float fc = ((float)width / 2) / tanf(half);
+  char buf[64];
+  snprintf(buf, sizeof buf, "%f", (double)fc);
+  return strtof(buf, nullptr);
+}
+
+gbr_status gbr_scene_create(gbr_scene** out) {
+  if (!out) return fail(GBR_INVALID_ARG, "null out");
+  *out = nullptr;
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  gbr_scene* s = new gbr_scene();
+  s->device = dev;
+  for (int f = 0; f < 6; f++) {
+    f3 a = face_angles(f);
+    float ang[3] = {a.x, a.y, a.z};
+    euler_cs(ang, s->face_cos[f], s->face_sin[f]);
+  }
+  gbr_status st = s->staging.reserve(64 * 1024);
+  if (st != GBR_OK) {
+    delete s;
+    return st;
+  }
+  *out = s;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_destroy(gbr_scene* s) {
+  if (!s) return GBR_OK;
+  cudaSetDevice(s->device);
+  cudaDeviceSynchronize();
+  s->tris.release(); s->descs.release(); s->lights.release(); s->atlas.release();
+  s->nums.release(); s->sizes.release(); s->shadow_dyn.release(); s->shadow_static.release();
+  s->ws.release();
+  s->staging.release();
+  delete s;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint32_t n) {
+  TRY(check_scene(s));
+  if (n && !tris) return fail(GBR_INVALID_ARG, "null triangles");
+  TRY(s->tris.reserve(n));
+  if (n) CU(cudaMemcpy(s->tris.p, tris, sizeof(gbr_triangle) * n, cudaMemcpyHostToDevice));
+  // object ids must index the descriptor table; checked against it at render time
+  uint32_t mx = 0;
+  for (uint32_t i = 0; i < n; i++) mx = std::max(mx, tris[i].vertices[0].object_id);
+  s->max_object_id = mx;
+  s->ntris = n;
+  s->static_dirty = true;
+  s->ws.rec_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(s->ws.rec_target, (uint64_t)n + 1024u), 0xFFFFFFF0u);
+  s->ws.bin_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(s->ws.bin_target, 4ull * s->ws.rec_target), 0xFFFFFFF0u);
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d, uint32_t n) {
+  TRY(check_scene(s));
+  if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
+  TRY(s->descs.reserve(n));
+  if (n) CU(cudaMemcpy(s->descs.p, d, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyHostToDevice));
+  uint32_t mt = 0;
+  for (uint32_t i = 0; i < n; i++) mt = std::max(mt, d[i].tid);
+  s->max_tid = mt;
+  s->ndescs = n;
+  s->static_dirty = true;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
+  TRY(check_scene(s));
+  if (n && !l) return fail(GBR_INVALID_ARG, "null lights");
+  for (uint32_t i = 0; i < n; i++)
+    if (l[i].shadow > 1) return fail(GBR_INVALID_ARG, "light %u: shadow must be 0 or 1", i);
+  s->host_lights.assign(l, l + n);
+  TRY(s->lights.reserve(n));
+  if (n) CU(cudaMemcpy(s->lights.p, l, sizeof(gbr_light) * n, cudaMemcpyHostToDevice));
+  uint32_t nd = 0, ns = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (l[i].shadow == 1) nd++;
+    if (l[i].shadow && l[i].is_static) ns++;
+  }
+  const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
+  TRY(s->shadow_dyn.reserve(std::max<size_t>(nd, 1) * 6 * face));
+  TRY(s->shadow_static.reserve(std::max<size_t>(ns, 1) * 6 * face));
+  if (nd != s->n_dyn || s->n_dyn == 0) CU(launch_fill_u32(s->shadow_dyn.p, kDepthClear, s->shadow_dyn.cap, 0));
+  CU(launch_fill_u32(s->shadow_static.p, kDepthClear, s->shadow_static.cap, 0));
+  CU(cudaDeviceSynchronize());
+  s->n_dyn = nd;
+  s->n_static = ns;
+  s->static_dirty = true;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_set_textures(gbr_scene* s, uint32_t n, const int32_t* sizes, const uint8_t* const* rgba) {
+  TRY(check_scene(s));
+  if (n && (!sizes || !rgba)) return fail(GBR_INVALID_ARG, "null texture arrays");
+  for (uint32_t i = 0; i < n; i++)
+    if (!rgba[i]) return fail(GBR_INVALID_ARG, "null texture %u", i);
+  std::vector<uint32_t> nums, pages;
+  TRY(pack_textures(n, sizes, nums, pages));
+  const size_t page_px = (size_t)kTexPage * kTexPage;
+  TRY(s->atlas.reserve(std::max<size_t>(pages.size(), 1) * page_px));
+  CU(cudaMemset(s->atlas.p, 0, s->atlas.cap * sizeof(uchar4)));
+  TRY(s->nums.reserve(std::max<size_t>(nums.size(), 2)));
+  TRY(s->sizes.reserve(std::max<size_t>(pages.size(), 2)));
+  if (!nums.empty()) CU(cudaMemcpy(s->nums.p, nums.data(), nums.size() * 4, cudaMemcpyHostToDevice));
+  if (!pages.empty()) CU(cudaMemcpy(s->sizes.p, pages.data(), pages.size() * 4, cudaMemcpyHostToDevice));
+  s->host_nums = nums;
+  s->host_sizes = pages;
+  s->mipmap_start = n;
+  s->npages = (uint32_t)pages.size();
+  if (n) {
+    std::vector<uint64_t> offs(n);
+    uint64_t total = 0;
+    int32_t maxs = 0;
+    for (uint32_t i = 0; i < n; i++) {
+      offs[i] = total;
+      total += (uint64_t)sizes[i] * sizes[i] * 4;
+      maxs = std::max(maxs, sizes[i]);
+    }
+    DevBuf<uint8_t> px;
+    DevBuf<uint64_t> d_offs;
+    DevBuf<int32_t> d_sz;
+    TRY(px.reserve(total));
+    TRY(d_offs.reserve(n));
+    TRY(d_sz.reserve(n));
+    for (uint32_t i = 0; i < n; i++)
+      CU(cudaMemcpy(px.p + offs[i], rgba[i], (size_t)sizes[i] * sizes[i] * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d_offs.p, offs.data(), n * 8, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d_sz.p, sizes, n * 4, cudaMemcpyHostToDevice));
+    CU(launch_texture_upload(s->atlas.p, s->nums.p, s->sizes.p, px.p, d_offs.p, d_sz.p, n, maxs, 0));
+    CU(launch_mips(s->atlas.p, s->nums.p, s->sizes.p, s->mipmap_start, d_sz.p, n, maxs, 0));
+    CU(cudaDeviceSynchronize());
+    px.release();
+    d_offs.release();
+    d_sz.release();
+  }
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_texture_layout(gbr_scene* s, uint32_t* nums, uint32_t* n_nums, uint32_t* sizes,
+                                    uint32_t* n_sizes, uint32_t* mipmap_start) {
+  if (!s || !n_nums || !n_sizes) return fail(GBR_INVALID_ARG, "null argument");
+  uint32_t cn = *n_nums, cs = *n_sizes;
+  *n_nums = (uint32_t)s->host_nums.size();
+  *n_sizes = (uint32_t)s->host_sizes.size();
+  if (mipmap_start) *mipmap_start = s->mipmap_start;
+  if (nums) memcpy(nums, s->host_nums.data(), 4 * std::min<size_t>(cn, s->host_nums.size()));
+  if (sizes) memcpy(sizes, s->host_sizes.data(), 4 * std::min<size_t>(cs, s->host_sizes.size()));
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_buffer(gbr_scene* s, int32_t which, const void** ptr, size_t* bytes) {
+  if (!s || !ptr || !bytes) return fail(GBR_INVALID_ARG, "null argument");
+  const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
+  switch (which) {
+    case 0: *ptr = s->atlas.p; *bytes = (size_t)s->npages * kTexPage * kTexPage * 4; return GBR_OK;
+    case 1: *ptr = s->shadow_dyn.p; *bytes = (size_t)s->n_dyn * 6 * face * 4; return GBR_OK;
+    case 2: *ptr = s->shadow_static.p; *bytes = (size_t)s->n_static * 6 * face * 4; return GBR_OK;
+    default: return fail(GBR_INVALID_ARG, "unknown buffer %d", which);
+  }
+}
+
+gbr_status gbr_scene_read_buffer(gbr_scene* s, int32_t which, void* dst, size_t offset, size_t bytes) {
+  TRY(check_scene(s));
+  const void* p = nullptr;
+  size_t total = 0;
+  TRY(gbr_scene_buffer(s, which, &p, &total));
+  if (!dst || offset > total || bytes > total - offset) return fail(GBR_INVALID_ARG, "read outside buffer");
+  if (bytes) CU(cudaMemcpy(dst, (const uint8_t*)p + offset, bytes, cudaMemcpyDefault));
+  return GBR_OK;
+}
+
+gbr_status gbr_texture_pack(uint32_t n, const int32_t* sizes, uint32_t* nums, uint32_t* n_nums,
+                            uint32_t* page_sizes, uint32_t* n_pages) {
+  if (!n_nums || !n_pages || (n && !sizes)) return fail(GBR_INVALID_ARG, "null argument");
+  std::vector<uint32_t> nv, pv;
+  TRY(pack_textures(n, sizes, nv, pv));
+  uint32_t cn = *n_nums, cp = *n_pages;
+  *n_nums = (uint32_t)nv.size();
+  *n_pages = (uint32_t)pv.size();
+  if (nums) memcpy(nums, nv.data(), 4 * std::min<size_t>(cn, nv.size()));
+  if (page_sizes) memcpy(page_sizes, pv.data(), 4 * std::min<size_t>(cp, pv.size()));
+  return GBR_OK;
+}
+
+gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
+  TRY(check_scene(s));
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
+  std::vector<ShadowJob> jobs;
+  std::vector<Surface> surfs;
+  uint32_t nn = 0, kk = 0, tb = 0, cb = 0;
+  auto add_job = [&](const gbr_light& L, int only_static, uint32_t* base) {
+    ShadowJob J{};
+    J.lpos[0] = L.pos[0]; J.lpos[1] = L.pos[1]; J.lpos[2] = L.pos[2];
+    J.only_static = only_static;
+    J.surface_base = (uint32_t)surfs.size();
+    for (int f = 0; f < 6; f++) {
+      Surface S{};
+      S.width = S.height = kLightBufferDim;
+      tile_layout(S, tb, cb);
+      S.depth = base + (size_t)f * face;
+      S.chunk = kOpSizeLight;
+      surfs.push_back(S);
+    }
+    jobs.push_back(J);
+  };
+  for (const gbr_light& L : s->host_lights) {
+    if (L.shadow == 1) add_job(L, 0, s->shadow_dyn.p + (size_t)(nn++) * 6 * face);
+    if (L.shadow && L.is_static && s->static_dirty) add_job(L, 1, s->shadow_static.p + (size_t)(kk++) * 6 * face);
+  }
+  if (jobs.empty()) return GBR_OK;
+  TRY(check_indices(s, false));
+  if (s->ntris == 0) {
+    for (auto& S : surfs) CU(launch_fill_u32(S.depth, kDepthClear, face, st));
+    s->static_dirty = false;
+    return GBR_OK;
+  }
+  TRY(s->ws.surf.reserve(surfs.size()));
+  TRY(s->ws.jobs.reserve(jobs.size()));
+  CU(cudaMemcpyAsync(s->ws.surf.p, surfs.data(), surfs.size() * sizeof(Surface), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(s->ws.jobs.p, jobs.data(), jobs.size() * sizeof(ShadowJob), cudaMemcpyHostToDevice, st));
+  TRY(run_pass(s, false, (uint32_t)jobs.size(), (uint32_t)surfs.size(), tb, cb, 0, st));
+  s->static_dirty = false;
+  return GBR_OK;
+}
+
+static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams, const gbr_view* views,
+                               const gbr_outputs* outs, cudaStream_t st) {
+  TRY(check_scene(s));
+  if (!n) return GBR_OK;
+  if (!cams || !views || !outs) return fail(GBR_INVALID_ARG, "null camera/view/output array");
+  size_t npix = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    TRY(validate_view(&views[i]));
+    npix += (size_t)views[i].width * views[i].height;
+  }
+  std::vector<Surface> surfs(n);
+  std::vector<ViewParams> vp(n);
+  uint32_t tb = 0, cb = 0;
+  size_t off = 0;
+  bool need_depth = false, need_id = false;
+  for (uint32_t i = 0; i < n; i++) {
+    if (!outs[i].depth) need_depth = true;
+    if (!outs[i].id) need_id = true;
+  }
+  TRY(s->ws.pix_rec.reserve(npix));
+  if (need_depth) TRY(s->ws.pix_depth.reserve(npix));
+  for (uint32_t i = 0; i < n; i++) {
+    const gbr_view& v = views[i];
+    Surface& S = surfs[i];
+    S.width = v.width;
+    S.height = v.height;
+    tile_layout(S, tb, cb);
+    S.depth = outs[i].depth ? outs[i].depth : s->ws.pix_depth.p + off;
+    S.id = outs[i].id;
+    S.rec = s->ws.pix_rec.p + off;
+    S.chunk = kOpSize;
+    ViewParams& V = vp[i];
+    memcpy(V.cpos, cams[i].pos, 12);
+    euler_cs(cams[i].rot, V.ccos, V.csin);
+    V.fov = v.fov_const > 0 ? v.fov_const : gbr_fov_const_from_hfov(v.hfov_deg, v.width);
+    V.surface = i;
+    V.use_linear = v.use_linear;
+    memcpy(V.clear, v.clear_col, 16);
+    V.rgba = outs[i].rgba;
+    V.normals = outs[i].normals;
+    off += (size_t)v.width * v.height;
+  }
+  (void)need_id;
+  TRY(check_indices(s, true));
+  TRY(s->ws.surf.reserve(n));
+  TRY(s->ws.views.reserve(n));
+  CU(cudaMemcpyAsync(s->ws.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(s->ws.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, st));
+  return run_pass(s, true, n, n, tb, cb, npix, st);
+}
+
+gbr_status gbr_render_view(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const gbr_outputs* out,
+                           void* stream) {
+  return render_views(s, 1, cam, view, out, (cudaStream_t)stream);
+}
+
+gbr_status gbr_render_batch(gbr_scene* s, uint32_t n, const gbr_camera* cams, const gbr_view* views,
+                            const gbr_outputs* outs, void* stream) {
+  return render_views(s, n, cams, views, outs, (cudaStream_t)stream);
+}
+
+gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, uint32_t* depth,
+                                uint32_t* id, uint8_t* rgba, void* stream) {
+  TRY(check_scene(s));
+  TRY(validate_view(view));
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t P = (size_t)view->width * view->height;
+  TRY(s->ws.pix_depth.reserve(P));
+  TRY(s->ws.pix_id.reserve(P));
+  TRY(s->ws.pix_rgba.reserve(P * 4));
+  gbr_outputs o{s->ws.pix_depth.p, s->ws.pix_id.p, s->ws.pix_rgba.p, nullptr};
+  TRY(render_views(s, 1, cam, view, &o, st));
+  if (depth) CU(cudaMemcpyAsync(depth, o.depth, P * 4, cudaMemcpyDeviceToHost, st));
+  if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, st));
+  if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
+  CU(cudaStreamSynchronize(st));
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_stats(gbr_scene* s, gbr_stats* out) {
+  if (!s || !out) return fail(GBR_INVALID_ARG, "null argument");
+  *out = s->stats;
+  return GBR_OK;
+}
+
+}  // extern "C"

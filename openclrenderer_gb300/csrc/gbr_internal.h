@@ -1,0 +1,144 @@
+// gbr_internal.h — device data layout and kernel launchers of the pipeline.
+//
+// Work flow of one pass (views or cube faces):
+//   setup   1 thread per (triangle, surface group): transform, clip, cull,
+//           bbox; appends RasterRecs (warp-aggregated atomics) and counts the
+//           16x16 "fine" tiles (or 128x128 "coarse" tiles for large
+//           triangles) each record touches
+//   scan    exclusive scan of the tile counts -> bin offsets
+//   fill    record indices into per-tile bins
+//   raster  1 CTA per fine tile, 1 thread per pixel: loops over the tile's
+//           fine bin and its coarse tile's bin; resolves the minimum depth in
+//           registers (kernel1), then the canonical id (kernel2).  Every pixel
+//           of a surface is written exactly once, so no clear pass and no
+//           global atomics are needed.
+//   shade   1 thread per view pixel (kernel3)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbr.h"
+#include "gbr_math.h"
+
+namespace gbr {
+
+constexpr int kTile = 16;                    // fine tile edge, pixels
+constexpr int kCoarse = 128;                 // coarse tile edge, pixels
+constexpr int kCoarseRatio = kCoarse / kTile;
+constexpr int kFineMaxTiles = 16;            // more fine tiles than this -> coarse bins
+constexpr int kRasterThreads = kTile * kTile;
+
+// Per visible clipped triangle on one surface: everything kernel1/kernel2
+// need per pixel, precomputed once (64 bytes).
+struct __align__(16) RasterRec {
+  float A, B, C, bound;  // depth plane; (2.0001*area)*sign
+  float s0, sa, sb, sign;
+  float t0, ta, tb;
+  uint32_t key;          // views: 2*triangle + clip sub-index (canonical id)
+  uint32_t xr;           // minx | maxx << 16
+  uint32_t yr;           // miny | maxy << 16
+  uint32_t surface;
+  uint32_t pad;
+};
+
+// Per view record: what kernel3 reads through the id (48 bytes).
+struct __align__(16) ShadeRec {
+  float4 p0;  // projected vertex 0 (x, y, z) + rconst
+  float4 p1;  // vertex 1 + triangle index (bits)
+  float4 p2;  // vertex 2 + object id (bits)
+};
+
+// One raster target: a view, or one face of a shadow cubemap.
+struct Surface {
+  int32_t width, height;
+  int32_t tiles_x, tiles_y;
+  int32_t ctiles_x, ctiles_y;
+  uint32_t tile_base, ctile_base;  // global tile numbering across surfaces
+  uint32_t* depth;                 // W*H
+  uint32_t* id;                    // W*H canonical id (views), else null
+  uint32_t* rec;                   // W*H record index for kernel3 (views), else null
+  int32_t chunk;                   // fragment size of the reference walk: 500 / 300
+  int32_t pad;
+};
+
+// Camera of one view (setup + shade).
+struct ViewParams {
+  float cpos[3], ccos[3], csin[3];
+  float fov;
+  uint32_t surface;
+  uint32_t use_linear;
+  float clear[4];
+  uint8_t* rgba;
+  uint16_t* normals;
+};
+
+// One cubemap render: a light, static or dynamic geometry, 6 surfaces.
+struct ShadowJob {
+  float lpos[3];
+  int32_t only_static;
+  uint32_t surface_base;
+  uint32_t pad[3];
+};
+
+struct Counters {
+  unsigned long long frag_ref;  // sum of ceil(area / chunk): the reference's work items
+  uint32_t nrec;                // records requested
+  uint32_t overflow;            // bit 0 records, bit 1 bins
+  uint32_t fine_total, coarse_total;
+  uint32_t pad[2];
+};
+
+struct SceneDev {
+  const gbr_triangle* tris;
+  uint32_t ntris;
+  const gbr_obj_g_descriptor* descs;
+  uint32_t ndescs;
+  const gbr_light* lights;
+  uint32_t nlights;
+  const uchar4* atlas;
+  const uint32_t* nums;
+  const uint32_t* sizes;
+  uint32_t mipmap_start;
+  const uint32_t* shadow_dyn;
+  const uint32_t* shadow_static;
+  float face_cos[6][3], face_sin[6][3];
+};
+
+struct Workspace {
+  RasterRec* rec;
+  ShadeRec* srec;  // may be null (shadow passes)
+  uint32_t rec_cap;
+  uint32_t* fine_count;
+  uint32_t* fine_off;
+  uint32_t nfine;
+  uint32_t* coarse_count;
+  uint32_t* coarse_off;
+  uint32_t ncoarse;
+  uint32_t* bins;
+  uint32_t bin_cap;
+  Counters* ctr;
+};
+
+// ---- launchers (gbr_kernels.cu) ----
+cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
+                               const Surface* d_surf, const Workspace& ws, cudaStream_t st);
+cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,
+                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
+cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
+cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
+cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,
+                          uint32_t ntiles, bool with_id, cudaStream_t st);
+cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
+                         const Surface* d_surf, uint32_t ntiles, const ShadeRec* srec,
+                         cudaStream_t st);
+cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
+                                  const uint8_t* pixels, const uint64_t* offsets,
+                                  const int32_t* tsizes, uint32_t ntex, int32_t max_size,
+                                  cudaStream_t st);
+cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
+                        uint32_t mipmap_start, const int32_t* tsizes, uint32_t ntex,
+                        int32_t max_size, cudaStream_t st);
+cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
+
+}  // namespace gbr

@@ -1,0 +1,935 @@
+// gbr_kernels.cu — sm_103a kernels of the triangle pipeline.
+//
+// Compiled with --fmad=false: every fused multiply-add below is an explicit
+// fmaf() standing for a `mad` of cl2.cl; all other float expressions round
+// after each operation, as the determinism contract in gbr_math.h requires.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbr_internal.h"
+
+namespace gbr {
+namespace {
+
+__device__ __forceinline__ f3 ld3(const float* p) { return mk3(__ldg(p), __ldg(p + 1), __ldg(p + 2)); }
+__device__ __forceinline__ f4 ld4(const float* p) {
+  float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  f4 r; r.x = v.x; r.y = v.y; r.z = v.z; r.w = v.w;
+  return r;
+}
+
+// Warp-aggregated allocation of n slots from *counter; every lane of the
+// warp must call it (n may be 0).  Returns this lane's first slot.
+__device__ __forceinline__ uint32_t warp_alloc(uint32_t* counter, uint32_t n) {
+  const unsigned full = 0xFFFFFFFFu;
+  int lane = threadIdx.x & 31;
+  uint32_t incl = n;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t v = __shfl_up_sync(full, incl, o);
+    if (lane >= o) incl += v;
+  }
+  uint32_t total = __shfl_sync(full, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(full, base, 31);
+  return base + incl - n;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// A visible clipped triangle before it becomes a record.
+struct Cand {
+  f3 p[3];
+  float rc;
+  float mm[4];
+  uint32_t key;
+};
+
+// prearrange's per-output culls (cl2.cl:4352-4377): returns false when the
+// output is culled or its bbox is empty (ceil(area/op_size) == 0).
+__device__ __forceinline__ bool cull_candidate(Cand& c, bool two_sided, float w, float h) {
+  const f3* p = c.p;
+  int valid = two_sided || backface_front(p[0], p[1], p[2]);
+  int cond = (p[0].x < 0 && p[1].x < 0 && p[2].x < 0) ||
+             (p[0].x >= w && p[1].x >= w && p[2].x >= w) ||
+             (p[0].y < 0 && p[1].y < 0 && p[2].y < 0) ||
+             (p[0].y >= h && p[1].y >= h && p[2].y >= h);
+  if (!valid || cond) return false;
+  f3 xpv = mk3(roundf(p[0].x), roundf(p[1].x), roundf(p[2].x));
+  f3 ypv = mk3(roundf(p[0].y), roundf(p[1].y), roundf(p[2].y));
+  c.rc = rconstant(xpv, ypv);
+  bbox4(p[0], p[1], p[2], w, h, c.mm);
+  return (c.mm[1] - c.mm[0]) * (c.mm[3] - c.mm[2]) > 0.0f;
+}
+
+__device__ __forceinline__ void make_rec(const Cand& c, uint32_t surface, RasterRec& R) {
+  const f3* p = c.p;
+  f3 xpv = mk3(roundf(p[0].x), roundf(p[1].x), roundf(p[2].x));
+  f3 ypv = mk3(roundf(p[0].y), roundf(p[1].y), roundf(p[2].y));
+  f3 depths = mk3(rcp(fdiv(p[0].z, kDepthFar)), rcp(fdiv(p[1].z, kDepthFar)),
+                  rcp(fdiv(p[2].z, kDepthFar)));
+  plane_const(depths, xpv, ypv, c.rc, &R.A, &R.B, &R.C);
+  EdgeTest e = make_edge(xpv.x, ypv.x, xpv.y, ypv.y, xpv.z, ypv.z);
+  R.s0 = e.s0; R.sa = e.sa; R.sb = e.sb; R.sign = e.sign;
+  R.t0 = e.t0; R.ta = e.ta; R.tb = e.tb; R.bound = e.bound;
+  R.key = c.key;
+  R.xr = (uint32_t)c.mm[0] | ((uint32_t)c.mm[1] << 16);
+  R.yr = (uint32_t)c.mm[2] | ((uint32_t)c.mm[3] << 16);
+  R.surface = surface;
+  R.pad = 0;
+}
+
+__device__ __forceinline__ void store_rec(RasterRec* dst, const RasterRec& R) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  d[0] = make_float4(R.A, R.B, R.C, R.bound);
+  d[1] = make_float4(R.s0, R.sa, R.sb, R.sign);
+  d[2] = make_float4(R.t0, R.ta, R.tb, __uint_as_float(R.key));
+  d[3] = make_float4(__uint_as_float(R.xr), __uint_as_float(R.yr), __uint_as_float(R.surface), 0.0f);
+}
+
+// Tile footprint of a bbox [minx,maxx) x [miny,maxy).
+struct Foot {
+  int tx0, tx1, ty0, ty1;  // inclusive fine tiles
+  bool coarse;
+};
+__device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr) {
+  Foot f;
+  int minx = xr & 0xFFFF, maxx = xr >> 16, miny = yr & 0xFFFF, maxy = yr >> 16;
+  f.tx0 = minx / kTile; f.tx1 = (maxx - 1) / kTile;
+  f.ty0 = miny / kTile; f.ty1 = (maxy - 1) / kTile;
+  f.coarse = (f.tx1 - f.tx0 + 1) * (f.ty1 - f.ty0 + 1) > kFineMaxTiles;
+  if (f.coarse) {
+    f.tx0 /= kCoarseRatio; f.tx1 /= kCoarseRatio;
+    f.ty0 /= kCoarseRatio; f.ty1 /= kCoarseRatio;
+  }
+  return f;
+}
+
+// Append the candidates of this lane (0..2) as records and count their bins.
+// Every lane of the warp must call it.
+__device__ void emit(const Cand* cands, int n, uint32_t surface, const Surface* surfs,
+                     const Workspace& ws, bool view) {
+  uint32_t base = warp_alloc(&ws.ctr->nrec, (uint32_t)n);
+  unsigned long long frags = 0;
+  const Surface& S = surfs[surface];
+  for (int i = 0; i < n; i++) {
+    uint32_t r = base + i;
+    const Cand& c = cands[i];
+    float area = (c.mm[1] - c.mm[0]) * (c.mm[3] - c.mm[2]);
+    frags += (unsigned long long)ceilf(fdiv(area, (float)S.chunk));
+    if (r >= ws.rec_cap) {
+      atomicOr(&ws.ctr->overflow, 1u);
+      continue;
+    }
+    RasterRec R;
+    make_rec(c, surface, R);
+    store_rec(ws.rec + r, R);
+    if (view) {
+      uint32_t tri = c.key >> 1;
+      ws.srec[r].p0 = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.rc);
+      ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
+      ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
+    }
+    Foot f = footprint(R.xr, R.yr);
+    if (!f.coarse) {
+      for (int ty = f.ty0; ty <= f.ty1; ty++)
+        for (int tx = f.tx0; tx <= f.tx1; tx++)
+          atomicAdd(&ws.fine_count[S.tile_base + ty * S.tiles_x + tx], 1u);
+    } else {
+      for (int ty = f.ty0; ty <= f.ty1; ty++)
+        for (int tx = f.tx0; tx <= f.tx1; tx++)
+          atomicAdd(&ws.coarse_count[S.ctile_base + ty * S.ctiles_x + tx], 1u);
+    }
+  }
+  frags = warp_sum_u64(frags);
+  if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&ws.ctr->frag_ref, frags);
+}
+
+// full_rotate_quat (cl2.cl:700-729): object -> camera space, clip, project.
+__device__ __forceinline__ int transform_clip(const f3 v[3], const gbr_obj_g_descriptor* G, f3 cpos,
+                                              f3 c, f3 s, float fov, float w, float h,
+                                              f3 out[2][3]) {
+  f4 q = ld4(G->world_rot_quat);
+  f3 wp = ld3(G->world_pos);
+  float scale = __ldg(&G->scale);
+  f3 pr[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) pr[k] = rot_cs(add3(rot_quat(mul3s(v[k], scale), q), wp), cpos, c, s);
+  f3 t[2][3];
+  int n = clip_tri(pr, t);
+  for (int i = 0; i < n; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) out[i][k] = depth_project1(t[i][k], w, h, fov);
+  return n;
+}
+
+__device__ __forceinline__ void load_tri_pos(const gbr_triangle* T, f3 v[3], uint32_t* o_id) {
+  const float* base = reinterpret_cast<const float*>(T);
+  float4 a = __ldg(reinterpret_cast<const float4*>(base));       // v0.pos
+  float4 b = __ldg(reinterpret_cast<const float4*>(base + 8));   // v0.vt, object_id, col
+  float4 c = __ldg(reinterpret_cast<const float4*>(base + 12));  // v1.pos
+  float4 d = __ldg(reinterpret_cast<const float4*>(base + 24));  // v2.pos
+  v[0] = mk3(a.x, a.y, a.z);
+  v[1] = mk3(c.x, c.y, c.z);
+  v[2] = mk3(d.x, d.y, d.z);
+  *o_id = __float_as_uint(b.z);
+}
+
+// prearrange (cl2.cl:4271-4409), one thread per (triangle, view).
+__global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewParams* __restrict__ views,
+                                                     const Surface* __restrict__ surfs, Workspace ws) {
+  uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
+  const ViewParams& V = views[blockIdx.y];
+  const Surface& S = surfs[V.surface];
+  Cand cands[2];
+  int n = 0;
+  if (tri < sc.ntris) {
+    f3 v[3];
+    uint32_t o_id;
+    load_tri_pos(sc.tris + tri, v, &o_id);
+    const gbr_obj_g_descriptor* G = sc.descs + o_id;
+    f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
+    if (!(fast_length3(sub3(ld3(G->world_pos), cpos)) > kDepthFar)) {
+      f3 c = mk3(V.ccos[0], V.ccos[1], V.ccos[2]);
+      f3 s = mk3(V.csin[0], V.csin[1], V.csin[2]);
+      float w = (float)S.width, h = (float)S.height;
+      f3 out[2][3];
+      int num = transform_clip(v, G, cpos, c, s, V.fov, w, h, out);
+      bool two = (__ldg(&G->feature_flag) & kFlagTwoSided) > 0;
+      for (int i = 0; i < num; i++) {
+        Cand& cd = cands[n];
+        cd.p[0] = out[i][0]; cd.p[1] = out[i][1]; cd.p[2] = out[i][2];
+        cd.key = tri * 2u + (uint32_t)i;
+        if (cull_candidate(cd, two, w, h)) n++;
+      }
+    }
+  }
+  emit(cands, n, V.surface, surfs, ws, true);
+}
+
+// prearrange_realtime_shadowing (cl2.cl:4419-4636), one thread per (triangle, light job).
+__global__ void __launch_bounds__(256) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
+                                                      const Surface* __restrict__ surfs, Workspace ws) {
+  uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
+  const ShadowJob& J = jobs[blockIdx.y];
+  const float L = (float)kLightBufferDim;
+  int mask = 0;
+  f3 v[3];
+  const gbr_obj_g_descriptor* G = nullptr;
+  f3 lpos = mk3(J.lpos[0], J.lpos[1], J.lpos[2]);
+  bool two = false;
+  if (tri < sc.ntris) {
+    uint32_t o_id;
+    load_tri_pos(sc.tris + tri, v, &o_id);
+    G = sc.descs + o_id;
+    int ff = __ldg(&G->feature_flag);
+    bool is_static = (ff & kFlagIsStatic) > 0;
+    two = (ff & kFlagTwoSided) > 0;
+    f3 wp = ld3(G->world_pos);
+    if (is_static == (J.only_static != 0) && !(fast_length3(sub3(wp, lpos)) > kDepthFar)) {
+      f4 q = ld4(G->world_rot_quat);
+      float scale = __ldg(&G->scale);
+      for (int k = 0; k < 3; k++) {
+        f3 r = add3(rot_quat(mul3s(v[k], scale), q), wp);
+        mask |= 1 << ret_cubeface(r, lpos);
+      }
+    }
+  }
+  for (int face = 0; face < 6; face++) {
+    Cand cands[2];
+    int n = 0;
+    if (mask & (1 << face)) {
+      f3 c = mk3(sc.face_cos[face][0], sc.face_cos[face][1], sc.face_cos[face][2]);
+      f3 s = mk3(sc.face_sin[face][0], sc.face_sin[face][1], sc.face_sin[face][2]);
+      f3 out[2][3];
+      int num = transform_clip(v, G, lpos, c, s, kLFov, L, L, out);
+      for (int i = 0; i < num; i++) {
+        Cand& cd = cands[n];
+        cd.p[0] = out[i][0]; cd.p[1] = out[i][1]; cd.p[2] = out[i][2];
+        cd.key = tri * 2u + (uint32_t)i;
+        if (cull_candidate(cd, two, L, L)) n++;
+      }
+    }
+    emit(cands, n, J.surface_base + face, surfs, ws, false);
+  }
+}
+
+// Exclusive scan of fine and coarse tile counts (one block); counts are reset
+// to zero to serve as fill cursors.
+constexpr int kScanThreads = 1024;
+__device__ void block_scan_array(uint32_t* count, uint32_t* off, uint32_t n, uint32_t* total,
+                                 uint32_t* sh) {
+  uint32_t per = (n + kScanThreads - 1) / kScanThreads;
+  uint32_t b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t s = 0;
+  for (uint32_t i = b; i < e; i++) s += count[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < kScanThreads; o <<= 1) {
+    uint32_t v = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = sh[threadIdx.x] - s;
+  for (uint32_t i = b; i < e; i++) {
+    uint32_t c = count[i];
+    off[i] = run;
+    run += c;
+    count[i] = 0;
+  }
+  if (threadIdx.x == kScanThreads - 1) *total = sh[threadIdx.x];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(Workspace ws) {
+  __shared__ uint32_t sh[kScanThreads];
+  block_scan_array(ws.fine_count, ws.fine_off, ws.nfine, &ws.ctr->fine_total, sh);
+  block_scan_array(ws.coarse_count, ws.coarse_off, ws.ncoarse, &ws.ctr->coarse_total, sh);
+  if (threadIdx.x == 0) {
+    uint64_t need = (uint64_t)ws.ctr->fine_total + ws.ctr->coarse_total;
+    if (need > ws.bin_cap) ws.ctr->overflow |= 2u;
+  }
+}
+
+// Scatter record indices into their tile bins.
+__global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __restrict__ surfs) {
+  uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
+  if (ws.ctr->overflow) return;
+  uint32_t coarse_base = ws.ctr->fine_total;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
+    float4 q = __ldg(reinterpret_cast<const float4*>(ws.rec + r) + 3);
+    uint32_t xr = __float_as_uint(q.x), yr = __float_as_uint(q.y), sid = __float_as_uint(q.z);
+    const Surface& S = surfs[sid];
+    Foot f = footprint(xr, yr);
+    if (!f.coarse) {
+      for (int ty = f.ty0; ty <= f.ty1; ty++)
+        for (int tx = f.tx0; tx <= f.tx1; tx++) {
+          uint32_t t = S.tile_base + ty * S.tiles_x + tx;
+          uint32_t pos = ws.fine_off[t] + atomicAdd(&ws.fine_count[t], 1u);
+          ws.bins[pos] = r;
+        }
+    } else {
+      for (int ty = f.ty0; ty <= f.ty1; ty++)
+        for (int tx = f.tx0; tx <= f.tx1; tx++) {
+          uint32_t t = S.ctile_base + ty * S.ctiles_x + tx;
+          uint32_t pos = coarse_base + ws.coarse_off[t] + atomicAdd(&ws.coarse_count[t], 1u);
+          ws.bins[pos] = r;
+        }
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t find_surface(const Surface* surfs, uint32_t nsurf, uint32_t tile) {
+  uint32_t lo = 0, hi = nsurf - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi + 1) >> 1;
+    if (surfs[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Per-pixel coverage of one record: bbox, the reference walk's skipped
+// pixels, then point_in_tri.  Returns false when the pixel is not drawn.
+__device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int chunk) {
+  uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+  int minx = xr & 0xFFFF, maxx = xr >> 16, miny = yr & 0xFFFF, maxy = yr >> 16;
+  if (px < minx || px >= maxx || py < miny || py >= maxy) return false;
+  if (px == minx && py > miny &&
+      !walk_visits(0, py - miny, maxx - minx, maxy - miny, (float)miny, chunk))
+    return false;
+  float fx = (float)px, fy = (float)py;
+  float sgn = q[1].w;
+  float s = ((q[1].x + q[1].y * fx) + q[1].z * fy) * sgn;
+  float t = ((q[2].x + q[2].y * fx) + q[2].z * fy) * sgn;
+  return s > -0.0001f && t > -0.0001f && (s + t) < q[0].w;
+}
+
+// kernel1 + kernel2 for one 16x16 tile: depth min, then the canonical id.
+__global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const Surface* __restrict__ surfs,
+                                                           uint32_t nsurf, int with_id) {
+  __shared__ float4 srec[kRasterThreads][4];
+  __shared__ uint32_t sidx[kRasterThreads];
+  __shared__ Surface S;
+  __shared__ uint32_t lists[4];
+  if (ws.ctr->overflow) return;
+  const uint32_t tile = blockIdx.x;
+  if (threadIdx.x == 0) {
+    uint32_t s = find_surface(surfs, nsurf, tile);
+    S = surfs[s];
+    uint32_t lt = tile - S.tile_base;
+    int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
+    uint32_t ct = S.ctile_base + (ty / kCoarseRatio) * S.ctiles_x + tx / kCoarseRatio;
+    lists[0] = ws.fine_off[tile];
+    lists[1] = ws.fine_count[tile];
+    lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
+    lists[3] = ws.coarse_count[ct];
+  }
+  __syncthreads();
+  const uint32_t lt = tile - S.tile_base;
+  const int px = (lt % S.tiles_x) * kTile + (threadIdx.x & (kTile - 1));
+  const int py = (lt / S.tiles_x) * kTile + (threadIdx.x / kTile);
+  const int chunk = S.chunk;
+  uint32_t best = kDepthClear, best_key = kNoId, best_rec = kNoId;
+  const int passes = with_id ? 2 : 1;
+  for (int pass = 0; pass < passes; pass++) {
+    for (int l = 0; l < 2; l++) {
+      const uint32_t base = lists[2 * l], cnt = lists[2 * l + 1];
+      for (uint32_t c0 = 0; c0 < cnt; c0 += kRasterThreads) {
+        uint32_t m = min((uint32_t)kRasterThreads, cnt - c0);
+        __syncthreads();
+        if (threadIdx.x < m) {
+          uint32_t r = ws.bins[base + c0 + threadIdx.x];
+          const float4* src = reinterpret_cast<const float4*>(ws.rec + r);
+          srec[threadIdx.x][0] = __ldg(src);
+          srec[threadIdx.x][1] = __ldg(src + 1);
+          srec[threadIdx.x][2] = __ldg(src + 2);
+          srec[threadIdx.x][3] = __ldg(src + 3);
+          sidx[threadIdx.x] = r;
+        }
+        __syncthreads();
+        for (uint32_t i = 0; i < m; i++) {
+          float4 q[4] = {srec[i][0], srec[i][1], srec[i][2], srec[i][3]};
+          if (!covers(q, px, py, chunk)) continue;
+          uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)px, (float)py);
+          if (pass == 0) {
+            best = min(best, d);
+          } else if (d > best - kBufError && d < best + kBufError) {
+            uint32_t key = __float_as_uint(q[2].w);
+            if (key < best_key) { best_key = key; best_rec = sidx[i]; }
+          }
+        }
+      }
+    }
+  }
+  if (px < S.width && py < S.height) {
+    size_t p = (size_t)py * S.width + px;
+    S.depth[p] = best;
+    if (with_id) {
+      if (S.id) S.id[p] = best_key;
+      S.rec[p] = best_rec;
+    }
+  }
+}
+
+// ---- kernel3 ------------------------------------------------------------------
+struct ShadeCtx {
+  SceneDev sc;
+  const ViewParams* V;
+  const Surface* S;
+};
+
+__device__ __forceinline__ float depth_to_dist(uint32_t d) { return fdiv((float)d, kMulInt) * kDepthFar; }
+
+__device__ __forceinline__ f4 read_tex_pre(const SceneDev& sc, float cx, float cy, int which, int slice,
+                                           float width) {
+  const float imax = 1.0f / 2048.0f;
+  float ihnum = width * imax;
+  float tnumy = floorf((float)which * ihnum);
+  float tnumx = (float)which - fdiv(tnumy, ihnum);
+  cx = clampf_(cx, 0.001f, width - 0.001f);
+  cy = clampf_(cy, 0.001f, width - 0.001f);
+  int ix = f2i_sat(fma_(tnumx, width, cx));
+  int iy = f2i_sat(fma_(tnumy, width, cy));
+  uchar4 t = __ldg(sc.atlas + ((size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix));
+  f4 r; r.x = t.x; r.y = t.y; r.z = t.z; r.w = t.w;
+  return r;
+}
+
+__device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, int slice, float width) {
+  float posx = floorf(mx), posy = floorf(my);
+  f4 c0 = read_tex_pre(sc, posx, posy, which, slice, width);
+  f4 c1 = read_tex_pre(sc, posx + 1, posy, which, slice, width);
+  f4 c2 = read_tex_pre(sc, posx, posy + 1, which, slice, width);
+  f4 c3 = read_tex_pre(sc, posx + 1, posy + 1, which, slice, width);
+  float ux = mx - posx, uy = my - posy;
+  float bx = 1.0f - ux, by = 1.0f - uy;
+  f4 r;
+  r.x = fma_(c0.x, bx, c1.x * ux) * by + fma_(c2.x, bx, c3.x * ux) * uy;
+  r.y = fma_(c0.y, bx, c1.y * ux) * by + fma_(c2.y, bx, c3.y * ux) * uy;
+  r.z = fma_(c0.z, bx, c1.z * ux) * by + fma_(c2.z, bx, c3.z * ux) * uy;
+  r.w = fma_(c0.w, bx, c1.w * ux) * by + fma_(c2.w, bx, c3.w * ux) * uy;
+  return r;
+}
+
+// texture_filter_diff (cl2.cl:1511-1573)
+__device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2) {
+  uint32_t nv = __ldg(sc.nums + tid2);
+  int slice = (int)(nv >> 16);
+  int tsize = (int)__ldg(sc.sizes + slice);
+  f2 vtm = texture_mod(vt);
+  float wx = vtdiff.x * (float)tsize, wy = vtdiff.y * (float)tsize;
+  float worst = fsqrt(wx * wx + wy * wy);
+  float wif = fmax_(log2_approx(worst), 0.0f);
+  float mip_lower = clampf_(floorf(wif), 0.0f, (float)kMipLevels);
+  float fmd = wif - mip_lower;
+  int tid_lower = mip_lower == 0.0f
+                      ? tid2
+                      : (int)(((mip_lower - 1.0f) + (float)sc.mipmap_start) + (float)(tid2 * kMipLevels));
+  int tid_higher = (int)((clampf_(mip_lower, 0.0f, kMipLevels - 1.0f) + (float)sc.mipmap_start) +
+                         (float)(tid2 * kMipLevels));
+  uint32_t lnv = __ldg(sc.nums + tid_lower), hnv = __ldg(sc.nums + tid_higher);
+  int sl = (int)(lnv >> 16), sh = (int)(hnv >> 16);
+  float szl = (float)__ldg(sc.sizes + sl), szh = (float)__ldg(sc.sizes + sh);
+  f4 c1 = bilinear_pre(sc, vtm.x * szl, vtm.y * szl, (int)(lnv & 0xFFFF), sl, szl);
+  f4 c2 = bilinear_pre(sc, vtm.x * szh, vtm.y * szh, (int)(hnv & 0xFFFF), sh, szh);
+  const float i255 = 1.0f / 255.0f;
+  f4 r;
+  r.x = (c1.x + (c2.x - c1.x) * fmd) * i255;
+  r.y = (c1.y + (c2.y - c1.y) * fmd) * i255;
+  r.z = (c1.z + (c2.z - c1.z) * fmd) * i255;
+  r.w = (c1.w + (c2.w - c1.w) * fmd) * i255;
+  return r;
+}
+
+// generate_ssao (cl2.cl:2194-2260)
+__device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth, int W, int H, float fov) {
+  uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)W * (uint32_t)H * (uint32_t)y));
+  float foffset = fdiv((float)seed2, kMulInt);
+  float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
+  float rad = kSsaoRad + fdiv(foffset, 2.0f);
+  float world_rad = fdiv(rad * fov, dep);
+  float acc = 0.0f;
+  for (int yy = -2; yy <= 2; yy++) {
+    float oy = roundf((float)yy * world_rad);
+    int wy = (int)clampf_((float)y + oy, 1.0f, (float)H - 2.0f);
+    for (int xx = -2; xx <= 2; xx++) {
+      float ox = roundf((float)xx * world_rad);
+      int wx = (int)clampf_((float)x + ox, 1.0f, (float)W - 2.0f);
+      float d2 = depth_to_dist(__ldg(depth + (size_t)wy * W + wx));
+      for (float z = -2.0f; z <= 2.0f; z += 1.0f)
+        if (d2 > dep + z) acc += 1.0f;
+    }
+  }
+  acc = fdiv(acc, 125.0f);
+  return 1.0f - fdiv(1.0f - acc, kSsaoDiv);
+}
+
+__device__ __forceinline__ float bilinear_interpolate(float cx, float cy, float v0, float v1, float v2,
+                                                      float v3) {
+  float mx = cx - 0.5f, my = cy - 0.5f;
+  float ux = mx - floorf(mx), uy = my - floorf(my);
+  float bx = 1.0f - ux, by = 1.0f - uy;
+  return (v0 * bx + v1 * ux) * by + (v2 * bx + v3 * ux) * uy;
+}
+
+// generate_hard_occlusion (cl2.cl:2536-2701), SMOOTH_SHADOWS
+__device__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 normal, f3 ptl, const uint32_t* buf,
+                                int face, f3 gpos, int shnum) {
+  ptl = fast_normalize3(ptl);
+  f3 c = mk3(sc.face_cos[face][0], sc.face_cos[face][1], sc.face_cos[face][2]);
+  f3 s = mk3(sc.face_sin[face][0], sc.face_sin[face][1], sc.face_sin[face][2]);
+  f3 local = rot_cs(gpos, lpos, c, s);
+  f3 post = depth_project1(local, (float)kLightBufferDim, (float)kLightBufferDim, kLFov);
+  float dpth = post.z;
+  const uint32_t* map = buf + (size_t)(face + shnum * 6) * kLightBufferDim * kLightBufferDim;
+  float px = clampf_(post.x, 3.0f, kLightBufferDim - 4.0f);
+  float py = clampf_(post.y, 3.0f, kLightBufferDim - 4.0f);
+  int ix = f2i_sat(px), iy = f2i_sat(py);
+  float acos_res = rational_acos(clampf_(dot3(normal, ptl), 0.05f, 0.95f));
+  float bias = clampf_(kShadowBias * gbr_tanf(acos_res), 0.1f * kShadowBias, kShadowBias);
+  uint32_t cond = 0;  // bit (yy+1)*4 + (xx+1)
+#pragma unroll
+  for (int yy = -1; yy <= 2; yy++)
+#pragma unroll
+    for (int xx = -1; xx <= 2; xx++) {
+      float ldp = depth_to_dist(__ldg(map + (iy + yy) * kLightBufferDim + ix + xx));
+      if (dpth > ldp + bias) cond |= 1u << ((yy + 1) * 4 + xx + 1);
+    }
+  float shadow = 0.0f;
+#pragma unroll
+  for (int yy = -1; yy <= 1; yy++)
+#pragma unroll
+    for (int xx = -1; xx <= 1; xx++) {
+      int b = (yy + 1) * 4 + xx + 1;
+      shadow += bilinear_interpolate((px + 0.5f) + (float)xx, (py + 0.5f) + (float)yy,
+                                     (float)((cond >> b) & 1u), (float)((cond >> (b + 1)) & 1u),
+                                     (float)((cond >> (b + 4)) & 1u), (float)((cond >> (b + 5)) & 1u));
+    }
+  return fdiv(shadow, 9.0f);
+}
+
+__device__ __forceinline__ f4 vertex_col(uint32_t c) {
+  f4 r;
+  r.x = fdiv((float)(c >> 24), 255.f);
+  r.y = fdiv((float)((c >> 16) & 0xFF), 255.f);
+  r.z = fdiv((float)((c >> 8) & 0xFF), 255.f);
+  r.w = fdiv((float)(c & 0xFF), 255.f);
+  return r;
+}
+
+__device__ __forceinline__ f3 tri_vec(const gbr_triangle* T, int k, int field) {
+  const float* b = reinterpret_cast<const float*>(T) + k * 12 + field;
+  return mk3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
+}
+
+__device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
+  return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
+}
+
+
+// kernel3 (cl2.cl:5792-6408) for one pixel of a view.
+__device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
+                            const ShadeRec* __restrict__ srec, int x, int y) {
+  const int W = S.width, H = S.height;
+  const size_t p = (size_t)y * W + x;
+  const uint32_t d = S.depth[p];
+  const uint32_t r = S.rec[p];
+  uint32_t* out = reinterpret_cast<uint32_t*>(V.rgba);
+  if (d == kDepthClear || r == kNoId) {
+    if (out) out[p] = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
+    if (V.normals) reinterpret_cast<uint32_t*>(V.normals)[p] = 0;
+    return;
+  }
+  const float fov = V.fov;
+  const f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
+  const f3 cc = mk3(V.ccos[0], V.ccos[1], V.ccos[2]);
+  const f3 cs = mk3(V.csin[0], V.csin[1], V.csin[2]);
+  const float4 q0 = __ldg(&srec[r].p0), q1 = __ldg(&srec[r].p1), q2 = __ldg(&srec[r].p2);
+  const f3 tp[3] = {mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), mk3(q2.x, q2.y, q2.z)};
+  const float rconst = q0.w;
+  const uint32_t tri = __float_as_uint(q1.w);
+  const gbr_triangle* T = sc.tris + tri;
+  const uint32_t o_id = __ldg(&T->vertices[0].object_id);
+  const gbr_obj_g_descriptor* G = sc.descs + o_id;
+  const float scale = __ldg(&G->scale);
+  const f3 wpos = ld3(G->world_pos);
+  const f4 q = ld4(G->world_rot_quat);
+  f3 p1 = mul3s(tri_vec(T, 0, 0), scale), p2 = mul3s(tri_vec(T, 1, 0), scale),
+     p3 = mul3s(tri_vec(T, 2, 0), scale);
+  const float* tb = reinterpret_cast<const float*>(T);
+  f2 vt1 = mk2(__ldg(tb + 8), __ldg(tb + 9)), vt2 = mk2(__ldg(tb + 20), __ldg(tb + 21)),
+     vt3 = mk2(__ldg(tb + 32), __ldg(tb + 33));
+  f3 n1 = tri_vec(T, 0, 4), n2 = tri_vec(T, 1, 4), n3 = tri_vec(T, 2, 4);
+
+  const float ldepth = depth_to_dist(d);
+  const float fx = (float)x, fy = (float)y;
+  f3 local = mk3(fdiv((fx - (float)W / 2.0f) * ldepth, fov), fdiv((fy - (float)H / 2.0f) * ldepth, fov),
+                 ldepth);
+  const f3 zero = mk3(0, 0, 0);
+  const f3 gpos = add3(back_rot_cs(local, zero, cc, cs), cpos);
+  f3 olocal = back_rot_quat(sub3(gpos, wpos), q);
+  float l1, l2, l3;
+  barycentric(olocal, p1, p2, p3, &l1, &l2, &l3);
+  f2 vt = mk2(fma_(vt1.x, l1, fma_(vt2.x, l2, vt3.x * l3)), fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
+  f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
+                  fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
+  normal = rot_quat(normal, q);
+
+  f4 col;
+  const uint32_t vc0 = __ldg(&T->vertices[0].vertex_col);
+  if (vc0 != 0) {
+    f4 c0 = vertex_col(vc0), c1 = vertex_col(__ldg(&T->vertices[1].vertex_col)),
+       c2 = vertex_col(__ldg(&T->vertices[2].vertex_col));
+    col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
+    col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
+    col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
+    col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
+  } else {
+    // get_vtdiff (cl2.cl:5691-5760)
+    f3 xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
+    f3 ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
+    f3 depths = mk3(rcp(tp[0].z), rcp(tp[1].z), rcp(tp[2].z));
+    float DA, DB, DC;
+    plane_const(depths, xpv, ypv, rconst, &DA, &DB, &DC);
+    float dmx = fma_(DA, fx + 1.0f, fma_(DB, fy, DC));
+    float dmy = fma_(DA, fx, fma_(DB, fy + 1.0f, DC));
+    float hw = (float)W / 2.0f, hh = (float)H / 2.0f;
+    f3 lmx = mk3(fdiv((fx + 1.0f) - hw, fov), fdiv(fy - hh, fov), 1.0f);
+    f3 lmy = mk3(fdiv(fx - hw, fov), fdiv((fy + 1.0f) - hh, fov), 1.0f);
+    lmx = mk3(fdiv(lmx.x, dmx), fdiv(lmx.y, dmx), fdiv(lmx.z, dmx));
+    lmy = mk3(fdiv(lmy.x, dmy), fdiv(lmy.y, dmy), fdiv(lmy.z, dmy));
+    f3 gmx = back_rot_quat(sub3(add3(back_rot_cs(lmx, zero, cc, cs), cpos), wpos), q);
+    f3 gmy = back_rot_quat(sub3(add3(back_rot_cs(lmy, zero, cc, cs), cpos), wpos), q);
+    float lx1, lx2, lx3, ly1, ly2, ly3;
+    barycentric(gmx, p1, p2, p3, &lx1, &lx2, &lx3);
+    barycentric(gmy, p1, p2, p3, &ly1, &ly2, &ly3);
+    f2 vtx = mk2(fma_(vt1.x, lx1, fma_(vt2.x, lx2, vt3.x * lx3)), fma_(vt1.y, lx1, fma_(vt2.y, lx2, vt3.y * lx3)));
+    f2 vty = mk2(fma_(vt1.x, ly1, fma_(vt2.x, ly2, vt3.x * ly3)), fma_(vt1.y, ly1, fma_(vt2.y, ly2, vt3.y * ly3)));
+    const float mip_bias = 1.0f / kMipBias;
+    f2 vtdiff = mk2((fabsf(vtx.x - vt.x) + fabsf(vty.x - vt.x)) * mip_bias,
+                    (fabsf(vtx.y - vt.y) + fabsf(vty.y - vt.y)) * mip_bias);
+    col = texture_filter_diff(sc, vt, vtdiff, (int)__ldg(&G->tid));
+  }
+  if (V.use_linear) {
+    col.x = gamma_fwd(col.x);
+    col.y = gamma_fwd(col.y);
+    col.z = gamma_fwd(col.z);
+  }
+  uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)y * (uint32_t)W * (uint32_t)H));
+  uint32_t seed3 = rand_xorshift(seed2);
+  uint32_t seed4 = rand_xorshift(seed3);
+  f3 rseed = mk3((fdiv((float)seed2, kMulInt) - 0.5f) * 2.0f, (fdiv((float)seed3, kMulInt) - 0.5f) * 2.0f,
+                 (fdiv((float)seed4, kMulInt) - 0.5f) * 2.0f);
+  const f3 l2p = fast_normalize3(sub3(cpos, gpos));
+  const int ff = __ldg(&G->feature_flag);
+  const bool two = (ff & kFlagTwoSided) > 0;
+  const bool recv_dyn = !((ff & kFlagNoDynShadows) > 0);
+  if (!backface_front(tp[0], tp[1], tp[2]) && two) normal = neg3(normal);
+  const float ssao = generate_ssao(x, y, S.depth, W, H, fov);
+  normal = fast_normalize3(normal);
+  const f3 lnormal = fast_normalize3(add3(normal, mk3(fdiv(rseed.x, 100.f), fdiv(rseed.y, 100.f), fdiv(rseed.z, 100.f))));
+  const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
+  const float g_diffuse = __ldg(&G->diffuse), g_spec_mult = __ldg(&G->spec_mult);
+  const float rough = clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f);
+  f3 dsum = mk3(0, 0, 0), ssum = mk3(0, 0, 0);
+  int shnum = 0, static_num = 0;
+  for (uint32_t i = 0; i < sc.nlights; i++) {
+    const gbr_light* L = sc.lights + i;
+    const f3 lpos = ld3(L->pos);
+    const uint32_t lshadow = __ldg(&L->shadow);
+    const int lstatic = __ldg(&L->is_static);
+    f3 ptl = sub3(lpos, gpos);
+    float occlusion = 1.0f;
+    if (lshadow && lstatic) {
+      int face = ret_cubeface(gpos, lpos);
+      occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
+      static_num++;
+    }
+    float distance = fast_length3(ptl);
+    float tt = fdiv(distance, __ldg(&L->radius)) + 1.0f;
+    float illum = fdiv(__ldg(&L->brightness), tt * tt);
+    const float cutoff = 0.1f;
+    illum -= cutoff;
+    illum *= fdiv(1.0f, 1.0f - cutoff);
+    if (illum <= 0) continue;
+    f3 lcol = ld3(L->col);
+    if (V.use_linear) lcol = mk3(gamma_fwd(lcol.x), gamma_fwd(lcol.y), gamma_fwd(lcol.z));
+    if (lshadow && recv_dyn) {
+      int face = ret_cubeface(gpos, lpos);
+      float dyn = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_dyn, face, gpos, shnum);
+      occlusion = fmin_(occlusion, dyn);
+      shnum++;
+    }
+    ptl = fast_normalize3(ptl);
+    float light = fmax_(dot3(ptl, lnormal) * occlusion, 0.0f);
+    float diffuse = (1.0f - ambient) * light;
+    float dscale = (((diffuse + ambient) * __ldg(&L->diffuse)) * g_diffuse) * illum;
+    dsum = add3(dsum, mul3s(lcol, dscale));
+    f3 Hv = fast_normalize3(add3(l2p, ptl));
+    float ndh = fmax_(0.0f, dot3(normal, Hv));
+    float ndv = fmax_(0.0f, dot3(normal, l2p));
+    float vdh = fmax_(0.0f, dot3(l2p, Hv));
+    float ndl = fmax_(0.0f, dot3(normal, ptl));
+    const float F0 = 0.4f;
+    float fresnel = F0 + (1.0f - F0) * powf(1.0f - vdh, 5.0f);
+    float alpha = rational_acos(ndh);
+    float microfacet = 0.8346f * expf(fdiv((-alpha) * alpha, rough * rough));
+    float sv = fdiv(2.0f * ndh, vdh);
+    float geometric = min3f(1.0f, sv * ndv, sv * ndl);
+    float spec = fdiv((fresnel * microfacet) * geometric, kPi * ndv);
+    float sscale = (spec * 0.4f) * illum;
+    ssum = add3(ssum, mul3s(mul3s(lcol, sscale), g_spec_mult));
+    ssum = mk3(fmax_(ssum.x, 0.0f), fmax_(ssum.y, 0.0f), fmax_(ssum.z, 0.0f));
+    ssum = mul3s(ssum, occlusion);
+  }
+  ssum = mul3s(ssum, ssao);
+  dsum = mul3s(dsum, ssao);
+  const float rsc = 0.7f;
+  f3 colclamp = add3(add3(mk3(col.x, col.y, col.z), zero), mul3s(ssum, rsc));
+  f3 sp2 = mul3s(ssum, 1.0f - rsc);
+  f3 fin = mk3(fma_(colclamp.x, dsum.x, sp2.x), fma_(colclamp.y, dsum.y, sp2.y), fma_(colclamp.z, dsum.z, sp2.z));
+  if (V.use_linear) fin = mk3(gamma_inv(fin.x), gamma_inv(fin.y), gamma_inv(fin.z));
+  if (out) out[p] = pack_rgba(fin.x, fin.y, fin.z, col.w);
+  if (V.normals) {
+    // encode_normal (cl2.cl:5618-5628)
+    float nx = normal.x, ny = normal.y, nz = normal.z;
+    if (nx * nx + ny * ny < 0.0001f) nx = 0.01f;
+    float l = fsqrt(nx * nx + ny * ny);
+    float sq = fsqrt(fmax_(nz * 0.5f + 0.5f, 0.0f));
+    float ex = fdiv(fdiv(nx, l) * sq + 1.0f, 2.0f) * 65536.0f - 1.0f;
+    float ey = fdiv(fdiv(ny, l) * sq + 1.0f, 2.0f) * 65536.0f - 1.0f;
+    uint32_t ux = min(f2u_sat(ex), 65535u), uy = min(f2u_sat(ey), 65535u);
+    reinterpret_cast<uint32_t*>(V.normals)[p] = ux | (uy << 16);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
+                                               const Surface* __restrict__ surfs, uint32_t nviews,
+                                               const ShadeRec* __restrict__ srec) {
+  __shared__ uint32_t s_id;
+  if (threadIdx.x == 0) s_id = find_surface(surfs, nviews, blockIdx.x);
+  __syncthreads();
+  const Surface& S = surfs[s_id];
+  const uint32_t lt = blockIdx.x - S.tile_base;
+  const int x = (lt % S.tiles_x) * kTile + (threadIdx.x & (kTile - 1));
+  const int y = (lt / S.tiles_x) * kTile + (threadIdx.x / kTile);
+  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, x, y);
+}
+
+// ---- texture atlas ----------------------------------------------------------------
+// Slot origin of texture descriptor tid as write_tex_array computes it
+// (cl2.cl:856-889).
+__device__ __forceinline__ void tex_slot(const uint32_t* nums, const uint32_t* sizes, uint32_t tid,
+                                         float* tnx, float* tny, int* slice, float* width) {
+  uint32_t nv = nums[tid];
+  *slice = (int)(nv >> 16);
+  int which = (int)(nv & 0xFFFF);
+  *width = (float)sizes[*slice];
+  float hnum = floorf(fdiv(2048.0f, *width));
+  float tnumy = floorf(fdiv((float)which, hnum));
+  *tny = tnumy;
+  *tnx = fma_(-tnumy, hnum, (float)which);
+}
+
+__device__ __forceinline__ void write_tex(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
+                                          uint32_t tid, float cx, float cy, uchar4 c) {
+  float tnx, tny, w;
+  int slice;
+  tex_slot(nums, sizes, tid, &tnx, &tny, &slice, &w);
+  float tx = tnx * w, ty = tny * w;
+  cx = clampf_(fmodf(cx, w), 0.001f, w - 0.001f);
+  cy = clampf_(fmodf(cy, w), 0.001f, w - 0.001f);
+  int ix = (int)(tx + cx), iy = (int)(ty + cy);
+  atlas[(size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix] = c;
+}
+
+__device__ __forceinline__ float4 read_tex(const uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
+                                           uint32_t tid, float cx, float cy) {
+  float tnx, tny, w;
+  int slice;
+  tex_slot(nums, sizes, tid, &tnx, &tny, &slice, &w);
+  cx = clampf_(cx, 0.001f, w - 0.001f);
+  cy = clampf_(cy, 0.001f, w - 0.001f);
+  int ix = f2i_sat(fma_(tnx, w, cx)), iy = f2i_sat(fma_(tny, w, cy));
+  uchar4 t = atlas[(size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix];
+  return make_float4(t.x, t.y, t.z, t.w);
+}
+
+// update_gpu_tex with flip (cl2.cl:923-953); blockIdx.z = texture.
+__global__ void k_tex_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes, const uint8_t* pixels,
+                             const uint64_t* offsets, const int32_t* tsizes) {
+  const uint32_t t = blockIdx.z;
+  const int s = tsizes[t];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= s || y >= s) return;
+  uchar4 c = reinterpret_cast<const uchar4*>(pixels + offsets[t])[(size_t)y * s + x];
+  float w = (float)sizes[nums[t] >> 16];
+  write_tex(atlas, nums, sizes, t, (float)x, w - (float)y, c);
+}
+
+// generate_mips / generate_mip_mips (cl2.cl:1070-1189): level src -> src+1
+// for every texture (blockIdx.z), grid over the base texture size.
+__global__ void k_mip(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                      const int32_t* tsizes, int level) {
+  const uint32_t t = blockIdx.z;
+  const int s = tsizes[t];
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= s || y >= s) return;
+  uint32_t src = level == 0 ? t : t * kMipLevels + mipmap_start + (uint32_t)(level - 1);
+  uint32_t dst = t * kMipLevels + mipmap_start + (uint32_t)level;
+  float w = (float)sizes[nums[src] >> 16];
+  if ((float)x >= w || (float)y >= w) return;
+  const float g[3] = {1.f, 2.f, 1.f};
+  float a0 = 0, a1 = 0, a2 = 0, a3 = 0, div = 0;
+  for (int j = -1; j <= 1; j++)
+    for (int i = -1; i <= 1; i++) {
+      float4 c = read_tex(atlas, nums, sizes, src, (float)(x * 2 + i), (float)(y * 2 + j));
+      c.w = fdiv(c.w, 255.f);
+      c.x *= c.w; c.y *= c.w; c.z *= c.w;
+      float gw = g[j + 1] * g[i + 1];
+      a0 += c.x * gw; a1 += c.y * gw; a2 += c.z * gw; a3 += c.w * gw;
+      div += gw;
+    }
+  a0 = fdiv(a0, div); a1 = fdiv(a1, div); a2 = fdiv(a2, div); a3 = fdiv(a3, div);
+  if (a3 > 0.00000001f) { a0 = fdiv(a0, a3); a1 = fdiv(a1, a3); a2 = fdiv(a2, a3); }
+  a3 *= 255.f;
+  float nw = (float)sizes[nums[dst] >> 16];
+  float yx0 = fdiv((float)(x * 2), w) * nw, yx1 = fdiv((float)(y * 2), w) * nw;
+  if (yx0 >= nw || yx1 >= nw) return;
+  uchar4 c = make_uchar4((unsigned char)f2u_sat(a0), (unsigned char)f2u_sat(a1), (unsigned char)f2u_sat(a2),
+                         (unsigned char)f2u_sat(a3));
+  write_tex(atlas, nums, sizes, dst, yx0, yx1, c);
+}
+
+__global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+int g_num_sms = 0;
+int num_sms() {
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 152;
+  }
+  return g_num_sms;
+}
+
+}  // namespace
+
+cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
+                               const Surface* d_surf, const Workspace& ws, cudaStream_t st) {
+  if (!sc.ntris || !nviews) return cudaSuccess;
+  dim3 grid((sc.ntris + 255) / 256, nviews);
+  k_setup_views<<<grid, 256, 0, st>>>(sc, d_views, d_surf, ws);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,
+                                const Surface* d_surf, const Workspace& ws, cudaStream_t st) {
+  if (!sc.ntris || !njobs) return cudaSuccess;
+  dim3 grid((sc.ntris + 255) / 256, njobs);
+  k_setup_shadow<<<grid, 256, 0, st>>>(sc, d_jobs, d_surf, ws);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scan(const Workspace& ws, cudaStream_t st) {
+  k_scan<<<1, kScanThreads, 0, st>>>(ws);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st) {
+  k_fill<<<num_sms() * 8, 256, 0, st>>>(ws, d_surf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, uint32_t ntiles,
+                          bool with_id, cudaStream_t st) {
+  if (!ntiles) return cudaSuccess;
+  k_raster<<<ntiles, kRasterThreads, 0, st>>>(ws, d_surf, nsurf, with_id ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
+                         uint32_t ntiles, const ShadeRec* srec, cudaStream_t st) {
+  if (!ntiles) return cudaSuccess;
+  k_shade<<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
+                                  const uint8_t* pixels, const uint64_t* offsets, const int32_t* tsizes,
+                                  uint32_t ntex, int32_t max_size, cudaStream_t st) {
+  if (!ntex) return cudaSuccess;
+  dim3 block(16, 16), grid((max_size + 15) / 16, (max_size + 15) / 16, ntex);
+  k_tex_upload<<<grid, block, 0, st>>>(atlas, nums, sizes, pixels, offsets, tsizes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                        const int32_t* tsizes, uint32_t ntex, int32_t max_size, cudaStream_t st) {
+  if (!ntex) return cudaSuccess;
+  dim3 block(16, 16), grid((max_size + 15) / 16, (max_size + 15) / 16, ntex);
+  for (int level = 0; level < kMipLevels; level++) {
+    k_mip<<<grid, block, 0, st>>>(atlas, nums, sizes, mipmap_start, tsizes, level);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st) {
+  if (!n) return cudaSuccess;
+  k_fill_u32<<<num_sms() * 4, 256, 0, st>>>(p, v, n);
+  return cudaGetLastError();
+}
+
+}  // namespace gbr

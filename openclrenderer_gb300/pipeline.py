@@ -1,0 +1,190 @@
+"""Python handle over the C ABI (include/gbr.h) for tests and benchmarks.
+
+GpuScene mirrors the reference's object_context + light + texture_context
+build (object_context.cpp:646-797, light.cpp:145-276,
+texture_context.cpp:350-517) and engine::render_tris /
+generate_realtime_shadowing (engine.cpp:1794, 1601).  Device outputs are torch
+tensors; torch only provides device memory and streams here.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _native
+from . import structs as S
+
+_P = ctypes.c_void_p
+
+
+def _np_ptr(a):
+    return _P(a.ctypes.data) if a is not None else None
+
+
+def _t_ptr(t):
+    return _P(t.data_ptr()) if t is not None else None
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return _P(stream.cuda_stream)
+
+
+def fov_const(hfov_deg, width):
+    return _native.load().gbr_fov_const_from_hfov(hfov_deg, width)
+
+
+def texture_pack(sizes):
+    """Host-only texture page packing; returns (nums, page_sizes)."""
+    L = _native.load()
+    sz = np.ascontiguousarray(sizes, np.int32)
+    nums = np.zeros(5 * max(len(sz), 1), np.uint32)
+    pages = np.zeros(5 * max(len(sz), 1), np.uint32)
+    nn, npg = _native.ctypes.c_uint32(len(nums)), _native.ctypes.c_uint32(len(pages))
+    _native.check(L.gbr_texture_pack(len(sz), _np_ptr(sz), _np_ptr(nums), ctypes.byref(nn),
+                                     _np_ptr(pages), ctypes.byref(npg)))
+    return nums[:nn.value].copy(), pages[:npg.value].copy()
+
+
+class OutputSet:
+    """Device buffers of one view (torch uint32/uint8/uint16 tensors)."""
+
+    def __init__(self, width, height, device="cuda", normals=False):
+        import torch
+        self.depth = torch.empty((height, width), dtype=torch.int32, device=device)
+        self.id = torch.empty((height, width), dtype=torch.int32, device=device)
+        self.rgba = torch.empty((height, width, 4), dtype=torch.uint8, device=device)
+        self.normals = torch.empty((height, width, 2), dtype=torch.int16, device=device) if normals else None
+
+    def as_struct(self):
+        class Out(ctypes.Structure):
+            _fields_ = [("depth", _P), ("id", _P), ("rgba", _P), ("normals", _P)]
+        return Out(self.depth.data_ptr(), self.id.data_ptr(), self.rgba.data_ptr(),
+                   self.normals.data_ptr() if self.normals is not None else None)
+
+    def numpy(self):
+        out = {"depth": self.depth.cpu().numpy().view(np.uint32),
+               "id": self.id.cpu().numpy().view(np.uint32),
+               "rgba": self.rgba.cpu().numpy()}
+        if self.normals is not None:
+            out["normals"] = self.normals.cpu().numpy().view(np.uint16)
+        return out
+
+
+class _Outs(ctypes.Structure):
+    _fields_ = [("depth", _P), ("id", _P), ("rgba", _P), ("normals", _P)]
+
+
+class GpuScene:
+    """A scene resident on the current CUDA device."""
+
+    def __init__(self, scene=None):
+        self.L = _native.load()
+        h = _P()
+        _native.check(self.L.gbr_scene_create(ctypes.byref(h)))
+        self.h = h
+        if scene is not None:
+            self.upload(scene)
+
+    def close(self):
+        if self.h:
+            self.L.gbr_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- build (object_context::build, light::build, texture_context::alloc_gpu)
+    def set_triangles(self, tris):
+        tris = np.ascontiguousarray(tris, S.TRIANGLE)
+        _native.check(self.L.gbr_scene_set_triangles(self.h, _np_ptr(tris), len(tris)))
+
+    def set_descriptors(self, descs):
+        descs = np.ascontiguousarray(descs, S.OBJ_DESC)
+        _native.check(self.L.gbr_scene_set_descriptors(self.h, _np_ptr(descs), len(descs)))
+
+    def set_lights(self, lights):
+        lights = np.ascontiguousarray(lights, S.LIGHT)
+        _native.check(self.L.gbr_scene_set_lights(self.h, _np_ptr(lights), len(lights)))
+
+    def set_textures(self, sizes, pixels):
+        sz = np.ascontiguousarray(sizes, np.int32)
+        px = [np.ascontiguousarray(p, np.uint8) for p in pixels]
+        ptrs = (ctypes.c_void_p * max(len(px), 1))(*[p.ctypes.data for p in px])
+        _native.check(self.L.gbr_scene_set_textures(self.h, len(px), _np_ptr(sz), ctypes.cast(ptrs, _P)))
+
+    def upload(self, scene):
+        self.set_triangles(scene.tris)
+        self.set_descriptors(scene.descs)
+        self.set_lights(scene.lights)
+        self.set_textures(scene.tex_sizes, scene.tex_pixels)
+
+    def texture_layout(self):
+        nums = np.zeros(4096, np.uint32)
+        sizes = np.zeros(4096, np.uint32)
+        nn, ns, ms = ctypes.c_uint32(4096), ctypes.c_uint32(4096), ctypes.c_uint32(0)
+        _native.check(self.L.gbr_scene_texture_layout(self.h, _np_ptr(nums), ctypes.byref(nn), _np_ptr(sizes),
+                                                      ctypes.byref(ns), ctypes.byref(ms)))
+        return nums[:nn.value].copy(), sizes[:ns.value].copy(), ms.value
+
+    def read_buffer(self, which):
+        ptr, nbytes = _P(), ctypes.c_size_t()
+        _native.check(self.L.gbr_scene_buffer(self.h, which, ctypes.byref(ptr), ctypes.byref(nbytes)))
+        out = np.empty(nbytes.value, np.uint8)
+        if nbytes.value:
+            _native.check(self.L.gbr_scene_read_buffer(self.h, which, _np_ptr(out), 0, nbytes.value))
+        return out
+
+    def atlas(self):
+        return self.read_buffer(0).reshape(-1, 2048, 2048, 4)
+
+    def cubemaps(self, static=False):
+        return self.read_buffer(2 if static else 1).view(np.uint32).reshape(-1, 6, 1024, 1024)
+
+    # ---- passes
+    def shadow_pass(self, stream=None):
+        _native.check(self.L.gbr_shadow_pass(self.h, _stream_ptr(stream)))
+
+    def render(self, cam, view, out=None, stream=None, normals=False):
+        cam = np.asarray(cam, S.CAMERA).reshape(1)
+        view = np.asarray(view, S.VIEW).reshape(1)
+        if out is None:
+            out = OutputSet(int(view[0]["width"]), int(view[0]["height"]), normals=normals)
+        o = out.as_struct()
+        _native.check(self.L.gbr_render_view(self.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(o),
+                                             _stream_ptr(stream)))
+        return out
+
+    def render_batch(self, cams, views, outs=None, stream=None):
+        cams = np.ascontiguousarray(np.stack([np.asarray(c, S.CAMERA) for c in cams]))
+        views = np.ascontiguousarray(np.stack([np.asarray(v, S.VIEW) for v in views]))
+        if outs is None:
+            outs = [OutputSet(int(v["width"]), int(v["height"])) for v in views]
+        arr = (_Outs * len(outs))()
+        for i, o in enumerate(outs):
+            arr[i] = _Outs(o.depth.data_ptr(), o.id.data_ptr(), o.rgba.data_ptr(),
+                           o.normals.data_ptr() if o.normals is not None else None)
+        _native.check(self.L.gbr_render_batch(self.h, len(outs), _np_ptr(cams), _np_ptr(views), arr,
+                                              _stream_ptr(stream)))
+        return outs
+
+    def render_host(self, cam, view, depth=None, ids=None, rgba=None, stream=None):
+        """render_tris with host output buffers (numpy; pinned or pageable)."""
+        cam = np.asarray(cam, S.CAMERA).reshape(1)
+        view = np.asarray(view, S.VIEW).reshape(1)
+        W, H = int(view[0]["width"]), int(view[0]["height"])
+        depth = np.empty((H, W), np.uint32) if depth is None else depth
+        ids = np.empty((H, W), np.uint32) if ids is None else ids
+        rgba = np.empty((H, W, 4), np.uint8) if rgba is None else rgba
+        _native.check(self.L.gbr_render_view_host(self.h, _np_ptr(cam), _np_ptr(view), _np_ptr(depth),
+                                                  _np_ptr(ids), _np_ptr(rgba), _stream_ptr(stream)))
+        return {"depth": depth, "id": ids, "rgba": rgba}
+
+    def stats(self):
+        st = np.zeros(1, S.STATS)
+        _native.check(self.L.gbr_scene_stats(self.h, _np_ptr(st)))
+        return {k: int(st[0][k]) for k in S.STATS.names}

@@ -1,0 +1,913 @@
+// gbr_oracle.cpp — TEST INFRASTRUCTURE ONLY.
+//
+// CPU restatement of OpenCLRenderer's cl2.cl triangle path, used as the parity
+// checker of the CUDA pipeline.  Only tests/, __graft_entry__.smoke() and the
+// CPU-baseline leg of bench.py may load it; the product never does.
+//
+// It follows the reference kernels step by step, on the reference's own work
+// decomposition:
+//   prearrange                   cl2.cl:4271-4409  (1 work item per triangle)
+//   kernel1                      cl2.cl:4985-5127  (1 work item per 500-pixel fragment,
+//                                                   literal float walk state machine)
+//   kernel2 (canonical id)       cl2.cl:5390-5546  (same walk; id = min triangle key
+//                                                   among fragments passing the +-20 test)
+//   kernel3                      cl2.cl:5792-6408  (1 work item per pixel)
+//   prearrange_realtime_shadowing cl2.cl:4419-4636
+//   kernel1_realtime_shadowing   cl2.cl:5129-5246
+//   update_gpu_tex / generate_mips / generate_mip_mips  cl2.cl:923-953, 1070-1189
+//   texture page packing         texture_context.cpp:94-261
+// with every implementation-defined builtin pinned by gbr_math.h.  Work items
+// run on std::threads; atomics are std::atomic.
+//
+// Parity pin: the restatement is checked against the reference's own cl2.cl
+// kernels compiled as C++ (oracle/clref), through golden fixtures.
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../include/gbr.h"
+#include "../openclrenderer_gb300/csrc/gbr_math.h"
+
+using namespace gbr;
+
+namespace {
+
+// ---- threading ------------------------------------------------------------
+template <class F>
+void parallel_for(int64_t n, int nthreads, F&& f) {
+  if (n <= 0) return;
+  if (nthreads <= 1 || n < 256) {
+    for (int64_t i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  const int64_t chunk = std::max<int64_t>(64, n / (int64_t)(nthreads * 16));
+  auto worker = [&]() {
+    for (;;) {
+      int64_t b = next.fetch_add(chunk);
+      if (b >= n) break;
+      int64_t e = std::min(n, b + chunk);
+      for (int64_t i = b; i < e; i++) f(i);
+    }
+  };
+  std::vector<std::thread> ts;
+  for (int t = 0; t < nthreads - 1; t++) ts.emplace_back(worker);
+  worker();
+  for (auto& t : ts) t.join();
+}
+
+inline void atomic_min_u32(std::atomic<uint32_t>* a, uint32_t v) {
+  uint32_t cur = a->load(std::memory_order_relaxed);
+  while (v < cur && !a->compare_exchange_weak(cur, v, std::memory_order_relaxed)) {
+  }
+}
+
+inline f3 v3(const float* p) { return mk3(p[0], p[1], p[2]); }
+inline f4 v4(const float* p) {
+  f4 r; r.x = p[0]; r.y = p[1]; r.z = p[2]; r.w = p[3];
+  return r;
+}
+
+// Host-side cosines/sines of Euler angles (the pinned native_cos/native_sin).
+void euler_cs(f3 ang, f3* c, f3* s) {
+  *c = mk3((float)cos((double)ang.x), (float)cos((double)ang.y), (float)cos((double)ang.z));
+  *s = mk3((float)sin((double)ang.x), (float)sin((double)ang.y), (float)sin((double)ang.z));
+}
+
+// ---- prearrange ------------------------------------------------------------
+struct Cut {
+  f3 p[3];
+};
+struct Frag {
+  uint32_t tri, a, ctri;
+  float rconst;
+  uint32_t o_id;
+};
+
+struct Setup {
+  // per triangle: number of clip outputs (the reference reserves this many
+  // cutdown slots, culled or not) and, per output, its fragment count (-1 culled)
+  std::vector<int> num;
+  std::vector<int> nfrag;  // 2 per triangle
+  std::vector<float> rconst;
+  std::vector<Cut> cut;    // 2 per triangle
+  std::vector<uint32_t> ctri_base;
+  std::vector<Frag> frags;
+};
+
+// full_rotate_quat (cl2.cl:700-729) + the per-output culls of prearrange.
+// Returns the clip outputs of triangle T for a camera (cpos, c, s).
+int project_tri(const gbr_triangle& T, const gbr_obj_g_descriptor& G, f3 cpos, f3 c, f3 s,
+                float fov, float w, float h, f3 out[2][3]) {
+  f4 q = v4(G.world_rot_quat);
+  f3 wp = v3(G.world_pos);
+  f3 pr[3];
+  for (int k = 0; k < 3; k++) {
+    f3 v = mul3s(v3(T.vertices[k].pos), G.scale);
+    f3 inter = rot_quat(v, q);
+    pr[k] = rot_cs(add3(inter, wp), cpos, c, s);
+  }
+  f3 tris[2][3];
+  int n = clip_tri(pr, tris);
+  for (int i = 0; i < n; i++)
+    for (int k = 0; k < 3; k++) out[i][k] = depth_project1(tris[i][k], w, h, fov);
+  return n;
+}
+
+// Per clip output: -1 when culled, else the fragment count ceil(area/chunk).
+int cull_and_count(const f3 p[3], bool two_sided, float w, float h, int chunk, float* rc) {
+  int valid = two_sided || backface_front(p[0], p[1], p[2]);
+  int cond = (p[0].x < 0 && p[1].x < 0 && p[2].x < 0) ||
+             (p[0].x >= w && p[1].x >= w && p[2].x >= w) ||
+             (p[0].y < 0 && p[1].y < 0 && p[2].y < 0) ||
+             (p[0].y >= h && p[1].y >= h && p[2].y >= h);
+  if (!valid || cond) return -1;
+  f3 xpv = mk3(roundf(p[0].x), roundf(p[1].x), roundf(p[2].x));
+  f3 ypv = mk3(roundf(p[0].y), roundf(p[1].y), roundf(p[2].y));
+  *rc = rconstant(xpv, ypv);
+  float mm[4];
+  bbox4(p[0], p[1], p[2], w, h, mm);
+  float area = (mm[1] - mm[0]) * (mm[3] - mm[2]);
+  return (int)ceilf(fdiv(area, (float)chunk));
+}
+
+void prearrange(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descriptor* descs,
+                f3 cpos, f3 crot, float fov, float w, float h, int nthreads, Setup* S) {
+  f3 c, s;
+  euler_cs(crot, &c, &s);
+  S->num.assign(n, 0);
+  S->nfrag.assign((size_t)n * 2, -1);
+  S->rconst.assign((size_t)n * 2, 0.0f);
+  S->cut.resize((size_t)n * 2);
+  parallel_for(n, nthreads, [&](int64_t id) {
+    const gbr_triangle& T = tris[id];
+    const gbr_obj_g_descriptor& G = descs[T.vertices[0].object_id];
+    if (fast_length3(sub3(v3(G.world_pos), cpos)) > kDepthFar) return;
+    f3 out[2][3];
+    int num = project_tri(T, G, cpos, c, s, fov, w, h, out);
+    S->num[id] = num;
+    bool two = (G.feature_flag & kFlagTwoSided) > 0;
+    for (int i = 0; i < num; i++) {
+      Cut& ct = S->cut[id * 2 + i];
+      ct.p[0] = out[i][0]; ct.p[1] = out[i][1]; ct.p[2] = out[i][2];
+      float rc = 0;
+      S->nfrag[id * 2 + i] = cull_and_count(ct.p, two, w, h, kOpSize, &rc);
+      S->rconst[id * 2 + i] = rc;
+    }
+  });
+  // The reference appends with atomics in arbitrary order; a serial prefix
+  // sum gives the same set of records in triangle order.
+  S->ctri_base.assign(n, 0);
+  uint64_t ctri = 0, nf = 0;
+  std::vector<uint64_t> fbase((size_t)n * 2, 0);
+  for (uint32_t id = 0; id < n; id++) {
+    S->ctri_base[id] = (uint32_t)ctri;
+    ctri += S->num[id];
+    for (int i = 0; i < 2; i++) {
+      fbase[id * 2 + i] = nf;
+      if (S->nfrag[id * 2 + i] > 0) nf += S->nfrag[id * 2 + i];
+    }
+  }
+  S->frags.resize(nf);
+  parallel_for(n, nthreads, [&](int64_t id) {
+    const gbr_triangle& T = tris[id];
+    for (int i = 0; i < 2; i++) {
+      int tn = S->nfrag[id * 2 + i];
+      for (int a = 0; a < tn; a++) {
+        Frag& f = S->frags[fbase[id * 2 + i] + a];
+        f.tri = (uint32_t)id;
+        f.a = (uint32_t)a;
+        f.ctri = (uint32_t)(id * 2 + i);  // index into S->cut
+        f.rconst = S->rconst[id * 2 + i];
+        f.o_id = T.vertices[0].object_id;
+      }
+    }
+  });
+}
+
+// ---- the literal fragment walk of kernel1 / kernel2 -------------------------
+// Visits pixels exactly as cl2.cl:5046-5126 (and 5455-5545, 5188-5245).
+template <class V>
+void walk(const f3 tp[3], float ew, float eh, int chunk, uint32_t distance, bool k2_guards,
+          V&& visit) {
+  float mm[4];
+  bbox4(tp[0], tp[1], tp[2], ew, eh, mm);
+  int width = (int)(mm[1] - mm[0]);
+  if (width <= 0) return;
+  int pixel_along = chunk * (int)distance;
+  int pcount = -1;
+  float x = ((float)((pixel_along + 0) % width) + mm[0]) - 1.0f;
+  float y = floorf(fdiv((float)(pixel_along + pcount), (float)width)) + mm[2];
+  float iwidth = fdiv(1.0f, (float)width);
+  float rwm = (float)((pixel_along + pcount) % width);
+  while (pcount < chunk) {
+    pcount++;
+    x += 1.0f;
+    rwm += 1.0f;
+    if (rwm >= (float)width) rwm = 0.0f;
+    float ty = y;
+    y = floorf(fma_((float)(pixel_along + pcount), iwidth, mm[2]));
+    x = y != ty ? rwm + mm[0] : x;
+    if (y >= mm[3]) break;
+    bool oob = x >= mm[1];
+    if (k2_guards) oob = oob || x < mm[0] || y < mm[2];
+    if (oob) continue;
+    visit(x, y);
+  }
+}
+
+// point_in_tri, written out as cl2.cl:4798-4807.
+bool point_in_tri(float px, float py, float p0x, float p0y, float p1x, float p1y, float p2x,
+                  float p2y) {
+  float A = 0.5f * ((((-p1y) * p2x + p0y * ((-p1x) + p2x)) + p0x * (p1y - p2y)) + p1x * p2y);
+  float sign = A < 0 ? -1.0f : 1.0f;
+  float s = (((p0y * p2x - p0x * p2y) + (p2y - p0y) * px) + (p0x - p2x) * py) * sign;
+  float t = (((p0x * p1y - p0y * p1x) + (p0y - p1y) * px) + (p1x - p0x) * py) * sign;
+  return s > -0.0001f && t > -0.0001f && (s + t) < (2.0001f * A) * sign;
+}
+
+struct FragGeom {
+  f3 xpv, ypv;
+  float A, B, C;
+};
+FragGeom frag_geom(const f3 tp[3], float rconst) {
+  FragGeom g;
+  g.xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
+  g.ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
+  f3 depths = mk3(rcp(fdiv(tp[0].z, kDepthFar)), rcp(fdiv(tp[1].z, kDepthFar)),
+                  rcp(fdiv(tp[2].z, kDepthFar)));
+  plane_const(depths, g.xpv, g.ypv, rconst, &g.A, &g.B, &g.C);
+  return g;
+}
+
+void kernel1(const Setup& S, float ew, float eh, std::atomic<uint32_t>* depth, int W,
+             int nthreads) {
+  parallel_for((int64_t)S.frags.size(), nthreads, [&](int64_t id) {
+    const Frag& f = S.frags[id];
+    const Cut& ct = S.cut[f.ctri];
+    FragGeom g = frag_geom(ct.p, f.rconst);
+    walk(ct.p, ew, eh, kOpSize, f.a, false, [&](float x, float y) {
+      if (point_in_tri(x, y, g.xpv.x, g.ypv.x, g.xpv.y, g.ypv.y, g.xpv.z, g.ypv.z)) {
+        uint32_t d = depth_at(g.A, g.B, g.C, x, y);
+        atomic_min_u32(&depth[(int)(y * (float)W) + (int)x], d);
+      }
+    });
+  });
+}
+
+void kernel2(const Setup& S, float ew, float eh, const uint32_t* depth,
+             std::atomic<uint32_t>* ids, int W, int nthreads) {
+  parallel_for((int64_t)S.frags.size(), nthreads, [&](int64_t id) {
+    const Frag& f = S.frags[id];
+    const Cut& ct = S.cut[f.ctri];
+    FragGeom g = frag_geom(ct.p, f.rconst);
+    uint32_t key = f.ctri;  // 2*triangle + clip_sub: the canonical id
+    walk(ct.p, ew, eh, kOpSize, f.a, true, [&](float x, float y) {
+      if (point_in_tri(x, y, g.xpv.x, g.ypv.x, g.xpv.y, g.ypv.y, g.xpv.z, g.ypv.z)) {
+        uint32_t my = depth_at(g.A, g.B, g.C, x, y);
+        size_t p = (size_t)((int)y * W + (int)x);
+        uint32_t val = depth[p];
+        int c2 = my > val - kBufError && my < val + kBufError;
+        if (c2) atomic_min_u32(&ids[p], key);
+      }
+    });
+  });
+}
+
+// ---- kernel3 ---------------------------------------------------------------
+struct Atlas {
+  const uint8_t* data;
+  const uint32_t* nums;
+  const uint32_t* sizes;
+  uint32_t mipmap_start;
+};
+
+f4 read_tex_pre(f2 coords, int which, int slice, float width, const Atlas& at) {
+  const float imax = 1.0f / 2048.0f;
+  float ihnum = width * imax;
+  float tnumy = floorf((float)which * ihnum);
+  float tnumx = (float)which - fdiv(tnumy, ihnum);
+  coords.x = clampf_(coords.x, 0.001f, width - 0.001f);
+  coords.y = clampf_(coords.y, 0.001f, width - 0.001f);
+  int cx = f2i_sat(fma_(tnumx, width, coords.x));
+  int cy = f2i_sat(fma_(tnumy, width, coords.y));
+  const uint8_t* t = at.data + ((size_t)slice * kTexPage * kTexPage + (size_t)cy * kTexPage + cx) * 4;
+  f4 r; r.x = t[0]; r.y = t[1]; r.z = t[2]; r.w = t[3];
+  return r;
+}
+
+f4 bilinear_pre(f2 m, int which, int slice, float width, const Atlas& at) {
+  f2 pos = mk2(floorf(m.x), floorf(m.y));
+  f4 c0 = read_tex_pre(pos, which, slice, width, at);
+  f4 c1 = read_tex_pre(mk2(pos.x + 1, pos.y), which, slice, width, at);
+  f4 c2 = read_tex_pre(mk2(pos.x, pos.y + 1), which, slice, width, at);
+  f4 c3 = read_tex_pre(mk2(pos.x + 1, pos.y + 1), which, slice, width, at);
+  f2 u = mk2(m.x - pos.x, m.y - pos.y);
+  f2 b = mk2(1.0f - u.x, 1.0f - u.y);
+  f4 r;
+  r.x = fma_(c0.x, b.x, c1.x * u.x) * b.y + fma_(c2.x, b.x, c3.x * u.x) * u.y;
+  r.y = fma_(c0.y, b.x, c1.y * u.x) * b.y + fma_(c2.y, b.x, c3.y * u.x) * u.y;
+  r.z = fma_(c0.z, b.x, c1.z * u.x) * b.y + fma_(c2.z, b.x, c3.z * u.x) * u.y;
+  r.w = fma_(c0.w, b.x, c1.w * u.x) * b.y + fma_(c2.w, b.x, c3.w * u.x) * u.y;
+  return r;
+}
+
+f4 texture_filter_diff(f2 vt, f2 vtdiff, int tid2, const Atlas& at) {
+  uint32_t nv = at.nums[tid2];
+  int slice = (int)(nv >> 16);
+  int tsize = (int)at.sizes[slice];
+  f2 vtm = texture_mod(vt);
+  float wx = vtdiff.x * (float)tsize, wy = vtdiff.y * (float)tsize;
+  float worst = fsqrt(wx * wx + wy * wy);
+  float wif = log2_approx(worst);
+  wif = fmax_(wif, 0.0f);
+  float mip_lower = floorf(wif);
+  mip_lower = clampf_(mip_lower, 0.0f, (float)kMipLevels);
+  float fmd = wif - mip_lower;
+  int tid_lower = mip_lower == 0.0f
+                      ? tid2
+                      : (int)(((mip_lower - 1.0f) + (float)at.mipmap_start) + (float)(tid2 * kMipLevels));
+  int tid_higher = (int)((clampf_(mip_lower, 0.0f, kMipLevels - 1.0f) + (float)at.mipmap_start) +
+                         (float)(tid2 * kMipLevels));
+  uint32_t lnv = at.nums[tid_lower], hnv = at.nums[tid_higher];
+  int sl = (int)(lnv >> 16), sh = (int)(hnv >> 16);
+  int wl = (int)(lnv & 0xFFFF), wh = (int)(hnv & 0xFFFF);
+  float szl = (float)at.sizes[sl], szh = (float)at.sizes[sh];
+  f4 c1 = bilinear_pre(mk2(vtm.x * szl, vtm.y * szl), wl, sl, szl, at);
+  f4 c2 = bilinear_pre(mk2(vtm.x * szh, vtm.y * szh), wh, sh, szh, at);
+  const float i255 = 1.0f / 255.0f;
+  f4 r;
+  r.x = (c1.x + (c2.x - c1.x) * fmd) * i255;
+  r.y = (c1.y + (c2.y - c1.y) * fmd) * i255;
+  r.z = (c1.z + (c2.z - c1.z) * fmd) * i255;
+  r.w = (c1.w + (c2.w - c1.w) * fmd) * i255;
+  return r;
+}
+
+struct ShadeView {
+  int W, H;
+  float fov;
+  f3 cpos, crot_c, crot_s;
+  f3 face_c[6], face_s[6];
+  uint32_t use_linear;
+  f4 clear;
+};
+
+f2 get_vtdiff(const f3 tp[3], float x, float y, const ShadeView& v,
+              const gbr_obj_g_descriptor& G, f2 vt, f3 p1, f3 p2, f3 p3, f2 vt1, f2 vt2, f2 vt3,
+              float rconst) {
+  f3 xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
+  f3 ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
+  f3 depths = mk3(rcp(tp[0].z), rcp(tp[1].z), rcp(tp[2].z));
+  float DA, DB, DC;
+  plane_const(depths, xpv, ypv, rconst, &DA, &DB, &DC);
+  float dmx = fma_(DA, x + 1.0f, fma_(DB, y, DC));
+  float dmy = fma_(DA, x, fma_(DB, y + 1.0f, DC));
+  float hw = (float)v.W / 2.0f, hh = (float)v.H / 2.0f;
+  f3 lmx = mk3(fdiv((x + 1.0f) - hw, v.fov), fdiv(y - hh, v.fov), 1.0f);
+  f3 lmy = mk3(fdiv(x - hw, v.fov), fdiv((y + 1.0f) - hh, v.fov), 1.0f);
+  lmx = mk3(fdiv(lmx.x, dmx), fdiv(lmx.y, dmx), fdiv(lmx.z, dmx));
+  lmy = mk3(fdiv(lmy.x, dmy), fdiv(lmy.y, dmy), fdiv(lmy.z, dmy));
+  f3 zero = mk3(0, 0, 0);
+  f3 wp = v3(G.world_pos);
+  f4 q = v4(G.world_rot_quat);
+  f3 gmx = back_rot_quat(sub3(add3(back_rot_cs(lmx, zero, v.crot_c, v.crot_s), v.cpos), wp), q);
+  f3 gmy = back_rot_quat(sub3(add3(back_rot_cs(lmy, zero, v.crot_c, v.crot_s), v.cpos), wp), q);
+  float lx1, lx2, lx3, ly1, ly2, ly3;
+  barycentric(gmx, p1, p2, p3, &lx1, &lx2, &lx3);
+  barycentric(gmy, p1, p2, p3, &ly1, &ly2, &ly3);
+  f2 vtx = mk2(fma_(vt1.x, lx1, fma_(vt2.x, lx2, vt3.x * lx3)),
+               fma_(vt1.y, lx1, fma_(vt2.y, lx2, vt3.y * lx3)));
+  f2 vty = mk2(fma_(vt1.x, ly1, fma_(vt2.x, ly2, vt3.x * ly3)),
+               fma_(vt1.y, ly1, fma_(vt2.y, ly2, vt3.y * ly3)));
+  f2 vdx = mk2(fabsf(vtx.x - vt.x), fabsf(vtx.y - vt.y));
+  f2 vdy = mk2(fabsf(vty.x - vt.x), fabsf(vty.y - vt.y));
+  const float mip_bias = 1.0f / kMipBias;
+  return mk2((vdx.x + vdy.x) * mip_bias, (vdx.y + vdy.y) * mip_bias);
+}
+
+float depth_to_dist(uint32_t d) { return fdiv((float)d, kMulInt) * kDepthFar; }
+
+float generate_ssao(int x, int y, const uint32_t* depth, const ShadeView& v) {
+  uint32_t seed1 = wang_hash((uint32_t)x + (uint32_t)v.W * (uint32_t)v.H * (uint32_t)y);
+  uint32_t seed2 = rand_xorshift(seed1);
+  float foffset = fdiv((float)seed2, kMulInt);
+  float dep = depth_to_dist(depth[(size_t)y * v.W + x]);
+  float rad = kSsaoRad;
+  rad += fdiv(foffset, 2.0f);
+  float world_rad = fdiv(rad * v.fov, dep);
+  const int samples = 2;
+  float acc = 0.0f;
+  for (int yy = -samples; yy <= samples; yy++) {
+    for (int xx = -samples; xx <= samples; xx++) {
+      float ox = roundf((float)xx * world_rad), oy = roundf((float)yy * world_rad);
+      float wx = (float)x + ox, wy = (float)y + oy;
+      wx = clampf_(wx, 1.0f, (float)v.W - 2.0f);
+      wy = clampf_(wy, 1.0f, (float)v.H - 2.0f);
+      float d2 = depth_to_dist(depth[(size_t)((int)wy * v.W + (int)wx)]);
+      for (float z = -samples; z <= samples; z += 1.0f)
+        if (d2 > dep + z) acc += 1.0f;
+    }
+  }
+  acc = fdiv(acc, 125.0f);
+  return 1.0f - fdiv(1.0f - acc, kSsaoDiv);
+}
+
+float bilinear_interpolate(float cx, float cy, const float val[4]) {
+  float mx = cx - 0.5f, my = cy - 0.5f;
+  float ux = mx - floorf(mx), uy = my - floorf(my);
+  float bx = 1.0f - ux, by = 1.0f - uy;
+  return (val[0] * bx + val[1] * ux) * by + (val[2] * bx + val[3] * ux) * uy;
+}
+
+float hard_occlusion(f3 lpos, f3 normal, f3 ptl, const uint32_t* buf, int face, f3 gpos,
+                     int shnum, const ShadeView& v) {
+  ptl = fast_normalize3(ptl);
+  f3 local = rot_cs(gpos, lpos, v.face_c[face], v.face_s[face]);
+  f3 post = depth_project1(local, (float)kLightBufferDim, (float)kLightBufferDim, kLFov);
+  float dpth = post.z;
+  const uint32_t* map = buf + (size_t)(face + shnum * 6) * kLightBufferDim * kLightBufferDim;
+  float px = clampf_(post.x, 3.0f, kLightBufferDim - 4.0f);
+  float py = clampf_(post.y, 3.0f, kLightBufferDim - 4.0f);
+  int ix = f2i_sat(px), iy = f2i_sat(py);
+  float acos_res = rational_acos(clampf_(dot3(normal, ptl), 0.05f, 0.95f));
+  float bias = kShadowBias * gbr_tanf(acos_res);
+  bias = clampf_(bias, 0.1f * kShadowBias, kShadowBias);
+  float cond[16];
+  for (int yy = -1; yy <= 2; yy++)
+    for (int xx = -1; xx <= 2; xx++) {
+      float ldp = depth_to_dist(map[(iy + yy) * kLightBufferDim + ix + xx]);
+      cond[(yy + 1) * 4 + xx + 1] = dpth > ldp + bias ? 1.0f : 0.0f;
+    }
+  float shadow = 0.0f;
+  for (int yy = -1; yy <= 1; yy++)
+    for (int xx = -1; xx <= 1; xx++) {
+      float val[4] = {cond[(yy + 1) * 4 + xx + 1], cond[(yy + 1) * 4 + xx + 2],
+                      cond[(yy + 2) * 4 + xx + 1], cond[(yy + 2) * 4 + xx + 2]};
+      shadow += bilinear_interpolate((px + 0.5f) + (float)xx, (py + 0.5f) + (float)yy, val);
+    }
+  return fdiv(shadow, 9.0f);
+}
+
+struct ShadeIn {
+  const gbr_triangle* tris;
+  const gbr_obj_g_descriptor* descs;
+  const gbr_light* lights;
+  uint32_t nlights;
+  Atlas atlas;
+  const uint32_t* shadow_dyn;
+  const uint32_t* shadow_static;
+};
+
+f4 vertex_col(uint32_t c) {
+  f4 r;
+  r.x = fdiv((float)(c >> 24), 255.f);
+  r.y = fdiv((float)((c >> 16) & 0xFF), 255.f);
+  r.z = fdiv((float)((c >> 8) & 0xFF), 255.f);
+  r.w = fdiv((float)(c & 0xFF), 255.f);
+  return r;
+}
+
+void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Setup& S,
+                   const uint32_t* depth, const uint32_t* ids, uint8_t* rgba, uint16_t* normals) {
+  size_t p = (size_t)y * v.W + x;
+  uint32_t d = depth[p];
+  uint32_t key = ids[p];
+  auto put = [&](float r, float g, float b, float a) {
+    rgba[p * 4 + 0] = (uint8_t)quant8(r);
+    rgba[p * 4 + 1] = (uint8_t)quant8(g);
+    rgba[p * 4 + 2] = (uint8_t)quant8(b);
+    rgba[p * 4 + 3] = (uint8_t)quant8(a);
+  };
+  if (d == kDepthClear || key == kNoId) {
+    put(v.clear.x, v.clear.y, v.clear.z, v.clear.w);
+    if (normals) { normals[p * 2] = 0; normals[p * 2 + 1] = 0; }
+    return;
+  }
+  uint32_t tri = key >> 1;
+  const Cut& ct = S.cut[key];
+  float rconst = S.rconst[key];
+  const gbr_triangle& T = in.tris[tri];
+  uint32_t o_id = T.vertices[0].object_id;
+  const gbr_obj_g_descriptor& G = in.descs[o_id];
+  f3 p1 = mul3s(v3(T.vertices[0].pos), G.scale);
+  f3 p2 = mul3s(v3(T.vertices[1].pos), G.scale);
+  f3 p3 = mul3s(v3(T.vertices[2].pos), G.scale);
+  f2 vt1 = mk2(T.vertices[0].vt[0], T.vertices[0].vt[1]);
+  f2 vt2 = mk2(T.vertices[1].vt[0], T.vertices[1].vt[1]);
+  f2 vt3 = mk2(T.vertices[2].vt[0], T.vertices[2].vt[1]);
+  f3 n1 = v3(T.vertices[0].normal), n2 = v3(T.vertices[1].normal), n3 = v3(T.vertices[2].normal);
+  float ldepth = depth_to_dist(d);
+  f3 local = mk3(fdiv(((float)x - (float)v.W / 2.0f) * ldepth, v.fov),
+                 fdiv(((float)y - (float)v.H / 2.0f) * ldepth, v.fov), ldepth);
+  f3 zero = mk3(0, 0, 0);
+  f3 gpos = add3(back_rot_cs(local, zero, v.crot_c, v.crot_s), v.cpos);
+  f4 q = v4(G.world_rot_quat);
+  f3 olocal = back_rot_quat(sub3(gpos, v3(G.world_pos)), q);
+  float l1, l2, l3;
+  barycentric(olocal, p1, p2, p3, &l1, &l2, &l3);
+  f2 vt = mk2(fma_(vt1.x, l1, fma_(vt2.x, l2, vt3.x * l3)),
+              fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
+  f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
+                  fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
+  normal = rot_quat(normal, q);
+  f4 col;
+  bool has_col = T.vertices[0].vertex_col != 0;
+  if (has_col) {
+    f4 c0 = vertex_col(T.vertices[0].vertex_col), c1 = vertex_col(T.vertices[1].vertex_col),
+       c2 = vertex_col(T.vertices[2].vertex_col);
+    col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
+    col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
+    col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
+    col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
+  } else {
+    f2 vtdiff = get_vtdiff(ct.p, (float)x, (float)y, v, G, vt, p1, p2, p3, vt1, vt2, vt3, rconst);
+    col = texture_filter_diff(vt, vtdiff, (int)G.tid, in.atlas);
+  }
+  if (v.use_linear) {
+    col.x = gamma_fwd(col.x);
+    col.y = gamma_fwd(col.y);
+    col.z = gamma_fwd(col.z);
+  }
+  uint32_t seed1 = wang_hash((uint32_t)x + (uint32_t)y * (uint32_t)v.W * (uint32_t)v.H);
+  uint32_t seed2 = rand_xorshift(seed1);
+  uint32_t seed3 = rand_xorshift(seed2);
+  uint32_t seed4 = rand_xorshift(seed3);
+  f3 rseed = mk3((fdiv((float)seed2, kMulInt) - 0.5f) * 2.0f, (fdiv((float)seed3, kMulInt) - 0.5f) * 2.0f,
+                 (fdiv((float)seed4, kMulInt) - 0.5f) * 2.0f);
+  f3 l2p = fast_normalize3(sub3(v.cpos, gpos));
+  int ff = G.feature_flag;
+  bool two = (ff & kFlagTwoSided) > 0;
+  bool recv_dyn = !((ff & kFlagNoDynShadows) > 0);
+  int is_front = backface_front(ct.p[0], ct.p[1], ct.p[2]);
+  if (!is_front && two) normal = neg3(normal);
+  float ssao = generate_ssao(x, y, depth, v);
+  normal = fast_normalize3(normal);
+  f3 lnormal = fast_normalize3(add3(normal, mk3(fdiv(rseed.x, 100.f), fdiv(rseed.y, 100.f), fdiv(rseed.z, 100.f))));
+  float ambient = v.use_linear ? gamma_fwd(kAmbient) : kAmbient;
+  f3 diffuse_sum = mk3(0, 0, 0), specular_sum = mk3(0, 0, 0);
+  int shnum = 0, static_num = 0;
+  for (uint32_t i = 0; i < in.nlights; i++) {
+    const gbr_light& L = in.lights[i];
+    f3 lpos = v3(L.pos);
+    f3 ptl = sub3(lpos, gpos);
+    float occlusion = 1.0f;
+    if (L.shadow && L.is_static) {
+      int face = ret_cubeface(gpos, lpos);
+      occlusion = 1.0f - hard_occlusion(lpos, normal, ptl, in.shadow_static, face, gpos, static_num, v);
+      static_num++;
+    }
+    float distance = fast_length3(ptl);
+    float tt = fdiv(distance, L.radius) + 1.0f;
+    float illum = fdiv(L.brightness, tt * tt);
+    const float cutoff = 0.1f;
+    illum -= cutoff;
+    illum *= fdiv(1.0f, 1.0f - cutoff);
+    if (illum <= 0) continue;
+    f3 lcol = v3(L.col);
+    if (v.use_linear) lcol = mk3(gamma_fwd(lcol.x), gamma_fwd(lcol.y), gamma_fwd(lcol.z));
+    if (L.shadow && recv_dyn) {
+      int face = ret_cubeface(gpos, lpos);
+      float dyn = 1.0f - hard_occlusion(lpos, normal, ptl, in.shadow_dyn, face, gpos, shnum, v);
+      occlusion = fmin_(occlusion, dyn);
+      shnum++;
+    }
+    ptl = fast_normalize3(ptl);
+    float light = dot3(ptl, lnormal);
+    light *= occlusion;
+    light = fmax_(light, 0.0f);
+    float diffuse = (1.0f - ambient) * light;
+    float dscale = (((diffuse + ambient) * L.diffuse) * G.diffuse) * illum;
+    diffuse_sum = add3(diffuse_sum, mul3s(lcol, dscale));
+    f3 H = fast_normalize3(add3(l2p, ptl));
+    f3 N = normal;
+    const float kS = 0.4f;
+    float ndh = fmax_(0.0f, dot3(N, H));
+    float ndv = fmax_(0.0f, dot3(N, l2p));
+    float vdh = fmax_(0.0f, dot3(l2p, H));
+    float ndl = fmax_(0.0f, dot3(N, ptl));
+    const float F0 = 0.4f;
+    float fresnel = F0 + (1.0f - F0) * powf(1.0f - vdh, 5.0f);
+    float rough = clampf_(1.0f - G.specular, 0.001f, 10.0f);
+    float alpha = rational_acos(ndh);
+    float microfacet = 0.8346f * expf(fdiv((-alpha) * alpha, rough * rough));
+    float sv = fdiv(2.0f * ndh, vdh);
+    float c1 = sv * ndv, c2 = sv * ndl;
+    float geometric = min3f(1.0f, c1, c2);
+    float spec = fdiv((fresnel * microfacet) * geometric, kPi * ndv);
+    float sscale = (spec * kS) * illum;
+    f3 sp = mul3s(mul3s(lcol, sscale), G.spec_mult);
+    specular_sum = add3(specular_sum, sp);
+    specular_sum = mk3(fmax_(specular_sum.x, 0.0f), fmax_(specular_sum.y, 0.0f), fmax_(specular_sum.z, 0.0f));
+    specular_sum = mul3s(specular_sum, occlusion);
+  }
+  specular_sum = mul3s(specular_sum, ssao);
+  diffuse_sum = mul3s(diffuse_sum, ssao);
+  const float rsc = 0.7f;
+  f3 colclamp = add3(add3(mk3(col.x, col.y, col.z), mk3(0, 0, 0)), mul3s(specular_sum, rsc));
+  f3 sp2 = mul3s(specular_sum, 1.0f - rsc);
+  f3 fin = mk3(fma_(colclamp.x, diffuse_sum.x, sp2.x), fma_(colclamp.y, diffuse_sum.y, sp2.y),
+               fma_(colclamp.z, diffuse_sum.z, sp2.z));
+  if (v.use_linear) fin = mk3(gamma_inv(fin.x), gamma_inv(fin.y), gamma_inv(fin.z));
+  put(fin.x, fin.y, fin.z, col.w);
+  if (normals) {
+    float nx = normal.x, ny = normal.y, nz = normal.z;
+    float len_sq = nx * nx + ny * ny;
+    if (len_sq < 0.0001f) nx = 0.01f;
+    float l = fsqrt(nx * nx + ny * ny);
+    float sq = fsqrt(fmax_(nz * 0.5f + 0.5f, 0.0f));
+    float rx = fdiv(nx, l) * sq, ry = fdiv(ny, l) * sq;
+    float ex = fdiv(rx + 1.0f, 2.0f) * 65536.0f - 1.0f;
+    float ey = fdiv(ry + 1.0f, 2.0f) * 65536.0f - 1.0f;
+    normals[p * 2] = (uint16_t)std::min<uint32_t>(f2u_sat(ex), 65535u);
+    normals[p * 2 + 1] = (uint16_t)std::min<uint32_t>(f2u_sat(ey), 65535u);
+  }
+}
+
+// ---- shadow cubemaps ---------------------------------------------------------
+struct ShadowFrag {
+  uint32_t face, a, ctri;
+  float rconst;
+};
+
+void shadow_light(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descriptor* descs,
+                  f3 lpos, int only_static, uint32_t* out, int nthreads) {
+  f3 fc[6], fs[6];
+  for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &fc[f], &fs[f]);
+  const float L = (float)kLightBufferDim;
+  // per triangle and face: up to 2 clip outputs
+  std::vector<Cut> cut((size_t)n * 12);
+  std::vector<float> nfr((size_t)n * 12, -1.0f);
+  std::vector<float> rcs((size_t)n * 12, 0.0f);
+  parallel_for(n, nthreads, [&](int64_t id) {
+    const gbr_triangle& T = tris[id];
+    const gbr_obj_g_descriptor& G = descs[T.vertices[0].object_id];
+    int ff = G.feature_flag;
+    if (!only_static && (ff & kFlagIsStatic) > 0) return;
+    if (only_static && !((ff & kFlagIsStatic) > 0)) return;
+    f3 wp = v3(G.world_pos);
+    if (fast_length3(sub3(wp, lpos)) > kDepthFar) return;
+    f4 q = v4(G.world_rot_quat);
+    int skip[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+      f3 r = add3(rot_quat(mul3s(v3(T.vertices[k].pos), G.scale), q), wp);
+      skip[ret_cubeface(r, lpos)] = 1;
+    }
+    bool two = (ff & kFlagTwoSided) > 0;
+    for (int f = 0; f < 6; f++) {
+      if (!skip[f]) continue;
+      f3 out2[2][3];
+      int num = project_tri(T, G, lpos, fc[f], fs[f], kLFov, L, L, out2);
+      for (int i = 0; i < num; i++) {
+        size_t s = (size_t)id * 12 + f * 2 + i;
+        cut[s].p[0] = out2[i][0]; cut[s].p[1] = out2[i][1]; cut[s].p[2] = out2[i][2];
+        float rc = 0;
+        int tn = cull_and_count(cut[s].p, two, L, L, kOpSizeLight, &rc);
+        nfr[s] = (float)tn;
+        rcs[s] = rc;
+      }
+    }
+  });
+  std::vector<ShadowFrag> frags;
+  for (size_t s = 0; s < (size_t)n * 12; s++) {
+    float tn = nfr[s];
+    for (uint32_t a = 0; (float)a < tn; a++)
+      frags.push_back(ShadowFrag{(uint32_t)((s % 12) / 2), a, (uint32_t)s, rcs[s]});
+  }
+  std::atomic<uint32_t>* dep = reinterpret_cast<std::atomic<uint32_t>*>(out);
+  parallel_for((int64_t)frags.size(), nthreads, [&](int64_t id) {
+    const ShadowFrag& f = frags[id];
+    const Cut& ct = cut[f.ctri];
+    FragGeom g = frag_geom(ct.p, f.rconst);
+    walk(ct.p, L, L, kOpSizeLight, f.a, false, [&](float x, float y) {
+      if (point_in_tri(x, y, g.xpv.x, g.ypv.x, g.xpv.y, g.ypv.y, g.xpv.z, g.ypv.z)) {
+        uint32_t d = depth_at(g.A, g.B, g.C, x, y);
+        atomic_min_u32(&dep[(size_t)((int)(y * L) + (int)x) + (size_t)f.face * kLightBufferDim * kLightBufferDim], d);
+      }
+    });
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+// engine.cpp:119-133 then the std::to_string / -D FOV_CONST round trip (engine.cpp:474-477).
+float oracle_fov_const(float hfov_deg, int width) {
+  float fov_radians = (float)((double)((hfov_deg / 360.f) * 2) * 3.14159265358979323846);
+  float half = fov_radians / 2;
+  float fc = ((float)width / 2) / tanf(half);
+  char buf[64];
+  snprintf(buf, sizeof buf, "%f", (double)fc);
+  return strtof(buf, nullptr);
+}
+
+// texture_context.cpp:94-261 page packing; update_gpu_tex with flip
+// (cl2.cl:923-953, texture.cpp:323-346); generate_mips + generate_mip_mips
+// (cl2.cl:1070-1189, texture.cpp:430-460).  atlas must hold n_pages*2048^2*4
+// bytes; returns the page count, or -1 on error / -2 if capacities are short.
+int oracle_build_textures(uint32_t n, const int32_t* sizes_in, const uint8_t* const* rgba,
+                          uint8_t* atlas, uint32_t atlas_pages, uint32_t* nums, uint32_t nums_cap,
+                          uint32_t* page_sizes, uint32_t sizes_cap, uint32_t* mipmap_start) {
+  std::map<int, int> size_to_num;
+  for (uint32_t i = 0; i < n; i++) {
+    size_to_num[sizes_in[i]]++;
+    for (int j = 0; j < kMipLevels; j++) size_to_num[sizes_in[i] / (1 << (j + 1))]++;
+  }
+  struct Page { int size, num; };
+  std::vector<Page> pages;
+  for (auto& kv : size_to_num) {
+    if (kv.first <= 0) return -1;
+    int maxp = (kTexPage / kv.first) * (kTexPage / kv.first);
+    int rem = kv.second;
+    while (rem >= maxp) { pages.push_back({kv.first, maxp}); rem -= maxp; }
+    if (rem > 0) pages.push_back({kv.first, rem});
+  }
+  if (pages.size() > sizes_cap || pages.size() > atlas_pages || n * 5 > nums_cap) return -2;
+  std::vector<Page> fp = pages;
+  auto take = [&](int size) -> int64_t {
+    for (size_t s = 0; s < fp.size(); s++)
+      if (fp[s].size == size && fp[s].num > 0) {
+        int fn = fp[s].num - 1;
+        fp[s].num--;
+        return (int64_t)((s << 16) | (uint32_t)fn);
+      }
+    return -1;
+  };
+  std::vector<uint32_t> desc;
+  for (uint32_t i = 0; i < n; i++) {
+    int64_t d = take(sizes_in[i]);
+    if (d < 0) return -1;
+    desc.push_back((uint32_t)d);
+  }
+  for (uint32_t i = 0; i < n; i++)
+    for (int j = 0; j < kMipLevels; j++) {
+      int64_t d = take(sizes_in[i] / (1 << (j + 1)));
+      if (d < 0) return -1;
+      desc.push_back((uint32_t)d);
+    }
+  for (size_t i = 0; i < desc.size(); i++) nums[i] = desc[i];
+  for (size_t i = 0; i < pages.size(); i++) page_sizes[i] = (uint32_t)pages[i].size;
+  *mipmap_start = n;
+  memset(atlas, 0, (size_t)pages.size() * kTexPage * kTexPage * 4);
+
+  // write_tex_array (cl2.cl:856-889) and read_tex_array (cl2.cl:785-821)
+  auto tex_xy = [&](uint32_t tid, float* tx, float* ty, int* slice, float* width) {
+    uint32_t nv = nums[tid];
+    *slice = (int)(nv >> 16);
+    int which = (int)(nv & 0xFFFF);
+    *width = (float)page_sizes[*slice];
+    float hnum = floorf(fdiv(2048.0f, *width));
+    float tnumy = floorf(fdiv((float)which, hnum));
+    float tnumx = fma_(-tnumy, hnum, (float)which);
+    *tx = tnumx;
+    *ty = tnumy;
+  };
+  auto write_tex = [&](const uint32_t c[4], float cx, float cy, uint32_t tid) {
+    float tnx, tny, w; int slice;
+    tex_xy(tid, &tnx, &tny, &slice, &w);
+    float tx = tnx * w, ty = tny * w;
+    cx = fmodf(cx, w); cy = fmodf(cy, w);
+    cx = clampf_(cx, 0.001f, w - 0.001f);
+    cy = clampf_(cy, 0.001f, w - 0.001f);
+    int ix = (int)(tx + cx), iy = (int)(ty + cy);
+    uint8_t* t = atlas + ((size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix) * 4;
+    for (int k = 0; k < 4; k++) t[k] = (uint8_t)c[k];
+  };
+  auto read_tex = [&](float cx, float cy, uint32_t tid, float out[4]) {
+    float tnx, tny, w; int slice;
+    tex_xy(tid, &tnx, &tny, &slice, &w);
+    cx = clampf_(cx, 0.001f, w - 0.001f);
+    cy = clampf_(cy, 0.001f, w - 0.001f);
+    int ix = f2i_sat(fma_(tnx, w, cx)), iy = f2i_sat(fma_(tny, w, cy));
+    const uint8_t* t = atlas + ((size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix) * 4;
+    for (int k = 0; k < 4; k++) out[k] = (float)t[k];
+  };
+  auto mip = [&](uint32_t src, uint32_t dst, int gw, int gh) {
+    float w = (float)page_sizes[nums[src] >> 16];
+    float nw = (float)page_sizes[nums[dst] >> 16];
+    const float gauss[3][3] = {{1, 2, 1}, {2, 4, 2}, {1, 2, 1}};
+    for (int y = 0; y < gh; y++)
+      for (int x = 0; x < gw; x++) {
+        if ((float)x >= w || (float)y >= w) continue;
+        float acc[4] = {0, 0, 0, 0};
+        float div = 0.f;
+        for (int j = -1; j <= 1; j++)
+          for (int i = -1; i <= 1; i++) {
+            float c[4];
+            read_tex((float)(x * 2 + i), (float)(y * 2 + j), src, c);
+            c[3] = fdiv(c[3], 255.f);
+            c[0] *= c[3]; c[1] *= c[3]; c[2] *= c[3];
+            float g = gauss[j + 1][i + 1];
+            for (int k = 0; k < 4; k++) acc[k] += c[k] * g;
+            div += g;
+          }
+        for (int k = 0; k < 4; k++) acc[k] = fdiv(acc[k], div);
+        if (acc[3] > 0.00000001f)
+          for (int k = 0; k < 3; k++) acc[k] = fdiv(acc[k], acc[3]);
+        acc[3] *= 255.f;
+        float yx0 = fdiv((float)(x * 2), w) * nw, yx1 = fdiv((float)(y * 2), w) * nw;
+        if (yx0 >= nw || yx1 >= nw) continue;
+        uint32_t c[4];
+        for (int k = 0; k < 4; k++) c[k] = f2u_sat(acc[k]);
+        write_tex(c, yx0, yx1, dst);
+      }
+  };
+  for (uint32_t t = 0; t < n; t++) {
+    int s = sizes_in[t];
+    float w = (float)page_sizes[nums[t] >> 16];
+    for (int y = 0; y < s; y++)
+      for (int x = 0; x < s; x++) {
+        const uint8_t* px = rgba[t] + ((size_t)y * s + x) * 4;
+        uint32_t c[4] = {px[0], px[1], px[2], px[3]};
+        float fy = (float)y;
+        fy = w - fy;  // flip = 1 (texture.cpp:344)
+        write_tex(c, (float)x, fy, t);
+      }
+    uint32_t m0 = t * kMipLevels + *mipmap_start;
+    mip(t, m0, s, s);
+    for (int l = 0; l < kMipLevels - 1; l++) mip(m0 + l, m0 + l + 1, s, s);
+  }
+  return (int)pages.size();
+}
+
+// Shadow cubemaps of every shadow-casting light (engine.cpp:1601-1790).
+// dyn: 6*1024^2 u32 per light with shadow==1; stat: per light with shadow && is_static.
+void oracle_shadow(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descriptor* descs,
+                   const gbr_light* lights, uint32_t nl, uint32_t* dyn, uint32_t* stat,
+                   int nthreads) {
+  const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
+  uint32_t nn = 0, kk = 0;
+  for (uint32_t i = 0; i < nl; i++) {
+    f3 lpos = v3(lights[i].pos);
+    if (lights[i].shadow == 1) {
+      uint32_t* out = dyn + (size_t)nn * 6 * face;
+      std::fill(out, out + 6 * face, kDepthClear);
+      shadow_light(tris, n, descs, lpos, 0, out, nthreads);
+      nn++;
+    }
+    if (lights[i].shadow && lights[i].is_static && stat) {
+      uint32_t* out = stat + (size_t)kk * 6 * face;
+      std::fill(out, out + 6 * face, kDepthClear);
+      shadow_light(tris, n, descs, lpos, 1, out, nthreads);
+      kk++;
+    }
+  }
+}
+
+// One view: prearrange -> kernel1 -> kernel2 -> kernel3 (render_tris).
+// Any output pointer may be NULL except depth and id.
+int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descriptor* descs,
+                  const gbr_light* lights, uint32_t nl, const uint8_t* atlas,
+                  const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                  const uint32_t* shadow_dyn, const uint32_t* shadow_static,
+                  const gbr_camera* cam, const gbr_view* view, uint32_t* depth, uint32_t* ids,
+                  uint8_t* rgba, uint16_t* normals, int nthreads, uint64_t* nfrags_out) {
+  const int W = view->width, H = view->height;
+  const float fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
+  f3 cpos = v3(cam->pos), crot = v3(cam->rot);
+  Setup S;
+  prearrange(tris, n, descs, cpos, crot, fov, (float)W, (float)H, nthreads, &S);
+  if (nfrags_out) *nfrags_out = S.frags.size();
+  const size_t P = (size_t)W * H;
+  std::fill(depth, depth + P, kDepthClear);
+  std::fill(ids, ids + P, kNoId);
+  kernel1(S, (float)W, (float)H, reinterpret_cast<std::atomic<uint32_t>*>(depth), W, nthreads);
+  kernel2(S, (float)W, (float)H, depth, reinterpret_cast<std::atomic<uint32_t>*>(ids), W, nthreads);
+  if (!rgba) return 0;
+  ShadeView v;
+  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos;
+  euler_cs(crot, &v.crot_c, &v.crot_s);
+  for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &v.face_c[f], &v.face_s[f]);
+  v.use_linear = view->use_linear;
+  v.clear.x = view->clear_col[0]; v.clear.y = view->clear_col[1];
+  v.clear.z = view->clear_col[2]; v.clear.w = view->clear_col[3];
+  ShadeIn in{tris, descs, lights, nl, Atlas{atlas, nums, sizes, mipmap_start}, shadow_dyn, shadow_static};
+  parallel_for((int64_t)P, nthreads, [&](int64_t p) {
+    kernel3_pixel((int)(p % W), (int)(p / W), v, in, S, depth, ids, rgba, normals);
+  });
+  return 0;
+}
+
+// The literal walk of one fragment, for unit tests: writes visited (x,y) pairs.
+int oracle_walk(const float* tp9, float ew, float eh, int chunk, uint32_t distance, int32_t* xy,
+                int cap) {
+  f3 tp[3] = {mk3(tp9[0], tp9[1], tp9[2]), mk3(tp9[3], tp9[4], tp9[5]), mk3(tp9[6], tp9[7], tp9[8])};
+  int n = 0;
+  walk(tp, ew, eh, chunk, distance, false, [&](float x, float y) {
+    if (n < cap) { xy[2 * n] = (int)x; xy[2 * n + 1] = (int)y; }
+    n++;
+  });
+  return n;
+}
+
+}  // extern "C"

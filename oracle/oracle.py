@@ -1,0 +1,134 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of the CPU oracle (gbr_oracle.cpp).
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as a
+checker; the product path never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "gbr_oracle.cpp")
+LIB = os.path.join(HERE, "liboracle.so")
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with the pinned float semantics (no contraction)."""
+    deps = [SRC, os.path.join(HERE, "..", "openclrenderer_gb300", "csrc", "gbr_math.h"),
+            os.path.join(HERE, "..", "include", "gbr.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-pthread", "-o", LIB + ".tmp", SRC]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        L.oracle_fov_const.restype = ctypes.c_float
+        L.oracle_fov_const.argtypes = [ctypes.c_float, ctypes.c_int]
+        L.oracle_build_textures.restype = ctypes.c_int
+        L.oracle_build_textures.argtypes = [ctypes.c_uint32, P, P, P, ctypes.c_uint32, P,
+                                            ctypes.c_uint32, P, ctypes.c_uint32, P]
+        L.oracle_shadow.restype = None
+        L.oracle_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int]
+        L.oracle_render.restype = ctypes.c_int
+        L.oracle_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P,
+                                    ctypes.c_uint32, P, P, P, P, P, P, P, P, ctypes.c_int, P]
+        L.oracle_walk.restype = ctypes.c_int
+        L.oracle_walk.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
+                                  P, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_threads():
+    return os.cpu_count() or 1
+
+
+def fov_const(hfov_deg, width):
+    return lib().oracle_fov_const(hfov_deg, width)
+
+
+class Textures:
+    """Atlas pages, descriptors (nums), page sizes and mipmap_start."""
+
+    def __init__(self, atlas, nums, sizes, mipmap_start):
+        self.atlas, self.nums, self.sizes, self.mipmap_start = atlas, nums, sizes, mipmap_start
+
+
+def build_textures(tex_sizes, tex_pixels):
+    n = len(tex_sizes)
+    sizes_in = np.asarray(tex_sizes, np.int32)
+    pix = [np.ascontiguousarray(p, np.uint8) for p in tex_pixels]
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[p.ctypes.data for p in pix])
+    max_pages = 5 * max(n, 1)
+    atlas = np.zeros((max_pages, 2048, 2048, 4), np.uint8) if n else np.zeros((1, 2048, 2048, 4), np.uint8)
+    nums = np.zeros(5 * max(n, 1), np.uint32)
+    sizes = np.zeros(max_pages, np.uint32)
+    ms = np.zeros(1, np.uint32)
+    npages = lib().oracle_build_textures(n, _p(sizes_in), ctypes.cast(ptrs, ctypes.c_void_p), _p(atlas),
+                                         max_pages, _p(nums), len(nums), _p(sizes), len(sizes), _p(ms))
+    if npages < 0:
+        raise ValueError(f"oracle_build_textures failed ({npages})")
+    return Textures(atlas[:max(npages, 1)].copy(), nums[:5 * n].copy(), sizes[:npages].copy(), int(ms[0]))
+
+
+def shadow(scene, nthreads=None):
+    """Dynamic and static cubemaps, u32 [n, 6, 1024, 1024] each."""
+    nthreads = nthreads or default_threads()
+    nd = int(sum(1 for l in scene.lights if l["shadow"] == 1))
+    ns = int(sum(1 for l in scene.lights if l["shadow"] and l["is_static"]))
+    dyn = np.full((max(nd, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    sta = np.full((max(ns, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    lib().oracle_shadow(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights),
+                        len(scene.lights), _p(dyn), _p(sta), nthreads)
+    return dyn, sta
+
+
+def render(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, shade=True,
+           nthreads=None, normals=False):
+    """Returns dict(depth, id, rgba[, normals], fragments)."""
+    nthreads = nthreads or default_threads()
+    W, H = int(view["width"]), int(view["height"])
+    depth = np.empty((H, W), np.uint32)
+    ids = np.empty((H, W), np.uint32)
+    rgba = np.empty((H, W, 4), np.uint8) if shade else None
+    nrm = np.empty((H, W, 2), np.uint16) if (shade and normals) else None
+    if shadow_dyn is None or shadow_static is None:
+        d, s = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32), np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+        shadow_dyn = d if shadow_dyn is None else shadow_dyn
+        shadow_static = s if shadow_static is None else shadow_static
+    cam = np.asarray(cam).reshape(1)
+    view = np.asarray(view).reshape(1)
+    nf = np.zeros(1, np.uint64)
+    lib().oracle_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights),
+                        len(scene.lights), _p(tex.atlas), _p(tex.nums), _p(tex.sizes),
+                        tex.mipmap_start, _p(shadow_dyn), _p(shadow_static), _p(cam), _p(view),
+                        _p(depth), _p(ids), _p(rgba), _p(nrm), nthreads, _p(nf))
+    out = {"depth": depth, "id": ids, "fragments": int(nf[0])}
+    if shade:
+        out["rgba"] = rgba
+    if nrm is not None:
+        out["normals"] = nrm
+    return out
+
+
+def walk(tp9, ew, eh, chunk, distance, cap=2048):
+    xy = np.zeros((cap, 2), np.int32)
+    tp = np.asarray(tp9, np.float32)
+    n = lib().oracle_walk(_p(tp), ew, eh, chunk, distance, _p(xy), cap)
+    return xy[:min(n, cap)]

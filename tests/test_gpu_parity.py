@@ -1,0 +1,207 @@
+"""GPU parity: the CUDA pipeline (through the C ABI) against the CPU oracle.
+
+Depth and canonical id must be bit-exact; RGBA8 within 1/255 per channel;
+texture atlas and shadow cubemaps bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from openclrenderer_gb300 import scenes  # noqa: E402
+from openclrenderer_gb300 import structs as S  # noqa: E402
+from openclrenderer_gb300.pipeline import GpuScene  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.scene_util import random_soup, screen_tri, tri_scene  # noqa: E402
+
+RGBA_TOL = 1  # levels of 1/255
+
+
+def run_both(sc, shadows=True, normals=False, cam=None, view=None):
+    cam = sc.cameras[0] if cam is None else cam
+    view = sc.views[0] if view is None else view
+    gs = GpuScene(sc)
+    if shadows:
+        gs.shadow_pass()
+    got = gs.render(cam, view, normals=normals).numpy()
+    torch.cuda.synchronize()
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    dyn = sta = None
+    if shadows:
+        dyn, sta = O.shadow(sc)
+    ref = O.render(sc, tex, cam, view, dyn, sta, normals=normals)
+    return gs, got, ref
+
+
+def assert_parity(got, ref, where=""):
+    d_bad = np.count_nonzero(got["depth"] != ref["depth"])
+    i_bad = np.count_nonzero(got["id"] != ref["id"])
+    diff = np.abs(got["rgba"].astype(np.int16) - ref["rgba"].astype(np.int16))
+    assert d_bad == 0, f"{where}: {d_bad} depth mismatches"
+    assert i_bad == 0, f"{where}: {i_bad} id mismatches"
+    assert diff.max() <= RGBA_TOL, f"{where}: rgba max diff {diff.max()} ({np.count_nonzero(diff > RGBA_TOL)} px)"
+
+
+def test_cubes_800x600_parity():
+    sc = scenes.plain_cubes()
+    gs, got, ref = run_both(sc, shadows=False)
+    assert (ref["depth"] != 0xFFFFFFFF).sum() > 10000
+    assert_parity(got, ref, "plain_cubes")
+    st = gs.stats()
+    assert st["fragments_ref"] == ref["fragments"]
+
+
+def test_texture_atlas_bit_exact():
+    sc = scenes.terrain(nx=64, nz=32, width=320, height=180, n_lights=2, n_textures=5, tex_size=64)
+    sc.tex_sizes = [64, 128, 32, 256, 64]
+    sc.tex_pixels = [np.random.default_rng(40 + i).integers(0, 256, (s, s, 4), dtype=np.uint8)
+                     for i, s in enumerate(sc.tex_sizes)]
+    gs = GpuScene(sc)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    nums, sizes, ms = gs.texture_layout()
+    assert np.array_equal(nums, tex.nums) and np.array_equal(sizes, tex.sizes) and ms == tex.mipmap_start
+    atlas = gs.atlas()
+    assert atlas.shape == tex.atlas.shape
+    assert np.array_equal(atlas, tex.atlas)
+
+
+def test_terrain_small_with_shadows():
+    sc = scenes.terrain(nx=128, nz=64, width=640, height=360, n_lights=4, n_textures=4, tex_size=128)
+    gs, got, ref = run_both(sc, shadows=True, normals=True)
+    dyn, _ = O.shadow(sc)
+    cube = gs.cubemaps()
+    assert np.array_equal(cube[:len(dyn)], dyn), f"{np.count_nonzero(cube[:len(dyn)] != dyn)} cubemap mismatches"
+    assert_parity(got, ref, "terrain_small")
+    nd = np.abs(got["normals"].astype(np.int32) - ref["normals"].astype(np.int32))
+    assert nd.max() <= 2
+
+
+def test_terrain_1080p_full_parity():
+    """The headline scene: 1,048,576 triangles, 16 lights, shadow cubemap."""
+    sc = scenes.terrain()
+    gs, got, ref = run_both(sc, shadows=True)
+    dyn, _ = O.shadow(sc)
+    assert np.array_equal(gs.cubemaps()[:1], dyn[:1])
+    assert (ref["depth"] != 0xFFFFFFFF).mean() > 0.9
+    assert_parity(got, ref, "terrain_1080p")
+
+
+def test_random_soup_parity():
+    for seed, (w, h) in zip((1, 2, 3), ((640, 480), (333, 197), (1024, 768))):
+        sc = random_soup(400, w, h, seed)
+        _, got, ref = run_both(sc, shadows=False)
+        assert_parity(got, ref, f"soup{seed}")
+
+
+def test_single_sided_culling_parity():
+    sc = random_soup(600, 512, 384, 9, two_sided=False)
+    _, got, ref = run_both(sc, shadows=False)
+    assert_parity(got, ref, "single_sided")
+
+
+def test_edge_cases_parity():
+    W, H = 256, 192
+    tl = [
+        screen_tri([10, 200, 30], [10, 20, 180], [100, 100, 100], W, H),           # plain
+        [(-30, -10, 10.0), (40, 0, 60.0), (0, 30, 80.0)],                         # 1 vertex behind near plane
+        [(-30, -10, 5.0), (40, 0, 10.0), (0, 30, 80.0)],                          # 2 vertices behind
+        [(-3000, -1000, 300000.0), (4000, 0, 360000.0), (0, 3000, 200000.0)],     # crosses far plane
+        screen_tri([-500, -400, -450], [10, 20, 30], [50, 50, 50], W, H),         # off-screen left
+        screen_tri([20, 20, 20], [20, 80, 140], [70, 70, 70], W, H),              # zero area (x collapses)
+        screen_tri([0.2, 0.4, 0.3], [100, 101, 100.6], [30, 30, 30], W, H),       # left-edge clamp
+        screen_tri([-200, 2 * W, -200], [-200, H // 2, 2 * H], [400, 400, 400], W, H),  # covers the screen
+        screen_tri([50, 52, 51], [60, 60, 61], [90, 90.5, 91], W, H),             # tiny
+        screen_tri([5, 250, 128], [5, 5, 190], [20.5, 20.5, 20.5], W, H),         # just past the near plane
+        [(-1e7, 5, 1000.0), (1e7, 10, 1000.0), (0, 2e6, 1000.0)],                 # huge coordinates
+    ]
+    sc = tri_scene(tl, W, H, descs=np.stack([S.make_descriptor(tid=0, feature_flag=S.FLAG_TWO_SIDED)]))
+    _, got, ref = run_both(sc, shadows=False)
+    assert_parity(got, ref, "edge_cases")
+
+
+def test_vertex_colours_and_objects():
+    W, H = 200, 150
+    tl = [(screen_tri([10, 150, 20], [10, 30, 140], [80, 90, 100], W, H), 0),
+          (screen_tri([60, 190, 100], [20, 60, 145], [70, 120, 95], W, H), 1)]
+    cols = [[0xFF0000FF, 0x00FF00FF, 0x0000FFFF], [0, 0, 0]]
+    descs = np.stack([S.make_descriptor(tid=0, feature_flag=S.FLAG_TWO_SIDED),
+                      S.make_descriptor(world_pos=(5, -3, 2), quat=(0.1, 0.2, 0.05, 0.97), scale=1.1, tid=0,
+                                        feature_flag=S.FLAG_TWO_SIDED, specular=0.5)])
+    sc = tri_scene(tl, W, H, descs=descs, vertex_cols=cols)
+    _, got, ref = run_both(sc, shadows=False)
+    assert_parity(got, ref, "vertex_colours")
+
+
+def test_empty_scene_and_far_object():
+    W, H = 64, 48
+    sc = tri_scene([screen_tri([10, 50, 20], [10, 10, 40], [100, 100, 100], W, H)], W, H,
+                   descs=np.stack([S.make_descriptor(world_pos=(0, 0, 400000.0), tid=0)]))
+    _, got, ref = run_both(sc, shadows=False)
+    assert np.all(got["depth"] == 0xFFFFFFFF) and np.all(got["id"] == 0xFFFFFFFF)
+    assert_parity(got, ref, "far_object")
+
+
+def test_rotated_cameras_parity():
+    sc = scenes.plain_cubes()
+    rng = np.random.default_rng(5)
+    for i in range(3):
+        cam = S.make_camera(rng.uniform(-100, 100, 3), (rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5),
+                                                        rng.uniform(-0.3, 0.3)))
+        view = S.make_view(480, 320, hfov_deg=float(rng.uniform(60, 120)), use_linear=i % 2)
+        _, got, ref = run_both(sc, shadows=False, cam=cam, view=view)
+        assert_parity(got, ref, f"cam{i}")
+
+
+def test_deterministic_repeat():
+    sc = scenes.terrain(nx=128, nz=64, width=480, height=270, n_lights=2, n_textures=2, tex_size=64)
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    a = gs.render(sc.cameras[0], sc.views[0]).numpy()
+    b = gs.render(sc.cameras[0], sc.views[0]).numpy()
+    for k in ("depth", "id", "rgba"):
+        assert np.array_equal(a[k], b[k])
+
+
+def test_render_host_matches_device():
+    sc = scenes.plain_cubes()
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    dev = gs.render(sc.cameras[0], sc.views[0]).numpy()
+    host = gs.render_host(sc.cameras[0], sc.views[0])
+    for k in ("depth", "id", "rgba"):
+        assert np.array_equal(dev[k], host[k])
+
+
+def test_batch_equals_single():
+    """Every view is identical alone and inside a batch of uneven resolutions."""
+    sc = scenes.spheres_batch(n_spheres=60, n_views=6)
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    outs = gs.render_batch(sc.cameras, sc.views)
+    torch.cuda.synchronize()
+    for cam, view, o in zip(sc.cameras, sc.views, outs):
+        single = gs.render(cam, view).numpy()
+        b = o.numpy()
+        for k in ("depth", "id", "rgba"):
+            assert np.array_equal(single[k], b[k]), k
+
+
+def test_invalid_arguments_rejected():
+    from openclrenderer_gb300._native import GbrError
+    sc = scenes.plain_cubes()
+    gs = GpuScene(sc)
+    with pytest.raises(GbrError):
+        gs.render(sc.cameras[0], S.make_view(5000, 100))
+    bad = sc.tris.copy()
+    bad[0]["vertices"][0]["object_id"] = 1000
+    gs.set_triangles(bad)
+    with pytest.raises(GbrError):
+        gs.render(sc.cameras[0], sc.views[0])
+    lights = sc.lights.copy()
+    lights[0]["shadow"] = 3
+    with pytest.raises(GbrError):
+        gs.set_lights(lights)
