@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 triangle pipeline: shaded Mpix/s.
+
+Workload (default): the 1920x1080 heightmap terrain of 1,048,576 triangles,
+16 point lights (light 0 with a 6x1024^2 shadow cubemap), 16 RGBA8 512^2
+textures.  One step = one frame of the reference's frame loop:
+generate_realtime_shadowing + render_tris (prearrange, kernel1, kernel2,
+kernel3), i.e. gbr_shadow_pass + gbr_render_view.
+
+  value  Mpix/s, device-timed (CUDA events on the launching stream), scene resident
+  e2e    Mpix/s through gbr_render_view_host: camera/view in from host memory,
+         depth + id + RGBA8 copied back to pinned host buffers every step
+
+--impl reference times the reference's CPU implementation of the same frame on
+the host cores (the oracle restatement of cl2.cl, all threads).
+Multi-GPU (torchrun): every rank renders its own frames (replicas); value is
+the whole job's pixels / max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from openclrenderer_gb300 import scenes  # noqa: E402
+from openclrenderer_gb300 import structs as S  # noqa: E402
+
+METRIC = "shaded Mpix/s @1080p 1M tris, batched/served vs plain on GB300; p50/p99 latency"
+WORKLOAD = "terrain_1080p_1M"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbr", choices=["gbr", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-views", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def scene_config(sc):
+    v = sc.views[0]
+    return {"workload": WORKLOAD, "width": int(v["width"]), "height": int(v["height"]),
+            "triangles": int(len(sc.tris)), "lights": int(len(sc.lights)),
+            "shadow_cubemaps": int(sum(1 for l in sc.lights if l["shadow"] == 1)),
+            "textures": f"{len(sc.tex_sizes)}x{sc.tex_sizes[0]}^2 RGBA8",
+            "l2": "inputs larger than L2 (151 MB of triangles + 80 MB atlas + 25 MB cubemap per step)",
+            "parallelism": "replicas"}
+
+
+# ---- clocks ----------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---- roofline ------------------------------------------------------------------
+def algorithmic_bytes(stage, T, T_vis, P, P_cov, n_cubes):
+    """Compulsory DRAM bytes of one launch of a stage (intermediates such as
+    records, bins and the per-pixel record map excluded):
+      shadow_setup / view_setup: 40 B per scene triangle (3 positions + object id)
+      shadow_raster: 6*1024^2*4 B per cubemap written
+      view_raster: depth + id written, 8 B per pixel
+      view_shade: depth + record map read and RGBA8 written (12 B/px), 96 B of
+                  vertex data (positions, normals, uv) per visible triangle,
+                  16 B of texels per covered pixel
+    """
+    if stage in ("shadow_setup", "view_setup"):
+        return 40 * T
+    if stage == "shadow_raster":
+        return 6 * 1024 * 1024 * 4 * n_cubes
+    if stage == "view_raster":
+        return 8 * P
+    if stage == "view_shade":
+        return 12 * P + 96 * T_vis + 16 * P_cov
+    return None
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(stage):
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch of `stage` from
+    the committed ncu summary, when one exists for this workload."""
+    p = os.path.join(ROOT, "profiles", "traffic_terrain_1080p.json")
+    if os.path.exists(p):
+        return json.load(open(p)).get(stage)
+    return None
+
+
+# ---- CPU (oracle) ----------------------------------------------------------------
+def cpu_frames(sc, seconds, max_frames, threads):
+    from oracle import oracle as O
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    cam, view = sc.cameras[0], sc.views[0]
+    P = int(view["width"]) * int(view["height"])
+    times = []
+    t_end = time.perf_counter() + seconds
+    while len(times) < max_frames and (not times or time.perf_counter() < t_end):
+        t0 = time.perf_counter()
+        dyn, sta = O.shadow(sc, nthreads=threads)
+        O.render(sc, tex, cam, view, dyn, sta, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    return P, times
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    sc = scenes.terrain()
+    threads = os.cpu_count() or 1
+    P, times = cpu_frames(sc, 1e9, args.warmup + args.steps, threads)
+    t = times[args.warmup:] or times
+    mpix = P * len(t) / sum(t) / 1e6
+    line = {"metric": METRIC, "value": round(mpix, 4), "unit": "Mpix/s", "n_gpus": args.gpus,
+            "steps": len(t), "warmup": args.warmup, "ms_per_step": round(1e3 * sum(t) / len(t), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded terrain generator)", "impl": "reference",
+            "config": scene_config(sc),
+            "cpu_baseline": {"value": round(mpix, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                             "sample": f"{len(t)} full frames (shadow cubemap + prearrange + kernel1 + kernel2 + "
+                                       f"kernel3) of the 1080p terrain, {threads} threads, cl2.cl restated in C++"},
+            "e2e": {"value": round(mpix, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU ------------------------------------------------------------------------
+def main():
+    args = parse()
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    import torch
+    import torch.distributed as dist
+    from openclrenderer_gb300.pipeline import GpuScene
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    sc = scenes.terrain()
+    cam, view = sc.cameras[0], sc.views[0]
+    W, H = int(view["width"]), int(view["height"])
+    P = W * H
+    gs = GpuScene(sc)
+    out = None
+    stream = torch.cuda.current_stream()
+
+    def step():
+        gs.shadow_pass(stream)
+        return gs.render(cam, view, out=out, stream=stream)
+
+    out = step()
+    for _ in range(max(args.warmup, 3) - 1):
+        step()
+    torch.cuda.synchronize()
+    depth = out.depth.cpu().numpy().view(np.uint32)
+    P_cov = int(np.count_nonzero(depth != 0xFFFFFFFF))
+    launches0 = gs.stats()["launches"]
+    gs.profile(True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    st = gs.stats()
+    gs.profile(False)
+    launches = st["launches"] - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * P / (ms * 1e-3) / 1e6
+
+    # per-stage device time and the roofline of the dominant kernel
+    per_call = {k: st["stage_ms"][k] / max(st["stage_calls"][k], 1) for k in S.STAGES}
+    dom = max(per_call, key=per_call.get)
+    T = len(sc.tris)
+    T_vis = st["view_records"]
+    n_cubes = int(sum(1 for l in sc.lights if l["shadow"] == 1))
+    peak, peak_kind = load_peaks()
+    alg = algorithmic_bytes(dom, T, T_vis, P, P_cov, n_cubes)
+    achieved = alg / (per_call[dom] * 1e-3) / 1e9 if alg else None
+    roof = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 2) if achieved else None,
+            "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": round(achieved / peak, 5) if achieved else None,
+            "algorithmic_bytes_per_launch": alg, "launch_ms": round(per_call[dom], 4),
+            "traffic": load_traffic(dom)}
+
+    # end to end through the host-buffer C ABI call
+    pin = torch.empty(P * 12, dtype=torch.uint8, pin_memory=True).numpy()
+    hd, hi, hr = pin[:4 * P].view(np.uint32), pin[4 * P:8 * P].view(np.uint32), pin[8 * P:]
+    for _ in range(2):
+        gs.shadow_pass(stream)
+        gs.render_host(cam, view, hd, hi, hr, stream=stream)
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s0 = time.perf_counter()
+        gs.shadow_pass(stream)
+        gs.render_host(cam, view, hd, hi, hr, stream=stream)
+        lat.append(time.perf_counter() - s0)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": round(world * P * args.steps / e2e_s / 1e6, 3), "unit": "Mpix/s",
+           "h2d_bytes_per_step": S.CAMERA.itemsize + S.VIEW.itemsize, "d2h_bytes_per_step": 12 * P,
+           "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+           "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3)}
+
+    # batched form: many views of the same scene per launch
+    batched = None
+    if not args.no_batch:
+        rng = np.random.default_rng(17)
+        cams = [S.make_camera((rng.uniform(-400, 400), rng.uniform(-60, 60), rng.uniform(-100, 200)),
+                              (scenes.TERRAIN_CAMERA_PITCH + rng.uniform(-0.1, 0.1), rng.uniform(-0.4, 0.4), 0))
+                for _ in range(args.batch_views)]
+        views = [view] * args.batch_views
+        outs = gs.render_batch(cams, views, stream=stream)
+        for _ in range(2):
+            gs.shadow_pass(stream)
+            gs.render_batch(cams, views, outs=outs, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nb = max(3, args.steps // 4)
+        e0.record(stream)
+        for _ in range(nb):
+            gs.shadow_pass(stream)
+            gs.render_batch(cams, views, outs=outs, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1) / nb
+        batched = {"views_per_launch": args.batch_views, "ms_per_batch": round(bms, 3),
+                   "value": round(world * P * args.batch_views / (bms * 1e-3) / 1e6, 2), "unit": "Mpix/s",
+                   "vs_plain": round((P * args.batch_views / bms) / (P / ms), 3)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        Pc, times = cpu_frames(sc, args.cpu_seconds, 8, threads)
+        t = times[1:] if len(times) > 1 else times
+        cpu = {"value": round(Pc * len(t) / sum(t) / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+               "sample": f"{len(t)} full frames of the 1080p terrain after 1 warm-up (shadow cubemap + prearrange + "
+                         f"kernel1 + kernel2 + kernel3), {threads} threads, cl2.cl restated in C++"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world,
+                "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded value-noise terrain, random textures)",
+                "config": scene_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": int(launches), "clocks": clk,
+                "stages_ms": {k: round(v, 4) for k, v in per_call.items()},
+                "batched": batched, "impl": "gbr",
+                "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],
+                           "view_bin_entries": st["view_bin_entries"], "shadow_records": st["shadow_records"]}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

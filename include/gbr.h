@@ -119,6 +119,13 @@ typedef struct gbr_stats {
   uint64_t shadow_bin_entries;
   uint64_t fragments_ref;   /* sum of ceil(bboxArea/500): the reference's kernel1 work items */
   uint64_t retries;         /* workspace grow-and-retry events */
+  uint64_t launches;        /* kernels launched by this scene since creation */
+  /* Per-stage device time (ms) and launch count accumulated while profiling is
+   * on (gbr_scene_profile), from CUDA events recorded on the launching stream.
+   * Stages: 0 shadow setup, 1 shadow scan, 2 shadow fill, 3 shadow raster,
+   * 4 view setup, 5 view scan, 6 view fill, 7 view raster, 8 view shade. */
+  double stage_ms[10];
+  uint64_t stage_calls[10];
 } gbr_stats;
 
 typedef struct gbr_scene gbr_scene;
@@ -199,6 +206,11 @@ gbr_status gbr_render_batch(gbr_scene* scene, uint32_t n, const gbr_camera* cams
 
 /* Counters of the last render / shadow pass on this scene. */
 gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
+
+/* Turn per-stage CUDA-event timing on (1) or off (0); turning it on clears
+ * the accumulated stage times (tracing; replaces the reference's PROFILING
+ * build, engine.hpp:625-640). */
+gbr_status gbr_scene_profile(gbr_scene* scene, int32_t enable);
 
 #ifdef __cplusplus
 }

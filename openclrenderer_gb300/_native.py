@@ -92,6 +92,7 @@ SIGNATURES = {
     "gbr_render_view_host": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "gbr_render_batch": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P]),
     "gbr_scene_stats": (ctypes.c_int, [_P, _P]),
+    "gbr_scene_profile": (ctypes.c_int, [_P, ctypes.c_int32]),
 }
 
 _lib = None

@@ -160,6 +160,8 @@ struct gbr_scene {
   HostBuf staging;     // surfaces / views / jobs / counters
   gbr_stats stats{};
   float face_cos[6][3], face_sin[6][3];
+  bool profile = false;
+  cudaEvent_t ev[20] = {};
 
   SceneDev dev() const {
     SceneDev d{};
@@ -263,17 +265,37 @@ gbr_status run_pass(gbr_scene* s, bool view, uint32_t nitems, uint32_t nsurf, ui
     CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
     CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(nfine, 1), st));
     CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(ncoarse, 1), st));
+    const int sb = view ? 4 : 0;  // first stage index of this pass
+    const int nst = view ? 5 : 4;
+    auto mark = [&](int k) -> cudaError_t { return s->profile ? cudaEventRecord(s->ev[k], st) : cudaSuccess; };
+    CU(mark(0));
     if (view)
       CU(launch_setup_views(sd, s->ws.views.p, nitems, s->ws.surf.p, ws, st));
     else
       CU(launch_setup_shadow(sd, s->ws.jobs.p, nitems, s->ws.surf.p, ws, st));
+    CU(mark(1));
     CU(launch_scan(ws, st));
+    CU(mark(2));
     CU(launch_fill(ws, s->ws.surf.p, st));
+    CU(mark(3));
     CU(launch_raster(ws, s->ws.surf.p, nsurf, nfine, view, st));
-    if (view) CU(launch_shade(sd, s->ws.views.p, nitems, s->ws.surf.p, nfine, ws.srec, st));
+    CU(mark(4));
+    if (view) {
+      CU(launch_shade(sd, s->ws.views.p, nitems, s->ws.surf.p, nfine, ws.srec, st));
+      CU(mark(5));
+    }
+    s->stats.launches += (uint64_t)nst;
     Counters* hc = reinterpret_cast<Counters*>(s->staging.p);
     CU(cudaMemcpyAsync(hc, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
+    if (s->profile) {
+      for (int k = 0; k < nst; k++) {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, s->ev[k], s->ev[k + 1]));
+        s->stats.stage_ms[sb + k] += ms;
+        s->stats.stage_calls[sb + k] += 1;
+      }
+    }
     Counters c = *hc;
     if (!c.overflow) {
       if (view) {
@@ -378,6 +400,8 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->nums.release(); s->sizes.release(); s->shadow_dyn.release(); s->shadow_static.release();
   s->ws.release();
   s->staging.release();
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e);
   delete s;
   return GBR_OK;
 }
@@ -647,6 +671,18 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, st));
   if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
+  TRY(check_scene(s));
+  if (enable && !s->ev[0])
+    for (auto& e : s->ev) CU(cudaEventCreate(&e));
+  s->profile = enable != 0;
+  if (enable) {
+    for (double& v : s->stats.stage_ms) v = 0;
+    for (uint64_t& v : s->stats.stage_calls) v = 0;
+  }
   return GBR_OK;
 }
 

@@ -187,4 +187,10 @@ class GpuScene:
     def stats(self):
         st = np.zeros(1, S.STATS)
         _native.check(self.L.gbr_scene_stats(self.h, _np_ptr(st)))
-        return {k: int(st[0][k]) for k in S.STATS.names}
+        out = {k: int(st[0][k]) for k in S.STATS.names if k not in ("stage_ms", "stage_calls")}
+        out["stage_ms"] = {n: float(st[0]["stage_ms"][i]) for i, n in enumerate(S.STAGES)}
+        out["stage_calls"] = {n: int(st[0]["stage_calls"][i]) for i, n in enumerate(S.STAGES)}
+        return out
+
+    def profile(self, enable=True):
+        _native.check(self.L.gbr_scene_profile(self.h, 1 if enable else 0))
