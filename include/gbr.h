@@ -212,6 +212,47 @@ gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
  * build, engine.hpp:625-640). */
 gbr_status gbr_scene_profile(gbr_scene* scene, int32_t enable);
 
+/* ---- allocation-free rendering -------------------------------------------
+ * For callers that cannot allocate device memory where they render: code
+ * running while another library owns the device memory pool, real-time loops
+ * that forbid cudaMalloc/cudaFree (and the device synchronisation cudaFree
+ * implies), or hosts that hand this library only pre-allocated buffers.
+ * The scene is passed as device pointers the caller owns. */
+#define GBR_NOALLOC_MAX_PIXELS 2097152u      /* width*height, e.g. 1920x1080 */
+#define GBR_NOALLOC_MAX_RECORDS 131072u      /* visible clipped triangles per frame */
+#define GBR_NOALLOC_MAX_BIN_ENTRIES 524288u  /* triangle-tile pairs per frame */
+
+typedef struct gbr_device_scene {
+  const gbr_triangle* tris;               /* device, ntris; object_id < ndescs */
+  uint32_t ntris;
+  const gbr_obj_g_descriptor* descs;      /* device, ndescs; tid < mipmap_start */
+  uint32_t ndescs;
+  const gbr_light* lights;                /* device, nlights; shadow 0 or 1 */
+  uint32_t nlights;
+  const uint8_t* atlas;                   /* device texture pages (2048^2 RGBA8 each) */
+  const uint32_t* nums;                   /* device slot descriptors */
+  const uint32_t* sizes;                  /* device page edge sizes */
+  uint32_t mipmap_start;
+  const uint32_t* shadow_dyn;             /* device cubemaps, 6*1024^2 u32 per shadow light */
+  const uint32_t* shadow_static;          /* device cubemaps of static shadow lights */
+} gbr_device_scene;
+
+/* gbr_render_view without any device allocation: no counterpart in the
+ * reference.  Renders one view of the scene described by device pointers into
+ * the caller's device outputs (depth and id required; rgba and normals
+ * optional), with identical results to gbr_render_view.  All scratch lives in
+ * one fixed static device array of about 25.3 MB inside the library, held by
+ * every GPU that loads it until the process exits.  Views above
+ * GBR_NOALLOC_MAX_PIXELS return GBR_INVALID_ARG; frames with more visible
+ * triangles or bin entries than the limits return GBR_BIN_OVERFLOW_RETRY (use
+ * gbr_render_view).  The array is shared by all calls and keeps the previous
+ * call's contents: calls that overlap on the GPU race, so serialise them.
+ * The first call on each device (with that device current) looks up the
+ * array's device address; make it before any stream capture.  Synchronises
+ * the stream before returning. */
+gbr_status gbr_render_view_noalloc(const gbr_device_scene* scene, const gbr_camera* cam,
+                                   const gbr_view* view, const gbr_outputs* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -358,6 +358,10 @@ gbr_status pack_textures(uint32_t n, const int32_t* sz, std::vector<uint32_t>& n
 
 }  // namespace
 
+namespace gbr {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace gbr
+
 extern "C" {
 
 const char* gbr_last_error_string(void) { return g_err.c_str(); }

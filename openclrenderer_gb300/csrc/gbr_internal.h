@@ -141,4 +141,7 @@ cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* siz
                         int32_t max_size, cudaStream_t st);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 
+// Sets the message gbr_last_error_string() returns on this thread (gbr_api.cu).
+void set_last_error(const char* msg);
+
 }  // namespace gbr
