@@ -349,15 +349,29 @@ __device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int ch
 }
 
 // kernel1 + kernel2 for one 16x16 tile: depth min, then the canonical id.
+//
+// Records staged 256 at a time in shared memory.  A record whose bbox covers
+// at most kSmallPx pixels of the tile is rasterised by one thread over just
+// those pixels, with shared-memory atomicMin on the tile's depth (pass 0) or
+// on the packed (key << 32 | record) of the id pass (pass 1).  Larger records
+// go to a per-pixel loop run by all 256 threads.  Both reductions are minima,
+// so the order of records does not change the result.
+constexpr int kSmallPx = 64;
+
 __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const Surface* __restrict__ surfs,
                                                            uint32_t nsurf, int with_id) {
   __shared__ float4 srec[kRasterThreads][4];
   __shared__ uint32_t sidx[kRasterThreads];
+  __shared__ uint32_t sdepth[kRasterThreads];
+  __shared__ unsigned long long sid[kRasterThreads];
+  __shared__ uint16_t sbig[kRasterThreads];
+  __shared__ int nbig;
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
   if (ws.ctr->overflow) return;
   const uint32_t tile = blockIdx.x;
-  if (threadIdx.x == 0) {
+  const int tid = threadIdx.x;
+  if (tid == 0) {
     uint32_t s = find_surface(surfs, nsurf, tile);
     S = surfs[s];
     uint32_t lt = tile - S.tile_base;
@@ -368,49 +382,89 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const S
     lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
     lists[3] = ws.coarse_count[ct];
   }
+  sdepth[tid] = kDepthClear;
+  sid[tid] = ~0ull;
   __syncthreads();
   const uint32_t lt = tile - S.tile_base;
-  const int px = (lt % S.tiles_x) * kTile + (threadIdx.x & (kTile - 1));
-  const int py = (lt / S.tiles_x) * kTile + (threadIdx.x / kTile);
+  const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
+  const int px = tx0 + (tid & (kTile - 1));
+  const int py = ty0 + (tid / kTile);
   const int chunk = S.chunk;
-  uint32_t best = kDepthClear, best_key = kNoId, best_rec = kNoId;
-  const int passes = with_id ? 2 : 1;
+  uint32_t best = kDepthClear;
+  unsigned long long best_id = ~0ull;
+  const int passes = (with_id && (lists[1] | lists[3])) ? 2 : ((lists[1] | lists[3]) ? 1 : 0);
   for (int pass = 0; pass < passes; pass++) {
     for (int l = 0; l < 2; l++) {
       const uint32_t base = lists[2 * l], cnt = lists[2 * l + 1];
       for (uint32_t c0 = 0; c0 < cnt; c0 += kRasterThreads) {
-        uint32_t m = min((uint32_t)kRasterThreads, cnt - c0);
+        const uint32_t m = min((uint32_t)kRasterThreads, cnt - c0);
         __syncthreads();
-        if (threadIdx.x < m) {
-          uint32_t r = ws.bins[base + c0 + threadIdx.x];
+        if (tid == 0) nbig = 0;
+        if ((uint32_t)tid < m) {
+          uint32_t r = ws.bins[base + c0 + tid];
           const float4* src = reinterpret_cast<const float4*>(ws.rec + r);
-          srec[threadIdx.x][0] = __ldg(src);
-          srec[threadIdx.x][1] = __ldg(src + 1);
-          srec[threadIdx.x][2] = __ldg(src + 2);
-          srec[threadIdx.x][3] = __ldg(src + 3);
-          sidx[threadIdx.x] = r;
+          srec[tid][0] = __ldg(src);
+          srec[tid][1] = __ldg(src + 1);
+          srec[tid][2] = __ldg(src + 2);
+          srec[tid][3] = __ldg(src + 3);
+          sidx[tid] = r;
         }
         __syncthreads();
-        for (uint32_t i = 0; i < m; i++) {
-          float4 q[4] = {srec[i][0], srec[i][1], srec[i][2], srec[i][3]};
+        if ((uint32_t)tid < m) {
+          const float4 q[4] = {srec[tid][0], srec[tid][1], srec[tid][2], srec[tid][3]};
+          const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+          const int bx0 = max((int)(xr & 0xFFFF), tx0), bx1 = min((int)(xr >> 16), tx0 + kTile);
+          const int by0 = max((int)(yr & 0xFFFF), ty0), by1 = min((int)(yr >> 16), ty0 + kTile);
+          const int area = (bx1 > bx0 && by1 > by0) ? (bx1 - bx0) * (by1 - by0) : 0;
+          if (area > kSmallPx) {
+            sbig[atomicAdd(&nbig, 1)] = (uint16_t)tid;
+          } else if (area > 0) {
+            const uint32_t key = __float_as_uint(q[2].w);
+            const unsigned long long packed = ((unsigned long long)key << 32) | sidx[tid];
+            for (int y = by0; y < by1; y++)
+              for (int x = bx0; x < bx1; x++) {
+                if (!covers(q, x, y, chunk)) continue;
+                uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
+                const int p = (y - ty0) * kTile + (x - tx0);
+                if (pass == 0) {
+                  atomicMin(&sdepth[p], d);
+                } else {
+                  const uint32_t fd = sdepth[p];
+                  if (d > fd - kBufError && d < fd + kBufError) atomicMin(&sid[p], packed);
+                }
+              }
+          }
+        }
+        __syncthreads();
+        const int nb = nbig;
+        for (int b = 0; b < nb; b++) {
+          const int i = sbig[b];
+          const float4 q[4] = {srec[i][0], srec[i][1], srec[i][2], srec[i][3]};
           if (!covers(q, px, py, chunk)) continue;
           uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)px, (float)py);
           if (pass == 0) {
             best = min(best, d);
           } else if (d > best - kBufError && d < best + kBufError) {
-            uint32_t key = __float_as_uint(q[2].w);
-            if (key < best_key) { best_key = key; best_rec = sidx[i]; }
+            const unsigned long long packed = ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[i];
+            best_id = min(best_id, packed);
           }
         }
       }
     }
+    __syncthreads();
+    if (pass == 0) {
+      // fold the per-pixel minima into the tile's depth; it is final from here on
+      best = min(best, sdepth[tid]);
+      sdepth[tid] = best;
+    }
   }
   if (px < S.width && py < S.height) {
-    size_t p = (size_t)py * S.width + px;
+    const size_t p = (size_t)py * S.width + px;
     S.depth[p] = best;
     if (with_id) {
-      if (S.id) S.id[p] = best_key;
-      S.rec[p] = best_rec;
+      const unsigned long long v = min(best_id, sid[tid]);
+      if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
+      S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;
     }
   }
 }
@@ -566,6 +620,21 @@ __device__ __forceinline__ f3 tri_vec(const gbr_triangle* T, int k, int field) {
   return mk3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
 }
 
+// Colour-only arithmetic of the light loop: every use below feeds the colour
+// continuously (no comparison, rounding or index depends on it), so the
+// approximate division is covered by the 1/255 colour tolerance.
+__device__ __forceinline__ float cdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ f3 cnormalize(f3 a) {
+  float r = rsqrtf(dot3(a, a));
+  return mk3(a.x * r, a.y * r, a.z * r);
+}
+__device__ __forceinline__ float c_rational_acos(float x) {
+  const float a = -0.939115566365855f, b = 0.9217841528914573f, c = -1.2845906244690837f,
+              d = 0.295624144969963174f;
+  float x2 = x * x;
+  return kPi / 2.0f + cdiv(a * x + ((b * x) * x) * x, (1.0f + (c * x) * x) + d * (x2 * x2));
+}
+
 __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
   return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
 }
@@ -664,14 +733,14 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   uint32_t seed4 = rand_xorshift(seed3);
   f3 rseed = mk3((fdiv((float)seed2, kMulInt) - 0.5f) * 2.0f, (fdiv((float)seed3, kMulInt) - 0.5f) * 2.0f,
                  (fdiv((float)seed4, kMulInt) - 0.5f) * 2.0f);
-  const f3 l2p = fast_normalize3(sub3(cpos, gpos));
+  const f3 l2p = cnormalize(sub3(cpos, gpos));
   const int ff = __ldg(&G->feature_flag);
   const bool two = (ff & kFlagTwoSided) > 0;
   const bool recv_dyn = !((ff & kFlagNoDynShadows) > 0);
   if (!backface_front(tp[0], tp[1], tp[2]) && two) normal = neg3(normal);
   const float ssao = generate_ssao(x, y, S.depth, W, H, fov);
   normal = fast_normalize3(normal);
-  const f3 lnormal = fast_normalize3(add3(normal, mk3(fdiv(rseed.x, 100.f), fdiv(rseed.y, 100.f), fdiv(rseed.z, 100.f))));
+  const f3 lnormal = cnormalize(add3(normal, mk3(fdiv(rseed.x, 100.f), fdiv(rseed.y, 100.f), fdiv(rseed.z, 100.f))));
   const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
   const float g_diffuse = __ldg(&G->diffuse), g_spec_mult = __ldg(&G->spec_mult);
   const float rough = clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f);
@@ -690,11 +759,11 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       static_num++;
     }
     float distance = fast_length3(ptl);
-    float tt = fdiv(distance, __ldg(&L->radius)) + 1.0f;
-    float illum = fdiv(__ldg(&L->brightness), tt * tt);
+    float tt = cdiv(distance, __ldg(&L->radius)) + 1.0f;
+    float illum = cdiv(__ldg(&L->brightness), tt * tt);
     const float cutoff = 0.1f;
     illum -= cutoff;
-    illum *= fdiv(1.0f, 1.0f - cutoff);
+    illum *= 1.0f / (1.0f - cutoff);
     if (illum <= 0) continue;
     f3 lcol = ld3(L->col);
     if (V.use_linear) lcol = mk3(gamma_fwd(lcol.x), gamma_fwd(lcol.y), gamma_fwd(lcol.z));
@@ -704,23 +773,24 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       occlusion = fmin_(occlusion, dyn);
       shnum++;
     }
-    ptl = fast_normalize3(ptl);
+    ptl = cnormalize(ptl);
     float light = fmax_(dot3(ptl, lnormal) * occlusion, 0.0f);
     float diffuse = (1.0f - ambient) * light;
     float dscale = (((diffuse + ambient) * __ldg(&L->diffuse)) * g_diffuse) * illum;
     dsum = add3(dsum, mul3s(lcol, dscale));
-    f3 Hv = fast_normalize3(add3(l2p, ptl));
+    f3 Hv = cnormalize(add3(l2p, ptl));
     float ndh = fmax_(0.0f, dot3(normal, Hv));
     float ndv = fmax_(0.0f, dot3(normal, l2p));
     float vdh = fmax_(0.0f, dot3(l2p, Hv));
     float ndl = fmax_(0.0f, dot3(normal, ptl));
     const float F0 = 0.4f;
-    float fresnel = F0 + (1.0f - F0) * powf(1.0f - vdh, 5.0f);
-    float alpha = rational_acos(ndh);
-    float microfacet = 0.8346f * expf(fdiv((-alpha) * alpha, rough * rough));
-    float sv = fdiv(2.0f * ndh, vdh);
+    float omv = 1.0f - vdh, omv2 = omv * omv;
+    float fresnel = F0 + (1.0f - F0) * ((omv2 * omv2) * omv);
+    float alpha = c_rational_acos(ndh);
+    float microfacet = 0.8346f * __expf(cdiv((-alpha) * alpha, rough * rough));
+    float sv = cdiv(2.0f * ndh, vdh);
     float geometric = min3f(1.0f, sv * ndv, sv * ndl);
-    float spec = fdiv((fresnel * microfacet) * geometric, kPi * ndv);
+    float spec = cdiv((fresnel * microfacet) * geometric, kPi * ndv);
     float sscale = (spec * 0.4f) * illum;
     ssum = add3(ssum, mul3s(mul3s(lcol, sscale), g_spec_mult));
     ssum = mk3(fmax_(ssum.x, 0.0f), fmax_(ssum.y, 0.0f), fmax_(ssum.z, 0.0f));
@@ -747,7 +817,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
-__global__ void __launch_bounds__(256) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
+__global__ void __launch_bounds__(256, 3) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec) {
   __shared__ uint32_t s_id;

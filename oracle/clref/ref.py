@@ -1,0 +1,85 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes wrapper of oracle/_ref/libclref.so (the
+reference's cl2.cl kernels compiled as C++).  Used to pin the oracle and to
+generate tests/golden fixtures; never imported by the product."""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_ref
+
+_lib = None
+P = ctypes.c_void_p
+
+
+def available():
+    return os.path.exists(build_ref.LIB) or os.path.exists(build_ref.REFERENCE_CL)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_ref.build()
+        L = ctypes.CDLL(build_ref.LIB)
+        L.ref_render.restype = ctypes.c_int64
+        L.ref_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32, P, P, P,
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P, P, P, P, P,
+                                 ctypes.c_int]
+        L.ref_shadow.restype = None
+        L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int]
+        L.ref_textures.restype = None
+        L.ref_textures.argtypes = [ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(P)
+
+
+def textures(tex_sizes, tex_pixels, nums, page_sizes, mipmap_start):
+    """Atlas built by the reference's update_gpu_tex / generate_mips kernels on
+    the page layout (nums, page_sizes) of the texture_context packing."""
+    n = len(tex_sizes)
+    sz = np.asarray(tex_sizes, np.int32)
+    px = [np.ascontiguousarray(p, np.uint8) for p in tex_pixels]
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[p.ctypes.data for p in px])
+    atlas = np.zeros((max(len(page_sizes), 1), 2048, 2048, 4), np.uint8)
+    nums = np.ascontiguousarray(nums, np.uint32)
+    page_sizes = np.ascontiguousarray(page_sizes, np.uint32)
+    lib().ref_textures(n, _p(sz), ctypes.cast(ptrs, P), _p(atlas), _p(nums), _p(page_sizes), mipmap_start)
+    return atlas
+
+
+def shadow(scene, nthreads=None):
+    nthreads = nthreads or (os.cpu_count() or 1)
+    nd = int(sum(1 for l in scene.lights if l["shadow"] == 1))
+    ns = int(sum(1 for l in scene.lights if l["shadow"] and l["is_static"]))
+    dyn = np.full((max(nd, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    sta = np.full((max(ns, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    lib().ref_shadow(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
+                     _p(dyn), _p(sta), nthreads)
+    return dyn, sta
+
+
+def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_dyn=None, shadow_static=None,
+           nthreads=None):
+    nthreads = nthreads or (os.cpu_count() or 1)
+    W, H = int(view["width"]), int(view["height"])
+    if shadow_dyn is None:
+        shadow_dyn = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    if shadow_static is None:
+        shadow_static = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    cam = np.concatenate([np.asarray(cam["pos"], np.float32), np.asarray(cam["rot"], np.float32)])
+    clear = np.asarray(view["clear_col"], np.float32)
+    depth = np.empty((H, W), np.uint32)
+    ids = np.empty((H, W), np.uint32)
+    rgba = np.empty((H, W, 4), np.uint8)
+    normals = np.empty((H, W, 2), np.uint16)
+    nums = np.ascontiguousarray(nums, np.uint32)
+    page_sizes = np.ascontiguousarray(page_sizes, np.uint32)
+    nf = lib().ref_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
+                          _p(atlas), _p(nums), _p(page_sizes), mipmap_start, _p(shadow_dyn), _p(shadow_static),
+                          _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
+                          _p(rgba), _p(normals), nthreads)
+    return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "fragments": int(nf)}

@@ -1,0 +1,62 @@
+"""Generate tests/golden/*.npz from the reference's own cl2.cl kernels.
+
+Runs oracle/_ref/libclref.so (cl2.cl's prearrange, kernel1, kernel2, kernel3,
+shadow and texture kernels compiled as C++ by oracle/clref, under the
+determinism contract of gbr_math.h) on seeded scenes and stores depth, id,
+RGBA8 and normals, SHA-256 digests of the shadow cubemap faces and atlas pages,
+and a digest of the scene bytes.  Needs the reference checkout; run from the
+repository root:  python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from openclrenderer_gb300 import scenes  # noqa: E402
+from openclrenderer_gb300 import structs as S  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from oracle.clref import ref as R  # noqa: E402
+from tests import golden_cases  # noqa: E402
+
+OUT = os.path.join(ROOT, "tests", "golden")
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def main():
+    for name, make in golden_cases.CASES.items():
+        sc, opts = make()
+        tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+        atlas = R.textures(sc.tex_sizes, sc.tex_pixels, tex.nums, tex.sizes, tex.mipmap_start)
+        dyn = sta = None
+        meta = {"scene_sha": golden_cases.scene_digest(sc), "atlas_pages": [sha(p) for p in atlas]}
+        if opts.get("shadows"):
+            dyn, sta = R.shadow(sc)
+            meta["cube_faces"] = [sha(dyn[l, f]) for l in range(dyn.shape[0]) for f in range(6)]
+            meta["cube_written"] = int(np.count_nonzero(dyn != 0xFFFFFFFF))
+        arrays = {}
+        for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+            fov = float(view["fov_const"]) if view["fov_const"] > 0 else O.fov_const(float(view["hfov_deg"]),
+                                                                                 int(view["width"]))
+            r = R.render(sc, atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov, dyn, sta)
+            arrays[f"depth{k}"] = r["depth"]
+            arrays[f"id{k}"] = r["id"]
+            arrays[f"rgba{k}"] = r["rgba"]
+            if opts.get("normals"):
+                arrays[f"normals{k}"] = r["normals"]
+            meta[f"fragments{k}"] = r["fragments"]
+        path = os.path.join(OUT, f"{name}.npz")
+        np.savez_compressed(path, meta=np.array(json.dumps(meta)), **arrays)
+        print(f"{name}: {os.path.getsize(path) / 1e3:.0f} kB, views {len(sc.views)}, "
+              f"fragments {[meta[k] for k in meta if k.startswith('fragments')]}")
+
+
+if __name__ == "__main__":
+    main()

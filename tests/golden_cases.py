@@ -1,0 +1,82 @@
+"""Seeded scenes of the golden fixtures (tests/golden/*.npz).  Shared by the
+fixture generator and the tests; the scene digest guards against a change in
+the generators or in numpy's random streams."""
+import hashlib
+
+import numpy as np
+
+from openclrenderer_gb300 import scenes
+from openclrenderer_gb300 import structs as S
+from tests.scene_util import random_soup, screen_tri, tri_scene
+
+
+def scene_digest(sc):
+    h = hashlib.sha256()
+    for a in (sc.tris, sc.descs, sc.lights, *sc.tex_pixels, *sc.cameras, *sc.views):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def cubes():
+    sc = scenes.plain_cubes()
+    sc.cameras.append(S.make_camera((40.0, -30.0, 100.0), (0.15, -0.2, 0.05)))
+    sc.views.append(S.make_view(640, 400, hfov_deg=75.0, use_linear=0))
+    return sc, {"normals": True}
+
+
+def terrain_shadow():
+    sc = scenes.terrain(nx=128, nz=64, width=320, height=180, n_lights=4, n_textures=4, tex_size=64)
+    return sc, {"shadows": True, "normals": True}
+
+
+def soups():
+    sc = random_soup(300, 320, 240, 21)
+    s2 = random_soup(300, 320, 240, 22, two_sided=False)
+    s2.tris["vertices"][:, 0]["object_id"] = 1
+    sc.tris = np.concatenate([sc.tris, s2.tris])
+    sc.descs = np.stack([sc.descs[0], S.make_descriptor(world_pos=(3, -2, 10), quat=(0.05, 0.1, 0.02, 0.99),
+                                                         scale=1.05, tid=0, specular=0.6)])
+    return sc, {}
+
+
+def edges():
+    W, H = 256, 192
+    tl = [
+        screen_tri([10, 200, 30], [10, 20, 180], [100, 100, 100], W, H),
+        [(-30, -10, 10.0), (40, 0, 60.0), (0, 30, 80.0)],
+        [(-30, -10, 5.0), (40, 0, 10.0), (0, 30, 80.0)],
+        [(-3000, -1000, 300000.0), (4000, 0, 360000.0), (0, 3000, 200000.0)],
+        screen_tri([-500, -400, -450], [10, 20, 30], [50, 50, 50], W, H),
+        screen_tri([20, 20, 20], [20, 80, 140], [70, 70, 70], W, H),
+        screen_tri([0.2, 0.4, 0.3], [100, 101, 100.6], [30, 30, 30], W, H),
+        screen_tri([-200, 2 * W, -200], [-200, H // 2, 2 * H], [400, 400, 400], W, H),
+        screen_tri([50, 52, 51], [60, 60, 61], [90, 90.5, 91], W, H),
+        screen_tri([5, 250, 128], [5, 5, 190], [20.5, 20.5, 20.5], W, H),
+        [(-1e7, 5, 1000.0), (1e7, 10, 1000.0), (0, 2e6, 1000.0)],
+    ]
+    cols = [[0, 0, 0]] * len(tl)
+    cols[0] = [0xFF0000FF, 0x00FF00FF, 0x0000FFFF]
+    sc = tri_scene(tl, W, H, descs=np.stack([S.make_descriptor(tid=0, feature_flag=S.FLAG_TWO_SIDED)]),
+                   vertex_cols=cols)
+    return sc, {}
+
+
+def wide_boxes():
+    """Large screen-aligned triangles whose bboxes hit rows where the
+    reference walk skips the left-column pixel."""
+    W, H = 800, 450
+    tl = []
+    rng = np.random.default_rng(31)
+    for i in range(40):
+        x0, y0 = rng.uniform(0, 300), rng.uniform(0, 200)
+        w, h = rng.uniform(200, 490), rng.uniform(80, 240)
+        z = rng.uniform(100, 3000)
+        tl.append(screen_tri([x0, x0 + w, x0], [y0, y0, y0 + h], [z, z * 1.01, z * 0.99], W, H))
+    cols = [[0xC08040FF, 0x4080C0FF, 0x80C040FF]] * len(tl)
+    sc = tri_scene(tl, W, H, descs=np.stack([S.make_descriptor(tid=0, feature_flag=S.FLAG_TWO_SIDED)]),
+                   vertex_cols=cols)
+    return sc, {}
+
+
+CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
+         "wide_boxes": wide_boxes}
