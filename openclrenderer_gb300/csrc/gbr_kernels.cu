@@ -350,22 +350,50 @@ __device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int ch
 
 // kernel1 + kernel2 for one 16x16 tile: depth min, then the canonical id.
 //
-// Records staged 256 at a time in shared memory.  A record whose bbox covers
-// at most kSmallPx pixels of the tile is rasterised by one thread over just
-// those pixels, with shared-memory atomicMin on the tile's depth (pass 0) or
-// on the packed (key << 32 | record) of the id pass (pass 1).  Larger records
-// go to a per-pixel loop run by all 256 threads.  Both reductions are minima,
-// so the order of records does not change the result.
-constexpr int kSmallPx = 64;
+// The tile's records (its fine bin, then its coarse tile's bin) are staged 256
+// at a time in shared memory.  Each record contributes the pixels of its bbox
+// clipped to the tile; an exclusive scan of those areas lays all
+// (record, pixel) tests of the chunk end to end, and the 256 threads walk that
+// list in strides (binary search for the owning record), so small and large
+// triangles are load-balanced alike.  Pass 0 resolves the minimum depth with
+// shared-memory atomicMin; pass 1 the minimum packed (key << 32 | record)
+// among tests within +-20 of the final depth.  Both are minima, so neither
+// bin order nor thread order changes the result.  When the whole list fits
+// one chunk, pass 1 reuses the staged records and offsets.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) swarp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < (kRasterThreads / 32) ? swarp[lane] : 0;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < (kRasterThreads / 32)) swarp[lane] = wi - w;
+    if (lane == (kRasterThreads / 32) - 1) *total = wi;
+  }
+  __syncthreads();
+  return swarp[warp] + incl - v;
+}
 
 __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const Surface* __restrict__ surfs,
                                                            uint32_t nsurf, int with_id) {
   __shared__ float4 srec[kRasterThreads][4];
   __shared__ uint32_t sidx[kRasterThreads];
+  __shared__ uint32_t soff[kRasterThreads + 1];
+  __shared__ uint32_t sgeo[kRasterThreads];  // lx0 | ly0 << 8 | bw << 16
   __shared__ uint32_t sdepth[kRasterThreads];
   __shared__ unsigned long long sid[kRasterThreads];
-  __shared__ uint16_t sbig[kRasterThreads];
-  __shared__ int nbig;
+  __shared__ uint32_t swarp[kRasterThreads / 32];
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
   if (ws.ctr->overflow) return;
@@ -387,82 +415,73 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const S
   __syncthreads();
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
-  const int px = tx0 + (tid & (kTile - 1));
-  const int py = ty0 + (tid / kTile);
   const int chunk = S.chunk;
-  uint32_t best = kDepthClear;
-  unsigned long long best_id = ~0ull;
-  const int passes = (with_id && (lists[1] | lists[3])) ? 2 : ((lists[1] | lists[3]) ? 1 : 0);
+  const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
+  const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
+  const bool resident = ntotal <= (uint32_t)kRasterThreads;
   for (int pass = 0; pass < passes; pass++) {
-    for (int l = 0; l < 2; l++) {
-      const uint32_t base = lists[2 * l], cnt = lists[2 * l + 1];
-      for (uint32_t c0 = 0; c0 < cnt; c0 += kRasterThreads) {
-        const uint32_t m = min((uint32_t)kRasterThreads, cnt - c0);
+    for (uint32_t c0 = 0; c0 < ntotal; c0 += kRasterThreads) {
+      const uint32_t m = min((uint32_t)kRasterThreads, ntotal - c0);
+      if (!(resident && pass == 1)) {
         __syncthreads();
-        if (tid == 0) nbig = 0;
+        uint32_t area = 0;
         if ((uint32_t)tid < m) {
-          uint32_t r = ws.bins[base + c0 + tid];
+          const uint32_t e = c0 + tid;
+          const uint32_t r = e < nfine ? ws.bins[lists[0] + e] : ws.bins[lists[2] + (e - nfine)];
           const float4* src = reinterpret_cast<const float4*>(ws.rec + r);
+          const float4 q3 = __ldg(src + 3);
           srec[tid][0] = __ldg(src);
           srec[tid][1] = __ldg(src + 1);
           srec[tid][2] = __ldg(src + 2);
-          srec[tid][3] = __ldg(src + 3);
+          srec[tid][3] = q3;
           sidx[tid] = r;
-        }
-        __syncthreads();
-        if ((uint32_t)tid < m) {
-          const float4 q[4] = {srec[tid][0], srec[tid][1], srec[tid][2], srec[tid][3]};
-          const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+          const uint32_t xr = __float_as_uint(q3.x), yr = __float_as_uint(q3.y);
           const int bx0 = max((int)(xr & 0xFFFF), tx0), bx1 = min((int)(xr >> 16), tx0 + kTile);
           const int by0 = max((int)(yr & 0xFFFF), ty0), by1 = min((int)(yr >> 16), ty0 + kTile);
-          const int area = (bx1 > bx0 && by1 > by0) ? (bx1 - bx0) * (by1 - by0) : 0;
-          if (area > kSmallPx) {
-            sbig[atomicAdd(&nbig, 1)] = (uint16_t)tid;
-          } else if (area > 0) {
-            const uint32_t key = __float_as_uint(q[2].w);
-            const unsigned long long packed = ((unsigned long long)key << 32) | sidx[tid];
-            for (int y = by0; y < by1; y++)
-              for (int x = bx0; x < bx1; x++) {
-                if (!covers(q, x, y, chunk)) continue;
-                uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
-                const int p = (y - ty0) * kTile + (x - tx0);
-                if (pass == 0) {
-                  atomicMin(&sdepth[p], d);
-                } else {
-                  const uint32_t fd = sdepth[p];
-                  if (d > fd - kBufError && d < fd + kBufError) atomicMin(&sid[p], packed);
-                }
-              }
+          if (bx1 > bx0 && by1 > by0) {
+            area = (uint32_t)((bx1 - bx0) * (by1 - by0));
+            sgeo[tid] = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 8) | ((uint32_t)(bx1 - bx0) << 16);
           }
         }
+        uint32_t off = block_excl_scan(area, swarp, &soff[kRasterThreads]);
+        soff[tid] = off;
         __syncthreads();
-        const int nb = nbig;
-        for (int b = 0; b < nb; b++) {
-          const int i = sbig[b];
-          const float4 q[4] = {srec[i][0], srec[i][1], srec[i][2], srec[i][3]};
-          if (!covers(q, px, py, chunk)) continue;
-          uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)px, (float)py);
-          if (pass == 0) {
-            best = min(best, d);
-          } else if (d > best - kBufError && d < best + kBufError) {
-            const unsigned long long packed = ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[i];
-            best_id = min(best_id, packed);
-          }
+      }
+      const uint32_t total = soff[kRasterThreads];
+      for (uint32_t t = tid; t < total; t += kRasterThreads) {
+        // owning record: the last i < m with soff[i] <= t
+        int lo = 0, hi = (int)m - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (soff[mid] <= t) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t g = sgeo[lo];
+        const uint32_t bw = g >> 16;
+        const uint32_t local = t - soff[lo];
+        const uint32_t ry = local / bw, rx = local - ry * bw;
+        const int lx = (int)(g & 0xFF) + (int)rx, ly = (int)((g >> 8) & 0xFF) + (int)ry;
+        const float4 q[4] = {srec[lo][0], srec[lo][1], srec[lo][2], srec[lo][3]};
+        const int x = tx0 + lx, y = ty0 + ly;
+        if (!covers(q, x, y, chunk)) continue;
+        const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
+        const int p = ly * kTile + lx;
+        if (pass == 0) {
+          atomicMin(&sdepth[p], d);
+        } else {
+          const uint32_t fd = sdepth[p];
+          if (d > fd - kBufError && d < fd + kBufError)
+            atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
         }
       }
     }
     __syncthreads();
-    if (pass == 0) {
-      // fold the per-pixel minima into the tile's depth; it is final from here on
-      best = min(best, sdepth[tid]);
-      sdepth[tid] = best;
-    }
   }
+  const int px = tx0 + (tid & (kTile - 1)), py = ty0 + (tid / kTile);
   if (px < S.width && py < S.height) {
     const size_t p = (size_t)py * S.width + px;
-    S.depth[p] = best;
+    S.depth[p] = sdepth[tid];
     if (with_id) {
-      const unsigned long long v = min(best_id, sid[tid]);
+      const unsigned long long v = sid[tid];
       if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
       S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;
     }

@@ -35,7 +35,7 @@ def build(force=False):
             os.path.join(ORACLE, "..", "openclrenderer_gb300", "csrc", "gbr_math.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-strict-aliasing", "-fwrapv", "-Wno-narrowing",
+    cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-strict-aliasing", "-fwrapv", "-Wno-narrowing",
            "-w", "-fPIC", "-shared", "-pthread", f'-DCLREF_KERNELS="{KERNELS}"', "-o", LIB + ".tmp",
            os.path.join(HERE, "harness.cpp")]
     subprocess.run(cmd, check=True)

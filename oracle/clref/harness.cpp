@@ -81,7 +81,7 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
                    const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
                    const uint32_t* shadow_dyn, const uint32_t* shadow_static, const float* cam, int W, int H,
                    float fov, uint32_t use_linear, const float* clear, uint32_t* depth, uint32_t* ids,
-                   uint8_t* rgba, uint16_t* normals, int nthreads) {
+                   uint8_t* rgba, uint16_t* normals, int nthreads, int ordered) {
   gbr_ref_W = W;
   gbr_ref_H = H;
   gbr_ref_FOV = fov;
@@ -95,10 +95,23 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
   std::vector<uint> b_before(ntris);
   uint tri_num = ntris, maxlen = 0xFFFFFFFFu, frag_count = 0, cut_count = 0;
   float4 c_pos(cam[0], cam[1], cam[2], cam[3]), c_rot(cam[4], cam[5], cam[6], cam[7]);
-  for (uint32_t id = 0; id < ntris; id++) {
-    gbr_ref_gid[0] = id;
-    b_before[id] = id == 0 ? 0 : cut_count;
-    prearrange(tris, &tri_num, c_pos, c_rot, frags, &maxlen, &frag_count, &cut_count, cut.data(), gobj);
+  if (ordered) {
+    for (uint32_t id = 0; id < ntris; id++) {
+      gbr_ref_gid[0] = id;
+      b_before[id] = id == 0 ? 0 : cut_count;
+      prearrange(tris, &tri_num, c_pos, c_rot, frags, &maxlen, &frag_count, &cut_count, cut.data(), gobj);
+    }
+  } else {
+    // timing mode: work items in parallel with the reference's atomics (item 0,
+    // which resets the counters, first)
+    if (ntris) {
+      gbr_ref_gid[0] = 0;
+      prearrange(tris, &tri_num, c_pos, c_rot, frags, &maxlen, &frag_count, &cut_count, cut.data(), gobj);
+    }
+    par_for((int64_t)ntris - 1, nthreads, [&](int64_t i) {
+      gbr_ref_gid[0] = (size_t)i + 1;
+      prearrange(tris, &tri_num, c_pos, c_rot, frags, &maxlen, &frag_count, &cut_count, cut.data(), gobj);
+    });
   }
   const uint nfrag = frag_count;
   for (size_t p = 0; p < P; p++) depth[p] = 0xFFFFFFFFu;
@@ -141,7 +154,7 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
       normals[p * 2] = drawn ? nrm[p].x : 0;
       normals[p * 2 + 1] = drawn ? nrm[p].y : 0;
     }
-    if (ids[p] != 0xFFFFFFFFu) {
+    if (ordered && ids[p] != 0xFFFFFFFFu) {
       uint f = ids[p];
       uint tri = frags[(size_t)f * 5 + 0];
       uint ctri = frags[(size_t)f * 5 + 2];
@@ -154,7 +167,7 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
 // Cubemaps of every shadow light (dynamic: lights with shadow == 1; static:
 // shadow && is_static), 6 * 1024^2 u32 each.
 void ref_shadow(const void* tris_in, uint32_t ntris, const void* descs, const void* lights_in, uint32_t nlights,
-                uint32_t* dyn, uint32_t* stat, int nthreads) {
+                uint32_t* dyn, uint32_t* stat, int nthreads, int ordered) {
   auto* tris = (struct triangle*)const_cast<void*>(tris_in);
   auto* gobj = (struct obj_g_descriptor*)const_cast<void*>(descs);
   auto* lights = (const struct light*)lights_in;
@@ -167,10 +180,21 @@ void ref_shadow(const void* tris_in, uint32_t ntris, const void* descs, const vo
     for (size_t i = 0; i < 6 * face; i++) out[i] = 0xFFFFFFFFu;
     uint tri_num = ntris, maxlen = 0xFFFFFFFFu, frag_count = 0, cut_count = 0;
     float4 lpos = L.pos, no_rot(0.f);
-    for (uint32_t id = 0; id < ntris; id++) {
-      gbr_ref_gid[0] = id;
+    if (ordered) {
+      for (uint32_t id = 0; id < ntris; id++) {
+        gbr_ref_gid[0] = id;
+        prearrange_realtime_shadowing(tris, &tri_num, lpos, no_rot, frags, &maxlen, &frag_count, &cut_count,
+                                      cut.data(), gobj, only_static);
+      }
+    } else if (ntris) {
+      gbr_ref_gid[0] = 0;
       prearrange_realtime_shadowing(tris, &tri_num, lpos, no_rot, frags, &maxlen, &frag_count, &cut_count,
                                     cut.data(), gobj, only_static);
+      par_for((int64_t)ntris - 1, nthreads, [&](int64_t i) {
+        gbr_ref_gid[0] = (size_t)i + 1;
+        prearrange_realtime_shadowing(tris, &tri_num, lpos, no_rot, frags, &maxlen, &frag_count, &cut_count,
+                                      cut.data(), gobj, only_static);
+      });
     }
     uint f_len = frag_count;
     par_for(frag_count, nthreads, [&](int64_t i) {

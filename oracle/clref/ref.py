@@ -24,9 +24,9 @@ def lib():
         L.ref_render.restype = ctypes.c_int64
         L.ref_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32, P, P, P,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P, P, P, P, P,
-                                 ctypes.c_int]
+                                 ctypes.c_int, ctypes.c_int]
         L.ref_shadow.restype = None
-        L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int]
+        L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int, ctypes.c_int]
         L.ref_textures.restype = None
         L.ref_textures.argtypes = [ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32]
         _lib = L
@@ -51,19 +51,21 @@ def textures(tex_sizes, tex_pixels, nums, page_sizes, mipmap_start):
     return atlas
 
 
-def shadow(scene, nthreads=None):
+def shadow(scene, nthreads=None, ordered=True):
+    """ordered=False runs prearrange's work items in parallel, as the reference
+    does (timing); ordered=True in order (pinning, deterministic ids)."""
     nthreads = nthreads or (os.cpu_count() or 1)
     nd = int(sum(1 for l in scene.lights if l["shadow"] == 1))
     ns = int(sum(1 for l in scene.lights if l["shadow"] and l["is_static"]))
     dyn = np.full((max(nd, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
     sta = np.full((max(ns, 1), 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
     lib().ref_shadow(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
-                     _p(dyn), _p(sta), nthreads)
+                     _p(dyn), _p(sta), nthreads, 1 if ordered else 0)
     return dyn, sta
 
 
 def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_dyn=None, shadow_static=None,
-           nthreads=None):
+           nthreads=None, ordered=True):
     nthreads = nthreads or (os.cpu_count() or 1)
     W, H = int(view["width"]), int(view["height"])
     if shadow_dyn is None:
@@ -81,5 +83,5 @@ def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_
     nf = lib().ref_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
                           _p(atlas), _p(nums), _p(page_sizes), mipmap_start, _p(shadow_dyn), _p(shadow_static),
                           _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
-                          _p(rgba), _p(normals), nthreads)
+                          _p(rgba), _p(normals), nthreads, 1 if ordered else 0)
     return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "fragments": int(nf)}
