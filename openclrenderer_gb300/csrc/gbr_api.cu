@@ -130,6 +130,11 @@ struct WorkMem {
   }
 };
 
+struct PassShape {
+  uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
+  size_t npix = 0;
+};
+
 void euler_cs(const float ang[3], float c[3], float s[3]) {
   for (int i = 0; i < 3; i++) {
     c[i] = (float)cos((double)ang[i]);
@@ -143,6 +148,8 @@ struct gbr_scene {
   int device = 0;
   DevBuf<gbr_triangle> tris;
   uint32_t ntris = 0;
+  DevBuf<float4> world;     // world-space vertices, 3 per triangle
+  bool world_dirty = true;  // triangles or descriptors changed since k_world ran
   DevBuf<gbr_obj_g_descriptor> descs;
   uint32_t ndescs = 0;
   DevBuf<gbr_light> lights;
@@ -156,8 +163,11 @@ struct gbr_scene {
   uint32_t n_dyn = 0, n_static = 0;
   uint32_t max_object_id = 0, max_tid = 0;
   bool static_dirty = true;
-  WorkMem ws;
-  HostBuf staging;     // surfaces / views / jobs / counters
+  WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
+  HostBuf staging;     // counters read back: view at 0, shadow at 256
+  bool shadow_pending = false;  // a shadow pass whose counters are not checked yet
+  cudaStream_t shadow_stream = nullptr;
+  PassShape shadow_shape;
   gbr_stats stats{};
   float face_cos[6][3], face_sin[6][3];
   bool profile = false;
@@ -167,6 +177,7 @@ struct gbr_scene {
     SceneDev d{};
     d.tris = tris.p;
     d.ntris = ntris;
+    d.world = world_dirty ? nullptr : world.p;
     d.descs = descs.p;
     d.ndescs = ndescs;
     d.lights = lights.p;
@@ -201,8 +212,10 @@ gbr_status check_indices(gbr_scene* s, bool shading) {
 }
 
 // Reserve pass scratch: records, bins and tile counters for the given surfaces.
+WorkMem& pass_mem(gbr_scene* s, bool view) { return view ? s->ws_view : s->ws_shadow; }
+
 gbr_status reserve_pass(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view, size_t npix) {
-  WorkMem& w = s->ws;
+  WorkMem& w = pass_mem(s, view);
   TRY(w.rec.reserve(w.rec_target));
   if (view) TRY(w.srec.reserve(w.rec_target));
   TRY(w.bins.reserve(w.bin_target));
@@ -216,7 +229,7 @@ gbr_status reserve_pass(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool vie
 }
 
 Workspace make_ws(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view) {
-  WorkMem& w = s->ws;
+  WorkMem& w = pass_mem(s, view);
   Workspace ws{};
   ws.rec = w.rec.p;
   ws.srec = view ? w.srec.p : nullptr;
@@ -254,67 +267,119 @@ gbr_status validate_view(const gbr_view* v) {
   return GBR_OK;
 }
 
-// Run one pass (views or shadow jobs) with grow-and-retry on scratch overflow.
-// The caller has filled s->ws.surf / views / jobs on the device.
-gbr_status run_pass(gbr_scene* s, bool view, uint32_t nitems, uint32_t nsurf, uint32_t nfine,
-                    uint32_t ncoarse, size_t npix, cudaStream_t st) {
+// World-space vertex cache (k_world), rebuilt when triangles or descriptors change.
+gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
+  if (!s->world_dirty) return GBR_OK;
+  TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
+  SceneDev sd = s->dev();
+  CU(launch_world(sd, s->world.p, st));
+  s->stats.launches += 1;
+  s->world_dirty = false;
+  return GBR_OK;
+}
+
+Counters* counter_slot(gbr_scene* s, bool view) {
+  return reinterpret_cast<Counters*>(static_cast<char*>(s->staging.p) + (view ? 0 : 256));
+}
+
+// Launch one pass (views or shadow jobs) and queue the read-back of its
+// counters; the caller synchronises and calls check_pass.  The caller has
+// filled the pass's surfaces / views / jobs on the device.
+gbr_status enqueue_pass(gbr_scene* s, bool view, uint32_t nitems, uint32_t nsurf, uint32_t nfine,
+                        uint32_t ncoarse, size_t npix, cudaStream_t st) {
+  TRY(ensure_world(s, st));
   const SceneDev sd = s->dev();
-  for (int attempt = 0; attempt < 6; attempt++) {
-    TRY(reserve_pass(s, nfine, ncoarse, view, npix));
-    Workspace ws = make_ws(s, nfine, ncoarse, view);
-    CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
-    CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(nfine, 1), st));
-    CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(ncoarse, 1), st));
-    const int sb = view ? 4 : 0;  // first stage index of this pass
-    const int nst = view ? 5 : 4;
-    auto mark = [&](int k) -> cudaError_t { return s->profile ? cudaEventRecord(s->ev[k], st) : cudaSuccess; };
-    CU(mark(0));
-    if (view)
-      CU(launch_setup_views(sd, s->ws.views.p, nitems, s->ws.surf.p, ws, st));
-    else
-      CU(launch_setup_shadow(sd, s->ws.jobs.p, nitems, s->ws.surf.p, ws, st));
-    CU(mark(1));
-    CU(launch_scan(ws, st));
-    CU(mark(2));
-    CU(launch_fill(ws, s->ws.surf.p, st));
-    CU(mark(3));
-    CU(launch_raster(ws, s->ws.surf.p, nsurf, nfine, view, st));
-    CU(mark(4));
-    if (view) {
-      CU(launch_shade(sd, s->ws.views.p, nitems, s->ws.surf.p, nfine, ws.srec, st));
-      CU(mark(5));
-    }
-    s->stats.launches += (uint64_t)nst;
-    Counters* hc = reinterpret_cast<Counters*>(s->staging.p);
-    CU(cudaMemcpyAsync(hc, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-    CU(cudaStreamSynchronize(st));
-    if (s->profile) {
-      for (int k = 0; k < nst; k++) {
-        float ms = 0.f;
-        CU(cudaEventElapsedTime(&ms, s->ev[k], s->ev[k + 1]));
+  WorkMem& wm = pass_mem(s, view);
+  TRY(reserve_pass(s, nfine, ncoarse, view, npix));
+  Workspace ws = make_ws(s, nfine, ncoarse, view);
+  CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
+  CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(nfine, 1), st));
+  CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(ncoarse, 1), st));
+  const int sb = view ? 4 : 0;  // first stage index of this pass
+  const int nst = view ? 5 : 4;
+  auto mark = [&](int k) -> cudaError_t { return s->profile ? cudaEventRecord(s->ev[sb * 2 + k], st) : cudaSuccess; };
+  CU(mark(0));
+  if (view)
+    CU(launch_setup_views(sd, wm.views.p, nitems, wm.surf.p, ws, st));
+  else
+    CU(launch_setup_shadow(sd, wm.jobs.p, nitems, wm.surf.p, ws, st));
+  CU(mark(1));
+  CU(launch_scan(ws, st));
+  CU(mark(2));
+  CU(launch_fill(ws, wm.surf.p, st));
+  CU(mark(3));
+  CU(launch_raster(ws, wm.surf.p, nsurf, nfine, view, st));
+  CU(mark(4));
+  if (view) {
+    CU(launch_shade(sd, wm.views.p, nitems, wm.surf.p, nfine, ws.srec, st));
+    CU(mark(5));
+  }
+  s->stats.launches += (uint64_t)nst;
+  CU(cudaMemcpyAsync(counter_slot(s, view), ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+  return GBR_OK;
+}
+
+// After the pass's stream is synchronised: record its counters and stage
+// times, and on overflow grow the targets.  Returns true when the pass fit.
+bool check_pass(gbr_scene* s, bool view) {
+  const Counters c = *counter_slot(s, view);
+  WorkMem& w = pass_mem(s, view);
+  if (s->profile) {
+    const int sb = view ? 4 : 0, nst = view ? 5 : 4;
+    for (int k = 0; k < nst; k++) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, s->ev[sb * 2 + k], s->ev[sb * 2 + k + 1]) == cudaSuccess) {
         s->stats.stage_ms[sb + k] += ms;
         s->stats.stage_calls[sb + k] += 1;
       }
     }
-    Counters c = *hc;
-    if (!c.overflow) {
-      if (view) {
-        s->stats.view_records = c.nrec;
-        s->stats.view_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
-        s->stats.fragments_ref = c.frag_ref;
-      } else {
-        s->stats.shadow_records = c.nrec;
-        s->stats.shadow_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
-      }
-      return GBR_OK;
-    }
-    s->stats.retries++;
-    if (c.overflow & 1u) s->ws.rec_target = (uint32_t)std::min<uint64_t>((uint64_t)c.nrec * 5 / 4 + 1024, 0xFFFFFFF0u);
-    uint64_t need_bins = (uint64_t)c.fine_total + c.coarse_total;
-    if (c.overflow & 1u) need_bins = std::max<uint64_t>(need_bins, (uint64_t)s->ws.rec_target * 4);
-    s->ws.bin_target = (uint32_t)std::min<uint64_t>(need_bins * 5 / 4 + 4096, 0xFFFFFFF0u);
   }
-  return fail(GBR_INTERNAL, "scratch kept overflowing after 6 attempts");
+  if (!c.overflow) {
+    if (view) {
+      s->stats.view_records = c.nrec;
+      s->stats.view_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
+      s->stats.fragments_ref = c.frag_ref;
+    } else {
+      s->stats.shadow_records = c.nrec;
+      s->stats.shadow_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
+    }
+    return true;
+  }
+  s->stats.retries++;
+  if (c.overflow & 1u) w.rec_target = (uint32_t)std::min<uint64_t>((uint64_t)c.nrec * 5 / 4 + 1024, 0xFFFFFFF0u);
+  uint64_t need_bins = (uint64_t)c.fine_total + c.coarse_total;
+  if (c.overflow & 1u) need_bins = std::max<uint64_t>(need_bins, (uint64_t)w.rec_target * 4);
+  w.bin_target = (uint32_t)std::min<uint64_t>(need_bins * 5 / 4 + 4096, 0xFFFFFFF0u);
+  return false;
+}
+
+// Run a shadow pass to completion (grow and retry until it fits).
+gbr_status run_shadow_sync(gbr_scene* s, const PassShape& sh, cudaStream_t st) {
+  for (int attempt = 0; attempt < 6; attempt++) {
+    TRY(enqueue_pass(s, false, sh.nitems, sh.nsurf, sh.nfine, sh.ncoarse, 0, st));
+    CU(cudaStreamSynchronize(st));
+    if (check_pass(s, false)) return GBR_OK;
+  }
+  return fail(GBR_INTERNAL, "shadow scratch kept overflowing after 6 attempts");
+}
+
+// Check a shadow pass whose counters are still pending.  Returns true in
+// *rerun when it overflowed and was re-run to completion (so whatever read the
+// cubemaps since must be re-run too).
+gbr_status settle_shadow(gbr_scene* s, bool already_synced, bool* rerun) {
+  *rerun = false;
+  if (!s->shadow_pending) return GBR_OK;
+  if (!already_synced) CU(cudaStreamSynchronize(s->shadow_stream));
+  s->shadow_pending = false;
+  if (check_pass(s, false)) return GBR_OK;
+  TRY(run_shadow_sync(s, s->shadow_shape, s->shadow_stream));
+  *rerun = true;
+  return GBR_OK;
+}
+
+gbr_status settle_shadow_quiet(gbr_scene* s) {
+  bool rerun = false;
+  return settle_shadow(s, false, &rerun);
 }
 
 // texture_context.cpp:94-261: page list and slot descriptors.
@@ -402,7 +467,10 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   cudaDeviceSynchronize();
   s->tris.release(); s->descs.release(); s->lights.release(); s->atlas.release();
   s->nums.release(); s->sizes.release(); s->shadow_dyn.release(); s->shadow_static.release();
-  s->ws.release();
+  s->ws_view.release();
+  s->ws_shadow.release();
+  s->ws_host.release();
+  s->world.release();
   s->staging.release();
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -421,8 +489,11 @@ gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint3
   s->max_object_id = mx;
   s->ntris = n;
   s->static_dirty = true;
-  s->ws.rec_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(s->ws.rec_target, (uint64_t)n + 1024u), 0xFFFFFFF0u);
-  s->ws.bin_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(s->ws.bin_target, 4ull * s->ws.rec_target), 0xFFFFFFF0u);
+  s->world_dirty = true;
+  for (WorkMem* w : {&s->ws_view, &s->ws_shadow}) {
+    w->rec_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(w->rec_target, (uint64_t)n + 1024u), 0xFFFFFFF0u);
+    w->bin_target = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(w->bin_target, 4ull * w->rec_target), 0xFFFFFFF0u);
+  }
   return GBR_OK;
 }
 
@@ -436,6 +507,7 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
   s->max_tid = mt;
   s->ndescs = n;
   s->static_dirty = true;
+  s->world_dirty = true;
   return GBR_OK;
 }
 
@@ -536,6 +608,7 @@ gbr_status gbr_scene_buffer(gbr_scene* s, int32_t which, const void** ptr, size_
 
 gbr_status gbr_scene_read_buffer(gbr_scene* s, int32_t which, void* dst, size_t offset, size_t bytes) {
   TRY(check_scene(s));
+  TRY(settle_shadow_quiet(s));
   const void* p = nullptr;
   size_t total = 0;
   TRY(gbr_scene_buffer(s, which, &p, &total));
@@ -560,6 +633,7 @@ gbr_status gbr_texture_pack(uint32_t n, const int32_t* sizes, uint32_t* nums, ui
 gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
   TRY(check_scene(s));
   cudaStream_t st = (cudaStream_t)stream;
+  TRY(settle_shadow_quiet(s));
   const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
   std::vector<ShadowJob> jobs;
   std::vector<Surface> surfs;
@@ -590,11 +664,23 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
     s->static_dirty = false;
     return GBR_OK;
   }
-  TRY(s->ws.surf.reserve(surfs.size()));
-  TRY(s->ws.jobs.reserve(jobs.size()));
-  CU(cudaMemcpyAsync(s->ws.surf.p, surfs.data(), surfs.size() * sizeof(Surface), cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(s->ws.jobs.p, jobs.data(), jobs.size() * sizeof(ShadowJob), cudaMemcpyHostToDevice, st));
-  TRY(run_pass(s, false, (uint32_t)jobs.size(), (uint32_t)surfs.size(), tb, cb, 0, st));
+  WorkMem& wm = s->ws_shadow;
+  TRY(wm.surf.reserve(surfs.size()));
+  TRY(wm.jobs.reserve(jobs.size()));
+  CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), surfs.size() * sizeof(Surface), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(wm.jobs.p, jobs.data(), jobs.size() * sizeof(ShadowJob), cudaMemcpyHostToDevice, st));
+  // wait for the copies of the small arrays before the host vectors go away
+  PassShape sh;
+  sh.nitems = (uint32_t)jobs.size();
+  sh.nsurf = (uint32_t)surfs.size();
+  sh.nfine = tb;
+  sh.ncoarse = cb;
+  TRY(enqueue_pass(s, false, sh.nitems, sh.nsurf, sh.nfine, sh.ncoarse, 0, st));
+  // The counters are checked at the next synchronisation point (render,
+  // read-back, stats), which re-runs this pass if its scratch overflowed.
+  s->shadow_pending = true;
+  s->shadow_stream = st;
+  s->shadow_shape = sh;
   s->static_dirty = false;
   return GBR_OK;
 }
@@ -618,17 +704,17 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     if (!outs[i].depth) need_depth = true;
     if (!outs[i].id) need_id = true;
   }
-  TRY(s->ws.pix_rec.reserve(npix));
-  if (need_depth) TRY(s->ws.pix_depth.reserve(npix));
+  TRY(s->ws_view.pix_rec.reserve(npix));
+  if (need_depth) TRY(s->ws_view.pix_depth.reserve(npix));
   for (uint32_t i = 0; i < n; i++) {
     const gbr_view& v = views[i];
     Surface& S = surfs[i];
     S.width = v.width;
     S.height = v.height;
     tile_layout(S, tb, cb);
-    S.depth = outs[i].depth ? outs[i].depth : s->ws.pix_depth.p + off;
+    S.depth = outs[i].depth ? outs[i].depth : s->ws_view.pix_depth.p + off;
     S.id = outs[i].id;
-    S.rec = s->ws.pix_rec.p + off;
+    S.rec = s->ws_view.pix_rec.p + off;
     S.chunk = kOpSize;
     ViewParams& V = vp[i];
     memcpy(V.cpos, cams[i].pos, 12);
@@ -643,11 +729,24 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   }
   (void)need_id;
   TRY(check_indices(s, true));
-  TRY(s->ws.surf.reserve(n));
-  TRY(s->ws.views.reserve(n));
-  CU(cudaMemcpyAsync(s->ws.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(s->ws.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, st));
-  return run_pass(s, true, n, n, tb, cb, npix, st);
+  WorkMem& wm = s->ws_view;
+  TRY(wm.surf.reserve(n));
+  TRY(wm.views.reserve(n));
+  CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, st));
+  CU(cudaMemcpyAsync(wm.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, st));
+  if (s->shadow_pending && s->shadow_stream != st) {
+    bool rerun = false;
+    TRY(settle_shadow(s, false, &rerun));
+  }
+  for (int attempt = 0; attempt < 8; attempt++) {
+    TRY(enqueue_pass(s, true, n, n, tb, cb, npix, st));
+    CU(cudaStreamSynchronize(st));
+    bool rerun = false;
+    TRY(settle_shadow(s, true, &rerun));  // same stream: already complete
+    bool fit = check_pass(s, true);
+    if (fit && !rerun) return GBR_OK;
+  }
+  return fail(GBR_INTERNAL, "scratch kept overflowing after 8 attempts");
 }
 
 gbr_status gbr_render_view(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const gbr_outputs* out,
@@ -666,10 +765,11 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   TRY(validate_view(view));
   cudaStream_t st = (cudaStream_t)stream;
   size_t P = (size_t)view->width * view->height;
-  TRY(s->ws.pix_depth.reserve(P));
-  TRY(s->ws.pix_id.reserve(P));
-  TRY(s->ws.pix_rgba.reserve(P * 4));
-  gbr_outputs o{s->ws.pix_depth.p, s->ws.pix_id.p, s->ws.pix_rgba.p, nullptr};
+  WorkMem& hw = s->ws_host;
+  TRY(hw.pix_depth.reserve(P));
+  TRY(hw.pix_id.reserve(P));
+  TRY(hw.pix_rgba.reserve(P * 4));
+  gbr_outputs o{hw.pix_depth.p, hw.pix_id.p, hw.pix_rgba.p, nullptr};
   TRY(render_views(s, 1, cam, view, &o, st));
   if (depth) CU(cudaMemcpyAsync(depth, o.depth, P * 4, cudaMemcpyDeviceToHost, st));
   if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, st));
@@ -692,6 +792,8 @@ gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
 
 gbr_status gbr_scene_stats(gbr_scene* s, gbr_stats* out) {
   if (!s || !out) return fail(GBR_INVALID_ARG, "null argument");
+  TRY(check_scene(s));
+  TRY(settle_shadow_quiet(s));
   *out = s->stats;
   return GBR_OK;
 }

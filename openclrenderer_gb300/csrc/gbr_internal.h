@@ -92,6 +92,10 @@ struct Counters {
 struct SceneDev {
   const gbr_triangle* tris;
   uint32_t ntris;
+  // world-space vertex positions, rot_quat(v * scale, q) + world_pos (the
+  // first half of full_rotate_quat, cl2.cl:700-710); w of vertex 0 holds the
+  // object id.  3 per triangle.
+  const float4* world;
   const gbr_obj_g_descriptor* descs;
   uint32_t ndescs;
   const gbr_light* lights;
@@ -121,6 +125,7 @@ struct Workspace {
 };
 
 // ---- launchers (gbr_kernels.cu) ----
+cudaError_t launch_world(const SceneDev& sc, float4* world, cudaStream_t st);
 cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,

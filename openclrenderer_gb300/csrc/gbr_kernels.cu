@@ -148,24 +148,6 @@ __device__ void emit(const Cand* cands, int n, uint32_t surface, const Surface* 
   if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&ws.ctr->frag_ref, frags);
 }
 
-// full_rotate_quat (cl2.cl:700-729): object -> camera space, clip, project.
-__device__ __forceinline__ int transform_clip(const f3 v[3], const gbr_obj_g_descriptor* G, f3 cpos,
-                                              f3 c, f3 s, float fov, float w, float h,
-                                              f3 out[2][3]) {
-  f4 q = ld4(G->world_rot_quat);
-  f3 wp = ld3(G->world_pos);
-  float scale = __ldg(&G->scale);
-  f3 pr[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) pr[k] = rot_cs(add3(rot_quat(mul3s(v[k], scale), q), wp), cpos, c, s);
-  f3 t[2][3];
-  int n = clip_tri(pr, t);
-  for (int i = 0; i < n; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) out[i][k] = depth_project1(t[i][k], w, h, fov);
-  return n;
-}
-
 __device__ __forceinline__ void load_tri_pos(const gbr_triangle* T, f3 v[3], uint32_t* o_id) {
   const float* base = reinterpret_cast<const float*>(T);
   float4 a = __ldg(reinterpret_cast<const float4*>(base));       // v0.pos
@@ -178,6 +160,66 @@ __device__ __forceinline__ void load_tri_pos(const gbr_triangle* T, f3 v[3], uin
   *o_id = __float_as_uint(b.z);
 }
 
+
+// World-space vertices of every triangle: rot_quat(v * scale, q) + world_pos,
+// the object half of full_rotate_quat (cl2.cl:700-710).  It does not depend on
+// the camera, so one pass serves the view and all cube faces until the
+// triangles or descriptors change.
+__global__ void __launch_bounds__(256) k_world(SceneDev sc, float4* __restrict__ world) {
+  const uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tri >= sc.ntris) return;
+  f3 v[3];
+  uint32_t o_id;
+  load_tri_pos(sc.tris + tri, v, &o_id);
+  const gbr_obj_g_descriptor* G = sc.descs + o_id;
+  const f4 qn = fast_normalize4(ld4(G->world_rot_quat));
+  const f3 wp = ld3(G->world_pos);
+  const float scale = __ldg(&G->scale);
+  float4* out = world + (size_t)tri * 3;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    f3 r = add3(rot_quat_n(mul3s(v[k], scale), qn), wp);
+    out[k] = make_float4(r.x, r.y, r.z, k == 0 ? __uint_as_float(o_id) : 0.0f);
+  }
+}
+
+// World-space vertices of a triangle: from the scene's cache when there is
+// one, else computed here with the same arithmetic as k_world.
+__device__ __forceinline__ void load_world(const SceneDev& sc, uint32_t tri, f3 w[3], uint32_t* o_id) {
+  if (!sc.world) {
+    f3 v[3];
+    load_tri_pos(sc.tris + tri, v, o_id);
+    const gbr_obj_g_descriptor* G = sc.descs + *o_id;
+    const f4 qn = fast_normalize4(ld4(G->world_rot_quat));
+    const f3 wp = ld3(G->world_pos);
+    const float scale = __ldg(&G->scale);
+#pragma unroll
+    for (int k = 0; k < 3; k++) w[k] = add3(rot_quat_n(mul3s(v[k], scale), qn), wp);
+    return;
+  }
+  const float4* p = sc.world + (size_t)tri * 3;
+  float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  w[0] = mk3(a.x, a.y, a.z);
+  w[1] = mk3(b.x, b.y, b.z);
+  w[2] = mk3(c.x, c.y, c.z);
+  *o_id = __float_as_uint(a.w);
+}
+
+// The camera half of full_rotate_quat (cl2.cl:700-729): world -> camera
+// space, near/far clip, projection.
+__device__ __forceinline__ int transform_clip(const f3 w[3], f3 cpos, f3 c, f3 s, float fov, float width,
+                                              float height, f3 out[2][3]) {
+  f3 pr[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) pr[k] = rot_cs(w[k], cpos, c, s);
+  f3 t[2][3];
+  int n = clip_tri(pr, t);
+  for (int i = 0; i < n; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) out[i][k] = depth_project1(t[i][k], width, height, fov);
+  return n;
+}
+
 // prearrange (cl2.cl:4271-4409), one thread per (triangle, view).
 __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewParams* __restrict__ views,
                                                      const Surface* __restrict__ surfs, Workspace ws) {
@@ -187,9 +229,9 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
   Cand cands[2];
   int n = 0;
   if (tri < sc.ntris) {
-    f3 v[3];
+    f3 wv[3];
     uint32_t o_id;
-    load_tri_pos(sc.tris + tri, v, &o_id);
+    load_world(sc, tri, wv, &o_id);
     const gbr_obj_g_descriptor* G = sc.descs + o_id;
     f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
     if (!(fast_length3(sub3(ld3(G->world_pos), cpos)) > kDepthFar)) {
@@ -197,7 +239,7 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
       f3 s = mk3(V.csin[0], V.csin[1], V.csin[2]);
       float w = (float)S.width, h = (float)S.height;
       f3 out[2][3];
-      int num = transform_clip(v, G, cpos, c, s, V.fov, w, h, out);
+      int num = transform_clip(wv, cpos, c, s, V.fov, w, h, out);
       bool two = (__ldg(&G->feature_flag) & kFlagTwoSided) > 0;
       for (int i = 0; i < num; i++) {
         Cand& cd = cands[n];
@@ -217,25 +259,19 @@ __global__ void __launch_bounds__(256) k_setup_shadow(SceneDev sc, const ShadowJ
   const ShadowJob& J = jobs[blockIdx.y];
   const float L = (float)kLightBufferDim;
   int mask = 0;
-  f3 v[3];
-  const gbr_obj_g_descriptor* G = nullptr;
+  f3 wv[3];
   f3 lpos = mk3(J.lpos[0], J.lpos[1], J.lpos[2]);
   bool two = false;
   if (tri < sc.ntris) {
     uint32_t o_id;
-    load_tri_pos(sc.tris + tri, v, &o_id);
-    G = sc.descs + o_id;
+    load_world(sc, tri, wv, &o_id);
+    const gbr_obj_g_descriptor* G = sc.descs + o_id;
     int ff = __ldg(&G->feature_flag);
     bool is_static = (ff & kFlagIsStatic) > 0;
     two = (ff & kFlagTwoSided) > 0;
     f3 wp = ld3(G->world_pos);
     if (is_static == (J.only_static != 0) && !(fast_length3(sub3(wp, lpos)) > kDepthFar)) {
-      f4 q = ld4(G->world_rot_quat);
-      float scale = __ldg(&G->scale);
-      for (int k = 0; k < 3; k++) {
-        f3 r = add3(rot_quat(mul3s(v[k], scale), q), wp);
-        mask |= 1 << ret_cubeface(r, lpos);
-      }
+      for (int k = 0; k < 3; k++) mask |= 1 << ret_cubeface(wv[k], lpos);
     }
   }
   for (int face = 0; face < 6; face++) {
@@ -245,7 +281,7 @@ __global__ void __launch_bounds__(256) k_setup_shadow(SceneDev sc, const ShadowJ
       f3 c = mk3(sc.face_cos[face][0], sc.face_cos[face][1], sc.face_cos[face][2]);
       f3 s = mk3(sc.face_sin[face][0], sc.face_sin[face][1], sc.face_sin[face][2]);
       f3 out[2][3];
-      int num = transform_clip(v, G, lpos, c, s, kLFov, L, L, out);
+      int num = transform_clip(wv, lpos, c, s, kLFov, L, L, out);
       for (int i = 0; i < num; i++) {
         Cand& cd = cands[n];
         cd.p[0] = out[i][0]; cd.p[1] = out[i][1]; cd.p[2] = out[i][2];
@@ -495,29 +531,45 @@ struct ShadeCtx {
   const Surface* S;
 };
 
-__device__ __forceinline__ float depth_to_dist(uint32_t d) { return fdiv((float)d, kMulInt) * kDepthFar; }
+// (float)d / 2^32 * 350000: the division by 2^32 only shifts the exponent
+// (no rounding, no underflow for d >= 1), so it is a multiplication by 2^-32.
+constexpr float kInvMulInt = 2.3283064365386963e-10f;
+__device__ __forceinline__ float depth_to_dist(uint32_t d) { return ((float)d * kInvMulInt) * kDepthFar; }
 
-__device__ __forceinline__ f4 read_tex_pre(const SceneDev& sc, float cx, float cy, int which, int slice,
-                                           float width) {
+// read_tex_array_all_precalculated (cl2.cl:823-851) with the slot origin
+// (tnumx, tnumy), which does not depend on the coordinates, computed once per
+// bilinear footprint.
+struct TexSlot {
+  float tnumx, tnumy, width;
+  const uchar4* page;
+};
+__device__ __forceinline__ TexSlot tex_slot_pre(const SceneDev& sc, int which, int slice, float width) {
   const float imax = 1.0f / 2048.0f;
   float ihnum = width * imax;
-  float tnumy = floorf((float)which * ihnum);
-  float tnumx = (float)which - fdiv(tnumy, ihnum);
-  cx = clampf_(cx, 0.001f, width - 0.001f);
-  cy = clampf_(cy, 0.001f, width - 0.001f);
-  int ix = f2i_sat(fma_(tnumx, width, cx));
-  int iy = f2i_sat(fma_(tnumy, width, cy));
-  uchar4 t = __ldg(sc.atlas + ((size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix));
+  TexSlot t;
+  t.tnumy = floorf((float)which * ihnum);
+  t.tnumx = (float)which - fdiv(t.tnumy, ihnum);
+  t.width = width;
+  t.page = sc.atlas + (size_t)slice * kTexPage * kTexPage;
+  return t;
+}
+__device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy) {
+  cx = clampf_(cx, 0.001f, ts.width - 0.001f);
+  cy = clampf_(cy, 0.001f, ts.width - 0.001f);
+  int ix = f2i_sat(fma_(ts.tnumx, ts.width, cx));
+  int iy = f2i_sat(fma_(ts.tnumy, ts.width, cy));
+  uchar4 t = __ldg(ts.page + ((size_t)iy * kTexPage + ix));
   f4 r; r.x = t.x; r.y = t.y; r.z = t.z; r.w = t.w;
   return r;
 }
 
 __device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, int slice, float width) {
+  const TexSlot ts = tex_slot_pre(sc, which, slice, width);
   float posx = floorf(mx), posy = floorf(my);
-  f4 c0 = read_tex_pre(sc, posx, posy, which, slice, width);
-  f4 c1 = read_tex_pre(sc, posx + 1, posy, which, slice, width);
-  f4 c2 = read_tex_pre(sc, posx, posy + 1, which, slice, width);
-  f4 c3 = read_tex_pre(sc, posx + 1, posy + 1, which, slice, width);
+  f4 c0 = read_tex_pre(ts, posx, posy);
+  f4 c1 = read_tex_pre(ts, posx + 1, posy);
+  f4 c2 = read_tex_pre(ts, posx, posy + 1);
+  f4 c3 = read_tex_pre(ts, posx + 1, posy + 1);
   float ux = mx - posx, uy = my - posy;
   float bx = 1.0f - ux, by = 1.0f - uy;
   f4 r;
@@ -561,7 +613,7 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
 // generate_ssao (cl2.cl:2194-2260)
 __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth, int W, int H, float fov) {
   uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)W * (uint32_t)H * (uint32_t)y));
-  float foffset = fdiv((float)seed2, kMulInt);
+  float foffset = (float)seed2 * kInvMulInt;
   float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
   float rad = kSsaoRad + fdiv(foffset, 2.0f);
   float world_rad = fdiv(rad * fov, dep);
@@ -750,8 +802,8 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)y * (uint32_t)W * (uint32_t)H));
   uint32_t seed3 = rand_xorshift(seed2);
   uint32_t seed4 = rand_xorshift(seed3);
-  f3 rseed = mk3((fdiv((float)seed2, kMulInt) - 0.5f) * 2.0f, (fdiv((float)seed3, kMulInt) - 0.5f) * 2.0f,
-                 (fdiv((float)seed4, kMulInt) - 0.5f) * 2.0f);
+  f3 rseed = mk3(((float)seed2 * kInvMulInt - 0.5f) * 2.0f, ((float)seed3 * kInvMulInt - 0.5f) * 2.0f,
+                 ((float)seed4 * kInvMulInt - 0.5f) * 2.0f);
   const f3 l2p = cnormalize(sub3(cpos, gpos));
   const int ff = __ldg(&G->feature_flag);
   const bool two = (ff & kFlagTwoSided) > 0;
@@ -953,6 +1005,12 @@ int num_sms() {
 }
 
 }  // namespace
+
+cudaError_t launch_world(const SceneDev& sc, float4* world, cudaStream_t st) {
+  if (!sc.ntris) return cudaSuccess;
+  k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st) {

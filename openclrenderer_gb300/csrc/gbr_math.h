@@ -19,7 +19,8 @@
 //   float -> uint       -> truncation, saturating to [0, UINT_MAX], NaN -> 0
 //   pow(x, n), n small integer -> repeated multiplication
 //   tan (shadow bias)   -> gbr_tanf below (Taylor series of sin and cos)
-//   denormals           -> flushed (nvcc -ftz=true; host sets FTZ/DAZ)
+//   denormals           -> kept (IEEE) on both sides; the reference flushes them,
+//                          but no denormal reaches the depth or id arithmetic
 //
 // Everything here is plain arithmetic written for this project; nothing is
 // taken from CUDA's math library.
@@ -163,6 +164,14 @@ GBR_HD f3 rot_quat(f3 p, f4 q) {
   f3 qv = mk3(q.x, q.y, q.z);
   f3 t = smul3(2.0f, cross3(qv, p));
   return add3(add3(p, smul3(q.w, t)), cross3(qv, t));
+}
+
+// rot_quat with the normalisation of q already done (qn = fast_normalize4(q)):
+// the same arithmetic, for callers that rotate several points by one q.
+GBR_HD f3 rot_quat_n(f3 p, f4 qn) {
+  f3 qv = mk3(qn.x, qn.y, qn.z);
+  f3 t = smul3(2.0f, cross3(qv, p));
+  return add3(add3(p, smul3(qn.w, t)), cross3(qv, t));
 }
 
 // Inverse quaternion rotation (cl2.cl:359-370, back_rot_quat).
