@@ -40,6 +40,24 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
   return v;
 }
 
+// Warp-aggregated "atomicAdd(&counter[key], 1)": lanes with the same key
+// share one atomic.  Every lane of the warp must call it; inactive lanes pass
+// active = false.  Returns this lane's old value + its rank within its key.
+__device__ __forceinline__ uint32_t agg_inc(uint32_t* counter, uint32_t key, bool active) {
+  const unsigned act = __ballot_sync(0xFFFFFFFFu, active);
+  uint32_t res = 0;
+  if (active) {
+    const int lane = threadIdx.x & 31;
+    const unsigned grp = __match_any_sync(act, key);
+    const int leader = __ffs(grp) - 1;
+    uint32_t old = 0;
+    if (lane == leader) old = atomicAdd(&counter[key], (uint32_t)__popc(grp));
+    old = __shfl_sync(grp, old, leader);
+    res = old + (uint32_t)__popc(grp & ((1u << lane) - 1u));
+  }
+  return res;
+}
+
 // A visible clipped triangle before it becomes a record.
 struct Cand {
   f3 p[3];
@@ -95,6 +113,13 @@ struct Foot {
   int tx0, tx1, ty0, ty1;  // inclusive fine tiles
   bool coarse;
 };
+__device__ __forceinline__ int foot_count(const Foot& f) { return (f.tx1 - f.tx0 + 1) * (f.ty1 - f.ty0 + 1); }
+// Global tile index (fine or coarse counter array) of the k-th tile of a footprint.
+__device__ __forceinline__ uint32_t foot_tile(const Foot& f, int k, const Surface& S) {
+  const int w = f.tx1 - f.tx0 + 1;
+  const int ty = f.ty0 + k / w, tx = f.tx0 + k % w;
+  return f.coarse ? S.ctile_base + ty * S.ctiles_x + tx : S.tile_base + ty * S.tiles_x + tx;
+}
 __device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr) {
   Foot f;
   int minx = xr & 0xFFFF, maxx = xr >> 16, miny = yr & 0xFFFF, maxy = yr >> 16;
@@ -115,6 +140,8 @@ __device__ void emit(const Cand* cands, int n, uint32_t surface, const Surface* 
   uint32_t base = warp_alloc(&ws.ctr->nrec, (uint32_t)n);
   unsigned long long frags = 0;
   const Surface& S = surfs[surface];
+  Foot feet[2];
+  int nt[2] = {0, 0};
   for (int i = 0; i < n; i++) {
     uint32_t r = base + i;
     const Cand& c = cands[i];
@@ -133,16 +160,23 @@ __device__ void emit(const Cand* cands, int n, uint32_t surface, const Surface* 
       ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
       ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
     }
-    Foot f = footprint(R.xr, R.yr);
-    if (!f.coarse) {
-      for (int ty = f.ty0; ty <= f.ty1; ty++)
-        for (int tx = f.tx0; tx <= f.tx1; tx++)
-          atomicAdd(&ws.fine_count[S.tile_base + ty * S.tiles_x + tx], 1u);
-    } else {
-      for (int ty = f.ty0; ty <= f.ty1; ty++)
-        for (int tx = f.tx0; tx <= f.tx1; tx++)
-          atomicAdd(&ws.coarse_count[S.ctile_base + ty * S.ctiles_x + tx], 1u);
-    }
+    feet[i] = footprint(R.xr, R.yr);
+    nt[i] = foot_count(feet[i]);
+  }
+  // tile counts, aggregated across the warp (neighbouring triangles usually
+  // share tiles): iterate over this lane's (record, tile) pairs in lockstep
+  const int total = nt[0] + nt[1];
+  int maxt = total;
+  for (int o = 16; o > 0; o >>= 1) maxt = max(maxt, __shfl_xor_sync(0xFFFFFFFFu, maxt, o));
+  for (int it = 0; it < maxt; it++) {
+    const bool act = it < total;
+    const int i = act && it >= nt[0] ? 1 : 0;
+    const int k = act ? (i ? it - nt[0] : it) : 0;
+    const bool coarse = act && feet[i].coarse;
+    const uint32_t tile = act ? foot_tile(feet[i], k, S) : 0u;
+    // fine and coarse counters live in different arrays: aggregate them separately
+    agg_inc(ws.fine_count, tile, act && !coarse);
+    agg_inc(ws.coarse_count, tile, act && coarse);
   }
   frags = warp_sum_u64(frags);
   if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&ws.ctr->frag_ref, frags);
@@ -331,30 +365,36 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Workspace ws) {
   }
 }
 
-// Scatter record indices into their tile bins.
+// Scatter record indices into their tile bins (cursor atomics aggregated
+// across the warp).
 __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __restrict__ surfs) {
-  uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
+  const uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
   if (ws.ctr->overflow) return;
-  uint32_t coarse_base = ws.ctr->fine_total;
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
-    float4 q = __ldg(reinterpret_cast<const float4*>(ws.rec + r) + 3);
-    uint32_t xr = __float_as_uint(q.x), yr = __float_as_uint(q.y), sid = __float_as_uint(q.z);
-    const Surface& S = surfs[sid];
-    Foot f = footprint(xr, yr);
-    if (!f.coarse) {
-      for (int ty = f.ty0; ty <= f.ty1; ty++)
-        for (int tx = f.tx0; tx <= f.tx1; tx++) {
-          uint32_t t = S.tile_base + ty * S.tiles_x + tx;
-          uint32_t pos = ws.fine_off[t] + atomicAdd(&ws.fine_count[t], 1u);
-          ws.bins[pos] = r;
-        }
-    } else {
-      for (int ty = f.ty0; ty <= f.ty1; ty++)
-        for (int tx = f.tx0; tx <= f.tx1; tx++) {
-          uint32_t t = S.ctile_base + ty * S.ctiles_x + tx;
-          uint32_t pos = coarse_base + ws.coarse_off[t] + atomicAdd(&ws.coarse_count[t], 1u);
-          ws.bins[pos] = r;
-        }
+  const uint32_t coarse_base = ws.ctr->fine_total;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t r0 = blockIdx.x * blockDim.x; r0 < nrec; r0 += stride) {
+    const uint32_t r = r0 + threadIdx.x;
+    const bool valid = r < nrec;
+    Foot f{0, 0, 0, 0, false};
+    const Surface* S = surfs;
+    int total = 0;
+    if (valid) {
+      float4 q = __ldg(reinterpret_cast<const float4*>(ws.rec + r) + 3);
+      S = surfs + __float_as_uint(q.z);
+      f = footprint(__float_as_uint(q.x), __float_as_uint(q.y));
+      total = foot_count(f);
+    }
+    int maxt = total;
+    for (int o = 16; o > 0; o >>= 1) maxt = max(maxt, __shfl_xor_sync(0xFFFFFFFFu, maxt, o));
+    for (int it = 0; it < maxt; it++) {
+      const bool act = it < total;
+      const uint32_t tile = act ? foot_tile(f, it, *S) : 0u;
+      const uint32_t pf = agg_inc(ws.fine_count, tile, act && !f.coarse);
+      const uint32_t pc = agg_inc(ws.coarse_count, tile, act && f.coarse);
+      if (act) {
+        const uint32_t pos = f.coarse ? coarse_base + ws.coarse_off[tile] + pc : ws.fine_off[tile] + pf;
+        ws.bins[pos] = r;
+      }
     }
   }
 }
