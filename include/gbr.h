@@ -152,7 +152,7 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* scene, const gbr_obj_g_descripto
 
 /* light::build (light.cpp:145-276): active lights and the shadow cubemaps
  * (6 * 1024^2 u32 per shadow-casting light, dynamic and static). Host array. */
-gbr_status gbr_scene_set_lights(gbr_scene* scene, const gbr_light* lights, uint32_t n);
+gbr_status gbr_scene_set_lights(gbr_scene* scene, const gbr_light* lights, uint32_t n); /* n <= 256 */
 
 /* texture_context::alloc_gpu (texture_context.cpp:350-517): pack n square RGBA8
  * textures (edge sizes[i], pixels rgba[i], in gpu-id order) into 2048^2 pages,

@@ -514,6 +514,7 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
 gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
   TRY(check_scene(s));
   if (n && !l) return fail(GBR_INVALID_ARG, "null lights");
+  if (n > (uint32_t)kMaxLights) return fail(GBR_INVALID_ARG, "%u lights: at most %d", n, kMaxLights);
   for (uint32_t i = 0; i < n; i++)
     if (l[i].shadow > 1) return fail(GBR_INVALID_ARG, "light %u: shadow must be 0 or 1", i);
   s->host_lights.assign(l, l + n);

@@ -28,6 +28,7 @@ constexpr int kCoarse = 128;                 // coarse tile edge, pixels
 constexpr int kCoarseRatio = kCoarse / kTile;
 constexpr int kFineMaxTiles = 16;            // more fine tiles than this -> coarse bins
 constexpr int kRasterThreads = kTile * kTile;
+constexpr int kMaxLights = 256;              // lights a scene may hold (staged in shared memory)
 
 // Per visible clipped triangle on one surface: everything kernel1/kernel2
 // need per pixel, precomputed once (64 bytes).

@@ -133,51 +133,62 @@ __device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr) {
   return f;
 }
 
-// Append the candidates of this lane (0..2) as records and count their bins.
-// Every lane of the warp must call it.
-__device__ void emit(const Cand* cands, int n, uint32_t surface, const Surface* surfs,
-                     const Workspace& ws, bool view) {
-  uint32_t base = warp_alloc(&ws.ctr->nrec, (uint32_t)n);
+// One candidate as a record (and shade record for views); returns its tile footprint.
+__device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t surface, const Workspace& ws, bool view,
+                                         Foot* foot) {
+  RasterRec R;
+  make_rec(c, surface, R);
+  store_rec(ws.rec + r, R);
+  if (view) {
+    uint32_t tri = c.key >> 1;
+    ws.srec[r].p0 = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.rc);
+    ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
+    ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
+  }
+  *foot = footprint(R.xr, R.yr);
+  return foot_count(*foot);
+}
+
+// Append this lane's candidates (n = 0, 1 or 2: c0, then c1) as records and
+// count their bins.  Every lane of the warp must call it.  Returns this lane's
+// reference fragment count (sum of ceil(area / chunk)).
+__device__ unsigned long long emit(const Cand& c0, const Cand& c1, int n, uint32_t surface, const Surface* surfs,
+                                   const Workspace& ws, bool view) {
+  const uint32_t base = warp_alloc(&ws.ctr->nrec, (uint32_t)n);
   unsigned long long frags = 0;
   const Surface& S = surfs[surface];
-  Foot feet[2];
-  int nt[2] = {0, 0};
-  for (int i = 0; i < n; i++) {
-    uint32_t r = base + i;
-    const Cand& c = cands[i];
-    float area = (c.mm[1] - c.mm[0]) * (c.mm[3] - c.mm[2]);
-    frags += (unsigned long long)ceilf(fdiv(area, (float)S.chunk));
-    if (r >= ws.rec_cap) {
-      atomicOr(&ws.ctr->overflow, 1u);
-      continue;
-    }
-    RasterRec R;
-    make_rec(c, surface, R);
-    store_rec(ws.rec + r, R);
-    if (view) {
-      uint32_t tri = c.key >> 1;
-      ws.srec[r].p0 = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.rc);
-      ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
-      ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
-    }
-    feet[i] = footprint(R.xr, R.yr);
-    nt[i] = foot_count(feet[i]);
+  Foot f0{0, 0, 0, 0, false}, f1{0, 0, 0, 0, false};
+  int n0 = 0, n1 = 0;
+  if (n > 0) {
+    frags += (unsigned long long)ceilf(fdiv((c0.mm[1] - c0.mm[0]) * (c0.mm[3] - c0.mm[2]), (float)S.chunk));
+    if (base < ws.rec_cap) n0 = write_rec(c0, base, surface, ws, view, &f0);
+    else atomicOr(&ws.ctr->overflow, 1u);
+  }
+  if (n > 1) {
+    frags += (unsigned long long)ceilf(fdiv((c1.mm[1] - c1.mm[0]) * (c1.mm[3] - c1.mm[2]), (float)S.chunk));
+    if (base + 1 < ws.rec_cap) n1 = write_rec(c1, base + 1, surface, ws, view, &f1);
+    else atomicOr(&ws.ctr->overflow, 1u);
   }
   // tile counts, aggregated across the warp (neighbouring triangles usually
   // share tiles): iterate over this lane's (record, tile) pairs in lockstep
-  const int total = nt[0] + nt[1];
+  const int total = n0 + n1;
   int maxt = total;
   for (int o = 16; o > 0; o >>= 1) maxt = max(maxt, __shfl_xor_sync(0xFFFFFFFFu, maxt, o));
   for (int it = 0; it < maxt; it++) {
     const bool act = it < total;
-    const int i = act && it >= nt[0] ? 1 : 0;
-    const int k = act ? (i ? it - nt[0] : it) : 0;
-    const bool coarse = act && feet[i].coarse;
-    const uint32_t tile = act ? foot_tile(feet[i], k, S) : 0u;
+    const bool second = it >= n0;
+    const Foot& f = second ? f1 : f0;
+    const int k = second ? it - n0 : it;
+    const bool coarse = act && f.coarse;
+    const uint32_t tile = act ? foot_tile(f, k, S) : 0u;
     // fine and coarse counters live in different arrays: aggregate them separately
     agg_inc(ws.fine_count, tile, act && !coarse);
     agg_inc(ws.coarse_count, tile, act && coarse);
   }
+  return frags;
+}
+
+__device__ __forceinline__ void add_frags(const Workspace& ws, unsigned long long frags) {
   frags = warp_sum_u64(frags);
   if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&ws.ctr->frag_ref, frags);
 }
@@ -242,15 +253,35 @@ __device__ __forceinline__ void load_world(const SceneDev& sc, uint32_t tri, f3 
 // The camera half of full_rotate_quat (cl2.cl:700-729): world -> camera
 // space, near/far clip, projection.
 __device__ __forceinline__ int transform_clip(const f3 w[3], f3 cpos, f3 c, f3 s, float fov, float width,
-                                              float height, f3 out[2][3]) {
-  f3 pr[3];
+                                              float height, f3 o0[3], f3 o1[3]) {
+  f3 t0[3], t1[3];
+  const int n = clip_tri_reg(rot_cs(w[0], cpos, c, s), rot_cs(w[1], cpos, c, s), rot_cs(w[2], cpos, c, s), t0, t1);
 #pragma unroll
-  for (int k = 0; k < 3; k++) pr[k] = rot_cs(w[k], cpos, c, s);
-  f3 t[2][3];
-  int n = clip_tri(pr, t);
-  for (int i = 0; i < n; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) out[i][k] = depth_project1(t[i][k], width, height, fov);
+  for (int k = 0; k < 3; k++) {
+    o0[k] = depth_project1(t0[k], width, height, fov);
+    o1[k] = depth_project1(t1[k], width, height, fov);
+  }
+  return n;
+}
+
+// prearrange's handling of one (triangle, surface): up to two clip outputs,
+// culled, as candidates c0 (first survivor) and c1.
+__device__ __forceinline__ int make_cands(const f3 w[3], f3 cpos, f3 c, f3 s, float fov, float width, float height,
+                                          bool two, uint32_t tri, Cand& c0, Cand& c1) {
+  f3 o0[3], o1[3];
+  const int num = transform_clip(w, cpos, c, s, fov, width, height, o0, o1);
+  int n = 0;
+  if (num > 0) {
+    c0.p[0] = o0[0]; c0.p[1] = o0[1]; c0.p[2] = o0[2];
+    c0.key = tri * 2u;
+    if (cull_candidate(c0, two, width, height)) n = 1;
+  }
+  if (num > 1) {
+    Cand& d = n ? c1 : c0;
+    d.p[0] = o1[0]; d.p[1] = o1[1]; d.p[2] = o1[2];
+    d.key = tri * 2u + 1u;
+    if (cull_candidate(d, two, width, height)) n++;
+  }
   return n;
 }
 
@@ -260,7 +291,7 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
   uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
   const ViewParams& V = views[blockIdx.y];
   const Surface& S = surfs[V.surface];
-  Cand cands[2];
+  Cand c0, c1;
   int n = 0;
   if (tri < sc.ntris) {
     f3 wv[3];
@@ -271,23 +302,15 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
     if (!(fast_length3(sub3(ld3(G->world_pos), cpos)) > kDepthFar)) {
       f3 c = mk3(V.ccos[0], V.ccos[1], V.ccos[2]);
       f3 s = mk3(V.csin[0], V.csin[1], V.csin[2]);
-      float w = (float)S.width, h = (float)S.height;
-      f3 out[2][3];
-      int num = transform_clip(wv, cpos, c, s, V.fov, w, h, out);
-      bool two = (__ldg(&G->feature_flag) & kFlagTwoSided) > 0;
-      for (int i = 0; i < num; i++) {
-        Cand& cd = cands[n];
-        cd.p[0] = out[i][0]; cd.p[1] = out[i][1]; cd.p[2] = out[i][2];
-        cd.key = tri * 2u + (uint32_t)i;
-        if (cull_candidate(cd, two, w, h)) n++;
-      }
+      const bool two = (__ldg(&G->feature_flag) & kFlagTwoSided) > 0;
+      n = make_cands(wv, cpos, c, s, V.fov, (float)S.width, (float)S.height, two, tri, c0, c1);
     }
   }
-  emit(cands, n, V.surface, surfs, ws, true);
+  add_frags(ws, emit(c0, c1, n, V.surface, surfs, ws, true));
 }
 
 // prearrange_realtime_shadowing (cl2.cl:4419-4636), one thread per (triangle, light job).
-__global__ void __launch_bounds__(256) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
+__global__ void __launch_bounds__(256, 3) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
                                                       const Surface* __restrict__ surfs, Workspace ws) {
   uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
   const ShadowJob& J = jobs[blockIdx.y];
@@ -308,57 +331,92 @@ __global__ void __launch_bounds__(256) k_setup_shadow(SceneDev sc, const ShadowJ
       for (int k = 0; k < 3; k++) mask |= 1 << ret_cubeface(wv[k], lpos);
     }
   }
+  unsigned long long frags = 0;
   for (int face = 0; face < 6; face++) {
-    Cand cands[2];
+    if (!__any_sync(0xFFFFFFFFu, mask & (1 << face))) continue;  // warp-uniform
+    Cand c0, c1;
     int n = 0;
     if (mask & (1 << face)) {
       f3 c = mk3(sc.face_cos[face][0], sc.face_cos[face][1], sc.face_cos[face][2]);
       f3 s = mk3(sc.face_sin[face][0], sc.face_sin[face][1], sc.face_sin[face][2]);
-      f3 out[2][3];
-      int num = transform_clip(wv, lpos, c, s, kLFov, L, L, out);
-      for (int i = 0; i < num; i++) {
-        Cand& cd = cands[n];
-        cd.p[0] = out[i][0]; cd.p[1] = out[i][1]; cd.p[2] = out[i][2];
-        cd.key = tri * 2u + (uint32_t)i;
-        if (cull_candidate(cd, two, L, L)) n++;
-      }
+      n = make_cands(wv, lpos, c, s, kLFov, L, L, two, tri, c0, c1);
     }
-    emit(cands, n, J.surface_base + face, surfs, ws, false);
+    frags += emit(c0, c1, n, J.surface_base + face, surfs, ws, false);
   }
+  add_frags(ws, frags);
 }
 
-// Exclusive scan of fine and coarse tile counts (one block); counts are reset
-// to zero to serve as fill cursors.
+// Exclusive scan of fine and coarse tile counts (one block of 1024 threads);
+// counts are reset to zero to serve as fill cursors.  Rounds of 8192 counts
+// are staged in shared memory with coalesced loads, each thread scans 8
+// contiguous values, and a block scan joins the threads.
 constexpr int kScanThreads = 1024;
-__device__ void block_scan_array(uint32_t* count, uint32_t* off, uint32_t n, uint32_t* total,
-                                 uint32_t* sh) {
-  uint32_t per = (n + kScanThreads - 1) / kScanThreads;
-  uint32_t b = threadIdx.x * per, e = min(n, b + per);
-  uint32_t s = 0;
-  for (uint32_t i = b; i < e; i++) s += count[i];
-  sh[threadIdx.x] = s;
+constexpr int kScanPer = 8;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+__device__ __forceinline__ uint32_t block_scan_1024(uint32_t v, uint32_t* swarp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) swarp[warp] = incl;
   __syncthreads();
-  for (int o = 1; o < kScanThreads; o <<= 1) {
-    uint32_t v = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+  if (warp == 0) {
+    const uint32_t w = swarp[lane];
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+      if (lane >= o) wi += t;
+    }
+    swarp[lane] = wi - w;
+    if (lane == 31) *total = wi;
+  }
+  __syncthreads();
+  return swarp[warp] + incl - v;
+}
+
+__device__ void block_scan_array(uint32_t* count, uint32_t* off, uint32_t n, uint32_t* total, uint32_t* sh,
+                                 uint32_t* swarp, uint32_t* sctot) {
+  uint32_t carry = 0;
+  for (uint32_t c0 = 0; c0 < n; c0 += kScanChunk) {
+    const uint32_t m = min((uint32_t)kScanChunk, n - c0);
+    for (uint32_t i = threadIdx.x; i < (uint32_t)kScanChunk; i += kScanThreads) sh[i] = i < m ? count[c0 + i] : 0u;
     __syncthreads();
-    sh[threadIdx.x] += v;
+    uint32_t v[kScanPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      v[k] = sh[threadIdx.x * kScanPer + k];
+      sum += v[k];
+    }
+    const uint32_t excl = block_scan_1024(sum, swarp, sctot);
+    uint32_t run = carry + excl;
+#pragma unroll
+    for (int k = 0; k < kScanPer; k++) {
+      sh[threadIdx.x * kScanPer + k] = run;
+      run += v[k];
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < m; i += kScanThreads) {
+      off[c0 + i] = sh[i];
+      count[c0 + i] = 0;
+    }
+    carry += *sctot;
     __syncthreads();
   }
-  uint32_t run = sh[threadIdx.x] - s;
-  for (uint32_t i = b; i < e; i++) {
-    uint32_t c = count[i];
-    off[i] = run;
-    run += c;
-    count[i] = 0;
-  }
-  if (threadIdx.x == kScanThreads - 1) *total = sh[threadIdx.x];
-  __syncthreads();
+  if (threadIdx.x == 0) *total = carry;
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(Workspace ws) {
-  __shared__ uint32_t sh[kScanThreads];
-  block_scan_array(ws.fine_count, ws.fine_off, ws.nfine, &ws.ctr->fine_total, sh);
-  block_scan_array(ws.coarse_count, ws.coarse_off, ws.ncoarse, &ws.ctr->coarse_total, sh);
+  __shared__ uint32_t sh[kScanChunk];
+  __shared__ uint32_t swarp[32];
+  __shared__ uint32_t sctot;
+  block_scan_array(ws.fine_count, ws.fine_off, ws.nfine, &ws.ctr->fine_total, sh, swarp, &sctot);
+  block_scan_array(ws.coarse_count, ws.coarse_off, ws.ncoarse, &ws.ctr->coarse_total, sh, swarp, &sctot);
+  __syncthreads();
   if (threadIdx.x == 0) {
     uint64_t need = (uint64_t)ws.ctr->fine_total + ws.ctr->coarse_total;
     if (need > ws.bin_cap) ws.ctr->overflow |= 2u;
@@ -650,27 +708,32 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
   return r;
 }
 
-// generate_ssao (cl2.cl:2194-2260)
+// generate_ssao (cl2.cl:2194-2260).  The 25 taps share 5 rows and 5
+// columns, so their rounded and clamped offsets are computed once; the depth
+// thresholds dep + z are computed once; and the count (at most 125, exact in
+// float) is kept in an integer.
 __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth, int W, int H, float fov) {
   uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)W * (uint32_t)H * (uint32_t)y));
   float foffset = (float)seed2 * kInvMulInt;
   float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
   float rad = kSsaoRad + fdiv(foffset, 2.0f);
   float world_rad = fdiv(rad * fov, dep);
-  float acc = 0.0f;
+  int wx[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) wx[k] = (int)clampf_((float)x + roundf((float)(k - 2) * world_rad), 1.0f, (float)W - 2.0f);
+  int acc = 0;
+#pragma unroll 1
   for (int yy = -2; yy <= 2; yy++) {
-    float oy = roundf((float)yy * world_rad);
-    int wy = (int)clampf_((float)y + oy, 1.0f, (float)H - 2.0f);
-    for (int xx = -2; xx <= 2; xx++) {
-      float ox = roundf((float)xx * world_rad);
-      int wx = (int)clampf_((float)x + ox, 1.0f, (float)W - 2.0f);
-      float d2 = depth_to_dist(__ldg(depth + (size_t)wy * W + wx));
-      for (float z = -2.0f; z <= 2.0f; z += 1.0f)
-        if (d2 > dep + z) acc += 1.0f;
+    const int wy = (int)clampf_((float)y + roundf((float)yy * world_rad), 1.0f, (float)H - 2.0f);
+    const uint32_t* row = depth + (size_t)wy * W;
+#pragma unroll
+    for (int xx = 0; xx < 5; xx++) {
+      const float d2 = depth_to_dist(__ldg(row + wx[xx]));
+      acc += (d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f);
     }
   }
-  acc = fdiv(acc, 125.0f);
-  return 1.0f - fdiv(1.0f - acc, kSsaoDiv);
+  const float facc = fdiv((float)acc, 125.0f);
+  return 1.0f - fdiv(1.0f - facc, kSsaoDiv);
 }
 
 __device__ __forceinline__ float bilinear_interpolate(float cx, float cy, float v0, float v1, float v2,
@@ -751,9 +814,21 @@ __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a
 }
 
 
+// A light as the shade loop reads it, staged once per CTA in shared memory;
+// col is already in linear space when the view renders linearly (the same
+// gamma_fwd every pixel would apply).
+struct SLight {
+  float px, py, pz, brightness;
+  float cr, cg, cb, radius;
+  float diffuse;
+  uint32_t shadow;
+  int32_t is_static;
+  uint32_t pad;
+};
+
 // kernel3 (cl2.cl:5792-6408) for one pixel of a view.
 __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
-                            const ShadeRec* __restrict__ srec, int x, int y) {
+                            const ShadeRec* __restrict__ srec, const SLight* __restrict__ lights, int x, int y) {
   const int W = S.width, H = S.height;
   const size_t p = (size_t)y * W + x;
   const uint32_t d = S.depth[p];
@@ -858,10 +933,10 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 dsum = mk3(0, 0, 0), ssum = mk3(0, 0, 0);
   int shnum = 0, static_num = 0;
   for (uint32_t i = 0; i < sc.nlights; i++) {
-    const gbr_light* L = sc.lights + i;
-    const f3 lpos = ld3(L->pos);
-    const uint32_t lshadow = __ldg(&L->shadow);
-    const int lstatic = __ldg(&L->is_static);
+    const SLight& L = lights[i];
+    const f3 lpos = mk3(L.px, L.py, L.pz);
+    const uint32_t lshadow = L.shadow;
+    const int lstatic = L.is_static;
     f3 ptl = sub3(lpos, gpos);
     float occlusion = 1.0f;
     if (lshadow && lstatic) {
@@ -870,14 +945,13 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       static_num++;
     }
     float distance = fast_length3(ptl);
-    float tt = cdiv(distance, __ldg(&L->radius)) + 1.0f;
-    float illum = cdiv(__ldg(&L->brightness), tt * tt);
+    float tt = cdiv(distance, L.radius) + 1.0f;
+    float illum = cdiv(L.brightness, tt * tt);
     const float cutoff = 0.1f;
     illum -= cutoff;
     illum *= 1.0f / (1.0f - cutoff);
     if (illum <= 0) continue;
-    f3 lcol = ld3(L->col);
-    if (V.use_linear) lcol = mk3(gamma_fwd(lcol.x), gamma_fwd(lcol.y), gamma_fwd(lcol.z));
+    const f3 lcol = mk3(L.cr, L.cg, L.cb);
     if (lshadow && recv_dyn) {
       int face = ret_cubeface(gpos, lpos);
       float dyn = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_dyn, face, gpos, shnum);
@@ -887,7 +961,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     ptl = cnormalize(ptl);
     float light = fmax_(dot3(ptl, lnormal) * occlusion, 0.0f);
     float diffuse = (1.0f - ambient) * light;
-    float dscale = (((diffuse + ambient) * __ldg(&L->diffuse)) * g_diffuse) * illum;
+    float dscale = (((diffuse + ambient) * L.diffuse) * g_diffuse) * illum;
     dsum = add3(dsum, mul3s(lcol, dscale));
     f3 Hv = cnormalize(add3(l2p, ptl));
     float ndh = fmax_(0.0f, dot3(normal, Hv));
@@ -932,13 +1006,30 @@ __global__ void __launch_bounds__(256, 3) k_shade(SceneDev sc, const ViewParams*
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec) {
   __shared__ uint32_t s_id;
+  __shared__ SLight slights[kMaxLights];
   if (threadIdx.x == 0) s_id = find_surface(surfs, nviews, blockIdx.x);
   __syncthreads();
   const Surface& S = surfs[s_id];
+  for (uint32_t i = threadIdx.x; i < sc.nlights; i += blockDim.x) {
+    const gbr_light* L = sc.lights + i;
+    SLight l;
+    l.px = L->pos[0]; l.py = L->pos[1]; l.pz = L->pos[2];
+    l.brightness = L->brightness;
+    l.radius = L->radius;
+    l.diffuse = L->diffuse;
+    l.shadow = L->shadow;
+    l.is_static = L->is_static;
+    l.pad = 0;
+    f3 c = mk3(L->col[0], L->col[1], L->col[2]);
+    if (views[s_id].use_linear) c = mk3(gamma_fwd(c.x), gamma_fwd(c.y), gamma_fwd(c.z));
+    l.cr = c.x; l.cg = c.y; l.cb = c.z;
+    slights[i] = l;
+  }
+  __syncthreads();
   const uint32_t lt = blockIdx.x - S.tile_base;
   const int x = (lt % S.tiles_x) * kTile + (threadIdx.x & (kTile - 1));
   const int y = (lt / S.tiles_x) * kTile + (threadIdx.x / kTile);
-  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, x, y);
+  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, slights, x, y);
 }
 
 // ---- texture atlas ----------------------------------------------------------------

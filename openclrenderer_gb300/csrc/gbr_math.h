@@ -239,6 +239,50 @@ GBR_HD int clip_tri(const f3 pts[3], f3 out[2][3]) {
   return 1;
 }
 
+// clip_tri with the same arithmetic and outputs, written with selects instead
+// of runtime-indexed arrays so that GPU code keeps everything in registers.
+GBR_HD f3 sel3(int i, f3 a, f3 b, f3 c) { return i == 0 ? a : (i == 1 ? b : c); }
+GBR_HD int clip_tri_reg(f3 a0, f3 a1, f3 a2, f3 o0[3], f3 o1[3]) {
+  const bool b0 = a0.z <= kDepthCutoff || a0.z > kDepthFar;
+  const bool b1 = a1.z <= kDepthCutoff || a1.z > kDepthFar;
+  const bool b2 = a2.z <= kDepthCutoff || a2.z > kDepthFar;
+  const int n_behind = (int)b0 + (int)b1 + (int)b2;
+  if (n_behind > 2) return 0;
+  if (n_behind == 0) {
+    o0[0] = a0; o0[1] = a1; o0[2] = a2;
+    return 1;
+  }
+  // the same g1/g2/g3 choice as generate_new_triangles
+  int g1, g2, g3, ib0 = 0, ib1 = 0, iv = 0;
+  if (n_behind == 1) {
+    const int id = b0 ? 0 : (b1 ? 1 : 2);
+    g1 = id;
+    g2 = (id + 1) >= 3 ? id - 2 : id + 1;
+    g3 = (id + 2) >= 3 ? id - 1 : id + 2;
+  } else {
+    ib0 = b0 ? 0 : 1;
+    ib1 = (b0 && b1) ? 1 : 2;
+    iv = !b0 ? 0 : (!b1 ? 1 : 2);
+    g2 = ib0;
+    g3 = ib1;
+    g1 = iv;
+  }
+  const f3 a = sel3(g1, a0, a1, a2), b = sel3(g2, a0, a1, a2), c = sel3(g3, a0, a1, a2);
+  float kb = kDepthCutoff - b.z, db = a.z - b.z;
+  float kc = kDepthCutoff - c.z, dc = a.z - c.z;
+  f3 p1 = mk3(b.x + fdiv(kb * (a.x - b.x), db), b.y + fdiv(kb * (a.y - b.y), db),
+              b.z + fdiv(kb * (a.z - b.z), db));
+  f3 p2 = mk3(c.x + fdiv(kc * (a.x - c.x), dc), c.y + fdiv(kc * (a.y - c.y), dc),
+              c.z + fdiv(kc * (a.z - c.z), dc));
+  if (n_behind == 1) {
+    o0[0] = p1; o0[1] = b; o0[2] = c;
+    o1[0] = p1; o1[1] = c; o1[2] = p2;
+    return 2;
+  }
+  for (int j = 0; j < 3; j++) o0[j] = (j == ib0) ? p1 : ((j == ib1) ? p2 : a);
+  return 1;
+}
+
 // Backface test on projected vertices (cl2.cl:491-494): 1 when front facing.
 GBR_HD int backface_front(f3 p0, f3 p1, f3 p2) {
   return cross3(sub3(p1, p0), sub3(p2, p0)).z < 0.0f;

@@ -124,6 +124,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   if (out->rgba && sc->ntris && (!sc->atlas || !sc->nums || !sc->sizes || sc->mipmap_start == 0))
     return nfail(GBR_INVALID_ARG, "shading needs the texture atlas, nums and sizes");
   if (sc->nlights && !sc->lights) return nfail(GBR_INVALID_ARG, "null lights");
+  if (sc->nlights > (uint32_t)kMaxLights) return nfail(GBR_INVALID_ARG, "more than 256 lights");
 
   Surface S{};
   S.width = view->width;
