@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--impl", default="gbr", choices=["gbr", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the binning-stress and mixed-batch sections")
     ap.add_argument("--batch-views", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
@@ -338,6 +339,61 @@ def main():
                    "value": round(world * P * args.batch_views / (bms * 1e-3) / 1e6, 2), "unit": "Mpix/s",
                    "vs_plain": round((P * args.batch_views / bms) / (P / ms), 3)}
 
+    # binning stress (2,000,000 sub-pixel + 1,000 screen-covering triangles, 2560x1440)
+    stress = None
+    if not args.no_extra:
+        st_sc = scenes.binning_stress()
+        sgs = GpuScene(st_sc)
+        scam, sview = st_sc.cameras[0], st_sc.views[0]
+        so = sgs.render(scam, sview, stream=stream)
+        sgs.render(scam, sview, out=so, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            sgs.render(scam, sview, out=so, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sms = e0.elapsed_time(e1) / 3
+        sst = sgs.stats()
+        stress = {"workload": "binning_stress_2560x1440_2M_subpixel_1k_fullscreen", "ms_per_frame": round(sms, 3),
+                  "value": round(2560 * 1440 / (sms * 1e-3) / 1e6, 2), "unit": "Mpix/s",
+                  "reference_fragments": sst["fragments_ref"], "records": sst["view_records"],
+                  "bin_entries": sst["view_bin_entries"]}
+        sgs.close()
+        del st_sc
+
+    # batched mixed resolutions: 64 views of 500 spheres (500k triangles) in one
+    # launch per stage, against the same 64 views rendered one call at a time
+    mixed = None
+    if not args.no_extra:
+        mb = scenes.spheres_batch()
+        mgs = GpuScene(mb)
+        mpix = sum(int(v["width"]) * int(v["height"]) for v in mb.views)
+        outs = mgs.render_batch(mb.cameras, mb.views, stream=stream)
+        mgs.render_batch(mb.cameras, mb.views, outs=outs, stream=stream)
+        singles = [mgs.render(c, v, stream=stream) for c, v in zip(mb.cameras, mb.views)]
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            mgs.render_batch(mb.cameras, mb.views, outs=outs, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1) / 3
+        e0.record(stream)
+        for _ in range(2):
+            for c, v, o in zip(mb.cameras, mb.views, singles):
+                mgs.render(c, v, out=o, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1) / 2
+        mixed = {"workload": "spheres_500x1000tris_64views_mixed_res", "views": len(mb.views), "pixels": mpix,
+                 "batched_ms": round(bms, 3), "plain_ms": round(pms, 3),
+                 "batched_mpix_s": round(mpix / (bms * 1e-3) / 1e6, 1),
+                 "plain_mpix_s": round(mpix / (pms * 1e-3) / 1e6, 1), "batched_vs_plain": round(pms / bms, 3)}
+        mgs.close()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -354,7 +410,7 @@ def main():
                 "config": scene_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk,
                 "stages_ms": {k: round(v, 4) for k, v in per_call.items()},
-                "batched": batched, "impl": "gbr",
+                "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "impl": "gbr",
                 "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],
                            "view_bin_entries": st["view_bin_entries"], "shadow_records": st["shadow_records"]}}
         print(json.dumps(line), flush=True)
