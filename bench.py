@@ -46,7 +46,9 @@ def parse():
     ap.add_argument("--impl", default="gbr", choices=["gbr", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--no-extra", action="store_true", help="skip the binning-stress and mixed-batch sections")
+    ap.add_argument("--no-extra", action="store_true", help="skip the binning-stress, mixed-batch and serving sections")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=150)
     ap.add_argument("--batch-views", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     return ap.parse_args()
@@ -222,6 +224,85 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+# ---- serving -----------------------------------------------------------------------
+def run_serving(args, stream):
+    """4 resident scenes (100k / 500k / 1M / 2M triangles); Poisson arrivals at
+    a sweep of offered loads; each request a random scene, camera pose and
+    resolution from {640x480, 1280x720, 1920x1080, 3840x2160}; results copied
+    to host memory.  Reports throughput and p50/p99 latency per load, and the
+    reference kernels' per-request CPU latency at each resolution."""
+    import torch
+    from openclrenderer_gb300.pipeline import GpuScene, Server
+    sizes = (100_000, 500_000, 1_000_000, 2_000_000)
+    scs = [scenes.serving_scene(n, seed=9 + i) for i, n in enumerate(sizes)]
+    gss = [GpuScene(sc) for sc in scs]
+    for g in gss:
+        g.shadow_pass(stream)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(9)
+    res = scenes.RESOLUTIONS_SERVE
+    maxp = max(w * h for w, h in res)
+    pool = [np.empty(maxp * 4, np.uint8) for _ in range(64)]
+    budget = 6 << 30
+    loads = []
+    for rate in (100.0, 400.0, 1600.0, float("inf")):
+        srv = Server(gss, hbm_budget_bytes=budget)
+        reqs = []
+        for k in range(args.serve_requests):
+            w, h = res[int(rng.integers(0, len(res)))]
+            reqs.append((int(rng.integers(0, len(sizes))), scenes.random_pose(rng), S.make_view(int(w), int(h))))
+        # warm the scenes' scratch for this mix
+        for s_i, cam, view in reqs[:8]:
+            srv.submit(s_i, cam, view, rgba=pool[0][:int(view["width"]) * int(view["height"]) * 4])
+        srv.drain()
+        srv.poll(cap=64)
+        srv.close()
+        srv = Server(gss, hbm_budget_bytes=budget)
+        t0 = time.perf_counter()
+        t_next = t0
+        for k, (s_i, cam, view) in enumerate(reqs):
+            if rate != float("inf"):
+                t_next += float(rng.exponential(1.0 / rate))
+                while time.perf_counter() < t_next:
+                    pass
+            P = int(view["width"]) * int(view["height"])
+            srv.submit(s_i, cam, view, rgba=pool[k % len(pool)][:P * 4], tag=k)
+        srv.drain()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        loads.append({"offered_req_per_s": None if rate == float("inf") else rate,
+                      "completed": st["completed"], "wall_s": round(wall, 3),
+                      "throughput_mpix_s": round(st["pixels_completed"] / wall / 1e6, 1),
+                      "throughput_req_s": round(st["completed"] / wall, 1),
+                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                      "mean_batch_views": round(st["mean_batch_views"], 2),
+                      "peak_admitted_mb": round(st["peak_admitted_bytes"] / 2 ** 20, 1)})
+    for g in gss:
+        g.close()
+    # reference kernels on the host cores, one request at each resolution (100k-triangle scene)
+    cpu_lat = {}
+    kind, R = cpu_impl()
+    if R is not None:
+        from oracle import oracle as O
+        sc = scs[0]
+        tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+        atlas = R.textures(sc.tex_sizes, sc.tex_pixels, tex.nums, tex.sizes, tex.mipmap_start)
+        dyn, sta = R.shadow(sc, ordered=False)
+        cam = scenes.random_pose(np.random.default_rng(1))
+        for w, h in res:
+            view = S.make_view(w, h)
+            t0 = time.perf_counter()
+            R.render(sc, atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, O.fov_const(90.0, w), dyn, sta,
+                     ordered=False)
+            cpu_lat[f"{w}x{h}"] = round(1e3 * (time.perf_counter() - t0), 1)
+    return {"workload": "4 resident scenes (100k/500k/1M/2M triangles), Poisson arrivals, resolutions "
+                        "640x480/1280x720/1920x1080/3840x2160", "hbm_budget_gb": budget / 2 ** 30,
+            "requests_per_load": args.serve_requests, "loads": loads,
+            "cpu_reference_latency_ms_100k_scene": cpu_lat, "cpu_kind": kind,
+            "cpu_threads": os.cpu_count()}
+
+
 # ---- GPU ------------------------------------------------------------------------
 def main():
     args = parse()
@@ -394,6 +475,10 @@ def main():
                  "plain_mpix_s": round(mpix / (pms * 1e-3) / 1e6, 1), "batched_vs_plain": round(pms / bms, 3)}
         mgs.close()
 
+    serving = None
+    if not args.no_extra and not args.no_serve:
+        serving = run_serving(args, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -410,7 +495,8 @@ def main():
                 "config": scene_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk,
                 "stages_ms": {k: round(v, 4) for k, v in per_call.items()},
-                "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "impl": "gbr",
+                "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "serving": serving,
+                "impl": "gbr",
                 "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],
                            "view_bin_entries": st["view_bin_entries"], "shadow_records": st["shadow_records"]}}
         print(json.dumps(line), flush=True)

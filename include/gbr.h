@@ -212,6 +212,65 @@ gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
  * build, engine.hpp:625-640). */
 gbr_status gbr_scene_profile(gbr_scene* scene, int32_t enable);
 
+/* ---- serving -----------------------------------------------------------------
+ * A request loop over resident scenes (the serving form of the pipeline; the
+ * reference renders one view per frame from one thread, engine.cpp:1794).
+ * Requests are admitted against an HBM budget for their framebuffers and
+ * scratch (gbr_server_config.hbm_budget_bytes); admitted requests of one scene
+ * are batched by that scene's worker (one host thread and CUDA stream per
+ * scene): while a batch is on the GPU, newly admitted requests queue and form
+ * the next batch, and batches of different scenes overlap on the device.
+ * Results are written to the request's host buffers.  Served scenes must not
+ * be used through other calls while the server runs. */
+typedef struct gbr_server gbr_server;
+
+typedef struct gbr_server_config {
+  uint64_t hbm_budget_bytes; /* device bytes admitted requests may hold at once */
+  uint32_t max_batch_views;  /* views per batch (0 = 64) */
+  uint32_t max_batch_pixels; /* pixels per batch (0 = 33177600, four 4K views) */
+} gbr_server_config;
+
+typedef struct gbr_request {
+  uint32_t scene;    /* index into the server's scenes */
+  uint32_t reserved;
+  gbr_camera cam;
+  gbr_view view;
+  uint32_t* depth;   /* host outputs, W*H each (any may be NULL) */
+  uint32_t* id;
+  uint8_t* rgba;
+  uint64_t user_tag;
+} gbr_request;
+
+typedef struct gbr_completion {
+  uint64_t request_id;
+  uint64_t user_tag;
+  int32_t status;     /* gbr_status of the request */
+  uint32_t batch_views;
+  double latency_ms;  /* submit to results in host memory */
+  double queue_ms;    /* submit to batch launch */
+} gbr_completion;
+
+typedef struct gbr_server_stats {
+  uint64_t submitted, completed, rejected, batches;
+  uint64_t pixels_completed;
+  uint64_t peak_admitted_bytes;
+  double p50_ms, p99_ms, mean_ms; /* latency over completed requests */
+  double mean_batch_views;
+  double wall_s;                  /* first submit to last completion */
+} gbr_server_stats;
+
+gbr_status gbr_server_create(gbr_scene* const* scenes, uint32_t n_scenes, const gbr_server_config* cfg,
+                             gbr_server** out);
+/* Non-blocking.  GBR_ADMISSION_REJECTED when the request alone exceeds the budget. */
+gbr_status gbr_server_submit(gbr_server* server, const gbr_request* req, uint64_t* request_id);
+/* Up to cap completions; waits up to wait_ms (0: no wait, <0: until one is ready). */
+gbr_status gbr_server_poll(gbr_server* server, gbr_completion* out, uint32_t cap, uint32_t* n,
+                           int32_t wait_ms);
+/* Wait until every submitted request has completed. */
+gbr_status gbr_server_drain(gbr_server* server);
+gbr_status gbr_server_stats_get(gbr_server* server, gbr_server_stats* out);
+gbr_status gbr_server_destroy(gbr_server* server);
+
 /* ---- allocation-free rendering -------------------------------------------
  * For callers that cannot allocate device memory where they render: code
  * running while another library owns the device memory pool, real-time loops

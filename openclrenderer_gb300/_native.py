@@ -13,7 +13,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libgbr.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
-SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_noalloc.cu"]
+SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_noalloc.cu", "gbr_server.cu"]
 HEADERS = ["gbr_math.h", "gbr_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -94,6 +94,12 @@ SIGNATURES = {
     "gbr_scene_stats": (ctypes.c_int, [_P, _P]),
     "gbr_scene_profile": (ctypes.c_int, [_P, ctypes.c_int32]),
     "gbr_render_view_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "gbr_server_create": (ctypes.c_int, [_P, _U32, _P, _P]),
+    "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),
+    "gbr_server_poll": (ctypes.c_int, [_P, _P, _U32, _P, ctypes.c_int32]),
+    "gbr_server_drain": (ctypes.c_int, [_P]),
+    "gbr_server_stats_get": (ctypes.c_int, [_P, _P]),
+    "gbr_server_destroy": (ctypes.c_int, [_P]),
 }
 
 _lib = None

@@ -425,6 +425,13 @@ gbr_status pack_textures(uint32_t n, const int32_t* sz, std::vector<uint32_t>& n
 
 namespace gbr {
 void set_last_error(const char* msg) { g_err = msg; }
+
+// depth + id + RGBA8 outputs and the record map (16 B/px), plus an estimate of
+// the records, shade records and bin entries a view of that size produces
+// (about one visible triangle per 4 pixels, 1.5 bins each: 30 B/px).
+uint64_t view_device_bytes(int32_t width, int32_t height) {
+  return (uint64_t)width * (uint64_t)height * 46u;
+}
 }  // namespace gbr
 
 extern "C" {

@@ -150,4 +150,9 @@ cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 // Sets the message gbr_last_error_string() returns on this thread (gbr_api.cu).
 void set_last_error(const char* msg);
 
+// Batch render of n views on one scene into device outputs (gbr_api.cu); the
+// C ABI's gbr_render_batch.  Bytes of device memory one view of w x h keeps
+// while it is rendered (outputs, record map, scratch estimate), for admission.
+uint64_t view_device_bytes(int32_t width, int32_t height);
+
 }  // namespace gbr

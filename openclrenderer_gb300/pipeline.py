@@ -194,3 +194,64 @@ class GpuScene:
 
     def profile(self, enable=True):
         _native.check(self.L.gbr_scene_profile(self.h, 1 if enable else 0))
+
+
+class Server:
+    """Serving loop over resident GpuScenes (gbr_server_*): HBM-budgeted
+    admission and continuous batching per scene, results in host memory."""
+
+    def __init__(self, scenes, hbm_budget_bytes=8 << 30, max_batch_views=0, max_batch_pixels=0):
+        self.L = _native.load()
+        self.scenes = list(scenes)
+        arr = (_P * len(self.scenes))(*[g.h.value for g in self.scenes])
+        cfg = np.zeros(1, S.SERVER_CONFIG)
+        cfg["hbm_budget_bytes"] = hbm_budget_bytes
+        cfg["max_batch_views"] = max_batch_views
+        cfg["max_batch_pixels"] = max_batch_pixels
+        h = _P()
+        _native.check(self.L.gbr_server_create(arr, len(self.scenes), _np_ptr(cfg), ctypes.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, scene, cam, view, depth=None, ids=None, rgba=None, tag=0):
+        """Queue one request; outputs are host numpy arrays the server fills.
+        Returns the request id (raises GbrError on rejection)."""
+        req = np.zeros(1, S.REQUEST)
+        req["scene"] = scene
+        req["cam"] = np.asarray(cam, S.CAMERA)
+        req["view"] = np.asarray(view, S.VIEW)
+        for k, a in (("depth", depth), ("id", ids), ("rgba", rgba)):
+            req[k] = a.ctypes.data if a is not None else 0
+        req["user_tag"] = tag
+        rid = ctypes.c_uint64()
+        _native.check(self.L.gbr_server_submit(self.h, _np_ptr(req), ctypes.byref(rid)))
+        self._keep[rid.value] = (depth, ids, rgba)
+        return rid.value
+
+    def poll(self, cap=256, wait_ms=0):
+        out = np.zeros(cap, S.COMPLETION)
+        n = ctypes.c_uint32()
+        _native.check(self.L.gbr_server_poll(self.h, _np_ptr(out), cap, ctypes.byref(n), wait_ms))
+        done = out[:n.value].copy()
+        for r in done["request_id"]:
+            self._keep.pop(int(r), None)
+        return done
+
+    def drain(self):
+        _native.check(self.L.gbr_server_drain(self.h))
+
+    def stats(self):
+        st = np.zeros(1, S.SERVER_STATS)
+        _native.check(self.L.gbr_server_stats_get(self.h, _np_ptr(st)))
+        return {k: (float(st[0][k]) if st.dtype[k].kind == "f" else int(st[0][k])) for k in S.SERVER_STATS.names}
+
+    def close(self):
+        if self.h:
+            self.L.gbr_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

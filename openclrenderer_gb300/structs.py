@@ -38,6 +38,21 @@ STATS = np.dtype([
 STAGES = ("shadow_setup", "shadow_scan", "shadow_fill", "shadow_raster",
           "view_setup", "view_scan", "view_fill", "view_raster", "view_shade")
 
+SERVER_CONFIG = np.dtype([("hbm_budget_bytes", "<u8"), ("max_batch_views", "<u4"), ("max_batch_pixels", "<u4")])
+REQUEST = np.dtype([
+    ("scene", "<u4"), ("reserved", "<u4"), ("cam", CAMERA), ("view", VIEW),
+    ("depth", "<u8"), ("id", "<u8"), ("rgba", "<u8"), ("user_tag", "<u8"),
+])
+COMPLETION = np.dtype([
+    ("request_id", "<u8"), ("user_tag", "<u8"), ("status", "<i4"), ("batch_views", "<u4"),
+    ("latency_ms", "<f8"), ("queue_ms", "<f8"),
+])
+SERVER_STATS = np.dtype([
+    ("submitted", "<u8"), ("completed", "<u8"), ("rejected", "<u8"), ("batches", "<u8"),
+    ("pixels_completed", "<u8"), ("peak_admitted_bytes", "<u8"), ("p50_ms", "<f8"), ("p99_ms", "<f8"),
+    ("mean_ms", "<f8"), ("mean_batch_views", "<f8"), ("wall_s", "<f8"),
+])
+
 assert VERTEX.itemsize == 48
 assert TRIANGLE.itemsize == 144
 assert OBJ_DESC.itemsize == 144

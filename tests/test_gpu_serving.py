@@ -1,0 +1,100 @@
+"""Serving loop: every request's result is the same alone and in the mix;
+admission respects the HBM budget; requests are batched continuously."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from openclrenderer_gb300 import _native, scenes  # noqa: E402
+from openclrenderer_gb300 import structs as S  # noqa: E402
+from openclrenderer_gb300.pipeline import GpuScene, Server  # noqa: E402
+
+
+def _scenes():
+    a = scenes.serving_scene(100_000, seed=9)
+    b = scenes.plain_cubes()
+    return [a, b]
+
+
+def _requests(n, rng):
+    out = []
+    res = ((320, 240), (640, 480), (800, 600), (1280, 720))
+    for i in range(n):
+        s = int(rng.integers(0, 2))
+        w, h = res[rng.integers(0, len(res))]
+        if s == 0:
+            cam = scenes.random_pose(rng)
+        else:
+            cam = S.make_camera(rng.uniform(-50, 50, 3), (rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2), 0.0))
+        out.append((s, cam, S.make_view(int(w), int(h), hfov_deg=90.0)))
+    return out
+
+
+def test_serving_results_identical_alone_and_in_mix():
+    scs = _scenes()
+    gss = [GpuScene(sc) for sc in scs]
+    for g in gss:
+        g.shadow_pass()
+    rng = np.random.default_rng(123)
+    reqs = _requests(40, rng)
+    # alone: one request at a time through the single-view host path
+    alone = [gss[s].render_host(cam, view) for s, cam, view in reqs]
+    torch.cuda.synchronize()
+    # in the mix: all submitted at once; a budget that holds only a few views
+    budget = 4 * 1280 * 720 * 46
+    srv = Server(gss, hbm_budget_bytes=budget)
+    outs = []
+    for k, (s, cam, view) in enumerate(reqs):
+        W, H = int(view["width"]), int(view["height"])
+        o = {"depth": np.zeros((H, W), np.uint32), "id": np.zeros((H, W), np.uint32),
+             "rgba": np.zeros((H, W, 4), np.uint8)}
+        outs.append(o)
+        srv.submit(s, cam, view, o["depth"], o["id"], o["rgba"], tag=k)
+    srv.drain()
+    done = srv.poll(cap=1024)
+    st = srv.stats()
+    srv.close()
+    assert len(done) == len(reqs) and np.all(done["status"] == 0)
+    assert st["completed"] == len(reqs)
+    assert st["peak_admitted_bytes"] <= budget
+    assert st["mean_batch_views"] > 1.0  # requests that queued together rendered together
+    for k, (a, b) in enumerate(zip(alone, outs)):
+        for key in ("depth", "id", "rgba"):
+            assert np.array_equal(a[key], b[key]), f"request {k} {key} differs in the mix"
+
+
+def test_serving_rejects_oversized_and_overlaps_scenes():
+    scs = _scenes()
+    gss = [GpuScene(sc) for sc in scs]
+    srv = Server(gss, hbm_budget_bytes=64 << 20)
+    big = S.make_view(3840, 2160)
+    with pytest.raises(_native.GbrError) as e:
+        srv.submit(0, scs[0].cameras[0] if scs[0].cameras else S.make_camera(), big)
+    assert e.value.status == "GBR_ADMISSION_REJECTED"
+    # Poisson-ish arrivals while earlier batches are on the GPU
+    rng = np.random.default_rng(7)
+    reqs = _requests(60, rng)
+    bufs = []
+    t0 = time.perf_counter()
+    for k, (s, cam, view) in enumerate(reqs):
+        W, H = int(view["width"]), int(view["height"])
+        rgba = np.zeros((H, W, 4), np.uint8)
+        bufs.append(rgba)
+        srv.submit(s, cam, view, None, None, rgba, tag=k)
+        time.sleep(float(rng.exponential(0.0005)))
+    srv.drain()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    done = srv.poll(cap=1024)
+    srv.close()
+    assert st["completed"] == len(reqs) and st["rejected"] == 1
+    assert np.all(done["status"] == 0)
+    assert st["p99_ms"] >= st["p50_ms"] > 0
+    assert wall < 30
+    assert any(int(b[..., 3].max()) > 0 for b in bufs)
