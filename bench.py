@@ -242,22 +242,21 @@ def run_serving(args, stream):
     rng = np.random.default_rng(9)
     res = scenes.RESOLUTIONS_SERVE
     maxp = max(w * h for w, h in res)
-    pool = [np.empty(maxp * 4, np.uint8) for _ in range(64)]
+    pinned = torch.empty(64 * maxp * 4, dtype=torch.uint8, pin_memory=True).numpy()
+    pool = [pinned[i * maxp * 4:(i + 1) * maxp * 4] for i in range(64)]
     budget = 6 << 30
     loads = []
     for rate in (100.0, 400.0, 1600.0, float("inf")):
-        srv = Server(gss, hbm_budget_bytes=budget)
         reqs = []
         for k in range(args.serve_requests):
             w, h = res[int(rng.integers(0, len(res)))]
             reqs.append((int(rng.integers(0, len(sizes))), scenes.random_pose(rng), S.make_view(int(w), int(h))))
-        # warm the scenes' scratch for this mix
-        for s_i, cam, view in reqs[:8]:
-            srv.submit(s_i, cam, view, rgba=pool[0][:int(view["width"]) * int(view["height"]) * 4])
+        srv = Server(gss, hbm_budget_bytes=budget)
+        # warm the scenes' scratch and the workers' output pools (largest views first)
+        for s_i, cam, view in sorted(reqs, key=lambda r: -int(r[2]["width"]) * int(r[2]["height"]))[:16]:
+            srv.submit(s_i, cam, view, rgba=pool[0][:int(view["width"]) * int(view["height"]) * 4], tag=0)
         srv.drain()
         srv.poll(cap=64)
-        srv.close()
-        srv = Server(gss, hbm_budget_bytes=budget)
         t0 = time.perf_counter()
         t_next = t0
         for k, (s_i, cam, view) in enumerate(reqs):
@@ -266,17 +265,22 @@ def run_serving(args, stream):
                 while time.perf_counter() < t_next:
                     pass
             P = int(view["width"]) * int(view["height"])
-            srv.submit(s_i, cam, view, rgba=pool[k % len(pool)][:P * 4], tag=k)
+            srv.submit(s_i, cam, view, rgba=pool[k % len(pool)][:P * 4], tag=1 + k)
         srv.drain()
         wall = time.perf_counter() - t0
+        done = srv.poll(cap=4096)
         st = srv.stats()
         srv.close()
+        lat = done["latency_ms"]
+        pix = sum(int(reqs[int(t) - 1][2]["width"]) * int(reqs[int(t) - 1][2]["height"]) for t in done["user_tag"])
         loads.append({"offered_req_per_s": None if rate == float("inf") else rate,
-                      "completed": st["completed"], "wall_s": round(wall, 3),
-                      "throughput_mpix_s": round(st["pixels_completed"] / wall / 1e6, 1),
-                      "throughput_req_s": round(st["completed"] / wall, 1),
-                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                      "mean_batch_views": round(st["mean_batch_views"], 2),
+                      "completed": int(len(done)), "ok": int(np.count_nonzero(done["status"] == 0)),
+                      "wall_s": round(wall, 3),
+                      "throughput_mpix_s": round(pix / wall / 1e6, 1),
+                      "throughput_req_s": round(len(done) / wall, 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                      "mean_batch_views": round(float(np.mean(done["batch_views"])), 2),
                       "peak_admitted_mb": round(st["peak_admitted_bytes"] / 2 ** 20, 1)})
     for g in gss:
         g.close()

@@ -707,11 +707,9 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   std::vector<ViewParams> vp(n);
   uint32_t tb = 0, cb = 0;
   size_t off = 0;
-  bool need_depth = false, need_id = false;
-  for (uint32_t i = 0; i < n; i++) {
+  bool need_depth = false;
+  for (uint32_t i = 0; i < n; i++)
     if (!outs[i].depth) need_depth = true;
-    if (!outs[i].id) need_id = true;
-  }
   TRY(s->ws_view.pix_rec.reserve(npix));
   if (need_depth) TRY(s->ws_view.pix_depth.reserve(npix));
   for (uint32_t i = 0; i < n; i++) {
@@ -735,7 +733,6 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     V.normals = outs[i].normals;
     off += (size_t)v.width * v.height;
   }
-  (void)need_id;
   TRY(check_indices(s, true));
   WorkMem& wm = s->ws_view;
   TRY(wm.surf.reserve(n));

@@ -38,14 +38,34 @@ struct Req {
   Clock::time_point t_submit, t_launch;
 };
 
+// Device outputs of one batch; two per worker so that a batch renders while
+// the previous one's results are still being copied to host memory.
+struct Pool {
+  uint8_t* p = nullptr;
+  size_t bytes = 0;
+  cudaEvent_t free_ev = nullptr;  // recorded after the pool's last copy
+  bool used = false;
+};
+
+struct Worker;
+
+// A batch in flight: completed from the stream by a host callback.
+struct Flight {
+  gbr_server* server;
+  Worker* worker;
+  std::vector<Req> batch;
+  Clock::time_point t_launch;
+  gbr_status status;
+};
+
 struct Worker {
   uint32_t scene_index = 0;
   gbr_scene* scene = nullptr;
   cudaStream_t stream = nullptr;
   std::deque<Req> pending;
   std::thread thread;
-  uint8_t* pool = nullptr;  // device outputs of the current batch
-  size_t pool_bytes = 0;
+  Pool pools[2];
+  int next_pool = 0;
 };
 
 }  // namespace
@@ -85,17 +105,27 @@ void admit_locked(gbr_server* s) {
   if (any) s->cv_work.notify_all();
 }
 
-gbr_status ensure_pool(Worker* w, size_t bytes) {
-  if (bytes <= w->pool_bytes) return GBR_OK;
-  if (w->pool) cudaFree(w->pool);
-  w->pool = nullptr;
-  w->pool_bytes = 0;
-  if (cudaMalloc(&w->pool, bytes) != cudaSuccess) {
+gbr_status ensure_pool(Pool& pl, size_t bytes) {
+  if (pl.used && cudaEventSynchronize(pl.free_ev) != cudaSuccess) return GBR_CUDA_ERROR;
+  if (bytes <= pl.bytes) return GBR_OK;
+  if (pl.p) cudaFree(pl.p);
+  pl.p = nullptr;
+  pl.bytes = 0;
+  if (cudaMalloc(&pl.p, bytes) != cudaSuccess) {
     cudaGetLastError();
     return GBR_OOM;
   }
-  w->pool_bytes = bytes;
+  pl.bytes = bytes;
   return GBR_OK;
+}
+
+void complete(gbr_server* s, std::vector<Req>& batch, gbr_status st, Clock::time_point t_launch);
+
+// Runs on a driver thread when the stream reaches the end of a batch's copies.
+void CUDART_CB on_batch_done(void* data) {
+  Flight* f = static_cast<Flight*>(data);
+  complete(f->server, f->batch, f->status, f->t_launch);
+  delete f;
 }
 
 void worker_loop(gbr_server* s, Worker* w) {
@@ -126,13 +156,15 @@ void worker_loop(gbr_server* s, Worker* w) {
       offs[i] = bytes;
       bytes += (size_t)batch[i].r.view.width * batch[i].r.view.height * 12 + 256;
     }
-    gbr_status st = ensure_pool(w, bytes);
+    Pool& pl = w->pools[w->next_pool];
+    w->next_pool ^= 1;
+    gbr_status st = ensure_pool(pl, bytes);
     std::vector<gbr_camera> cams(batch.size());
     std::vector<gbr_view> views(batch.size());
     std::vector<gbr_outputs> outs(batch.size());
-    for (size_t i = 0; i < batch.size(); i++) {
+    for (size_t i = 0; i < batch.size() && st == GBR_OK; i++) {
       const size_t P = (size_t)batch[i].r.view.width * batch[i].r.view.height;
-      uint8_t* b = w->pool + offs[i];
+      uint8_t* b = pl.p + offs[i];
       cams[i] = batch[i].r.cam;
       views[i] = batch[i].r.view;
       outs[i] = gbr_outputs{reinterpret_cast<uint32_t*>(b), reinterpret_cast<uint32_t*>(b + 4 * P), b + 8 * P,
@@ -151,35 +183,50 @@ void worker_loop(gbr_server* s, Worker* w) {
         if (r.rgba && cudaMemcpyAsync(r.rgba, outs[i].rgba, 4 * P, cudaMemcpyDeviceToHost, w->stream) != cudaSuccess)
           st = GBR_CUDA_ERROR;
       }
-      if (cudaStreamSynchronize(w->stream) != cudaSuccess) st = GBR_CUDA_ERROR;
     }
-    const Clock::time_point t_done = Clock::now();
-    {
-      std::lock_guard<std::mutex> lk(s->mu);
-      for (const Req& q : batch) {
-        gbr_completion c{};
-        c.request_id = q.id;
-        c.user_tag = q.r.user_tag;
-        c.status = st;
-        c.batch_views = (uint32_t)batch.size();
-        c.latency_ms = ms_between(q.t_submit, t_done);
-        c.queue_ms = ms_between(q.t_submit, t_launch);
-        s->done.push_back(c);
-        s->admitted_bytes -= q.bytes;
-        s->completed++;
-        s->in_system--;
-        if (st == GBR_OK) {
-          s->latencies.push_back(c.latency_ms);
-          s->pixels_completed += (uint64_t)q.r.view.width * q.r.view.height;
-        }
+    if (st == GBR_OK) {
+      Flight* f = new Flight{s, w, std::move(batch), t_launch, GBR_OK};
+      if (cudaEventRecord(pl.free_ev, w->stream) == cudaSuccess &&
+          cudaLaunchHostFunc(w->stream, on_batch_done, f) == cudaSuccess) {
+        pl.used = true;
+        continue;  // completed from the stream; take the next batch now
       }
-      s->batches++;
-      s->batch_views += batch.size();
-      s->t_last = t_done;
-      admit_locked(s);
+      batch = std::move(f->batch);
+      delete f;
+      st = GBR_CUDA_ERROR;
     }
-    s->cv_done.notify_all();
+    cudaStreamSynchronize(w->stream);
+    complete(s, batch, st, t_launch);
   }
+}
+
+void complete(gbr_server* s, std::vector<Req>& batch, gbr_status st, Clock::time_point t_launch) {
+  const Clock::time_point t_done = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    for (const Req& q : batch) {
+      gbr_completion c{};
+      c.request_id = q.id;
+      c.user_tag = q.r.user_tag;
+      c.status = st;
+      c.batch_views = (uint32_t)batch.size();
+      c.latency_ms = ms_between(q.t_submit, t_done);
+      c.queue_ms = ms_between(q.t_submit, t_launch);
+      s->done.push_back(c);
+      s->admitted_bytes -= q.bytes;
+      s->completed++;
+      s->in_system--;
+      if (st == GBR_OK) {
+        s->latencies.push_back(c.latency_ms);
+        s->pixels_completed += (uint64_t)q.r.view.width * q.r.view.height;
+      }
+    }
+    s->batches++;
+    s->batch_views += batch.size();
+    s->t_last = t_done;
+    admit_locked(s);
+  }
+  s->cv_done.notify_all();
 }
 
 }  // namespace
@@ -202,7 +249,9 @@ gbr_status gbr_server_create(gbr_scene* const* scenes, uint32_t n, const gbr_ser
     Worker* w = new Worker();
     w->scene_index = i;
     w->scene = scenes[i];
-    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->pools[0].free_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->pools[1].free_ev, cudaEventDisableTiming) != cudaSuccess) {
       delete w;
       for (Worker* x : s->workers) delete x;
       delete s;
@@ -297,13 +346,21 @@ gbr_status gbr_server_stats_get(gbr_server* s, gbr_server_stats* out) {
 gbr_status gbr_server_destroy(gbr_server* s) {
   if (!s) return GBR_OK;
   {
+    std::unique_lock<std::mutex> lk(s->mu);
+    s->cv_done.wait(lk, [&] { return s->in_system == 0; });
+  }
+  {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
   }
   s->cv_work.notify_all();
   for (Worker* w : s->workers) {
     if (w->thread.joinable()) w->thread.join();
-    if (w->pool) cudaFree(w->pool);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (Pool& pl : w->pools) {
+      if (pl.p) cudaFree(pl.p);
+      if (pl.free_ev) cudaEventDestroy(pl.free_ev);
+    }
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
   }
