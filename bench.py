@@ -316,7 +316,7 @@ def main():
         return
     import torch
     import torch.distributed as dist
-    from openclrenderer_gb300.pipeline import GpuScene
+    from openclrenderer_gb300.pipeline import Batch, GpuScene
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -419,10 +419,27 @@ def main():
             gs.render_batch(cams, views, outs=outs, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
+        bms_plain = e0.elapsed_time(e1) / nb
+        # the same frame as one captured graph (shadow cubemap + 16 views), autotuned
+        gb = Batch(gs, views, outs=outs, with_shadow=True)
+        pick = gb.autotune(cams, reps=3, stream=stream)
+        gb.render(cams, stream=stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(nb):
+            gb.launch(cams, stream=stream)
+        gb.wait()
+        e1.record(stream)
+        torch.cuda.synchronize()
         bms = e0.elapsed_time(e1) / nb
+        info = gb.info()
+        gb.close()
         batched = {"views_per_launch": args.batch_views, "ms_per_batch": round(bms, 3),
                    "value": round(world * P * args.batch_views / (bms * 1e-3) / 1e6, 2), "unit": "Mpix/s",
-                   "vs_plain": round((P * args.batch_views / bms) / (P / ms), 3)}
+                   "vs_plain": round((P * args.batch_views / bms) / (P / ms), 3),
+                   "form": "captured graph (shadow cubemap + views), autotuned",
+                   "ms_per_batch_uncaptured": round(bms_plain, 3), "tuning": pick,
+                   "graph_nodes": info["graph_nodes"]}
 
     # binning stress (2,000,000 sub-pixel + 1,000 screen-covering triangles, 2560x1440)
     stress = None
@@ -465,7 +482,26 @@ def main():
             mgs.render_batch(mb.cameras, mb.views, outs=outs, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
+        bms_uncaptured = e0.elapsed_time(e1) / 3
+        # stage times of one uncaptured batch
+        mgs.profile(True)
+        mgs.render_batch(mb.cameras, mb.views, outs=outs, stream=stream)
+        mst = mgs.stats()
+        mgs.profile(False)
+        batch_stages = {k: round(v, 4) for k, v in mst["stage_ms"].items() if k.startswith("view")}
+        # captured graph, autotuned
+        gb = Batch(mgs, mb.views, outs=outs)
+        pick = gb.autotune(mb.cameras, reps=3, stream=stream)
+        gb.render(mb.cameras, stream=stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            gb.launch(mb.cameras, stream=stream)
+        gb.wait()
+        e1.record(stream)
+        torch.cuda.synchronize()
         bms = e0.elapsed_time(e1) / 3
+        gb.close()
         e0.record(stream)
         for _ in range(2):
             for c, v, o in zip(mb.cameras, mb.views, singles):
@@ -475,6 +511,8 @@ def main():
         pms = e0.elapsed_time(e1) / 2
         mixed = {"workload": "spheres_500x1000tris_64views_mixed_res", "views": len(mb.views), "pixels": mpix,
                  "batched_ms": round(bms, 3), "plain_ms": round(pms, 3),
+                 "form": "captured graph, autotuned", "batched_uncaptured_ms": round(bms_uncaptured, 3),
+                 "tuning": pick["view"], "batch_stage_ms": batch_stages,
                  "batched_mpix_s": round(mpix / (bms * 1e-3) / 1e6, 1),
                  "plain_mpix_s": round(mpix / (pms * 1e-3) / 1e6, 1), "batched_vs_plain": round(pms / bms, 3)}
         mgs.close()

@@ -212,6 +212,68 @@ gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
  * build, engine.hpp:625-640). */
 gbr_status gbr_scene_profile(gbr_scene* scene, int32_t enable);
 
+/* ---- tuning --------------------------------------------------------------------
+ * Shape of the binning and raster stages.  No shape changes any result (every
+ * per-pixel resolve is a minimum); they trade bin traffic against raster work.
+ * The reference has fixed work-group sizes instead (op_size 500 / 300,
+ * cl2.cl:4271-4409, and the gws estimates of engine.cpp:1836,1899). */
+enum { GBR_PASS_SHADOW = 0, GBR_PASS_VIEW = 1 };
+
+typedef struct gbr_tuning {
+  int32_t raster_threads;  /* threads of one 16x16 raster tile: 128, 256 or 512 */
+  int32_t coarse_tile;     /* coarse bin edge in pixels: 64, 128 or 256 */
+  int32_t fine_max_tiles;  /* records touching more 16x16 tiles go to coarse bins: 1..256 */
+  float scratch_headroom;  /* record / bin scratch kept, as a multiple of the need: 1.05..4 */
+} gbr_tuning;
+
+/* Defaults: 256 threads, 128-pixel coarse tiles, 16 fine tiles, 1.25. */
+gbr_status gbr_scene_set_tuning(gbr_scene* scene, int32_t pass, const gbr_tuning* t);
+gbr_status gbr_scene_get_tuning(gbr_scene* scene, int32_t pass, gbr_tuning* t);
+
+/* ---- captured batches ----------------------------------------------------------
+ * A fixed set of views (resolutions, fields of view, outputs) of one scene
+ * whose whole frame -- optionally the dynamic shadow cubemaps first, then
+ * setup, binning, raster and shading of every view -- is one CUDA graph,
+ * replayed with new cameras by each launch.  Batches own their scratch, so
+ * single-view calls on the same scene do not invalidate them; a change of the
+ * scene's triangles, descriptors, lights or textures re-captures the graph at
+ * the next launch, and so does a scratch overflow (after which the frame is
+ * rendered again).  No counterpart in the reference (one view per frame). */
+typedef struct gbr_batch gbr_batch;
+
+#define GBR_BATCH_WITH_SHADOW 1 /* re-render the dynamic cubemaps in every launch */
+
+typedef struct gbr_batch_info {
+  uint32_t views;
+  uint32_t graph_nodes;   /* nodes of the captured graph */
+  uint64_t captures;      /* graph captures so far */
+  uint64_t launches;      /* graph launches so far (reruns included) */
+  uint64_t reruns;        /* launches repeated after a scratch overflow */
+  uint64_t scratch_bytes; /* device bytes of the batch's own scratch */
+} gbr_batch_info;
+
+gbr_status gbr_batch_create(gbr_scene* scene, uint32_t n, const gbr_view* views, const gbr_outputs* outs,
+                            int32_t flags, gbr_batch** out);
+/* Launch one frame with n cameras; returns without waiting.  A launch waits
+ * for the batch's previous frame first. */
+gbr_status gbr_batch_launch(gbr_batch* batch, const gbr_camera* cams, void* stream);
+/* Wait for the last launch and check its scratch bounds (rendering it again
+ * when they overflowed). */
+gbr_status gbr_batch_wait(gbr_batch* batch);
+/* gbr_batch_launch + gbr_batch_wait. */
+gbr_status gbr_batch_render(gbr_batch* batch, const gbr_camera* cams, void* stream);
+/* Autotuner: times `reps` graph launches per candidate shape (coordinate
+ * descent over raster threads, coarse tile edge and fine-tile limit, for the
+ * view pass and, with GBR_BATCH_WITH_SHADOW, the shadow pass), keeps the
+ * fastest, and sizes the scratch to the measured need times the headroom.
+ * Picks and the best frame time (ms) are returned when the pointers are set. */
+gbr_status gbr_batch_autotune(gbr_batch* batch, const gbr_camera* cams, void* stream, int32_t reps,
+                              gbr_tuning* view_pick, gbr_tuning* shadow_pick, float* best_ms);
+gbr_status gbr_batch_set_tuning(gbr_batch* batch, int32_t pass, const gbr_tuning* t);
+gbr_status gbr_batch_get_tuning(gbr_batch* batch, int32_t pass, gbr_tuning* t);
+gbr_status gbr_batch_get_info(gbr_batch* batch, gbr_batch_info* out);
+gbr_status gbr_batch_destroy(gbr_batch* batch);
+
 /* ---- serving -----------------------------------------------------------------
  * A request loop over resident scenes (the serving form of the pipeline; the
  * reference renders one view per frame from one thread, engine.cpp:1794).

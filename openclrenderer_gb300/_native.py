@@ -13,8 +13,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libgbr.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
-SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_noalloc.cu", "gbr_server.cu"]
-HEADERS = ["gbr_math.h", "gbr_internal.h"]
+SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_server.cu"]
+HEADERS = ["gbr_math.h", "gbr_internal.h", "gbr_scene.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
@@ -93,6 +93,17 @@ SIGNATURES = {
     "gbr_render_batch": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P]),
     "gbr_scene_stats": (ctypes.c_int, [_P, _P]),
     "gbr_scene_profile": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "gbr_scene_set_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    "gbr_scene_get_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    "gbr_batch_create": (ctypes.c_int, [_P, _U32, _P, _P, ctypes.c_int32, _P]),
+    "gbr_batch_launch": (ctypes.c_int, [_P, _P, _P]),
+    "gbr_batch_wait": (ctypes.c_int, [_P]),
+    "gbr_batch_render": (ctypes.c_int, [_P, _P, _P]),
+    "gbr_batch_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P]),
+    "gbr_batch_set_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    "gbr_batch_get_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
+    "gbr_batch_get_info": (ctypes.c_int, [_P, _P]),
+    "gbr_batch_destroy": (ctypes.c_int, [_P]),
     "gbr_render_view_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "gbr_server_create": (ctypes.c_int, [_P, _U32, _P, _P]),
     "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),

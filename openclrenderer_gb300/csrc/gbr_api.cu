@@ -15,6 +15,7 @@
 
 #include "../../include/gbr.h"
 #include "gbr_internal.h"
+#include "gbr_scene.h"
 
 static_assert(sizeof(gbr_vertex) == 48, "vertex layout");
 static_assert(sizeof(gbr_triangle) == 144, "triangle layout");
@@ -30,8 +31,10 @@ static_assert(sizeof(gbr::ShadeRec) == 48, "shade record");
 using namespace gbr;
 
 namespace {
-
 thread_local std::string g_err;
+}  // namespace
+
+namespace gbr {
 
 gbr_status fail(gbr_status s, const char* fmt, ...) {
   char buf[512];
@@ -43,98 +46,6 @@ gbr_status fail(gbr_status s, const char* fmt, ...) {
   return s;
 }
 
-#define CU(call)                                                                          \
-  do {                                                                                    \
-    cudaError_t e_ = (call);                                                              \
-    if (e_ != cudaSuccess)                                                                \
-      return fail(e_ == cudaErrorMemoryAllocation ? GBR_OOM : GBR_CUDA_ERROR, "%s: %s (%s:%d)", \
-                  #call, cudaGetErrorString(e_), __FILE__, __LINE__);                      \
-  } while (0)
-
-#define TRY(expr)                        \
-  do {                                   \
-    gbr_status s_ = (expr);              \
-    if (s_ != GBR_OK) return s_;         \
-  } while (0)
-
-// Device buffer that only grows.
-template <class T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t cap = 0;  // elements
-  gbr_status reserve(size_t n) {
-    if (n <= cap && p) return GBR_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t m = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc(&p, m * sizeof(T));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      p = nullptr;
-      return fail(GBR_OOM, "cudaMalloc of %zu bytes failed: %s", m * sizeof(T), cudaGetErrorString(e));
-    }
-    cap = m;
-    return GBR_OK;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-};
-
-// Pinned host staging buffer that only grows.
-struct HostBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  gbr_status reserve(size_t n) {
-    if (n <= bytes && p) return GBR_OK;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(n, 64));
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      p = nullptr;
-      return fail(GBR_OOM, "cudaMallocHost of %zu bytes failed", n);
-    }
-    bytes = std::max<size_t>(n, 64);
-    return GBR_OK;
-  }
-  void release() {
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
-// Scratch memory of one pass (records, bins, tile counters, per-pixel record
-// indices of the views).
-struct WorkMem {
-  DevBuf<RasterRec> rec;
-  DevBuf<ShadeRec> srec;
-  DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins;
-  DevBuf<Counters> ctr;
-  DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
-  DevBuf<uint8_t> pix_rgba;
-  DevBuf<Surface> surf;
-  DevBuf<ViewParams> views;
-  DevBuf<ShadowJob> jobs;
-  uint32_t rec_target = 0, bin_target = 0;
-  void release() {
-    rec.release(); srec.release(); fine_count.release(); fine_off.release();
-    coarse_count.release(); coarse_off.release(); bins.release(); ctr.release();
-    pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
-    surf.release(); views.release(); jobs.release();
-  }
-};
-
-struct PassShape {
-  uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
-  size_t npix = 0;
-};
-
 void euler_cs(const float ang[3], float c[3], float s[3]) {
   for (int i = 0; i < 3; i++) {
     c[i] = (float)cos((double)ang[i]);
@@ -142,67 +53,12 @@ void euler_cs(const float ang[3], float c[3], float s[3]) {
   }
 }
 
-}  // namespace
-
-struct gbr_scene {
-  int device = 0;
-  DevBuf<gbr_triangle> tris;
-  uint32_t ntris = 0;
-  DevBuf<float4> world;     // world-space vertices, 3 per triangle
-  bool world_dirty = true;  // triangles or descriptors changed since k_world ran
-  DevBuf<gbr_obj_g_descriptor> descs;
-  uint32_t ndescs = 0;
-  DevBuf<gbr_light> lights;
-  std::vector<gbr_light> host_lights;
-  DevBuf<uchar4> atlas;
-  DevBuf<uint32_t> nums, sizes;
-  std::vector<uint32_t> host_nums, host_sizes;
-  uint32_t mipmap_start = 0;
-  uint32_t npages = 0;
-  DevBuf<uint32_t> shadow_dyn, shadow_static;
-  uint32_t n_dyn = 0, n_static = 0;
-  uint32_t max_object_id = 0, max_tid = 0;
-  bool static_dirty = true;
-  WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
-  HostBuf staging;     // counters read back: view at 0, shadow at 256
-  bool shadow_pending = false;  // a shadow pass whose counters are not checked yet
-  cudaStream_t shadow_stream = nullptr;
-  PassShape shadow_shape;
-  gbr_stats stats{};
-  float face_cos[6][3], face_sin[6][3];
-  bool profile = false;
-  cudaEvent_t ev[20] = {};
-
-  SceneDev dev() const {
-    SceneDev d{};
-    d.tris = tris.p;
-    d.ntris = ntris;
-    d.world = world_dirty ? nullptr : world.p;
-    d.descs = descs.p;
-    d.ndescs = ndescs;
-    d.lights = lights.p;
-    d.nlights = (uint32_t)host_lights.size();
-    d.atlas = atlas.p;
-    d.nums = nums.p;
-    d.sizes = sizes.p;
-    d.mipmap_start = mipmap_start;
-    d.shadow_dyn = shadow_dyn.p;
-    d.shadow_static = shadow_static.p;
-    memcpy(d.face_cos, face_cos, sizeof face_cos);
-    memcpy(d.face_sin, face_sin, sizeof face_sin);
-    return d;
-  }
-};
-
-namespace {
-
 gbr_status check_scene(gbr_scene* s) {
   if (!s) return fail(GBR_INVALID_ARG, "null scene");
   CU(cudaSetDevice(s->device));
   return GBR_OK;
 }
 
-// Every index the kernels follow must stay inside its table.
 gbr_status check_indices(gbr_scene* s, bool shading) {
   if (s->ntris && s->max_object_id >= s->ndescs)
     return fail(GBR_INVALID_ARG, "triangle object_id %u but only %u descriptors", s->max_object_id, s->ndescs);
@@ -211,46 +67,25 @@ gbr_status check_indices(gbr_scene* s, bool shading) {
   return GBR_OK;
 }
 
-// Reserve pass scratch: records, bins and tile counters for the given surfaces.
-WorkMem& pass_mem(gbr_scene* s, bool view) { return view ? s->ws_view : s->ws_shadow; }
-
-gbr_status reserve_pass(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view, size_t npix) {
-  WorkMem& w = pass_mem(s, view);
+gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view) {
   TRY(w.rec.reserve(w.rec_target));
   if (view) TRY(w.srec.reserve(w.rec_target));
   TRY(w.bins.reserve(w.bin_target));
-  TRY(w.fine_count.reserve(nfine));
-  TRY(w.fine_off.reserve(nfine));
-  TRY(w.coarse_count.reserve(ncoarse));
-  TRY(w.coarse_off.reserve(ncoarse));
+  TRY(w.fine_count.reserve(sh.nfine));
+  TRY(w.fine_off.reserve(sh.nfine));
+  TRY(w.coarse_count.reserve(sh.ncoarse));
+  TRY(w.coarse_off.reserve(sh.ncoarse));
   TRY(w.ctr.reserve(1));
-  if (view) TRY(w.pix_rec.reserve(npix));
+  if (view) TRY(w.pix_rec.reserve(sh.npix));
   return GBR_OK;
 }
 
-Workspace make_ws(gbr_scene* s, uint32_t nfine, uint32_t ncoarse, bool view) {
-  WorkMem& w = pass_mem(s, view);
-  Workspace ws{};
-  ws.rec = w.rec.p;
-  ws.srec = view ? w.srec.p : nullptr;
-  ws.rec_cap = (uint32_t)std::min<size_t>(w.rec.cap, 0xFFFFFFF0u);
-  ws.fine_count = w.fine_count.p;
-  ws.fine_off = w.fine_off.p;
-  ws.nfine = nfine;
-  ws.coarse_count = w.coarse_count.p;
-  ws.coarse_off = w.coarse_off.p;
-  ws.ncoarse = ncoarse;
-  ws.bins = w.bins.p;
-  ws.bin_cap = (uint32_t)std::min<size_t>(w.bins.cap, 0xFFFFFFF0u);
-  ws.ctr = w.ctr.p;
-  return ws;
-}
-
-void tile_layout(Surface& S, uint32_t& tile_base, uint32_t& ctile_base) {
+void tile_layout(Surface& S, uint32_t& tile_base, uint32_t& ctile_base, int coarse_shift) {
+  const int coarse = kTile << coarse_shift;
   S.tiles_x = (S.width + kTile - 1) / kTile;
   S.tiles_y = (S.height + kTile - 1) / kTile;
-  S.ctiles_x = (S.width + kCoarse - 1) / kCoarse;
-  S.ctiles_y = (S.height + kCoarse - 1) / kCoarse;
+  S.ctiles_x = (S.width + coarse - 1) / coarse;
+  S.ctiles_y = (S.height + coarse - 1) / coarse;
   S.tile_base = tile_base;
   S.ctile_base = ctile_base;
   tile_base += (uint32_t)(S.tiles_x * S.tiles_y);
@@ -267,7 +102,50 @@ gbr_status validate_view(const gbr_view* v) {
   return GBR_OK;
 }
 
-// World-space vertex cache (k_world), rebuilt when triangles or descriptors change.
+void fill_view_params(const gbr_camera& cam, const gbr_view& v, const gbr_outputs& o, uint32_t surface,
+                      ViewParams& V) {
+  memcpy(V.cpos, cam.pos, 12);
+  euler_cs(cam.rot, V.ccos, V.csin);
+  V.fov = v.fov_const > 0 ? v.fov_const : gbr_fov_const_from_hfov(v.hfov_deg, v.width);
+  V.surface = surface;
+  V.use_linear = v.use_linear;
+  memcpy(V.clear, v.clear_col, 16);
+  V.rgba = o.rgba;
+  V.normals = o.normals;
+}
+
+void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector<ShadowJob>& jobs,
+                   std::vector<Surface>& surfs, PassShape& sh) {
+  const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
+  jobs.clear();
+  surfs.clear();
+  uint32_t nn = 0, kk = 0, tb = 0, cb = 0;
+  auto add_job = [&](const gbr_light& L, int only_static, uint32_t* base) {
+    ShadowJob J{};
+    J.lpos[0] = L.pos[0]; J.lpos[1] = L.pos[1]; J.lpos[2] = L.pos[2];
+    J.only_static = only_static;
+    J.surface_base = (uint32_t)surfs.size();
+    for (int f = 0; f < 6; f++) {
+      Surface S{};
+      S.width = S.height = kLightBufferDim;
+      tile_layout(S, tb, cb, coarse_shift);
+      S.depth = base + (size_t)f * face;
+      S.chunk = kOpSizeLight;
+      surfs.push_back(S);
+    }
+    jobs.push_back(J);
+  };
+  for (const gbr_light& L : s->host_lights) {
+    if (L.shadow == 1) add_job(L, 0, s->shadow_dyn.p + (size_t)(nn++) * 6 * face);
+    if (L.shadow && L.is_static && with_static) add_job(L, 1, s->shadow_static.p + (size_t)(kk++) * 6 * face);
+  }
+  sh = PassShape{};
+  sh.nitems = (uint32_t)jobs.size();
+  sh.nsurf = (uint32_t)surfs.size();
+  sh.nfine = tb;
+  sh.ncoarse = cb;
+}
+
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   if (!s->world_dirty) return GBR_OK;
   TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
@@ -278,62 +156,49 @@ gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   return GBR_OK;
 }
 
-Counters* counter_slot(gbr_scene* s, bool view) {
-  return reinterpret_cast<Counters*>(static_cast<char*>(s->staging.p) + (view ? 0 : 256));
-}
-
-// Launch one pass (views or shadow jobs) and queue the read-back of its
-// counters; the caller synchronises and calls check_pass.  The caller has
-// filled the pass's surfaces / views / jobs on the device.
-gbr_status enqueue_pass(gbr_scene* s, bool view, uint32_t nitems, uint32_t nsurf, uint32_t nfine,
-                        uint32_t ncoarse, size_t npix, cudaStream_t st) {
-  TRY(ensure_world(s, st));
+gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
+                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st) {
   const SceneDev sd = s->dev();
-  WorkMem& wm = pass_mem(s, view);
-  TRY(reserve_pass(s, nfine, ncoarse, view, npix));
-  Workspace ws = make_ws(s, nfine, ncoarse, view);
+  Workspace ws{};
+  ws.rec = wm.rec.p;
+  ws.srec = view ? wm.srec.p : nullptr;
+  ws.rec_cap = (uint32_t)std::min<size_t>(wm.rec.cap, 0xFFFFFFF0u);
+  ws.fine_count = wm.fine_count.p;
+  ws.fine_off = wm.fine_off.p;
+  ws.nfine = sh.nfine;
+  ws.coarse_count = wm.coarse_count.p;
+  ws.coarse_off = wm.coarse_off.p;
+  ws.ncoarse = sh.ncoarse;
+  ws.bins = wm.bins.p;
+  ws.bin_cap = (uint32_t)std::min<size_t>(wm.bins.cap, 0xFFFFFFF0u);
+  ws.ctr = wm.ctr.p;
+  ws.fine_max = tu.fine_max;
+  ws.coarse_shift = tu.coarse_shift;
   CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
-  CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(nfine, 1), st));
-  CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(ncoarse, 1), st));
-  const int sb = view ? 4 : 0;  // first stage index of this pass
-  const int nst = view ? 5 : 4;
-  auto mark = [&](int k) -> cudaError_t { return s->profile ? cudaEventRecord(s->ev[sb * 2 + k], st) : cudaSuccess; };
+  CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.nfine, 1), st));
+  CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.ncoarse, 1), st));
+  auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
   CU(mark(0));
   if (view)
-    CU(launch_setup_views(sd, wm.views.p, nitems, wm.surf.p, ws, st));
+    CU(launch_setup_views(sd, wm.views.p, sh.nitems, wm.surf.p, ws, st));
   else
-    CU(launch_setup_shadow(sd, wm.jobs.p, nitems, wm.surf.p, ws, st));
+    CU(launch_setup_shadow(sd, wm.jobs.p, sh.nitems, wm.surf.p, ws, st));
   CU(mark(1));
   CU(launch_scan(ws, st));
   CU(mark(2));
   CU(launch_fill(ws, wm.surf.p, st));
   CU(mark(3));
-  CU(launch_raster(ws, wm.surf.p, nsurf, nfine, view, st));
+  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, st));
   CU(mark(4));
   if (view) {
-    CU(launch_shade(sd, wm.views.p, nitems, wm.surf.p, nfine, ws.srec, st));
+    CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st));
     CU(mark(5));
   }
-  s->stats.launches += (uint64_t)nst;
-  CU(cudaMemcpyAsync(counter_slot(s, view), ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+  CU(cudaMemcpyAsync(host_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
   return GBR_OK;
 }
 
-// After the pass's stream is synchronised: record its counters and stage
-// times, and on overflow grow the targets.  Returns true when the pass fit.
-bool check_pass(gbr_scene* s, bool view) {
-  const Counters c = *counter_slot(s, view);
-  WorkMem& w = pass_mem(s, view);
-  if (s->profile) {
-    const int sb = view ? 4 : 0, nst = view ? 5 : 4;
-    for (int k = 0; k < nst; k++) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, s->ev[sb * 2 + k], s->ev[sb * 2 + k + 1]) == cudaSuccess) {
-        s->stats.stage_ms[sb + k] += ms;
-        s->stats.stage_calls[sb + k] += 1;
-      }
-    }
-  }
+bool absorb_counters(gbr_scene* s, const Counters& c, WorkMem& w, float headroom, bool view) {
   if (!c.overflow) {
     if (view) {
       s->stats.view_records = c.nrec;
@@ -346,17 +211,61 @@ bool check_pass(gbr_scene* s, bool view) {
     return true;
   }
   s->stats.retries++;
-  if (c.overflow & 1u) w.rec_target = (uint32_t)std::min<uint64_t>((uint64_t)c.nrec * 5 / 4 + 1024, 0xFFFFFFF0u);
+  const double h = std::min(std::max((double)headroom, 1.05), 4.0);
+  if (c.overflow & 1u)
+    w.rec_target = (uint32_t)std::min<double>((double)c.nrec * h + 1024.0, (double)0xFFFFFFF0u);
   uint64_t need_bins = (uint64_t)c.fine_total + c.coarse_total;
   if (c.overflow & 1u) need_bins = std::max<uint64_t>(need_bins, (uint64_t)w.rec_target * 4);
-  w.bin_target = (uint32_t)std::min<uint64_t>(need_bins * 5 / 4 + 4096, 0xFFFFFFF0u);
+  w.bin_target = (uint32_t)std::min<double>((double)need_bins * h + 4096.0, (double)0xFFFFFFF0u);
   return false;
+}
+
+}  // namespace gbr
+
+namespace {
+
+WorkMem& pass_mem(gbr_scene* s, bool view) { return view ? s->ws_view : s->ws_shadow; }
+
+Counters* counter_slot(gbr_scene* s, bool view) {
+  return reinterpret_cast<Counters*>(static_cast<char*>(s->staging.p) + (view ? 0 : 256));
+}
+
+// Launch one pass (views or shadow jobs) on the scene's own scratch and queue
+// the read-back of its counters; the caller synchronises and calls
+// check_pass.  The caller has filled the pass's surfaces / views / jobs on
+// the device.
+gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream_t st) {
+  TRY(ensure_world(s, st));
+  WorkMem& wm = pass_mem(s, view);
+  TRY(reserve_pass(wm, sh, view));
+  cudaEvent_t* ev = s->profile ? s->ev + (view ? 8 : 0) : nullptr;
+  TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st));
+  s->stats.launches += pass_kernels(view);
+  return GBR_OK;
+}
+
+// After the pass's stream is synchronised: record its counters and stage
+// times, and on overflow grow the targets.  Returns true when the pass fit.
+bool check_pass(gbr_scene* s, bool view) {
+  const Counters c = *counter_slot(s, view);
+  if (s->profile) {
+    const int sb = view ? 4 : 0, nst = (int)pass_kernels(view);
+    for (int k = 0; k < nst; k++) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, s->ev[sb * 2 + k], s->ev[sb * 2 + k + 1]) == cudaSuccess) {
+        s->stats.stage_ms[sb + k] += ms;
+        s->stats.stage_calls[sb + k] += 1;
+      }
+    }
+  }
+  const Tuning& tu = s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW];
+  return absorb_counters(s, c, pass_mem(s, view), tu.headroom, view);
 }
 
 // Run a shadow pass to completion (grow and retry until it fits).
 gbr_status run_shadow_sync(gbr_scene* s, const PassShape& sh, cudaStream_t st) {
   for (int attempt = 0; attempt < 6; attempt++) {
-    TRY(enqueue_pass(s, false, sh.nitems, sh.nsurf, sh.nfine, sh.ncoarse, 0, st));
+    TRY(enqueue_pass(s, false, sh, st));
     CU(cudaStreamSynchronize(st));
     if (check_pass(s, false)) return GBR_OK;
   }
@@ -381,6 +290,42 @@ gbr_status settle_shadow_quiet(gbr_scene* s) {
   bool rerun = false;
   return settle_shadow(s, false, &rerun);
 }
+
+}  // namespace
+
+namespace gbr {
+
+gbr_status settle_scene_shadow(gbr_scene* s) { return settle_shadow_quiet(s); }
+
+gbr_status tuning_from_abi(const gbr_tuning* t, Tuning* out) {
+  if (!t || !out) return fail(GBR_INVALID_ARG, "null tuning");
+  if (t->raster_threads != 128 && t->raster_threads != 256 && t->raster_threads != 512)
+    return fail(GBR_INVALID_ARG, "raster_threads %d: must be 128, 256 or 512", t->raster_threads);
+  int shift = -1;
+  for (int k = 2; k <= 4; k++)
+    if (t->coarse_tile == (kTile << k)) shift = k;
+  if (shift < 0) return fail(GBR_INVALID_ARG, "coarse_tile %d: must be 64, 128 or 256", t->coarse_tile);
+  if (t->fine_max_tiles < 1 || t->fine_max_tiles > 256)
+    return fail(GBR_INVALID_ARG, "fine_max_tiles %d: must be in 1..256", t->fine_max_tiles);
+  if (!(t->scratch_headroom >= 1.05f && t->scratch_headroom <= 4.0f))
+    return fail(GBR_INVALID_ARG, "scratch_headroom %g: must be in 1.05..4", (double)t->scratch_headroom);
+  out->raster_threads = t->raster_threads;
+  out->coarse_shift = shift;
+  out->fine_max = t->fine_max_tiles;
+  out->headroom = t->scratch_headroom;
+  return GBR_OK;
+}
+
+void tuning_to_abi(const Tuning& t, gbr_tuning* out) {
+  out->raster_threads = t.raster_threads;
+  out->coarse_tile = kTile << t.coarse_shift;
+  out->fine_max_tiles = t.fine_max;
+  out->scratch_headroom = t.headroom;
+}
+
+}  // namespace gbr
+
+namespace {
 
 // texture_context.cpp:94-261: page list and slot descriptors.
 gbr_status pack_textures(uint32_t n, const int32_t* sz, std::vector<uint32_t>& nums,
@@ -487,6 +432,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
 
 gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint32_t n) {
   TRY(check_scene(s));
+  s->version++;  // captured batches re-capture
   if (n && !tris) return fail(GBR_INVALID_ARG, "null triangles");
   TRY(s->tris.reserve(n));
   if (n) CU(cudaMemcpy(s->tris.p, tris, sizeof(gbr_triangle) * n, cudaMemcpyHostToDevice));
@@ -506,6 +452,7 @@ gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint3
 
 gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d, uint32_t n) {
   TRY(check_scene(s));
+  s->version++;  // captured batches re-capture
   if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
   TRY(s->descs.reserve(n));
   if (n) CU(cudaMemcpy(s->descs.p, d, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyHostToDevice));
@@ -520,6 +467,7 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
 
 gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
   TRY(check_scene(s));
+  s->version++;  // captured batches re-capture
   if (n && !l) return fail(GBR_INVALID_ARG, "null lights");
   if (n > (uint32_t)kMaxLights) return fail(GBR_INVALID_ARG, "%u lights: at most %d", n, kMaxLights);
   for (uint32_t i = 0; i < n; i++)
@@ -546,6 +494,7 @@ gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
 
 gbr_status gbr_scene_set_textures(gbr_scene* s, uint32_t n, const int32_t* sizes, const uint8_t* const* rgba) {
   TRY(check_scene(s));
+  s->version++;  // captured batches re-capture
   if (n && (!sizes || !rgba)) return fail(GBR_INVALID_ARG, "null texture arrays");
   for (uint32_t i = 0; i < n; i++)
     if (!rgba[i]) return fail(GBR_INVALID_ARG, "null texture %u", i);
@@ -645,26 +594,8 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
   const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
   std::vector<ShadowJob> jobs;
   std::vector<Surface> surfs;
-  uint32_t nn = 0, kk = 0, tb = 0, cb = 0;
-  auto add_job = [&](const gbr_light& L, int only_static, uint32_t* base) {
-    ShadowJob J{};
-    J.lpos[0] = L.pos[0]; J.lpos[1] = L.pos[1]; J.lpos[2] = L.pos[2];
-    J.only_static = only_static;
-    J.surface_base = (uint32_t)surfs.size();
-    for (int f = 0; f < 6; f++) {
-      Surface S{};
-      S.width = S.height = kLightBufferDim;
-      tile_layout(S, tb, cb);
-      S.depth = base + (size_t)f * face;
-      S.chunk = kOpSizeLight;
-      surfs.push_back(S);
-    }
-    jobs.push_back(J);
-  };
-  for (const gbr_light& L : s->host_lights) {
-    if (L.shadow == 1) add_job(L, 0, s->shadow_dyn.p + (size_t)(nn++) * 6 * face);
-    if (L.shadow && L.is_static && s->static_dirty) add_job(L, 1, s->shadow_static.p + (size_t)(kk++) * 6 * face);
-  }
+  PassShape sh;
+  shadow_layout(s, s->static_dirty, s->tune[GBR_PASS_SHADOW].coarse_shift, jobs, surfs, sh);
   if (jobs.empty()) return GBR_OK;
   TRY(check_indices(s, false));
   if (s->ntris == 0) {
@@ -677,13 +608,7 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
   TRY(wm.jobs.reserve(jobs.size()));
   CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), surfs.size() * sizeof(Surface), cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(wm.jobs.p, jobs.data(), jobs.size() * sizeof(ShadowJob), cudaMemcpyHostToDevice, st));
-  // wait for the copies of the small arrays before the host vectors go away
-  PassShape sh;
-  sh.nitems = (uint32_t)jobs.size();
-  sh.nsurf = (uint32_t)surfs.size();
-  sh.nfine = tb;
-  sh.ncoarse = cb;
-  TRY(enqueue_pass(s, false, sh.nitems, sh.nsurf, sh.nfine, sh.ncoarse, 0, st));
+  TRY(enqueue_pass(s, false, sh, st));
   // The counters are checked at the next synchronisation point (render,
   // read-back, stats), which re-runs this pass if its scratch overflowed.
   s->shadow_pending = true;
@@ -707,6 +632,7 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   std::vector<ViewParams> vp(n);
   uint32_t tb = 0, cb = 0;
   size_t off = 0;
+  const int cshift = s->tune[GBR_PASS_VIEW].coarse_shift;
   bool need_depth = false;
   for (uint32_t i = 0; i < n; i++)
     if (!outs[i].depth) need_depth = true;
@@ -717,20 +643,12 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     Surface& S = surfs[i];
     S.width = v.width;
     S.height = v.height;
-    tile_layout(S, tb, cb);
+    tile_layout(S, tb, cb, cshift);
     S.depth = outs[i].depth ? outs[i].depth : s->ws_view.pix_depth.p + off;
     S.id = outs[i].id;
     S.rec = s->ws_view.pix_rec.p + off;
     S.chunk = kOpSize;
-    ViewParams& V = vp[i];
-    memcpy(V.cpos, cams[i].pos, 12);
-    euler_cs(cams[i].rot, V.ccos, V.csin);
-    V.fov = v.fov_const > 0 ? v.fov_const : gbr_fov_const_from_hfov(v.hfov_deg, v.width);
-    V.surface = i;
-    V.use_linear = v.use_linear;
-    memcpy(V.clear, v.clear_col, 16);
-    V.rgba = outs[i].rgba;
-    V.normals = outs[i].normals;
+    fill_view_params(cams[i], v, outs[i], i, vp[i]);
     off += (size_t)v.width * v.height;
   }
   TRY(check_indices(s, true));
@@ -743,8 +661,13 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     bool rerun = false;
     TRY(settle_shadow(s, false, &rerun));
   }
+  PassShape sh;
+  sh.nitems = sh.nsurf = n;
+  sh.nfine = tb;
+  sh.ncoarse = cb;
+  sh.npix = npix;
   for (int attempt = 0; attempt < 8; attempt++) {
-    TRY(enqueue_pass(s, true, n, n, tb, cb, npix, st));
+    TRY(enqueue_pass(s, true, sh, st));
     CU(cudaStreamSynchronize(st));
     bool rerun = false;
     TRY(settle_shadow(s, true, &rerun));  // same stream: already complete
@@ -792,6 +715,23 @@ gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
     for (double& v : s->stats.stage_ms) v = 0;
     for (uint64_t& v : s->stats.stage_calls) v = 0;
   }
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_set_tuning(gbr_scene* s, int32_t pass, const gbr_tuning* t) {
+  TRY(check_scene(s));
+  if (pass != GBR_PASS_SHADOW && pass != GBR_PASS_VIEW) return fail(GBR_INVALID_ARG, "pass %d", pass);
+  Tuning tu;
+  TRY(tuning_from_abi(t, &tu));
+  TRY(settle_shadow_quiet(s));  // a pending shadow pass is re-run with the shape it was laid out for
+  s->tune[pass] = tu;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_get_tuning(gbr_scene* s, int32_t pass, gbr_tuning* t) {
+  if (!s || !t) return fail(GBR_INVALID_ARG, "null argument");
+  if (pass != GBR_PASS_SHADOW && pass != GBR_PASS_VIEW) return fail(GBR_INVALID_ARG, "pass %d", pass);
+  tuning_to_abi(s->tune[pass], t);
   return GBR_OK;
 }
 

@@ -24,10 +24,12 @@
 namespace gbr {
 
 constexpr int kTile = 16;                    // fine tile edge, pixels
-constexpr int kCoarse = 128;                 // coarse tile edge, pixels
-constexpr int kCoarseRatio = kCoarse / kTile;
+constexpr int kTilePixels = kTile * kTile;
+// Defaults of the tunable binning / raster shape (Tuning below):
+constexpr int kCoarseShift = 3;              // coarse tile edge = kTile << shift = 128 pixels
+constexpr int kCoarse = kTile << kCoarseShift;
 constexpr int kFineMaxTiles = 16;            // more fine tiles than this -> coarse bins
-constexpr int kRasterThreads = kTile * kTile;
+constexpr int kRasterThreads = kTilePixels;  // threads of one raster CTA
 constexpr int kMaxLights = 256;              // lights a scene may hold (staged in shared memory)
 
 // Per visible clipped triangle on one surface: everything kernel1/kernel2
@@ -110,6 +112,16 @@ struct SceneDev {
   float face_cos[6][3], face_sin[6][3];
 };
 
+// Shape of a pass that does not change its results (every resolve is a
+// minimum): coarse tile edge, the fine/coarse binning threshold, the raster
+// CTA size, and the headroom of scratch growth after an overflow.
+struct Tuning {
+  int32_t raster_threads = kRasterThreads;  // 128, 256 or 512
+  int32_t coarse_shift = kCoarseShift;      // 2, 3 or 4 (64, 128, 256 pixels)
+  int32_t fine_max = kFineMaxTiles;         // 1..256
+  float headroom = 1.25f;                   // 1.05..4
+};
+
 struct Workspace {
   RasterRec* rec;
   ShadeRec* srec;  // may be null (shadow passes)
@@ -123,6 +135,8 @@ struct Workspace {
   uint32_t* bins;
   uint32_t bin_cap;
   Counters* ctr;
+  int32_t fine_max;      // Tuning::fine_max
+  int32_t coarse_shift;  // Tuning::coarse_shift
 };
 
 // ---- launchers (gbr_kernels.cu) ----
@@ -134,7 +148,7 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,
-                          uint32_t ntiles, bool with_id, cudaStream_t st);
+                          uint32_t ntiles, bool with_id, int threads, cudaStream_t st);
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                          const Surface* d_surf, uint32_t ntiles, const ShadeRec* srec,
                          cudaStream_t st);

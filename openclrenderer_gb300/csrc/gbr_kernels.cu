@@ -120,15 +120,18 @@ __device__ __forceinline__ uint32_t foot_tile(const Foot& f, int k, const Surfac
   const int ty = f.ty0 + k / w, tx = f.tx0 + k % w;
   return f.coarse ? S.ctile_base + ty * S.ctiles_x + tx : S.tile_base + ty * S.tiles_x + tx;
 }
-__device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr) {
+// Records touching more than ws.fine_max fine tiles go to the coarse bins
+// (tiles of kTile << ws.coarse_shift pixels).
+__device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr, const Workspace& ws) {
   Foot f;
   int minx = xr & 0xFFFF, maxx = xr >> 16, miny = yr & 0xFFFF, maxy = yr >> 16;
   f.tx0 = minx / kTile; f.tx1 = (maxx - 1) / kTile;
   f.ty0 = miny / kTile; f.ty1 = (maxy - 1) / kTile;
-  f.coarse = (f.tx1 - f.tx0 + 1) * (f.ty1 - f.ty0 + 1) > kFineMaxTiles;
+  f.coarse = (f.tx1 - f.tx0 + 1) * (f.ty1 - f.ty0 + 1) > ws.fine_max;
   if (f.coarse) {
-    f.tx0 /= kCoarseRatio; f.tx1 /= kCoarseRatio;
-    f.ty0 /= kCoarseRatio; f.ty1 /= kCoarseRatio;
+    const int sh = ws.coarse_shift;
+    f.tx0 >>= sh; f.tx1 >>= sh;
+    f.ty0 >>= sh; f.ty1 >>= sh;
   }
   return f;
 }
@@ -145,7 +148,7 @@ __device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t sur
     ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
     ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
   }
-  *foot = footprint(R.xr, R.yr);
+  *foot = footprint(R.xr, R.yr, ws);
   return foot_count(*foot);
 }
 
@@ -439,7 +442,7 @@ __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __res
     if (valid) {
       float4 q = __ldg(reinterpret_cast<const float4*>(ws.rec + r) + 3);
       S = surfs + __float_as_uint(q.z);
-      f = footprint(__float_as_uint(q.x), __float_as_uint(q.y));
+      f = footprint(__float_as_uint(q.x), __float_as_uint(q.y), ws);
       total = foot_count(f);
     }
     int maxt = total;
@@ -494,6 +497,7 @@ __device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int ch
 // among tests within +-20 of the final depth.  Both are minima, so neither
 // bin order nor thread order changes the result.  When the whole list fits
 // one chunk, pass 1 reuses the staged records and offsets.
+template <int NT>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t incl = v;
@@ -505,29 +509,32 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp,
   if (lane == 31) swarp[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    uint32_t w = lane < (kRasterThreads / 32) ? swarp[lane] : 0;
+    uint32_t w = lane < (NT / 32) ? swarp[lane] : 0;
     uint32_t wi = w;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
       if (lane >= o) wi += t;
     }
-    if (lane < (kRasterThreads / 32)) swarp[lane] = wi - w;
-    if (lane == (kRasterThreads / 32) - 1) *total = wi;
+    if (lane < (NT / 32)) swarp[lane] = wi - w;
+    if (lane == (NT / 32) - 1) *total = wi;
   }
   __syncthreads();
   return swarp[warp] + incl - v;
 }
 
-__global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const Surface* __restrict__ surfs,
-                                                           uint32_t nsurf, int with_id) {
-  __shared__ float4 srec[kRasterThreads][4];
-  __shared__ uint32_t sidx[kRasterThreads];
-  __shared__ uint32_t soff[kRasterThreads + 1];
-  __shared__ uint32_t sgeo[kRasterThreads];  // lx0 | ly0 << 8 | bw << 16
-  __shared__ uint32_t sdepth[kRasterThreads];
-  __shared__ unsigned long long sid[kRasterThreads];
-  __shared__ uint32_t swarp[kRasterThreads / 32];
+// NT threads per CTA (128, 256 or 512): the records are staged NT at a time
+// and the (record, pixel) list is walked in strides of NT.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_raster(Workspace ws, const Surface* __restrict__ surfs, uint32_t nsurf,
+                                               int with_id) {
+  __shared__ float4 srec[NT][4];
+  __shared__ uint32_t sidx[NT];
+  __shared__ uint32_t soff[NT + 1];
+  __shared__ uint32_t sgeo[NT];  // lx0 | ly0 << 8 | bw << 16
+  __shared__ uint32_t sdepth[kTilePixels];
+  __shared__ unsigned long long sid[kTilePixels];
+  __shared__ uint32_t swarp[NT / 32];
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
   if (ws.ctr->overflow) return;
@@ -538,24 +545,26 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const S
     S = surfs[s];
     uint32_t lt = tile - S.tile_base;
     int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
-    uint32_t ct = S.ctile_base + (ty / kCoarseRatio) * S.ctiles_x + tx / kCoarseRatio;
+    uint32_t ct = S.ctile_base + (ty >> ws.coarse_shift) * S.ctiles_x + (tx >> ws.coarse_shift);
     lists[0] = ws.fine_off[tile];
     lists[1] = ws.fine_count[tile];
     lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
     lists[3] = ws.coarse_count[ct];
   }
-  sdepth[tid] = kDepthClear;
-  sid[tid] = ~0ull;
+  for (int p = tid; p < kTilePixels; p += NT) {
+    sdepth[p] = kDepthClear;
+    sid[p] = ~0ull;
+  }
   __syncthreads();
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
   const int chunk = S.chunk;
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
-  const bool resident = ntotal <= (uint32_t)kRasterThreads;
+  const bool resident = ntotal <= (uint32_t)NT;
   for (int pass = 0; pass < passes; pass++) {
-    for (uint32_t c0 = 0; c0 < ntotal; c0 += kRasterThreads) {
-      const uint32_t m = min((uint32_t)kRasterThreads, ntotal - c0);
+    for (uint32_t c0 = 0; c0 < ntotal; c0 += NT) {
+      const uint32_t m = min((uint32_t)NT, ntotal - c0);
       if (!(resident && pass == 1)) {
         __syncthreads();
         uint32_t area = 0;
@@ -577,12 +586,12 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const S
             sgeo[tid] = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 8) | ((uint32_t)(bx1 - bx0) << 16);
           }
         }
-        uint32_t off = block_excl_scan(area, swarp, &soff[kRasterThreads]);
+        uint32_t off = block_excl_scan<NT>(area, swarp, &soff[NT]);
         soff[tid] = off;
         __syncthreads();
       }
-      const uint32_t total = soff[kRasterThreads];
-      for (uint32_t t = tid; t < total; t += kRasterThreads) {
+      const uint32_t total = soff[NT];
+      for (uint32_t t = tid; t < total; t += NT) {
         // owning record: the last i < m with soff[i] <= t
         int lo = 0, hi = (int)m - 1;
         while (lo < hi) {
@@ -610,14 +619,16 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster(Workspace ws, const S
     }
     __syncthreads();
   }
-  const int px = tx0 + (tid & (kTile - 1)), py = ty0 + (tid / kTile);
-  if (px < S.width && py < S.height) {
-    const size_t p = (size_t)py * S.width + px;
-    S.depth[p] = sdepth[tid];
-    if (with_id) {
-      const unsigned long long v = sid[tid];
-      if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
-      S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;
+  for (int lp = tid; lp < kTilePixels; lp += NT) {
+    const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
+    if (px < S.width && py < S.height) {
+      const size_t p = (size_t)py * S.width + px;
+      S.depth[p] = sdepth[lp];
+      if (with_id) {
+        const unsigned long long v = sid[lp];
+        if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
+        S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;
+      }
     }
   }
 }
@@ -1170,9 +1181,14 @@ cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t
 }
 
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, uint32_t ntiles,
-                          bool with_id, cudaStream_t st) {
+                          bool with_id, int threads, cudaStream_t st) {
   if (!ntiles) return cudaSuccess;
-  k_raster<<<ntiles, kRasterThreads, 0, st>>>(ws, d_surf, nsurf, with_id ? 1 : 0);
+  const int wid = with_id ? 1 : 0;
+  switch (threads) {
+    case 128: k_raster<128><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf, wid); break;
+    case 512: k_raster<512><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf, wid); break;
+    default: k_raster<256><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf, wid); break;
+  }
   return cudaGetLastError();
 }
 

@@ -189,6 +189,8 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   ws.rec_cap = (uint32_t)kMaxRecords;
   ws.bins = reinterpret_cast<uint32_t*>(base + kOffBins);
   ws.bin_cap = (uint32_t)kMaxBins;
+  ws.fine_max = kFineMaxTiles;
+  ws.coarse_shift = kCoarseShift;
   Surface* d_surf = reinterpret_cast<Surface*>(base + kOffSurface);
   ViewParams* d_view = reinterpret_cast<ViewParams*>(base + kOffView);
 
@@ -207,7 +209,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   NA_CU(launch_setup_views(d, d_view, 1, d_surf, ws, s), "setup launch failed");
   NA_CU(launch_scan(ws, s), "scan launch failed");
   NA_CU(launch_fill(ws, d_surf, s), "fill launch failed");
-  NA_CU(launch_raster(ws, d_surf, 1, nfine, true, s), "raster launch failed");
+  NA_CU(launch_raster(ws, d_surf, 1, nfine, true, kRasterThreads, s), "raster launch failed");
   NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws.srec, s), "shade launch failed");
   Counters c{};
   NA_CU(cudaMemcpyAsync(&c, ws.ctr, sizeof c, cudaMemcpyDeviceToHost, s), "counter read-back failed");

@@ -1,0 +1,207 @@
+// gbr_scene.h — host-side state of a scene (device buffers, pass scratch,
+// tuning) and the pass drivers shared by the single-call API (gbr_api.cu) and
+// the captured batches (gbr_batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/gbr.h"
+#include "gbr_internal.h"
+
+namespace gbr {
+
+// Records the message for gbr_last_error_string() and returns s.
+gbr_status fail(gbr_status s, const char* fmt, ...);
+
+#define CU(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess)                                                                        \
+      return ::gbr::fail(e_ == cudaErrorMemoryAllocation ? GBR_OOM : GBR_CUDA_ERROR, "%s: %s (%s:%d)", \
+                         #call, cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+  } while (0)
+
+#define TRY(expr)                \
+  do {                           \
+    gbr_status s_ = (expr);      \
+    if (s_ != GBR_OK) return s_; \
+  } while (0)
+
+// Device buffer that only grows.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  gbr_status reserve(size_t n) {
+    if (n <= cap && p) return GBR_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t m = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, m * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(GBR_OOM, "cudaMalloc of %zu bytes failed: %s", m * sizeof(T), cudaGetErrorString(e));
+    }
+    cap = m;
+    return GBR_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Pinned host staging buffer that only grows.
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  gbr_status reserve(size_t n) {
+    if (n <= bytes && p) return GBR_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(n, 64));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(GBR_OOM, "cudaMallocHost of %zu bytes failed", n);
+    }
+    bytes = std::max<size_t>(n, 64);
+    return GBR_OK;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+// Scratch memory of one pass (records, bins, tile counters, per-pixel record
+// indices of the views).
+struct WorkMem {
+  DevBuf<RasterRec> rec;
+  DevBuf<ShadeRec> srec;
+  DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins;
+  DevBuf<Counters> ctr;
+  DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
+  DevBuf<uint8_t> pix_rgba;
+  DevBuf<Surface> surf;
+  DevBuf<ViewParams> views;
+  DevBuf<ShadowJob> jobs;
+  uint32_t rec_target = 0, bin_target = 0;
+  void release() {
+    rec.release(); srec.release(); fine_count.release(); fine_off.release();
+    coarse_count.release(); coarse_off.release(); bins.release(); ctr.release();
+    pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
+    surf.release(); views.release(); jobs.release();
+  }
+};
+
+struct PassShape {
+  uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
+  size_t npix = 0;
+};
+
+void euler_cs(const float ang[3], float c[3], float s[3]);
+
+}  // namespace gbr
+
+struct gbr_scene {
+  int device = 0;
+  gbr::DevBuf<gbr_triangle> tris;
+  uint32_t ntris = 0;
+  gbr::DevBuf<float4> world;  // world-space vertices, 3 per triangle
+  bool world_dirty = true;    // triangles or descriptors changed since k_world ran
+  gbr::DevBuf<gbr_obj_g_descriptor> descs;
+  uint32_t ndescs = 0;
+  gbr::DevBuf<gbr_light> lights;
+  std::vector<gbr_light> host_lights;
+  gbr::DevBuf<uchar4> atlas;
+  gbr::DevBuf<uint32_t> nums, sizes;
+  std::vector<uint32_t> host_nums, host_sizes;
+  uint32_t mipmap_start = 0;
+  uint32_t npages = 0;
+  gbr::DevBuf<uint32_t> shadow_dyn, shadow_static;
+  uint32_t n_dyn = 0, n_static = 0;
+  uint32_t max_object_id = 0, max_tid = 0;
+  bool static_dirty = true;
+  gbr::WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
+  gbr::HostBuf staging;         // counters read back: view at 0, shadow at 256
+  bool shadow_pending = false;  // a shadow pass whose counters are not checked yet
+  cudaStream_t shadow_stream = nullptr;
+  gbr::PassShape shadow_shape;
+  gbr_stats stats{};
+  float face_cos[6][3], face_sin[6][3];
+  bool profile = false;
+  cudaEvent_t ev[20] = {};
+  gbr::Tuning tune[2];   // [GBR_PASS_SHADOW], [GBR_PASS_VIEW]
+  uint64_t version = 1;  // bumped whenever a device pointer or table a pass reads changes
+
+  gbr::SceneDev dev() const {
+    gbr::SceneDev d{};
+    d.tris = tris.p;
+    d.ntris = ntris;
+    d.world = world_dirty ? nullptr : world.p;
+    d.descs = descs.p;
+    d.ndescs = ndescs;
+    d.lights = lights.p;
+    d.nlights = (uint32_t)host_lights.size();
+    d.atlas = atlas.p;
+    d.nums = nums.p;
+    d.sizes = sizes.p;
+    d.mipmap_start = mipmap_start;
+    d.shadow_dyn = shadow_dyn.p;
+    d.shadow_static = shadow_static.p;
+    for (int f = 0; f < 6; f++)
+      for (int k = 0; k < 3; k++) {
+        d.face_cos[f][k] = face_cos[f][k];
+        d.face_sin[f][k] = face_sin[f][k];
+      }
+    return d;
+  }
+};
+
+namespace gbr {
+
+gbr_status check_scene(gbr_scene* s);
+// Every index the kernels follow must stay inside its table.
+gbr_status check_indices(gbr_scene* s, bool shading);
+gbr_status validate_view(const gbr_view* v);
+// World-space vertex cache (k_world), rebuilt when triangles or descriptors change.
+gbr_status ensure_world(gbr_scene* s, cudaStream_t st);
+// Fine and coarse tile numbering of a surface; advances the running bases.
+void tile_layout(Surface& S, uint32_t& tile_base, uint32_t& ctile_base, int coarse_shift);
+// Camera and output pointers of one view as the setup and shade kernels read them.
+void fill_view_params(const gbr_camera& cam, const gbr_view& v, const gbr_outputs& o, uint32_t surface,
+                      ViewParams& V);
+// Cube-face surfaces and jobs of the shadow-casting lights (dynamic cubemaps,
+// and the static ones when with_static).
+void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector<ShadowJob>& jobs,
+                   std::vector<Surface>& surfs, PassShape& sh);
+// Scratch of a pass sized to the memory's targets (no allocation when it fits).
+gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view);
+// Launches of one pass on the pass's scratch: counter clears, setup, scan,
+// fill, raster and (views) shade, then the read-back of the counters into
+// host_ctr.  Allocates nothing, so it can be captured into a graph.  ev, when
+// not null, holds the stage events (profiling).
+gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
+                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st);
+// Kernel launches of one pass (for the launch statistics).
+inline uint32_t pass_kernels(bool view) { return view ? 5u : 4u; }
+// Record a finished pass's counters in the scene's statistics; on overflow
+// grow the memory's targets by the tuning's headroom and return false.
+bool absorb_counters(gbr_scene* s, const Counters& c, WorkMem& w, float headroom, bool view);
+// Wait for (and check) a shadow pass of the scene still in flight.
+gbr_status settle_scene_shadow(gbr_scene* s);
+// gbr_tuning <-> Tuning, with the range checks of the C ABI.
+gbr_status tuning_from_abi(const gbr_tuning* t, Tuning* out);
+void tuning_to_abi(const Tuning& t, gbr_tuning* out);
+
+}  // namespace gbr

@@ -7,6 +7,7 @@ generate_realtime_shadowing (engine.cpp:1794, 1601).  Device outputs are torch
 tensors; torch only provides device memory and streams here.
 """
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -84,11 +85,14 @@ class GpuScene:
         h = _P()
         _native.check(self.L.gbr_scene_create(ctypes.byref(h)))
         self.h = h
+        self._batches = weakref.WeakSet()  # closed before the scene
         if scene is not None:
             self.upload(scene)
 
     def close(self):
         if self.h:
+            for b in list(self._batches):
+                b.close()
             self.L.gbr_scene_destroy(self.h)
             self.h = None
 
@@ -194,6 +198,91 @@ class GpuScene:
 
     def profile(self, enable=True):
         _native.check(self.L.gbr_scene_profile(self.h, 1 if enable else 0))
+
+    def set_tuning(self, pass_kind, **kw):
+        """Binning / raster shape of the view (S.PASS_VIEW) or shadow pass."""
+        t = np.asarray(S.make_tuning(**{**self.tuning(pass_kind), **kw}), S.TUNING).reshape(1)
+        _native.check(self.L.gbr_scene_set_tuning(self.h, pass_kind, _np_ptr(t)))
+
+    def tuning(self, pass_kind):
+        t = np.zeros(1, S.TUNING)
+        _native.check(self.L.gbr_scene_get_tuning(self.h, pass_kind, _np_ptr(t)))
+        return _tuning_dict(t[0])
+
+
+def _tuning_dict(t):
+    return {k: (float(t[k]) if k == "scratch_headroom" else int(t[k])) for k in S.TUNING.names}
+
+
+class Batch:
+    """A captured batch (gbr_batch_*): fixed views and device outputs of one
+    scene, one CUDA graph per frame, replayed with new cameras."""
+
+    def __init__(self, scene, views, outs=None, with_shadow=False):
+        self.L = _native.load()
+        self.scene = scene
+        self.views = np.ascontiguousarray(np.stack([np.asarray(v, S.VIEW) for v in views]))
+        self.outs = outs if outs is not None else [OutputSet(int(v["width"]), int(v["height"])) for v in self.views]
+        arr = (_Outs * len(self.outs))()
+        for i, o in enumerate(self.outs):
+            arr[i] = _Outs(o.depth.data_ptr(), o.id.data_ptr(), o.rgba.data_ptr(),
+                           o.normals.data_ptr() if o.normals is not None else None)
+        h = _P()
+        flags = S.BATCH_WITH_SHADOW if with_shadow else 0
+        _native.check(self.L.gbr_batch_create(scene.h, len(self.outs), _np_ptr(self.views), arr, flags,
+                                              ctypes.byref(h)))
+        self.h = h
+        scene._batches.add(self)
+
+    @staticmethod
+    def _cams(cams):
+        return np.ascontiguousarray(np.stack([np.asarray(c, S.CAMERA) for c in cams]))
+
+    def render(self, cams, stream=None):
+        c = self._cams(cams)
+        _native.check(self.L.gbr_batch_render(self.h, _np_ptr(c), _stream_ptr(stream)))
+        return self.outs
+
+    def launch(self, cams, stream=None):
+        self._pending = self._cams(cams)
+        _native.check(self.L.gbr_batch_launch(self.h, _np_ptr(self._pending), _stream_ptr(stream)))
+
+    def wait(self):
+        _native.check(self.L.gbr_batch_wait(self.h))
+        return self.outs
+
+    def autotune(self, cams, reps=3, stream=None):
+        c = self._cams(cams)
+        vt, st = np.zeros(1, S.TUNING), np.zeros(1, S.TUNING)
+        ms = ctypes.c_float()
+        _native.check(self.L.gbr_batch_autotune(self.h, _np_ptr(c), _stream_ptr(stream), reps, _np_ptr(vt),
+                                                _np_ptr(st), ctypes.byref(ms)))
+        return {"view": _tuning_dict(vt[0]), "shadow": _tuning_dict(st[0]), "best_ms": ms.value}
+
+    def set_tuning(self, pass_kind, **kw):
+        t = np.asarray(S.make_tuning(**{**self.tuning(pass_kind), **kw}), S.TUNING).reshape(1)
+        _native.check(self.L.gbr_batch_set_tuning(self.h, pass_kind, _np_ptr(t)))
+
+    def tuning(self, pass_kind):
+        t = np.zeros(1, S.TUNING)
+        _native.check(self.L.gbr_batch_get_tuning(self.h, pass_kind, _np_ptr(t)))
+        return _tuning_dict(t[0])
+
+    def info(self):
+        i = np.zeros(1, S.BATCH_INFO)
+        _native.check(self.L.gbr_batch_get_info(self.h, _np_ptr(i)))
+        return {k: int(i[0][k]) for k in S.BATCH_INFO.names}
+
+    def close(self):
+        if self.h:
+            self.L.gbr_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

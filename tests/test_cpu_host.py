@@ -56,6 +56,8 @@ int main(void){
  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(gbr_vertex), sizeof(gbr_triangle), sizeof(gbr_obj_g_descriptor),
         sizeof(gbr_light), sizeof(gbr_camera), sizeof(gbr_view), sizeof(gbr_stats));
  printf("%zu %zu %zu %zu\n", sizeof(gbr_server_config), sizeof(gbr_request), sizeof(gbr_completion), sizeof(gbr_server_stats));
+ printf("%zu %zu %zu %d %d %d\n", sizeof(gbr_tuning), sizeof(gbr_batch_info), offsetof(gbr_batch_info, captures),
+        GBR_PASS_SHADOW, GBR_PASS_VIEW, GBR_BATCH_WITH_SHADOW);
  printf("%zu %zu %zu %zu %zu %zu\n", offsetof(gbr_vertex, object_id), offsetof(gbr_obj_g_descriptor, scale),
         offsetof(gbr_obj_g_descriptor, feature_flag), offsetof(gbr_light, shadow), offsetof(gbr_light, is_static),
         offsetof(gbr_stats, stage_ms));
@@ -64,7 +66,10 @@ int main(void){
     out = _compile_c(tmp_path, code, "layout").split()
     sizes = list(map(int, out[:7]))
     serving = list(map(int, out[7:11]))
-    offs = list(map(int, out[11:]))
+    batch = list(map(int, out[11:17]))
+    offs = list(map(int, out[17:]))
+    assert batch == [S.TUNING.itemsize, S.BATCH_INFO.itemsize, S.BATCH_INFO.fields["captures"][1],
+                     S.PASS_SHADOW, S.PASS_VIEW, S.BATCH_WITH_SHADOW]
     assert serving == [S.SERVER_CONFIG.itemsize, S.REQUEST.itemsize, S.COMPLETION.itemsize, S.SERVER_STATS.itemsize]
     assert sizes == [S.VERTEX.itemsize, S.TRIANGLE.itemsize, S.OBJ_DESC.itemsize, S.LIGHT.itemsize,
                      S.CAMERA.itemsize, S.VIEW.itemsize, S.STATS.itemsize]
