@@ -149,9 +149,10 @@ void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   if (!s->world_dirty) return GBR_OK;
   TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
+  TRY(s->objq.reserve((size_t)std::max<uint32_t>(s->ndescs, 1) * 2));
   SceneDev sd = s->dev();
-  CU(launch_world(sd, s->world.p, st));
-  s->stats.launches += 1;
+  CU(launch_world(sd, s->world.p, s->objq.p, st));
+  s->stats.launches += 2;
   s->world_dirty = false;
   return GBR_OK;
 }
@@ -423,6 +424,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->ws_shadow.release();
   s->ws_host.release();
   s->world.release();
+  s->objq.release();
   s->staging.release();
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);

@@ -99,6 +99,9 @@ struct SceneDev {
   // first half of full_rotate_quat, cl2.cl:700-710); w of vertex 0 holds the
   // object id.  3 per triangle.
   const float4* world;
+  // per object: fast_normalize4(world_rot_quat), then the normalised inverse
+  // back_rot_quat applies (cl2.cl:350-370); 2 per descriptor, or null
+  const float4* objq;
   const gbr_obj_g_descriptor* descs;
   uint32_t ndescs;
   const gbr_light* lights;
@@ -140,7 +143,7 @@ struct Workspace {
 };
 
 // ---- launchers (gbr_kernels.cu) ----
-cudaError_t launch_world(const SceneDev& sc, float4* world, cudaStream_t st);
+cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st);
 cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,

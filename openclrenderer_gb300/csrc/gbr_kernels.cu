@@ -231,6 +231,26 @@ __global__ void __launch_bounds__(256) k_world(SceneDev sc, float4* __restrict__
   }
 }
 
+// Per object: the normalised rotation quaternion rot_quat applies, and the
+// normalised inverse back_rot_quat applies (conjugate / |q|^2, normalised by
+// rot_quat) -- the same arithmetic every pixel of kernel3 would repeat.
+__device__ __forceinline__ f4 quat_inverse_n(f4 q) {
+  f4 conj; conj.x = -q.x; conj.y = -q.y; conj.z = -q.z; conj.w = q.w;
+  float len_sq = dot4(conj, conj);
+  f4 n; n.x = fdiv(conj.x, len_sq); n.y = fdiv(conj.y, len_sq);
+  n.z = fdiv(conj.z, len_sq); n.w = fdiv(conj.w, len_sq);
+  return fast_normalize4(n);
+}
+
+__global__ void __launch_bounds__(256) k_objects(SceneDev sc, float4* __restrict__ objq) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= sc.ndescs) return;
+  const f4 q = ld4(sc.descs[o].world_rot_quat);
+  const f4 qn = fast_normalize4(q), qi = quat_inverse_n(q);
+  objq[2 * o] = make_float4(qn.x, qn.y, qn.z, qn.w);
+  objq[2 * o + 1] = make_float4(qi.x, qi.y, qi.z, qi.w);
+}
+
 // World-space vertices of a triangle: from the scene's cache when there is
 // one, else computed here with the same arithmetic as k_world.
 __device__ __forceinline__ void load_world(const SceneDev& sc, uint32_t tri, f3 w[3], uint32_t* o_id) {
@@ -645,6 +665,9 @@ struct ShadeCtx {
 constexpr float kInvMulInt = 2.3283064365386963e-10f;
 __device__ __forceinline__ float depth_to_dist(uint32_t d) { return ((float)d * kInvMulInt) * kDepthFar; }
 
+// Exact byte -> float without a conversion instruction: 2^23 + b, minus 2^23.
+__device__ __forceinline__ float u8f(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
+
 // read_tex_array_all_precalculated (cl2.cl:823-851) with the slot origin
 // (tnumx, tnumy), which does not depend on the coordinates, computed once per
 // bilinear footprint.
@@ -652,12 +675,14 @@ struct TexSlot {
   float tnumx, tnumy, width;
   const uchar4* page;
 };
+// Page edges are powers of two (16..2048), so the slot row which*w/2048 and
+// column are exact in integers: floor(which / hnum) and which mod hnum.
 __device__ __forceinline__ TexSlot tex_slot_pre(const SceneDev& sc, int which, int slice, float width) {
-  const float imax = 1.0f / 2048.0f;
-  float ihnum = width * imax;
+  const int hnum = kTexPage / (int)width;
   TexSlot t;
-  t.tnumy = floorf((float)which * ihnum);
-  t.tnumx = (float)which - fdiv(t.tnumy, ihnum);
+  const int row = which / hnum;
+  t.tnumy = (float)row;
+  t.tnumx = (float)(which - row * hnum);
   t.width = width;
   t.page = sc.atlas + (size_t)slice * kTexPage * kTexPage;
   return t;
@@ -667,8 +692,8 @@ __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy
   cy = clampf_(cy, 0.001f, ts.width - 0.001f);
   int ix = f2i_sat(fma_(ts.tnumx, ts.width, cx));
   int iy = f2i_sat(fma_(ts.tnumy, ts.width, cy));
-  uchar4 t = __ldg(ts.page + ((size_t)iy * kTexPage + ix));
-  f4 r; r.x = t.x; r.y = t.y; r.z = t.z; r.w = t.w;
+  const uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(ts.page) + ((size_t)iy * kTexPage + ix));
+  f4 r; r.x = u8f(t & 0xFF); r.y = u8f((t >> 8) & 0xFF); r.z = u8f((t >> 16) & 0xFF); r.w = u8f(t >> 24);
   return r;
 }
 
@@ -743,8 +768,9 @@ __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth,
       acc += (d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f);
     }
   }
-  const float facc = fdiv((float)acc, 125.0f);
-  return 1.0f - fdiv(1.0f - facc, kSsaoDiv);
+  // the occlusion scales the colour only: approximate divisions
+  const float facc = (float)acc * (1.0f / 125.0f);
+  return 1.0f - (1.0f - facc) * (1.0f / kSsaoDiv);
 }
 
 __device__ __forceinline__ float bilinear_interpolate(float cx, float cy, float v0, float v1, float v2,
@@ -791,12 +817,14 @@ __device__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 normal, f3 ptl, 
   return fdiv(shadow, 9.0f);
 }
 
+// Vertex colour channels (colour path: multiplication by 1/255).
 __device__ __forceinline__ f4 vertex_col(uint32_t c) {
+  const float k = 1.0f / 255.0f;
   f4 r;
-  r.x = fdiv((float)(c >> 24), 255.f);
-  r.y = fdiv((float)((c >> 16) & 0xFF), 255.f);
-  r.z = fdiv((float)((c >> 8) & 0xFF), 255.f);
-  r.w = fdiv((float)(c & 0xFF), 255.f);
+  r.x = u8f(c >> 24) * k;
+  r.y = u8f((c >> 16) & 0xFF) * k;
+  r.z = u8f((c >> 8) & 0xFF) * k;
+  r.w = u8f(c & 0xFF) * k;
   return r;
 }
 
@@ -824,6 +852,43 @@ __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a
   return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
 }
 
+
+// Barycentrics (cl2.cl:5372-5384) split into the per-triangle part and the
+// per-point part; bary_exact is barycentric() bit for bit.
+struct BaryFrame {
+  f3 a, v0, v1;
+  float d00, d01, d11, denom;
+};
+__device__ __forceinline__ BaryFrame bary_frame(f3 a, f3 b, f3 c) {
+  BaryFrame f;
+  f.a = a;
+  f.v0 = sub3(b, a);
+  f.v1 = sub3(c, a);
+  f.d00 = dot3(f.v0, f.v0);
+  f.d01 = dot3(f.v0, f.v1);
+  f.d11 = dot3(f.v1, f.v1);
+  f.denom = f.d00 * f.d11 - f.d01 * f.d01;
+  return f;
+}
+__device__ __forceinline__ void bary_exact(const BaryFrame& f, f3 p, float* u, float* v, float* w) {
+  f3 v2 = sub3(p, f.a);
+  float d20 = dot3(v2, f.v0), d21 = dot3(v2, f.v1);
+  *v = fdiv(f.d11 * d20 - f.d01 * d21, f.denom);
+  *w = fdiv(f.d00 * d21 - f.d01 * d20, f.denom);
+  *u = (1.0f - *v) - *w;
+}
+// Colour-only square root (approximate; exact IEEE result for 0, negative,
+// infinite and NaN inputs).
+__device__ __forceinline__ float csqrt(float x) {
+  return (x > 0.0f && x < 3.0e38f) ? x * rsqrtf(x) : fsqrt(x);
+}
+// gamma_inv (cl2.cl:5778-5782) on the colour path.
+__device__ __forceinline__ float c_gamma_inv(float c) {
+  float s1 = csqrt(c);
+  float s2 = csqrt(s1);
+  float s3 = csqrt(s2);
+  return (0.585122381f * s1 + 0.783140355f * s2) - 0.368262736f * s3;
+}
 
 // A light as the shade loop reads it, staged once per CTA in shared memory;
 // col is already in linear space when the view renders linearly (the same
@@ -863,9 +928,19 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const gbr_obj_g_descriptor* G = sc.descs + o_id;
   const float scale = __ldg(&G->scale);
   const f3 wpos = ld3(G->world_pos);
-  const f4 q = ld4(G->world_rot_quat);
+  f4 qn, qi;  // rot_quat's and back_rot_quat's normalised quaternions
+  if (sc.objq) {
+    const float4 a = __ldg(sc.objq + 2 * o_id), b = __ldg(sc.objq + 2 * o_id + 1);
+    qn.x = a.x; qn.y = a.y; qn.z = a.z; qn.w = a.w;
+    qi.x = b.x; qi.y = b.y; qi.z = b.z; qi.w = b.w;
+  } else {
+    const f4 q = ld4(G->world_rot_quat);
+    qn = fast_normalize4(q);
+    qi = quat_inverse_n(q);
+  }
   f3 p1 = mul3s(tri_vec(T, 0, 0), scale), p2 = mul3s(tri_vec(T, 1, 0), scale),
      p3 = mul3s(tri_vec(T, 2, 0), scale);
+  const BaryFrame bf = bary_frame(p1, p2, p3);
   const float* tb = reinterpret_cast<const float*>(T);
   f2 vt1 = mk2(__ldg(tb + 8), __ldg(tb + 9)), vt2 = mk2(__ldg(tb + 20), __ldg(tb + 21)),
      vt3 = mk2(__ldg(tb + 32), __ldg(tb + 33));
@@ -877,13 +952,13 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
                  ldepth);
   const f3 zero = mk3(0, 0, 0);
   const f3 gpos = add3(back_rot_cs(local, zero, cc, cs), cpos);
-  f3 olocal = back_rot_quat(sub3(gpos, wpos), q);
+  f3 olocal = rot_quat_n(sub3(gpos, wpos), qi);
   float l1, l2, l3;
-  barycentric(olocal, p1, p2, p3, &l1, &l2, &l3);
+  bary_exact(bf, olocal, &l1, &l2, &l3);
   f2 vt = mk2(fma_(vt1.x, l1, fma_(vt2.x, l2, vt3.x * l3)), fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
   f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
                   fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
-  normal = rot_quat(normal, q);
+  normal = rot_quat_n(normal, qn);
 
   f4 col;
   const uint32_t vc0 = __ldg(&T->vertices[0].vertex_col);
@@ -895,7 +970,10 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
     col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
   } else {
-    // get_vtdiff (cl2.cl:5691-5760)
+    // get_vtdiff (cl2.cl:5691-5760).  The 1/z plane extrapolated to the
+    // neighbouring pixels is ill-conditioned for triangles seen edge-on (it
+    // can cross zero), so this stays in IEEE arithmetic: rounding differences
+    // there would pick other mip levels.
     f3 xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
     f3 ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
     f3 depths = mk3(rcp(tp[0].z), rcp(tp[1].z), rcp(tp[2].z));
@@ -908,11 +986,11 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     f3 lmy = mk3(fdiv(fx - hw, fov), fdiv((fy + 1.0f) - hh, fov), 1.0f);
     lmx = mk3(fdiv(lmx.x, dmx), fdiv(lmx.y, dmx), fdiv(lmx.z, dmx));
     lmy = mk3(fdiv(lmy.x, dmy), fdiv(lmy.y, dmy), fdiv(lmy.z, dmy));
-    f3 gmx = back_rot_quat(sub3(add3(back_rot_cs(lmx, zero, cc, cs), cpos), wpos), q);
-    f3 gmy = back_rot_quat(sub3(add3(back_rot_cs(lmy, zero, cc, cs), cpos), wpos), q);
+    f3 gmx = rot_quat_n(sub3(add3(back_rot_cs(lmx, zero, cc, cs), cpos), wpos), qi);
+    f3 gmy = rot_quat_n(sub3(add3(back_rot_cs(lmy, zero, cc, cs), cpos), wpos), qi);
     float lx1, lx2, lx3, ly1, ly2, ly3;
-    barycentric(gmx, p1, p2, p3, &lx1, &lx2, &lx3);
-    barycentric(gmy, p1, p2, p3, &ly1, &ly2, &ly3);
+    bary_exact(bf, gmx, &lx1, &lx2, &lx3);
+    bary_exact(bf, gmy, &ly1, &ly2, &ly3);
     f2 vtx = mk2(fma_(vt1.x, lx1, fma_(vt2.x, lx2, vt3.x * lx3)), fma_(vt1.y, lx1, fma_(vt2.y, lx2, vt3.y * lx3)));
     f2 vty = mk2(fma_(vt1.x, ly1, fma_(vt2.x, ly2, vt3.x * ly3)), fma_(vt1.y, ly1, fma_(vt2.y, ly2, vt3.y * ly3)));
     const float mip_bias = 1.0f / kMipBias;
@@ -937,7 +1015,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   if (!backface_front(tp[0], tp[1], tp[2]) && two) normal = neg3(normal);
   const float ssao = generate_ssao(x, y, S.depth, W, H, fov);
   normal = fast_normalize3(normal);
-  const f3 lnormal = cnormalize(add3(normal, mk3(fdiv(rseed.x, 100.f), fdiv(rseed.y, 100.f), fdiv(rseed.z, 100.f))));
+  const f3 lnormal = cnormalize(add3(normal, mk3(rseed.x * 0.01f, rseed.y * 0.01f, rseed.z * 0.01f)));
   const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
   const float g_diffuse = __ldg(&G->diffuse), g_spec_mult = __ldg(&G->spec_mult);
   const float rough = clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f);
@@ -955,7 +1033,12 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
       static_num++;
     }
-    float distance = fast_length3(ptl);
+    // The distance only feeds the colour, except through the cutoff below,
+    // which for a shadow light also decides which cubemap later shadow lights
+    // read (shnum): exact for shadow lights, approximate otherwise.
+    const float d2 = dot3(ptl, ptl);
+    const float rinv = rsqrtf(d2);
+    const float distance = (!lshadow && d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
     float tt = cdiv(distance, L.radius) + 1.0f;
     float illum = cdiv(L.brightness, tt * tt);
     const float cutoff = 0.1f;
@@ -969,7 +1052,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       occlusion = fmin_(occlusion, dyn);
       shnum++;
     }
-    ptl = cnormalize(ptl);
+    ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
     float light = fmax_(dot3(ptl, lnormal) * occlusion, 0.0f);
     float diffuse = (1.0f - ambient) * light;
     float dscale = (((diffuse + ambient) * L.diffuse) * g_diffuse) * illum;
@@ -998,7 +1081,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 colclamp = add3(add3(mk3(col.x, col.y, col.z), zero), mul3s(ssum, rsc));
   f3 sp2 = mul3s(ssum, 1.0f - rsc);
   f3 fin = mk3(fma_(colclamp.x, dsum.x, sp2.x), fma_(colclamp.y, dsum.y, sp2.y), fma_(colclamp.z, dsum.z, sp2.z));
-  if (V.use_linear) fin = mk3(gamma_inv(fin.x), gamma_inv(fin.y), gamma_inv(fin.z));
+  if (V.use_linear) fin = mk3(c_gamma_inv(fin.x), c_gamma_inv(fin.y), c_gamma_inv(fin.z));
   if (out) out[p] = pack_rgba(fin.x, fin.y, fin.z, col.w);
   if (V.normals) {
     // encode_normal (cl2.cl:5618-5628)
@@ -1148,9 +1231,9 @@ int num_sms() {
 
 }  // namespace
 
-cudaError_t launch_world(const SceneDev& sc, float4* world, cudaStream_t st) {
-  if (!sc.ntris) return cudaSuccess;
-  k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
+cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st) {
+  if (sc.ndescs) k_objects<<<(sc.ndescs + 255) / 256, 256, 0, st>>>(sc, objq);
+  if (sc.ntris) k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
   return cudaGetLastError();
 }
 

@@ -118,6 +118,7 @@ struct gbr_scene {
   gbr::DevBuf<gbr_triangle> tris;
   uint32_t ntris = 0;
   gbr::DevBuf<float4> world;  // world-space vertices, 3 per triangle
+  gbr::DevBuf<float4> objq;   // per descriptor: normalised quaternion and normalised inverse
   bool world_dirty = true;    // triangles or descriptors changed since k_world ran
   gbr::DevBuf<gbr_obj_g_descriptor> descs;
   uint32_t ndescs = 0;
@@ -149,6 +150,7 @@ struct gbr_scene {
     d.tris = tris.p;
     d.ntris = ntris;
     d.world = world_dirty ? nullptr : world.p;
+    d.objq = world_dirty ? nullptr : objq.p;
     d.descs = descs.p;
     d.ndescs = ndescs;
     d.lights = lights.p;
