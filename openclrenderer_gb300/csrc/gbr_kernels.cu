@@ -747,7 +747,9 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
 // generate_ssao (cl2.cl:2194-2260).  The 25 taps share 5 rows and 5
 // columns, so their rounded and clamped offsets are computed once; the depth
 // thresholds dep + z are computed once; and the count (at most 125, exact in
-// float) is kept in an integer.
+// float) is kept in an integer.  Far from the camera (world_rad < 0.25) every
+// offset rounds to 0 and all 25 taps read the same pixel; when that holds for
+// the whole warp, the pixel is read once and its count taken 25 times.
 __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth, int W, int H, float fov) {
   uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)W * (uint32_t)H * (uint32_t)y));
   float foffset = (float)seed2 * kInvMulInt;
@@ -758,14 +760,20 @@ __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth,
 #pragma unroll
   for (int k = 0; k < 5; k++) wx[k] = (int)clampf_((float)x + roundf((float)(k - 2) * world_rad), 1.0f, (float)W - 2.0f);
   int acc = 0;
+  if (__all_sync(__activemask(), world_rad < 0.25f)) {
+    const int wy = (int)clampf_((float)y, 1.0f, (float)H - 2.0f);
+    const float d2 = depth_to_dist(__ldg(depth + (size_t)wy * W + wx[2]));
+    acc = 25 * ((d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f));
+  } else {
 #pragma unroll 1
-  for (int yy = -2; yy <= 2; yy++) {
-    const int wy = (int)clampf_((float)y + roundf((float)yy * world_rad), 1.0f, (float)H - 2.0f);
-    const uint32_t* row = depth + (size_t)wy * W;
+    for (int yy = -2; yy <= 2; yy++) {
+      const int wy = (int)clampf_((float)y + roundf((float)yy * world_rad), 1.0f, (float)H - 2.0f);
+      const uint32_t* row = depth + (size_t)wy * W;
 #pragma unroll
-    for (int xx = 0; xx < 5; xx++) {
-      const float d2 = depth_to_dist(__ldg(row + wx[xx]));
-      acc += (d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f);
+      for (int xx = 0; xx < 5; xx++) {
+        const float d2 = depth_to_dist(__ldg(row + wx[xx]));
+        acc += (d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f);
+      }
     }
   }
   // the occlusion scales the colour only: approximate divisions
@@ -828,10 +836,6 @@ __device__ __forceinline__ f4 vertex_col(uint32_t c) {
   return r;
 }
 
-__device__ __forceinline__ f3 tri_vec(const gbr_triangle* T, int k, int field) {
-  const float* b = reinterpret_cast<const float*>(T) + k * 12 + field;
-  return mk3(__ldg(b), __ldg(b + 1), __ldg(b + 2));
-}
 
 // Colour-only arithmetic of the light loop: every use below feeds the colour
 // continuously (no comparison, rounding or index depends on it), so the
@@ -923,8 +927,12 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const f3 tp[3] = {mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), mk3(q2.x, q2.y, q2.z)};
   const float rconst = q0.w;
   const uint32_t tri = __float_as_uint(q1.w);
-  const gbr_triangle* T = sc.tris + tri;
-  const uint32_t o_id = __ldg(&T->vertices[0].object_id);
+  // the triangle as 9 float4 loads: per vertex pos, normal, (vt, object_id, vertex_col)
+  const float4* tv = reinterpret_cast<const float4*>(sc.tris + tri);
+  const float4 va0 = __ldg(tv + 0), vb0 = __ldg(tv + 1), vc0v = __ldg(tv + 2);
+  const float4 va1 = __ldg(tv + 3), vb1 = __ldg(tv + 4), vc1v = __ldg(tv + 5);
+  const float4 va2 = __ldg(tv + 6), vb2 = __ldg(tv + 7), vc2v = __ldg(tv + 8);
+  const uint32_t o_id = __float_as_uint(vc0v.z);
   const gbr_obj_g_descriptor* G = sc.descs + o_id;
   const float scale = __ldg(&G->scale);
   const f3 wpos = ld3(G->world_pos);
@@ -938,13 +946,11 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     qn = fast_normalize4(q);
     qi = quat_inverse_n(q);
   }
-  f3 p1 = mul3s(tri_vec(T, 0, 0), scale), p2 = mul3s(tri_vec(T, 1, 0), scale),
-     p3 = mul3s(tri_vec(T, 2, 0), scale);
+  f3 p1 = mul3s(mk3(va0.x, va0.y, va0.z), scale), p2 = mul3s(mk3(va1.x, va1.y, va1.z), scale),
+     p3 = mul3s(mk3(va2.x, va2.y, va2.z), scale);
   const BaryFrame bf = bary_frame(p1, p2, p3);
-  const float* tb = reinterpret_cast<const float*>(T);
-  f2 vt1 = mk2(__ldg(tb + 8), __ldg(tb + 9)), vt2 = mk2(__ldg(tb + 20), __ldg(tb + 21)),
-     vt3 = mk2(__ldg(tb + 32), __ldg(tb + 33));
-  f3 n1 = tri_vec(T, 0, 4), n2 = tri_vec(T, 1, 4), n3 = tri_vec(T, 2, 4);
+  f2 vt1 = mk2(vc0v.x, vc0v.y), vt2 = mk2(vc1v.x, vc1v.y), vt3 = mk2(vc2v.x, vc2v.y);
+  f3 n1 = mk3(vb0.x, vb0.y, vb0.z), n2 = mk3(vb1.x, vb1.y, vb1.z), n3 = mk3(vb2.x, vb2.y, vb2.z);
 
   const float ldepth = depth_to_dist(d);
   const float fx = (float)x, fy = (float)y;
@@ -961,10 +967,9 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   normal = rot_quat_n(normal, qn);
 
   f4 col;
-  const uint32_t vc0 = __ldg(&T->vertices[0].vertex_col);
+  const uint32_t vc0 = __float_as_uint(vc0v.w);
   if (vc0 != 0) {
-    f4 c0 = vertex_col(vc0), c1 = vertex_col(__ldg(&T->vertices[1].vertex_col)),
-       c2 = vertex_col(__ldg(&T->vertices[2].vertex_col));
+    f4 c0 = vertex_col(vc0), c1 = vertex_col(__float_as_uint(vc1v.w)), c2 = vertex_col(__float_as_uint(vc2v.w));
     col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
     col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
     col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
@@ -1096,7 +1101,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
-__global__ void __launch_bounds__(256, 3) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
+__global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec) {
   __shared__ uint32_t s_id;
