@@ -489,14 +489,13 @@ __device__ __forceinline__ uint32_t find_surface(const Surface* surfs, uint32_t 
   return lo;
 }
 
-// Per-pixel coverage of one record: bbox, the reference walk's skipped
-// pixels, then point_in_tri.  Returns false when the pixel is not drawn.
-__device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int chunk) {
-  uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
-  int minx = xr & 0xFFFF, maxx = xr >> 16, miny = yr & 0xFFFF, maxy = yr >> 16;
-  if (px < minx || px >= maxx || py < miny || py >= maxy) return false;
+// Coverage of a pixel known to lie inside the record's bbox: the reference
+// walk's skipped left-column pixels, then point_in_tri.
+__device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py, int chunk) {
+  const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
   if (px == minx && py > miny &&
-      !walk_visits(0, py - miny, maxx - minx, maxy - miny, (float)miny, chunk))
+      !walk_visits(0, py - miny, (int)(xr >> 16) - minx, (int)(yr >> 16) - miny, (float)miny, chunk))
     return false;
   float fx = (float)px, fy = (float)py;
   float sgn = q[1].w;
@@ -507,16 +506,23 @@ __device__ __forceinline__ bool covers(const float4 q[4], int px, int py, int ch
 
 // kernel1 + kernel2 for one 16x16 tile: depth min, then the canonical id.
 //
-// The tile's records (its fine bin, then its coarse tile's bin) are staged 256
-// at a time in shared memory.  Each record contributes the pixels of its bbox
-// clipped to the tile; an exclusive scan of those areas lays all
-// (record, pixel) tests of the chunk end to end, and the 256 threads walk that
-// list in strides (binary search for the owning record), so small and large
-// triangles are load-balanced alike.  Pass 0 resolves the minimum depth with
-// shared-memory atomicMin; pass 1 the minimum packed (key << 32 | record)
-// among tests within +-20 of the final depth.  Both are minima, so neither
-// bin order nor thread order changes the result.  When the whole list fits
-// one chunk, pass 1 reuses the staged records and offsets.
+// The tile's records (its fine bin, then its coarse tile's bin) are staged NT
+// at a time in shared memory, keeping those whose bbox meets the tile.  Each
+// contributes the pixels of its bbox clipped to the tile; one block scan
+// (packing the record count and the pixel count) compacts them and lays all
+// (record, pixel) tests of the chunk end to end.  Each warp takes one
+// contiguous range of that list, finds its first record by binary search,
+// and then maps 32 tests at a time to records with one ballot of the record
+// starts inside the window (every staged record has at least one pixel, so
+// at most 32 start there), so small and large triangles are load-balanced
+// alike.  Pass 0 resolves the minimum depth with shared-memory atomicMin;
+// pass 1 the minimum packed (key << 32 | record) among tests within +-20 of
+// the final depth.  Both are minima, so neither bin order nor thread order
+// changes the result.  When the whole list fits one chunk and each lane has
+// at most kRasterCache windows, pass 1 reuses the covered tests of pass 0
+// kept in registers.
+constexpr int kRasterCache = 8;
+
 template <int NT>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -543,23 +549,27 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp,
   return swarp[warp] + incl - v;
 }
 
-// NT threads per CTA (128, 256 or 512): the records are staged NT at a time
-// and the (record, pixel) list is walked in strides of NT.
-template <int NT>
-__global__ void __launch_bounds__(NT) k_raster(Workspace ws, const Surface* __restrict__ surfs, uint32_t nsurf,
-                                               int with_id) {
+// NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
+// (views) or only the depth (cube faces).
+template <int NT, bool ID>
+__global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
+                                                          uint32_t nsurf) {
+  constexpr bool with_id = ID;
+  constexpr int NW = NT / 32;
+  constexpr uint32_t kCountShift = 18;  // scan word: pixels (< 2^18) | records << 18
   __shared__ float4 srec[NT][4];
   __shared__ uint32_t sidx[NT];
   __shared__ uint32_t soff[NT + 1];
-  __shared__ uint32_t sgeo[NT];  // lx0 | ly0 << 8 | bw << 16
+  __shared__ uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
   __shared__ uint32_t sdepth[kTilePixels];
   __shared__ unsigned long long sid[kTilePixels];
-  __shared__ uint32_t swarp[NT / 32];
+  __shared__ uint32_t swarp[NW];
+  __shared__ uint32_t sscan;
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
   if (ws.ctr->overflow) return;
   const uint32_t tile = blockIdx.x;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) {
     uint32_t s = find_surface(surfs, nsurf, tile);
     S = surfs[s];
@@ -582,58 +592,119 @@ __global__ void __launch_bounds__(NT) k_raster(Workspace ws, const Surface* __re
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
   const bool resident = ntotal <= (uint32_t)NT;
+  // covered tests of pass 0 (resident case): depth, and pixel | staged record << 8 | 1 << 31
+  uint32_t cache_d[kRasterCache], cache_m[kRasterCache];
+  bool cached = false;
   for (int pass = 0; pass < passes; pass++) {
     for (uint32_t c0 = 0; c0 < ntotal; c0 += NT) {
       const uint32_t m = min((uint32_t)NT, ntotal - c0);
       if (!(resident && pass == 1)) {
         __syncthreads();
-        uint32_t area = 0;
+        uint32_t area = 0, r = 0, geo = 0;
+        float4 q0, q1, q2, q3;
         if ((uint32_t)tid < m) {
           const uint32_t e = c0 + tid;
-          const uint32_t r = e < nfine ? ws.bins[lists[0] + e] : ws.bins[lists[2] + (e - nfine)];
+          r = e < nfine ? ws.bins[lists[0] + e] : ws.bins[lists[2] + (e - nfine)];
           const float4* src = reinterpret_cast<const float4*>(ws.rec + r);
-          const float4 q3 = __ldg(src + 3);
-          srec[tid][0] = __ldg(src);
-          srec[tid][1] = __ldg(src + 1);
-          srec[tid][2] = __ldg(src + 2);
-          srec[tid][3] = q3;
-          sidx[tid] = r;
+          q0 = __ldg(src);
+          q1 = __ldg(src + 1);
+          q2 = __ldg(src + 2);
+          q3 = __ldg(src + 3);
           const uint32_t xr = __float_as_uint(q3.x), yr = __float_as_uint(q3.y);
           const int bx0 = max((int)(xr & 0xFFFF), tx0), bx1 = min((int)(xr >> 16), tx0 + kTile);
           const int by0 = max((int)(yr & 0xFFFF), ty0), by1 = min((int)(yr >> 16), ty0 + kTile);
           if (bx1 > bx0 && by1 > by0) {
-            area = (uint32_t)((bx1 - bx0) * (by1 - by0));
-            sgeo[tid] = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 8) | ((uint32_t)(bx1 - bx0) << 16);
+            const uint32_t bw = (uint32_t)(bx1 - bx0);
+            area = bw * (uint32_t)(by1 - by0);
+            geo = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 4) | (bw << 8) | (((65536u + bw - 1) / bw) << 13);
           }
         }
-        uint32_t off = block_excl_scan<NT>(area, swarp, &soff[NT]);
-        soff[tid] = off;
+        const uint32_t word = area ? (area | (1u << kCountShift)) : 0u;
+        const uint32_t off = block_excl_scan<NT>(word, swarp, &sscan);
+        if (area) {
+          const uint32_t slot = off >> kCountShift;
+          srec[slot][0] = q0;
+          srec[slot][1] = q1;
+          srec[slot][2] = q2;
+          srec[slot][3] = q3;
+          sidx[slot] = r;
+          sgeo[slot] = geo;
+          soff[slot] = off & ((1u << kCountShift) - 1);
+        }
+        if (tid == 0) soff[sscan >> kCountShift] = sscan & ((1u << kCountShift) - 1);
         __syncthreads();
       }
-      const uint32_t total = soff[NT];
-      for (uint32_t t = tid; t < total; t += NT) {
-        // owning record: the last i < m with soff[i] <= t
-        int lo = 0, hi = (int)m - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (soff[mid] <= t) lo = mid; else hi = mid - 1;
-        }
-        const uint32_t g = sgeo[lo];
-        const uint32_t bw = g >> 16;
-        const uint32_t local = t - soff[lo];
-        const uint32_t ry = local / bw, rx = local - ry * bw;
-        const int lx = (int)(g & 0xFF) + (int)rx, ly = (int)((g >> 8) & 0xFF) + (int)ry;
-        const float4 q[4] = {srec[lo][0], srec[lo][1], srec[lo][2], srec[lo][3]};
-        const int x = tx0 + lx, y = ty0 + ly;
-        if (!covers(q, x, y, chunk)) continue;
-        const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
-        const int p = ly * kTile + lx;
-        if (pass == 0) {
-          atomicMin(&sdepth[p], d);
-        } else {
-          const uint32_t fd = sdepth[p];
+      const uint32_t nstaged = sscan >> kCountShift;
+      const uint32_t total = soff[nstaged];
+      if (resident && pass == 1 && cached) {
+        // pass 1 from the tests pass 0 kept
+#pragma unroll
+        for (int g = 0; g < kRasterCache; g++) {
+          if (!(cache_m[g] >> 31)) continue;
+          const int p = (int)(cache_m[g] & 0xFF);
+          const uint32_t lo = (cache_m[g] >> 8) & 0x3FF;
+          const uint32_t d = cache_d[g], fd = sdepth[p];
           if (d > fd - kBufError && d < fd + kBufError)
-            atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
+            atomicMin(&sid[p], ((unsigned long long)__float_as_uint(srec[lo][2].w) << 32) | sidx[lo]);
+        }
+        continue;
+      }
+      // this warp's contiguous range of the test list, in windows of 32
+      const uint32_t per = ((total + NW * 32 - 1) / (NW * 32)) * 32;
+      const uint32_t start = min(total, (uint32_t)warp * per), end = min(total, start + per);
+      const bool keep = resident && pass == 0 && with_id && per <= 32u * kRasterCache;
+      if (keep) {
+#pragma unroll
+        for (int g = 0; g < kRasterCache; g++) cache_m[g] = 0;
+        cached = true;
+      }
+      if (start < end) {
+        // first record: the last staged record with soff <= start (warp-uniform)
+        int rec = 0, hi = (int)nstaged - 1;
+        while (rec < hi) {
+          const int mid = (rec + hi + 1) >> 1;
+          if (soff[mid] <= start) rec = mid; else hi = mid - 1;
+        }
+#pragma unroll 1
+        for (uint32_t base = start, g = 0; base < end; base += 32, g++) {
+          // record starts inside (base, base + 32): at most 32 records
+          const uint32_t nxt = (uint32_t)rec + 1 + lane;
+          const uint32_t pos = nxt < nstaged ? soff[nxt] - base : 32u;
+          const uint32_t starts = __reduce_or_sync(0xFFFFFFFFu, pos < 32u ? (1u << pos) : 0u);
+          const uint32_t upto = lane == 31 ? starts : starts & ((2u << lane) - 1u);
+          const uint32_t lo = (uint32_t)rec + __popc(upto);
+          const uint32_t t = base + lane;
+          if (t < end) {
+            const uint32_t geo = sgeo[lo];
+            const uint32_t local = t - soff[lo];
+            const uint32_t bw = (geo >> 8) & 0x1F;
+            const uint32_t ry = (local * (geo >> 13)) >> 16, rx = local - ry * bw;
+            const int lx = (int)(geo & 0xF) + (int)rx, ly = (int)((geo >> 4) & 0xF) + (int)ry;
+            const float4 q[4] = {srec[lo][0], srec[lo][1], srec[lo][2], srec[lo][3]};
+            const int x = tx0 + lx, y = ty0 + ly;
+            if (covers_in_bbox(q, x, y, chunk)) {
+              const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
+              const int p = ly * kTile + lx;
+              if (pass == 0) {
+                atomicMin(&sdepth[p], d);
+                if (keep) {
+#pragma unroll
+                  for (int k = 0; k < kRasterCache; k++)
+                    if (k == (int)g) {
+                      cache_d[k] = d;
+                      cache_m[k] = (uint32_t)p | (lo << 8) | (1u << 31);
+                    }
+                }
+              } else {
+                const uint32_t fd = sdepth[p];
+                if (d > fd - kBufError && d < fd + kBufError)
+                  atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
+              }
+            }
+          }
+          // the record of test base + 32: lane 31's, or the next one if it starts there
+          rec = (int)((uint32_t)rec + __popc(starts));
+          if ((uint32_t)rec + 1 < nstaged && soff[rec + 1] == base + 32) rec++;
         }
       }
     }
@@ -1272,10 +1343,13 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
                           bool with_id, int threads, cudaStream_t st) {
   if (!ntiles) return cudaSuccess;
   const int wid = with_id ? 1 : 0;
-  switch (threads) {
-    case 128: k_raster<128><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf, wid); break;
-    case 512: k_raster<512><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf, wid); break;
-    default: k_raster<256><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf, wid); break;
+  switch (threads * 2 + wid) {
+    case 256: k_raster<128, false><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf); break;
+    case 257: k_raster<128, true><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf); break;
+    case 1024: k_raster<512, false><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf); break;
+    case 1025: k_raster<512, true><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf); break;
+    case 513: k_raster<256, true><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf); break;
+    default: k_raster<256, false><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf); break;
   }
   return cudaGetLastError();
 }
