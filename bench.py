@@ -61,6 +61,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(ms, world, device=None):
+    """The slowest rank's step time, on every rank (all-reduce MAX; the
+    process group is NCCL on GPUs, gloo in the CPU tests)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mpix_per_s(pixels_per_step, world, ms):
+    """Whole-job throughput: every rank renders pixels_per_step per step
+    (replicas, weak scaling), the job takes the slowest rank's time."""
+    return world * pixels_per_step / (ms * 1e-3) / 1e6
+
+
 def scene_config(sc):
     v = sc.views[0]
     return {"workload": WORKLOAD, "width": int(v["width"]), "height": int(v["height"]),
@@ -196,6 +214,21 @@ def cpu_frames(sc, seconds, max_frames, threads):
             O.render(sc, tex, cam, view, dyn, sta, nthreads=threads)
         times.append(time.perf_counter() - t0)
     return kind, P, times
+
+
+def host_cpu():
+    """nproc and the CPU model of this host (for the CPU baseline record)."""
+    model = None
+    try:
+        for line in open("/proc/cpuinfo"):
+            k, _, v = line.partition(":")
+            if k.strip() in ("model name", "Model", "CPU part") and v.strip():
+                model = v.strip()
+                if k.strip() == "model name":
+                    break
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model or "unknown", "machine": os.uname().machine}
 
 
 def cpu_sample_text(kind, n, threads):
@@ -357,12 +390,10 @@ def main():
     st = gs.stats()
     gs.profile(False)
     launches = st["launches"] - launches0
+    ms = max_over_ranks(ms, world, "cuda")
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
-    value = world * P / (ms * 1e-3) / 1e6
+    value = job_mpix_per_s(P, world, ms)
 
     # per-stage device time and the roofline of the dominant kernel
     per_call = {k: st["stage_ms"][k] / max(st["stage_calls"][k], 1) for k in S.STAGES}
@@ -527,7 +558,12 @@ def main():
         kind, Pc, times = cpu_frames(sc, args.cpu_seconds, 8, threads)
         t = times[1:] if len(times) > 1 else times
         cpu = {"value": round(Pc * len(t) / sum(t) / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": kind,
-               "sample": cpu_sample_text(kind, len(t), threads) + ", after 1 warm-up frame"}
+               "sample": cpu_sample_text(kind, len(t), threads) + ", after 1 warm-up frame",
+               "host": host_cpu()}
+        # one frame on one core, for the single-thread figure
+        _, _, t1 = cpu_frames(sc, 0.0, 1, 1)
+        cpu["single_thread"] = {"value": round(Pc / t1[0] / 1e6, 4), "unit": "Mpix/s", "cores": 1,
+                                "sample": cpu_sample_text(kind, 1, 1)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world,
@@ -537,6 +573,13 @@ def main():
                 "config": scene_config(sc), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": int(launches), "clocks": clk,
                 "stages_ms": {k: round(v, 4) for k, v in per_call.items()},
+                "covered_mpix_s": round(job_mpix_per_s(P_cov, world, ms), 3),
+                "raster_samples": {
+                    "view": st["view_samples"], "shadow": st["shadow_samples"],
+                    "view_gsamples_per_s": round(st["view_samples"] / (per_call["view_raster"] * 1e-3) / 1e9, 3),
+                    "shadow_gsamples_per_s": round(st["shadow_samples"] / (per_call["shadow_raster"] * 1e-3) / 1e9, 3),
+                    "note": "covered pixel-samples (point_in_tri passes) resolved per second by the raster kernels "
+                            "with shared-memory atomics; no measured atomic peak is available for a fraction"},
                 "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "serving": serving,
                 "impl": "gbr",
                 "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],

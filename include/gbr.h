@@ -126,6 +126,11 @@ typedef struct gbr_stats {
    * 4 view setup, 5 view scan, 6 view fill, 7 view raster, 8 view shade. */
   double stage_ms[10];
   uint64_t stage_calls[10];
+  /* Covered pixel-samples of the last view / shadow pass: (record, pixel)
+   * pairs passing point_in_tri, i.e. the reference's kernel1 atomic_min calls
+   * on distinct pixels. */
+  uint64_t view_samples;
+  uint64_t shadow_samples;
 } gbr_stats;
 
 typedef struct gbr_scene gbr_scene;

@@ -205,9 +205,11 @@ bool absorb_counters(gbr_scene* s, const Counters& c, WorkMem& w, float headroom
       s->stats.view_records = c.nrec;
       s->stats.view_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
       s->stats.fragments_ref = c.frag_ref;
+      s->stats.view_samples = c.samples;
     } else {
       s->stats.shadow_records = c.nrec;
       s->stats.shadow_bin_entries = (uint64_t)c.fine_total + c.coarse_total;
+      s->stats.shadow_samples = c.samples;
     }
     return true;
   }

@@ -89,7 +89,7 @@ struct Counters {
   uint32_t nrec;                // records requested
   uint32_t overflow;            // bit 0 records, bit 1 bins
   uint32_t fine_total, coarse_total;
-  uint32_t pad[2];
+  unsigned long long samples;   // covered pixel-samples (point_in_tri passes) of the depth pass
 };
 
 struct SceneDev {

@@ -565,6 +565,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
   __shared__ unsigned long long sid[kTilePixels];
   __shared__ uint32_t swarp[NW];
   __shared__ uint32_t sscan;
+  __shared__ uint32_t ssamples;
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
   if (ws.ctr->overflow) return;
@@ -580,6 +581,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
     lists[1] = ws.fine_count[tile];
     lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
     lists[3] = ws.coarse_count[ct];
+    ssamples = 0;
   }
   for (int p = tid; p < kTilePixels; p += NT) {
     sdepth[p] = kDepthClear;
@@ -674,6 +676,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
           const uint32_t upto = lane == 31 ? starts : starts & ((2u << lane) - 1u);
           const uint32_t lo = (uint32_t)rec + __popc(upto);
           const uint32_t t = base + lane;
+          bool hit = false;
           if (t < end) {
             const uint32_t geo = sgeo[lo];
             const uint32_t local = t - soff[lo];
@@ -682,7 +685,8 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
             const int lx = (int)(geo & 0xF) + (int)rx, ly = (int)((geo >> 4) & 0xF) + (int)ry;
             const float4 q[4] = {srec[lo][0], srec[lo][1], srec[lo][2], srec[lo][3]};
             const int x = tx0 + lx, y = ty0 + ly;
-            if (covers_in_bbox(q, x, y, chunk)) {
+            hit = covers_in_bbox(q, x, y, chunk);
+            if (hit) {
               const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
               const int p = ly * kTile + lx;
               if (pass == 0) {
@@ -702,6 +706,10 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
               }
             }
           }
+          if (pass == 0) {
+            const uint32_t hits = __ballot_sync(0xFFFFFFFFu, hit);
+            if (lane == 0 && hits) atomicAdd(&ssamples, (uint32_t)__popc(hits));
+          }
           // the record of test base + 32: lane 31's, or the next one if it starts there
           rec = (int)((uint32_t)rec + __popc(starts));
           if ((uint32_t)rec + 1 < nstaged && soff[rec + 1] == base + 32) rec++;
@@ -710,6 +718,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
     }
     __syncthreads();
   }
+  if (tid == 0 && ssamples) atomicAdd(&ws.ctr->samples, (unsigned long long)ssamples);
   for (int lp = tid; lp < kTilePixels; lp += NT) {
     const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
     if (px < S.width && py < S.height) {

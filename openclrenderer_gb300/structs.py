@@ -34,6 +34,7 @@ STATS = np.dtype([
     ("view_records", "<u8"), ("view_bin_entries", "<u8"), ("shadow_records", "<u8"),
     ("shadow_bin_entries", "<u8"), ("fragments_ref", "<u8"), ("retries", "<u8"),
     ("launches", "<u8"), ("stage_ms", "<f8", 10), ("stage_calls", "<u8", 10),
+    ("view_samples", "<u8"), ("shadow_samples", "<u8"),
 ])
 STAGES = ("shadow_setup", "shadow_scan", "shadow_fill", "shadow_raster",
           "view_setup", "view_scan", "view_fill", "view_raster", "view_shade")

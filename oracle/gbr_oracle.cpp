@@ -357,6 +357,7 @@ struct ShadeView {
   int W, H;
   float fov;
   f3 cpos, crot_c, crot_s;
+  f3 crot;  // the Euler angles themselves (the FP64 shading takes exact cos / sin)
   f3 face_c[6], face_s[6];
   uint32_t use_linear;
   f4 clear;
@@ -633,6 +634,312 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
   }
 }
 
+// ---- FP64 shading reference ------------------------------------------------
+// kernel3 (cl2.cl:5792-6408) evaluated in double precision with exact library
+// functions (sqrt, exp, pow, tan, division) where the float pipeline uses the
+// vendor's native_* approximations or float rounding.  The reference's own
+// formula approximations stay (rational_acos unless exact_acos, the sRGB
+// polynomials, log2_approx), so the difference to this is the floating-point
+// error of a float implementation.  Inputs: the same depth, canonical id,
+// clipped triangles, atlas and cubemaps as the float path.
+struct D3 { double x, y, z; };
+struct D4 { double x, y, z, w; };
+inline D3 d3(double x, double y, double z) { return D3{x, y, z}; }
+inline D3 d3f(f3 a) { return D3{a.x, a.y, a.z}; }
+inline D3 d3p(const float* p) { return D3{p[0], p[1], p[2]}; }
+inline D3 operator+(D3 a, D3 b) { return d3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline D3 operator-(D3 a, D3 b) { return d3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline D3 operator*(D3 a, double s) { return d3(a.x * s, a.y * s, a.z * s); }
+inline double dotd(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline D3 crossd(D3 a, D3 b) { return d3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline D3 normd(D3 a) { return a * (1.0 / std::sqrt(dotd(a, a))); }
+inline double clampd(double x, double lo, double hi) { return std::fmin(std::fmax(x, lo), hi); }
+
+struct CamD { D3 c, s; };
+inline CamD camd(f3 ang) {
+  return CamD{d3(std::cos((double)ang.x), std::cos((double)ang.y), std::cos((double)ang.z)),
+              d3(std::sin((double)ang.x), std::sin((double)ang.y), std::sin((double)ang.z))};
+}
+// rot / back_rot (cl2.cl:220-348) in double
+inline D3 rotd(D3 p, D3 cpos, const CamD& k) {
+  D3 r = p - cpos, c = k.c, s = k.s;
+  double a = s.z * r.y + c.z * r.x, b = c.y * r.z + s.y * a, d = c.z * r.y - s.z * r.x;
+  return d3(c.y * a - s.y * r.z, s.x * b + c.x * d, c.x * b - s.x * d);
+}
+inline D3 back_rotd(D3 p, D3 cpos, const CamD& k) {
+  D3 r = p - cpos, c = k.c, s = k.s;
+  return d3(c.z * (c.y * r.x + s.x * s.y * r.y + c.x * s.y * r.z) + s.z * (s.x * r.z - c.x * r.y),
+            s.z * c.y * r.x + (c.x * c.z + s.x * s.y * s.z) * r.y + (-s.x * c.z + c.x * s.y * s.z) * r.z,
+            -s.y * r.x + c.y * (s.x * r.y + c.x * r.z));
+}
+inline D4 qnormd(D4 q) {
+  double l = std::sqrt(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
+  return D4{q.x / l, q.y / l, q.z / l, q.w / l};
+}
+inline D3 rot_quatd(D3 p, D4 q) {  // q normalised
+  D3 qv = d3(q.x, q.y, q.z);
+  D3 t = crossd(qv, p) * 2.0;
+  return p + t * q.w + crossd(qv, t);
+}
+inline D4 qinvd(D4 q) { return qnormd(D4{-q.x, -q.y, -q.z, q.w}); }
+inline void baryd(D3 p, D3 a, D3 b, D3 c, double* u, double* v, double* w) {
+  D3 v0 = b - a, v1 = c - a, v2 = p - a;
+  double d00 = dotd(v0, v0), d01 = dotd(v0, v1), d11 = dotd(v1, v1), d20 = dotd(v2, v0), d21 = dotd(v2, v1);
+  double den = d00 * d11 - d01 * d01;
+  *v = (d11 * d20 - d01 * d21) / den;
+  *w = (d00 * d21 - d01 * d20) / den;
+  *u = 1.0 - *v - *w;
+}
+inline double gamma_fwd_d(double c) { return 0.012522878 * c + 0.682171111 * c * c + 0.305306011 * c * c * c; }
+inline double gamma_inv_d(double c) {
+  double s1 = std::sqrt(c), s2 = std::sqrt(s1), s3 = std::sqrt(s2);
+  return 0.585122381 * s1 + 0.783140355 * s2 - 0.368262736 * s3;
+}
+inline double rational_acos_d(double x, bool exact) {
+  if (exact) return std::acos(x);
+  const double a = -0.939115566365855, b = 0.9217841528914573, c = -1.2845906244690837, d = 0.295624144969963174;
+  return 3.14159265358979323846 / 2.0 + (a * x + b * x * x * x) / (1.0 + c * x * x + d * x * x * x * x);
+}
+// log2_approx (cl2.cl:1498-1505): exponent plus a quadratic in the mantissa
+inline double log2_approx_d(double v) {
+  int e = 0;
+  double f = std::frexp(v, &e);  // v = f * 2^e, f in [0.5, 1)
+  double m = 2.0 * f;            // mantissa in [1, 2)
+  return (double)(e - 2) + ((-0.3358287811 * m + 2.0) * m - 0.65871759316667);
+}
+inline double depth_to_dist_d(uint32_t d) { return (double)d / 4294967296.0 * 350000.0; }
+
+D4 read_tex_d(double cx, double cy, int which, int slice, double width, const Atlas& at) {
+  const int hnum = kTexPage / (int)width;
+  const int tny = which / hnum, tnx = which - tny * hnum;
+  cx = clampd(cx, 0.001, width - 0.001);
+  cy = clampd(cy, 0.001, width - 0.001);
+  int ix = (int)(tnx * width + cx), iy = (int)(tny * width + cy);
+  const uint8_t* t = at.data + ((size_t)slice * kTexPage * kTexPage + (size_t)iy * kTexPage + ix) * 4;
+  return D4{(double)t[0], (double)t[1], (double)t[2], (double)t[3]};
+}
+D4 bilinear_d(double mx, double my, int which, int slice, double width, const Atlas& at) {
+  double px = std::floor(mx), py = std::floor(my);
+  D4 c0 = read_tex_d(px, py, which, slice, width, at), c1 = read_tex_d(px + 1, py, which, slice, width, at);
+  D4 c2 = read_tex_d(px, py + 1, which, slice, width, at), c3 = read_tex_d(px + 1, py + 1, which, slice, width, at);
+  double ux = mx - px, uy = my - py, bx = 1 - ux, by = 1 - uy;
+  auto mix = [&](double a, double b, double c, double d) { return (a * bx + b * ux) * by + (c * bx + d * ux) * uy; };
+  return D4{mix(c0.x, c1.x, c2.x, c3.x), mix(c0.y, c1.y, c2.y, c3.y), mix(c0.z, c1.z, c2.z, c3.z),
+            mix(c0.w, c1.w, c2.w, c3.w)};
+}
+inline double tex_mod_d(double v) {
+  v = v >= 1.0 ? 1.0 - (v - std::floor(v)) : v;
+  v = v < 0.0 ? (1.0 + std::fabs(v)) - std::fabs(std::floor(v)) : v;
+  return v;
+}
+D4 texture_filter_d(double vtx, double vty, double dx, double dy, int tid2, const Atlas& at) {
+  uint32_t nv = at.nums[tid2];
+  int slice = (int)(nv >> 16);
+  double tsize = (double)at.sizes[slice];
+  double mx = tex_mod_d(vtx), my = tex_mod_d(vty);
+  double wx = dx * tsize, wy = dy * tsize;
+  double worst = std::sqrt(wx * wx + wy * wy);
+  double wif = std::fmax(log2_approx_d(worst), 0.0);
+  double lower = clampd(std::floor(wif), 0.0, (double)kMipLevels);
+  double fmd = wif - lower;
+  int tl = lower == 0.0 ? tid2 : (int)((lower - 1.0) + at.mipmap_start + tid2 * kMipLevels);
+  int th = (int)(clampd(lower, 0.0, kMipLevels - 1.0) + at.mipmap_start + tid2 * kMipLevels);
+  uint32_t lnv = at.nums[tl], hnv = at.nums[th];
+  int sl = (int)(lnv >> 16), sh = (int)(hnv >> 16);
+  double szl = at.sizes[sl], szh = at.sizes[sh];
+  D4 c1 = bilinear_d(mx * szl, my * szl, (int)(lnv & 0xFFFF), sl, szl, at);
+  D4 c2 = bilinear_d(mx * szh, my * szh, (int)(hnv & 0xFFFF), sh, szh, at);
+  return D4{(c1.x + (c2.x - c1.x) * fmd) / 255.0, (c1.y + (c2.y - c1.y) * fmd) / 255.0,
+            (c1.z + (c2.z - c1.z) * fmd) / 255.0, (c1.w + (c2.w - c1.w) * fmd) / 255.0};
+}
+inline int ret_cubeface_d(D3 p, D3 l) {
+  D3 r = p - l;
+  double ax = std::fabs(r.x), ay = std::fabs(r.y), az = std::fabs(r.z);
+  if (ax >= ay && ax >= az) return r.x < 0.0 ? 4 : 5;
+  if (ay > ax && ay >= az) return r.y < 0.0 ? 1 : 3;
+  if (az > ax && az > ay && r.z < 0.0) return 2;
+  return 0;
+}
+double hard_occlusion_d(D3 lpos, D3 normal, D3 ptl, const uint32_t* buf, int face, D3 gpos, int shnum,
+                        const CamD* faces, bool exact_acos) {
+  ptl = normd(ptl);
+  D3 local = rotd(gpos, lpos, faces[face]);
+  const double L = kLightBufferDim;
+  double k = 512.0 / local.z;
+  double px = local.x * k + L / 2, py = local.y * k + L / 2, dpth = local.z;
+  const uint32_t* map = buf + (size_t)(face + shnum * 6) * kLightBufferDim * kLightBufferDim;
+  px = clampd(px, 3.0, L - 4.0);
+  py = clampd(py, 3.0, L - 4.0);
+  int ix = (int)px, iy = (int)py;
+  double ac = rational_acos_d(clampd(dotd(normal, ptl), 0.05, 0.95), exact_acos);
+  double bias = clampd(50.0 * std::tan(ac), 5.0, 50.0);
+  double cond[16];
+  for (int yy = -1; yy <= 2; yy++)
+    for (int xx = -1; xx <= 2; xx++)
+      cond[(yy + 1) * 4 + xx + 1] =
+          dpth > depth_to_dist_d(map[(iy + yy) * kLightBufferDim + ix + xx]) + bias ? 1.0 : 0.0;
+  double sh = 0.0;
+  for (int yy = -1; yy <= 1; yy++)
+    for (int xx = -1; xx <= 1; xx++) {
+      double cx = px + 0.5 + xx, cy = py + 0.5 + yy;
+      double mx = cx - 0.5, my = cy - 0.5, ux = mx - std::floor(mx), uy = my - std::floor(my);
+      int b = (yy + 1) * 4 + xx + 1;
+      sh += (cond[b] * (1 - ux) + cond[b + 1] * ux) * (1 - uy) + (cond[b + 4] * (1 - ux) + cond[b + 5] * ux) * uy;
+    }
+  return sh / 9.0;
+}
+
+void kernel3_pixel_fp64(int x, int y, const ShadeView& v, const ShadeIn& in, const Setup& S,
+                        const uint32_t* depth, const uint32_t* ids, bool exact_acos, double* out) {
+  const size_t p = (size_t)y * v.W + x;
+  const uint32_t d = depth[p], key = ids[p];
+  double* o = out + p * 4;
+  if (d == kDepthClear || key == kNoId) {
+    o[0] = clampd(v.clear.x, 0, 1); o[1] = clampd(v.clear.y, 0, 1);
+    o[2] = clampd(v.clear.z, 0, 1); o[3] = clampd(v.clear.w, 0, 1);
+    return;
+  }
+  const uint32_t tri = key >> 1;
+  const Cut& ct = S.cut[key];
+  const gbr_triangle& T = in.tris[tri];
+  const gbr_obj_g_descriptor& G = in.descs[T.vertices[0].object_id];
+  const CamD cam = camd(v.crot);
+  CamD faces[6];
+  for (int f = 0; f < 6; f++) faces[f] = camd(face_angles(f));
+  const double fov = v.fov, W = v.W, H = v.H;
+  const D3 cpos = d3f(v.cpos), wpos = d3p(G.world_pos);
+  const D4 q = qnormd(D4{G.world_rot_quat[0], G.world_rot_quat[1], G.world_rot_quat[2], G.world_rot_quat[3]});
+  const D4 qi = qinvd(D4{G.world_rot_quat[0], G.world_rot_quat[1], G.world_rot_quat[2], G.world_rot_quat[3]});
+  const D3 p1 = d3p(T.vertices[0].pos) * G.scale, p2 = d3p(T.vertices[1].pos) * G.scale,
+           p3 = d3p(T.vertices[2].pos) * G.scale;
+  const double ld = depth_to_dist_d(d);
+  const D3 gpos = back_rotd(d3((x - W / 2) * ld / fov, (y - H / 2) * ld / fov, ld), d3(0, 0, 0), cam) + cpos;
+  double l1, l2, l3;
+  baryd(rot_quatd(gpos - wpos, qi), p1, p2, p3, &l1, &l2, &l3);
+  auto interp2 = [&](int c, double a, double b, double cc) {
+    return T.vertices[0].vt[c] * a + T.vertices[1].vt[c] * b + T.vertices[2].vt[c] * cc;
+  };
+  const double vtx = interp2(0, l1, l2, l3), vty = interp2(1, l1, l2, l3);
+  D3 normal = d3p(T.vertices[0].normal) * l1 + d3p(T.vertices[1].normal) * l2 + d3p(T.vertices[2].normal) * l3;
+  normal = rot_quatd(normal, q);
+  D4 col;
+  if (T.vertices[0].vertex_col != 0) {
+    D4 acc{0, 0, 0, 0};
+    const double w3[3] = {l1, l2, l3};
+    for (int k = 0; k < 3; k++) {
+      uint32_t c = T.vertices[k].vertex_col;
+      acc.x += (c >> 24) / 255.0 * w3[k];
+      acc.y += ((c >> 16) & 0xFF) / 255.0 * w3[k];
+      acc.z += ((c >> 8) & 0xFF) / 255.0 * w3[k];
+      acc.w += (c & 0xFF) / 255.0 * w3[k];
+    }
+    col = acc;
+  } else {
+    // get_vtdiff (cl2.cl:5691-5760) in double
+    double xp[3], yp[3], dp[3];
+    for (int k = 0; k < 3; k++) {
+      xp[k] = std::round((double)ct.p[k].x);
+      yp[k] = std::round((double)ct.p[k].y);
+      dp[k] = 1.0 / (double)ct.p[k].z;
+    }
+    const double rc = 1.0 / ((xp[1] * yp[2] + xp[0] * (yp[1] - yp[2]) - xp[2] * yp[1]) + (xp[2] - xp[1]) * yp[0]);
+    const double A = ((dp[1] * yp[2] + dp[0] * (yp[1] - yp[2]) - dp[2] * yp[1]) + (dp[2] - dp[1]) * yp[0]) * rc;
+    const double B = -((dp[1] * xp[2] + dp[0] * (xp[1] - xp[2]) - dp[2] * xp[1]) + (dp[2] - dp[1]) * xp[0]) * rc;
+    const double C = dp[0] - A * xp[0] - B * yp[0];
+    const double dmx = A * (x + 1) + B * y + C, dmy = A * x + B * (y + 1) + C;
+    const D3 lmx = d3((x + 1 - W / 2) / fov / dmx, (y - H / 2) / fov / dmx, 1.0 / dmx);
+    const D3 lmy = d3((x - W / 2) / fov / dmy, (y + 1 - H / 2) / fov / dmy, 1.0 / dmy);
+    double a1, a2, a3, b1, b2, b3;
+    baryd(rot_quatd(back_rotd(lmx, d3(0, 0, 0), cam) + cpos - wpos, qi), p1, p2, p3, &a1, &a2, &a3);
+    baryd(rot_quatd(back_rotd(lmy, d3(0, 0, 0), cam) + cpos - wpos, qi), p1, p2, p3, &b1, &b2, &b3);
+    const double mb = 1.0 / 1.1;
+    const double dx = (std::fabs(interp2(0, a1, a2, a3) - vtx) + std::fabs(interp2(0, b1, b2, b3) - vtx)) * mb;
+    const double dy = (std::fabs(interp2(1, a1, a2, a3) - vty) + std::fabs(interp2(1, b1, b2, b3) - vty)) * mb;
+    col = texture_filter_d(vtx, vty, dx, dy, (int)G.tid, in.atlas);
+  }
+  if (v.use_linear) {
+    col.x = gamma_fwd_d(col.x);
+    col.y = gamma_fwd_d(col.y);
+    col.z = gamma_fwd_d(col.z);
+  }
+  const uint32_t s1 = wang_hash((uint32_t)x + (uint32_t)y * (uint32_t)v.W * (uint32_t)v.H);
+  const uint32_t s2 = rand_xorshift(s1), s3 = rand_xorshift(s2), s4 = rand_xorshift(s3);
+  const D3 rseed = d3((s2 / 4294967296.0 - 0.5) * 2, (s3 / 4294967296.0 - 0.5) * 2, (s4 / 4294967296.0 - 0.5) * 2);
+  const D3 l2p = normd(cpos - gpos);
+  const int ff = G.feature_flag;
+  const bool two = (ff & kFlagTwoSided) > 0, recv_dyn = !((ff & kFlagNoDynShadows) > 0);
+  if (!backface_front(ct.p[0], ct.p[1], ct.p[2]) && two) normal = normal * -1.0;
+  // SSAO (cl2.cl:2194-2260)
+  double ssao;
+  {
+    const uint32_t ss2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)v.W * (uint32_t)v.H * (uint32_t)y));
+    const double dep = depth_to_dist_d(d);
+    const double wr = (2.0 + (ss2 / 4294967296.0) / 2.0) * fov / dep;
+    double acc = 0;
+    for (int yy = -2; yy <= 2; yy++)
+      for (int xx = -2; xx <= 2; xx++) {
+        int wx = (int)clampd(x + std::round(xx * wr), 1.0, W - 2.0);
+        int wy = (int)clampd(y + std::round(yy * wr), 1.0, H - 2.0);
+        double d2 = depth_to_dist_d(depth[(size_t)wy * v.W + wx]);
+        for (int z = -2; z <= 2; z++) acc += d2 > dep + z ? 1.0 : 0.0;
+      }
+    ssao = 1.0 - (1.0 - acc / 125.0) / 2.5;
+  }
+  normal = normd(normal);
+  const D3 lnormal = normd(normal + rseed * 0.01);
+  const double ambient = v.use_linear ? gamma_fwd_d(0.2) : 0.2;
+  const double rough = clampd(1.0 - G.specular, 0.001, 10.0);
+  D3 dsum = d3(0, 0, 0), ssum = d3(0, 0, 0);
+  int shnum = 0, static_num = 0;
+  for (uint32_t i = 0; i < in.nlights; i++) {
+    const gbr_light& L = in.lights[i];
+    const D3 lpos = d3p(L.pos);
+    D3 ptl = lpos - gpos;
+    double occ = 1.0;
+    if (L.shadow && L.is_static) {
+      occ = 1.0 - hard_occlusion_d(lpos, normal, ptl, in.shadow_static, ret_cubeface_d(gpos, lpos), gpos,
+                                   static_num, faces, exact_acos);
+      static_num++;
+    }
+    const double dist = std::sqrt(dotd(ptl, ptl));
+    const double tt = dist / L.radius + 1.0;
+    double illum = (L.brightness / (tt * tt) - 0.1) / 0.9;
+    if (illum <= 0) continue;
+    D3 lcol = d3p(L.col);
+    if (v.use_linear) lcol = d3(gamma_fwd_d(lcol.x), gamma_fwd_d(lcol.y), gamma_fwd_d(lcol.z));
+    if (L.shadow && recv_dyn) {
+      double dyn = 1.0 - hard_occlusion_d(lpos, normal, ptl, in.shadow_dyn, ret_cubeface_d(gpos, lpos), gpos,
+                                          shnum, faces, exact_acos);
+      occ = std::fmin(occ, dyn);
+      shnum++;
+    }
+    ptl = normd(ptl);
+    const double light = std::fmax(dotd(ptl, lnormal) * occ, 0.0);
+    const double dscale = (((1.0 - ambient) * light + ambient) * L.diffuse) * G.diffuse * illum;
+    dsum = dsum + lcol * dscale;
+    const D3 Hv = normd(l2p + ptl);
+    const double ndh = std::fmax(0.0, dotd(normal, Hv)), ndv = std::fmax(0.0, dotd(normal, l2p));
+    const double vdh = std::fmax(0.0, dotd(l2p, Hv)), ndl = std::fmax(0.0, dotd(normal, ptl));
+    const double fresnel = 0.4 + 0.6 * std::pow(1.0 - vdh, 5.0);
+    const double alpha = rational_acos_d(ndh, exact_acos);
+    const double micro = 0.8346 * std::exp(-alpha * alpha / (rough * rough));
+    const double sv = 2.0 * ndh / vdh;
+    const double geom = std::fmin(std::fmin(1.0, sv * ndv), sv * ndl);
+    const double spec = fresnel * micro * geom / (3.14159265358979323846 * ndv);
+    ssum = ssum + lcol * (spec * 0.4 * illum * G.spec_mult);
+    ssum = d3(std::fmax(ssum.x, 0.0), std::fmax(ssum.y, 0.0), std::fmax(ssum.z, 0.0)) * occ;
+  }
+  ssum = ssum * ssao;
+  dsum = dsum * ssao;
+  D3 fin = d3((col.x + ssum.x * 0.7) * dsum.x + ssum.x * 0.3, (col.y + ssum.y * 0.7) * dsum.y + ssum.y * 0.3,
+              (col.z + ssum.z * 0.7) * dsum.z + ssum.z * 0.3);
+  if (v.use_linear) fin = d3(gamma_inv_d(fin.x), gamma_inv_d(fin.y), gamma_inv_d(fin.z));
+  o[0] = clampd(fin.x, 0, 1);
+  o[1] = clampd(fin.y, 0, 1);
+  o[2] = clampd(fin.z, 0, 1);
+  o[3] = clampd(col.w, 0, 1);
+}
+
 // ---- shadow cubemaps ---------------------------------------------------------
 struct ShadowFrag {
   uint32_t face, a, ctri;
@@ -885,7 +1192,7 @@ int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
   kernel2(S, (float)W, (float)H, depth, reinterpret_cast<std::atomic<uint32_t>*>(ids), W, nthreads);
   if (!rgba) return 0;
   ShadeView v;
-  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos;
+  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot;
   euler_cs(crot, &v.crot_c, &v.crot_s);
   for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &v.face_c[f], &v.face_s[f]);
   v.use_linear = view->use_linear;
@@ -894,6 +1201,36 @@ int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
   ShadeIn in{tris, descs, lights, nl, Atlas{atlas, nums, sizes, mipmap_start}, shadow_dyn, shadow_static};
   parallel_for((int64_t)P, nthreads, [&](int64_t p) {
     kernel3_pixel((int)(p % W), (int)(p / W), v, in, S, depth, ids, rgba, normals);
+  });
+  return 0;
+}
+
+// kernel3 in double precision (see kernel3_pixel_fp64) over the depth / id
+// of the float path: rgba64 gets H*W*4 colours in [0, 1] before quantisation.
+int oracle_render_fp64(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descriptor* descs,
+                       const gbr_light* lights, uint32_t nl, const uint8_t* atlas, const uint32_t* nums,
+                       const uint32_t* sizes, uint32_t mipmap_start, const uint32_t* shadow_dyn,
+                       const uint32_t* shadow_static, const gbr_camera* cam, const gbr_view* view,
+                       double* rgba64, int exact_acos, int nthreads) {
+  const int W = view->width, H = view->height;
+  const float fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
+  f3 cpos = v3(cam->pos), crot = v3(cam->rot);
+  Setup S;
+  prearrange(tris, n, descs, cpos, crot, fov, (float)W, (float)H, nthreads, &S);
+  const size_t P = (size_t)W * H;
+  std::vector<uint32_t> depth(P, kDepthClear), ids(P, kNoId);
+  kernel1(S, (float)W, (float)H, reinterpret_cast<std::atomic<uint32_t>*>(depth.data()), W, nthreads);
+  kernel2(S, (float)W, (float)H, depth.data(), reinterpret_cast<std::atomic<uint32_t>*>(ids.data()), W, nthreads);
+  ShadeView v;
+  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot;
+  euler_cs(crot, &v.crot_c, &v.crot_s);
+  for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &v.face_c[f], &v.face_s[f]);
+  v.use_linear = view->use_linear;
+  v.clear.x = view->clear_col[0]; v.clear.y = view->clear_col[1];
+  v.clear.z = view->clear_col[2]; v.clear.w = view->clear_col[3];
+  ShadeIn in{tris, descs, lights, nl, Atlas{atlas, nums, sizes, mipmap_start}, shadow_dyn, shadow_static};
+  parallel_for((int64_t)P, nthreads, [&](int64_t p) {
+    kernel3_pixel_fp64((int)(p % W), (int)(p / W), v, in, S, depth.data(), ids.data(), exact_acos != 0, rgba64);
   });
   return 0;
 }

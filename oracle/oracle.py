@@ -44,6 +44,9 @@ def lib():
         L.oracle_render.restype = ctypes.c_int
         L.oracle_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P,
                                     ctypes.c_uint32, P, P, P, P, P, P, P, P, ctypes.c_int, P]
+        L.oracle_render_fp64.restype = ctypes.c_int
+        L.oracle_render_fp64.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32,
+                                         P, P, P, P, P, ctypes.c_int, ctypes.c_int]
         L.oracle_walk.restype = ctypes.c_int
         L.oracle_walk.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
                                   P, ctypes.c_int]
@@ -125,6 +128,42 @@ def render(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, shade=Tru
     if nrm is not None:
         out["normals"] = nrm
     return out
+
+
+def render_fp64(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, exact_acos=False, nthreads=None):
+    """kernel3 in double precision over the float path's depth / id: (H, W, 4)
+    float64 colours in [0, 1] before quantisation."""
+    nthreads = nthreads or default_threads()
+    W, H = int(view["width"]), int(view["height"])
+    out = np.empty((H, W, 4), np.float64)
+    if shadow_dyn is None:
+        shadow_dyn = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    if shadow_static is None:
+        shadow_static = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    cam = np.asarray(cam).reshape(1)
+    view = np.asarray(view).reshape(1)
+    lib().oracle_render_fp64(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights),
+                             len(scene.lights), _p(tex.atlas), _p(tex.nums), _p(tex.sizes), tex.mipmap_start,
+                             _p(shadow_dyn), _p(shadow_static), _p(cam), _p(view), _p(out),
+                             1 if exact_acos else 0, nthreads)
+    return out
+
+
+def shading_error(rgba8, fp64, mask=None):
+    """Per-channel max / mean absolute error of an RGBA8 image against the FP64
+    colours (in units of 1/255; includes the 0.5/255 of quantisation), and the
+    fraction of channels whose rounded FP64 value differs."""
+    err = np.abs(rgba8.astype(np.float64) / 255.0 - fp64) * 255.0
+    q = np.floor(np.clip(fp64, 0, 1) * 255.0 + 0.5)
+    off = np.abs(rgba8.astype(np.float64) - q)
+    if mask is not None:
+        err, off = err[mask], off[mask]
+    else:
+        err, off = err.reshape(-1, 4), off.reshape(-1, 4)
+    return {"max_abs_levels": [round(float(v), 4) for v in err.max(0)],
+            "mean_abs_levels": [round(float(v), 5) for v in err.mean(0)],
+            "frac_levels_off": [round(float(v), 6) for v in (off > 0).mean(0)],
+            "max_levels_off": [int(v) for v in off.max(0)]}
 
 
 def walk(tp9, ew, eh, chunk, distance, cap=2048):
