@@ -158,7 +158,10 @@ gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
 }
 
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
-                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st) {
+                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom,
+                       cudaEvent_t join) {
+  const bool split = geom != nullptr && geom != st;
+  if (!split) geom = st;
   const SceneDev sd = s->dev();
   Workspace ws{};
   ws.rec = wm.rec.p;
@@ -175,25 +178,30 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   ws.ctr = wm.ctr.p;
   ws.fine_max = tu.fine_max;
   ws.coarse_shift = tu.coarse_shift;
-  CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), st));
-  CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.nfine, 1), st));
-  CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.ncoarse, 1), st));
-  auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
-  CU(mark(0));
+  CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), geom));
+  CU(cudaMemsetAsync(ws.fine_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.nfine, 1), geom));
+  CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.ncoarse, 1), geom));
+  auto mark = [&](int k, cudaStream_t on) -> cudaError_t { return ev ? cudaEventRecord(ev[k], on) : cudaSuccess; };
+  CU(mark(0, geom));
   if (view)
-    CU(launch_setup_views(sd, wm.views.p, sh.nitems, wm.surf.p, ws, st));
+    CU(launch_setup_views(sd, wm.views.p, sh.nitems, wm.surf.p, ws, geom));
   else
-    CU(launch_setup_shadow(sd, wm.jobs.p, sh.nitems, wm.surf.p, ws, st));
-  CU(mark(1));
-  CU(launch_scan(ws, st));
-  CU(mark(2));
-  CU(launch_fill(ws, wm.surf.p, st));
-  CU(mark(3));
-  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, st));
-  CU(mark(4));
+    CU(launch_setup_shadow(sd, wm.jobs.p, sh.nitems, wm.surf.p, ws, geom));
+  CU(mark(1, geom));
+  CU(launch_scan(ws, geom));
+  CU(mark(2, geom));
+  CU(launch_fill(ws, wm.surf.p, geom));
+  CU(mark(3, geom));
+  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom));
+  CU(mark(4, geom));
+  if (split) {
+    CU(cudaEventRecord(join, geom));
+    CU(cudaStreamWaitEvent(st, join, 0));
+  }
   if (view) {
+    CU(mark(6, st));
     CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st));
-    CU(mark(5));
+    CU(mark(5, st));
   }
   CU(cudaMemcpyAsync(host_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
   return GBR_OK;
@@ -237,12 +245,14 @@ Counters* counter_slot(gbr_scene* s, bool view) {
 // the read-back of its counters; the caller synchronises and calls
 // check_pass.  The caller has filled the pass's surfaces / views / jobs on
 // the device.
-gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream_t st) {
+gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream_t st,
+                        cudaStream_t geom = nullptr) {
   TRY(ensure_world(s, st));
   WorkMem& wm = pass_mem(s, view);
   TRY(reserve_pass(wm, sh, view));
   cudaEvent_t* ev = s->profile ? s->ev + (view ? 8 : 0) : nullptr;
-  TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st));
+  TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st,
+                  geom, s->geom_done));
   s->stats.launches += pass_kernels(view);
   return GBR_OK;
 }
@@ -255,7 +265,9 @@ bool check_pass(gbr_scene* s, bool view) {
     const int sb = view ? 4 : 0, nst = (int)pass_kernels(view);
     for (int k = 0; k < nst; k++) {
       float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, s->ev[sb * 2 + k], s->ev[sb * 2 + k + 1]) == cudaSuccess) {
+      // shading: from its own start event (it may first wait for a shadow pass)
+      cudaEvent_t a = k == 4 ? s->ev[sb * 2 + 6] : s->ev[sb * 2 + k], b = s->ev[sb * 2 + k + 1];
+      if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) {
         s->stats.stage_ms[sb + k] += ms;
         s->stats.stage_calls[sb + k] += 1;
       }
@@ -283,6 +295,7 @@ gbr_status settle_shadow(gbr_scene* s, bool already_synced, bool* rerun) {
   if (!s->shadow_pending) return GBR_OK;
   if (!already_synced) CU(cudaStreamSynchronize(s->shadow_stream));
   s->shadow_pending = false;
+  s->pre_shadow_valid = false;
   if (check_pass(s, false)) return GBR_OK;
   TRY(run_shadow_sync(s, s->shadow_shape, s->shadow_stream));
   *rerun = true;
@@ -292,6 +305,14 @@ gbr_status settle_shadow(gbr_scene* s, bool already_synced, bool* rerun) {
 gbr_status settle_shadow_quiet(gbr_scene* s) {
   bool rerun = false;
   return settle_shadow(s, false, &rerun);
+}
+
+// The aux stream and the two events of the shadow / view overlap.
+gbr_status ensure_aux(gbr_scene* s) {
+  if (!s->aux) CU(cudaStreamCreateWithFlags(&s->aux, cudaStreamNonBlocking));
+  if (!s->pre_shadow) CU(cudaEventCreateWithFlags(&s->pre_shadow, cudaEventDisableTiming));
+  if (!s->geom_done) CU(cudaEventCreateWithFlags(&s->geom_done, cudaEventDisableTiming));
+  return GBR_OK;
 }
 
 }  // namespace
@@ -430,6 +451,9 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->staging.release();
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
+  if (s->pre_shadow) cudaEventDestroy(s->pre_shadow);
+  if (s->geom_done) cudaEventDestroy(s->geom_done);
+  if (s->aux) cudaStreamDestroy(s->aux);
   delete s;
   return GBR_OK;
 }
@@ -612,7 +636,12 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
   TRY(wm.jobs.reserve(jobs.size()));
   CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), surfs.size() * sizeof(Surface), cudaMemcpyHostToDevice, st));
   CU(cudaMemcpyAsync(wm.jobs.p, jobs.data(), jobs.size() * sizeof(ShadowJob), cudaMemcpyHostToDevice, st));
+  // the stream's work before this pass: what a view pass on the same stream
+  // may run after while this pass renders
+  TRY(ensure_aux(s));
+  CU(cudaEventRecord(s->pre_shadow, st));
   TRY(enqueue_pass(s, false, sh, st));
+  s->pre_shadow_valid = true;
   // The counters are checked at the next synchronisation point (render,
   // read-back, stats), which re-runs this pass if its scratch overflowed.
   s->shadow_pending = true;
@@ -659,19 +688,28 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   WorkMem& wm = s->ws_view;
   TRY(wm.surf.reserve(n));
   TRY(wm.views.reserve(n));
-  CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, st));
-  CU(cudaMemcpyAsync(wm.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, st));
   if (s->shadow_pending && s->shadow_stream != st) {
     bool rerun = false;
     TRY(settle_shadow(s, false, &rerun));
   }
+  // A shadow pass queued on this stream only feeds shading: the geometry
+  // stages run beside it on the aux stream, after the work queued before it.
+  const bool overlap = s->overlap && s->shadow_pending && s->shadow_stream == st && s->pre_shadow_valid &&
+                       !s->world_dirty;
+  cudaStream_t geom = st;
+  if (overlap) {
+    geom = s->aux;
+    CU(cudaStreamWaitEvent(geom, s->pre_shadow, 0));
+  }
+  CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, geom));
+  CU(cudaMemcpyAsync(wm.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, geom));
   PassShape sh;
   sh.nitems = sh.nsurf = n;
   sh.nfine = tb;
   sh.ncoarse = cb;
   sh.npix = npix;
   for (int attempt = 0; attempt < 8; attempt++) {
-    TRY(enqueue_pass(s, true, sh, st));
+    TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
     CU(cudaStreamSynchronize(st));
     bool rerun = false;
     TRY(settle_shadow(s, true, &rerun));  // same stream: already complete

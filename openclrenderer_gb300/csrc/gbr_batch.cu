@@ -28,6 +28,8 @@ struct gbr_batch {
   HostBuf stage;
   size_t ctr_off = 0;
   cudaStream_t cap_stream = nullptr;
+  cudaStream_t cap_aux = nullptr;  // the views' geometry branch of the graph
+  cudaEvent_t fork = nullptr, join = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   size_t nodes = 0;
@@ -126,19 +128,21 @@ gbr_status capture(gbr_batch* b) {
   TRY(ensure_world(s, b->cap_stream));
   CU(cudaStreamSynchronize(b->cap_stream));
 
-  // the frame, captured
+  // the frame, captured: the views' geometry on a branch beside the shadow
+  // pass, joined before shading
   CU(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
   gbr_status st = GBR_OK;
-  cudaError_t ce = cudaSuccess;
-  if (shadow)
+  cudaError_t ce = cudaEventRecord(b->fork, b->cap_stream);
+  if (ce == cudaSuccess) ce = cudaStreamWaitEvent(b->cap_aux, b->fork, 0);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(b->wv.views.p, b->params(), b->n * sizeof(ViewParams), cudaMemcpyHostToDevice,
+                         b->cap_aux);
+  if (ce == cudaSuccess && shadow)
     st = launch_pass(s, b->wsh, b->tune[GBR_PASS_SHADOW], false, b->sshape, b->shadow_ctr(), nullptr,
                      b->cap_stream);
-  if (st == GBR_OK) {
-    ce = cudaMemcpyAsync(b->wv.views.p, b->params(), b->n * sizeof(ViewParams), cudaMemcpyHostToDevice,
-                         b->cap_stream);
-    if (ce == cudaSuccess)
-      st = launch_pass(s, b->wv, b->tune[GBR_PASS_VIEW], true, b->vshape, b->view_ctr(), nullptr, b->cap_stream);
-  }
+  if (ce == cudaSuccess && st == GBR_OK)
+    st = launch_pass(s, b->wv, b->tune[GBR_PASS_VIEW], true, b->vshape, b->view_ctr(), nullptr, b->cap_stream,
+                     b->cap_aux, b->join);
   cudaGraph_t g = nullptr;
   cudaError_t ee = cudaStreamEndCapture(b->cap_stream, &g);
   if (st != GBR_OK) {
@@ -243,7 +247,10 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
   b->tune[0] = s->tune[0];
   b->tune[1] = s->tune[1];
   cudaError_t e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap_aux, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gbr_batch_destroy(b);
     return fail(GBR_CUDA_ERROR, "stream / event creation failed: %s", cudaGetErrorString(e));
@@ -401,7 +408,10 @@ gbr_status gbr_batch_destroy(gbr_batch* b) {
   b->wsh.release();
   b->stage.release();
   if (b->done) cudaEventDestroy(b->done);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+  if (b->cap_aux) cudaStreamDestroy(b->cap_aux);
   delete b;
   return GBR_OK;
 }

@@ -143,6 +143,13 @@ struct gbr_scene {
   bool profile = false;
   cudaEvent_t ev[20] = {};
   gbr::Tuning tune[2];   // [GBR_PASS_SHADOW], [GBR_PASS_VIEW]
+  // The view pass's geometry stages overlap a shadow pass queued on the same
+  // stream: they run on aux after pre_shadow (the stream's work before that
+  // shadow pass), and shading waits for geom_done.
+  cudaStream_t aux = nullptr;
+  cudaEvent_t pre_shadow = nullptr, geom_done = nullptr;
+  bool pre_shadow_valid = false;  // pre_shadow marks the pending shadow pass's start
+  bool overlap = true;
   uint64_t version = 1;  // bumped whenever a device pointer or table a pass reads changes
 
   gbr::SceneDev dev() const {
@@ -190,11 +197,16 @@ void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector
 // Scratch of a pass sized to the memory's targets (no allocation when it fits).
 gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view);
 // Launches of one pass on the pass's scratch: counter clears, setup, scan,
-// fill, raster and (views) shade, then the read-back of the counters into
-// host_ctr.  Allocates nothing, so it can be captured into a graph.  ev, when
-// not null, holds the stage events (profiling).
+// fill and raster on geom, then (views) shade and the read-back of the
+// counters into host_ctr on st.  When geom differs from st, join is recorded
+// on geom after the raster and st waits for it before shading, so the
+// geometry can run beside whatever st does first (the shadow pass).
+// Allocates nothing, so it can be captured into a graph.  ev, when not null,
+// holds the stage events (profiling): [0..4] around the geometry stages,
+// [5] after shading, [6] before shading.
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
-                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st);
+                       Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom = nullptr,
+                       cudaEvent_t join = nullptr);
 // Kernel launches of one pass (for the launch statistics).
 inline uint32_t pass_kernels(bool view) { return view ? 5u : 4u; }
 // Record a finished pass's counters in the scene's statistics; on overflow
