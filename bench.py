@@ -315,6 +315,28 @@ def run_serving(args, stream):
                       "p99_ms": round(float(np.percentile(lat, 99)), 3),
                       "mean_batch_views": round(float(np.mean(done["batch_views"])), 2),
                       "peak_admitted_mb": round(st["peak_admitted_bytes"] / 2 ** 20, 1)})
+    # the plain single-view pipeline on the same requests (the burst list), one
+    # call at a time with the same host outputs: the served-vs-plain ratio
+    for s_i, cam, view in reqs[:4]:
+        P = int(view["width"]) * int(view["height"])
+        gss[s_i].render_host(cam, view, False, False,
+                             pool[0][:P * 4].reshape(int(view["height"]), int(view["width"]), 4), stream=stream)
+    t0 = time.perf_counter()
+    pix = 0
+    plain_lat = []
+    for k, (s_i, cam, view) in enumerate(reqs):
+        P = int(view["width"]) * int(view["height"])
+        s0 = time.perf_counter()
+        gss[s_i].render_host(cam, view, False, False,
+                             pool[k % len(pool)][:P * 4].reshape(int(view["height"]), int(view["width"]), 4),
+                             stream=stream)
+        plain_lat.append(1e3 * (time.perf_counter() - s0))
+        pix += P
+    plain_wall = time.perf_counter() - t0
+    plain = {"form": "gbr_render_view_host per request, sequential", "throughput_mpix_s": round(pix / plain_wall / 1e6, 1),
+             "p50_ms": round(float(np.percentile(plain_lat, 50)), 3),
+             "p99_ms": round(float(np.percentile(plain_lat, 99)), 3)}
+    plain["served_burst_vs_plain"] = round(loads[-1]["throughput_mpix_s"] / plain["throughput_mpix_s"], 3)
     for g in gss:
         g.close()
     # reference kernels on the host cores, one request at each resolution (100k-triangle scene)
@@ -335,7 +357,7 @@ def run_serving(args, stream):
             cpu_lat[f"{w}x{h}"] = round(1e3 * (time.perf_counter() - t0), 1)
     return {"workload": "4 resident scenes (100k/500k/1M/2M triangles), Poisson arrivals, resolutions "
                         "640x480/1280x720/1920x1080/3840x2160", "hbm_budget_gb": budget / 2 ** 30,
-            "requests_per_load": args.serve_requests, "loads": loads,
+            "requests_per_load": args.serve_requests, "loads": loads, "plain_sequential": plain,
             "cpu_reference_latency_ms_100k_scene": cpu_lat, "cpu_kind": kind,
             "cpu_threads": os.cpu_count()}
 

@@ -209,6 +209,19 @@ gbr_status gbr_render_view_host(gbr_scene* scene, const gbr_camera* cam, const g
 gbr_status gbr_render_batch(gbr_scene* scene, uint32_t n, const gbr_camera* cams,
                             const gbr_view* views, const gbr_outputs* outs, void* stream);
 
+/* Device framebuffer of one view (the reference's depth_buffer[2] +
+ * g_id_screen_tex + g_screen of object_context_data, object_context.hpp:82-165,
+ * and cl_gl_interop_texture's surface): depth u32, id u32, RGBA8 and optionally
+ * normals ushort2, W*H each.  gbr_framebuffer_outputs gives the device
+ * pointers for gbr_render_view / gbr_render_batch. */
+typedef struct gbr_framebuffer gbr_framebuffer;
+gbr_status gbr_framebuffer_create(int32_t width, int32_t height, int32_t with_normals, gbr_framebuffer** out);
+gbr_status gbr_framebuffer_outputs(gbr_framebuffer* fb, gbr_outputs* out, int32_t* width, int32_t* height);
+/* Copy one plane to host memory (which: 0 depth, 1 id, 2 rgba, 3 normals);
+ * bytes must be the plane's size (W*H*4).  Synchronises the device. */
+gbr_status gbr_framebuffer_read(gbr_framebuffer* fb, int32_t which, void* host, size_t bytes);
+gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb);
+
 /* Counters of the last render / shadow pass on this scene. */
 gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
 

@@ -93,6 +93,10 @@ SIGNATURES = {
     "gbr_render_batch": (ctypes.c_int, [_P, _U32, _P, _P, _P, _P]),
     "gbr_scene_stats": (ctypes.c_int, [_P, _P]),
     "gbr_scene_profile": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "gbr_framebuffer_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P]),
+    "gbr_framebuffer_outputs": (ctypes.c_int, [_P, _P, _P, _P]),
+    "gbr_framebuffer_read": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_size_t]),
+    "gbr_framebuffer_destroy": (ctypes.c_int, [_P]),
     "gbr_scene_set_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
     "gbr_scene_get_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
     "gbr_batch_create": (ctypes.c_int, [_P, _U32, _P, _P, ctypes.c_int32, _P]),

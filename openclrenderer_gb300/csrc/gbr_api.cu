@@ -198,7 +198,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
     CU(cudaEventRecord(join, geom));
     CU(cudaStreamWaitEvent(st, join, 0));
   }
-  if (view) {
+  if (view && sh.shade) {
     CU(mark(6, st));
     CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st));
     CU(mark(5, st));
@@ -253,7 +253,8 @@ gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream
   cudaEvent_t* ev = s->profile ? s->ev + (view ? 8 : 0) : nullptr;
   TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st,
                   geom, s->geom_done));
-  s->stats.launches += pass_kernels(view);
+  s->stats.launches += pass_kernels(view) - (view && !sh.shade ? 1u : 0u);
+  if (view) s->view_shaded = sh.shade;
   return GBR_OK;
 }
 
@@ -264,6 +265,7 @@ bool check_pass(gbr_scene* s, bool view) {
   if (s->profile) {
     const int sb = view ? 4 : 0, nst = (int)pass_kernels(view);
     for (int k = 0; k < nst; k++) {
+      if (view && k == 4 && !s->view_shaded) continue;
       float ms = 0.f;
       // shading: from its own start event (it may first wait for a shadow pass)
       cudaEvent_t a = k == 4 ? s->ev[sb * 2 + 6] : s->ev[sb * 2 + k], b = s->ev[sb * 2 + k + 1];
@@ -708,6 +710,9 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   sh.nfine = tb;
   sh.ncoarse = cb;
   sh.npix = npix;
+  sh.shade = false;
+  for (uint32_t i = 0; i < n; i++)
+    if (outs[i].rgba || outs[i].normals) sh.shade = true;
   for (int attempt = 0; attempt < 8; attempt++) {
     TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
     CU(cudaStreamSynchronize(st));
@@ -757,6 +762,75 @@ gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
     for (double& v : s->stats.stage_ms) v = 0;
     for (uint64_t& v : s->stats.stage_calls) v = 0;
   }
+  return GBR_OK;
+}
+
+}  // extern "C"
+
+struct gbr_framebuffer {
+  int device = 0;
+  int32_t width = 0, height = 0;
+  DevBuf<uint32_t> depth, id, rgba, normals;
+};
+
+extern "C" {
+
+gbr_status gbr_framebuffer_create(int32_t width, int32_t height, int32_t with_normals, gbr_framebuffer** out) {
+  if (!out) return fail(GBR_INVALID_ARG, "null out");
+  *out = nullptr;
+  if (width < 1 || height < 1 || width > kMaxWalkWidth || height > kMaxWalkHeight)
+    return fail(GBR_INVALID_ARG, "framebuffer %dx%d outside 1..%d x 1..%d", width, height, kMaxWalkWidth,
+                kMaxWalkHeight);
+  gbr_framebuffer* fb = new gbr_framebuffer();
+  cudaError_t e = cudaGetDevice(&fb->device);
+  const size_t P = (size_t)width * height;
+  gbr_status st = e == cudaSuccess ? GBR_OK : fail(GBR_CUDA_ERROR, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (st == GBR_OK) st = fb->depth.reserve(P);
+  if (st == GBR_OK) st = fb->id.reserve(P);
+  if (st == GBR_OK) st = fb->rgba.reserve(P);
+  if (st == GBR_OK && with_normals) st = fb->normals.reserve(P);
+  if (st != GBR_OK) {
+    gbr_framebuffer_destroy(fb);
+    return st;
+  }
+  fb->width = width;
+  fb->height = height;
+  *out = fb;
+  return GBR_OK;
+}
+
+gbr_status gbr_framebuffer_outputs(gbr_framebuffer* fb, gbr_outputs* out, int32_t* width, int32_t* height) {
+  if (!fb || !out) return fail(GBR_INVALID_ARG, "null argument");
+  out->depth = fb->depth.p;
+  out->id = fb->id.p;
+  out->rgba = reinterpret_cast<uint8_t*>(fb->rgba.p);
+  out->normals = reinterpret_cast<uint16_t*>(fb->normals.p);
+  if (width) *width = fb->width;
+  if (height) *height = fb->height;
+  return GBR_OK;
+}
+
+gbr_status gbr_framebuffer_read(gbr_framebuffer* fb, int32_t which, void* host, size_t bytes) {
+  if (!fb || !host) return fail(GBR_INVALID_ARG, "null argument");
+  const DevBuf<uint32_t>* planes[4] = {&fb->depth, &fb->id, &fb->rgba, &fb->normals};
+  if (which < 0 || which > 3 || !planes[which]->p) return fail(GBR_INVALID_ARG, "no framebuffer plane %d", which);
+  const size_t P = (size_t)fb->width * fb->height * 4;
+  if (bytes != P) return fail(GBR_INVALID_ARG, "plane is %zu bytes, not %zu", P, bytes);
+  CU(cudaSetDevice(fb->device));
+  CU(cudaDeviceSynchronize());
+  CU(cudaMemcpy(host, planes[which]->p, P, cudaMemcpyDeviceToHost));
+  return GBR_OK;
+}
+
+gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb) {
+  if (!fb) return GBR_OK;
+  cudaSetDevice(fb->device);
+  cudaDeviceSynchronize();
+  fb->depth.release();
+  fb->id.release();
+  fb->rgba.release();
+  fb->normals.release();
+  delete fb;
   return GBR_OK;
 }
 

@@ -92,6 +92,9 @@ gbr_status capture(gbr_batch* b) {
   b->vshape.nfine = tb;
   b->vshape.ncoarse = cb;
   b->vshape.npix = npix;
+  b->vshape.shade = false;
+  for (uint32_t i = 0; i < b->n; i++)
+    if (b->outs[i].rgba || b->outs[i].normals) b->vshape.shade = true;
   if (b->wv.rec_target == 0) {
     b->wv.rec_target = std::max(s->ws_view.rec_target, s->ntris + 1024u);
     b->wv.bin_target = std::max(s->ws_view.bin_target, 4u * b->wv.rec_target);
@@ -169,7 +172,8 @@ gbr_status launch_graph(gbr_batch* b, const gbr_camera* cams, cudaStream_t st) {
   CU(cudaGraphLaunch(b->exec, st));
   CU(cudaEventRecord(b->done, st));
   b->launches++;
-  b->s->stats.launches += pass_kernels(true) + (b->sshape.nitems ? pass_kernels(false) : 0u);
+  b->s->stats.launches += pass_kernels(true) - (b->vshape.shade ? 0u : 1u) +
+                          (b->sshape.nitems ? pass_kernels(false) : 0u);
   b->in_flight = true;
   b->last_stream = st;
   return GBR_OK;

@@ -107,6 +107,7 @@ struct WorkMem {
 struct PassShape {
   uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
   size_t npix = 0;
+  bool shade = true;  // views: some view wants RGBA or normals (else depth / id only)
 };
 
 void euler_cs(const float ang[3], float c[3], float s[3]);
@@ -150,6 +151,7 @@ struct gbr_scene {
   cudaEvent_t pre_shadow = nullptr, geom_done = nullptr;
   bool pre_shadow_valid = false;  // pre_shadow marks the pending shadow pass's start
   bool overlap = true;
+  bool view_shaded = true;  // the last view pass ran kernel3
   uint64_t version = 1;  // bumped whenever a device pointer or table a pass reads changes
 
   gbr::SceneDev dev() const {

@@ -177,13 +177,14 @@ class GpuScene:
         return outs
 
     def render_host(self, cam, view, depth=None, ids=None, rgba=None, stream=None):
-        """render_tris with host output buffers (numpy; pinned or pageable)."""
+        """render_tris with host output buffers (numpy; pinned or pageable).
+        None allocates a buffer; False skips that output's copy."""
         cam = np.asarray(cam, S.CAMERA).reshape(1)
         view = np.asarray(view, S.VIEW).reshape(1)
         W, H = int(view[0]["width"]), int(view[0]["height"])
-        depth = np.empty((H, W), np.uint32) if depth is None else depth
-        ids = np.empty((H, W), np.uint32) if ids is None else ids
-        rgba = np.empty((H, W, 4), np.uint8) if rgba is None else rgba
+        depth = np.empty((H, W), np.uint32) if depth is None else (None if depth is False else depth)
+        ids = np.empty((H, W), np.uint32) if ids is None else (None if ids is False else ids)
+        rgba = np.empty((H, W, 4), np.uint8) if rgba is None else (None if rgba is False else rgba)
         _native.check(self.L.gbr_render_view_host(self.h, _np_ptr(cam), _np_ptr(view), _np_ptr(depth),
                                                   _np_ptr(ids), _np_ptr(rgba), _stream_ptr(stream)))
         return {"depth": depth, "id": ids, "rgba": rgba}

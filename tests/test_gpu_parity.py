@@ -90,6 +90,33 @@ def test_terrain_1080p_full_parity():
     assert_parity(got, ref, "terrain_1080p")
 
 
+def test_multiple_and_static_shadow_lights():
+    """Three dynamic shadow lights (one also static), a plain light, static
+    objects (drawn only into the static cubemaps, dynamic ones only into the
+    dynamic cubemaps) and objects that receive no dynamic shadows
+    (cl2.cl:4460-4464, 6126-6181; engine.cpp:1700-1783)."""
+    sc = scenes.plain_cubes()
+    descs = sc.descs.copy()
+    for i in range(len(descs)):
+        ff = S.FLAG_TWO_SIDED
+        if i % 3 == 0:
+            ff |= S.FLAG_IS_STATIC
+        if i % 5 == 0:
+            ff |= S.FLAG_NO_DYN_SHADOWS
+        descs[i]["feature_flag"] = ff
+    sc.descs = descs
+    sc.lights = np.stack([S.make_light((-200, -150, 800), (1, 0.9, 0.8), radius=3000.0, shadow=1),
+                          S.make_light((250, 100, 1200), (0.7, 0.8, 1), radius=2500.0, shadow=1, is_static=1),
+                          S.make_light((0, 300, 400), (1, 1, 1), radius=2000.0, shadow=1),
+                          S.make_light((100, -100, 100), (1, 1, 1), radius=4000.0)])
+    gs, got, ref = run_both(sc, shadows=True, normals=True)
+    dyn, sta = O.shadow(sc)
+    assert np.array_equal(gs.cubemaps(), dyn[:3])
+    assert np.array_equal(gs.cubemaps(static=True), sta[:1])
+    assert (dyn[:3] != 0xFFFFFFFF).sum() > 1000 and (sta[0] != 0xFFFFFFFF).sum() > 1000
+    assert_parity(got, ref, "multi_shadow")
+
+
 def test_random_soup_parity():
     for seed, (w, h) in zip((1, 2, 3), ((640, 480), (333, 197), (1024, 768))):
         sc = random_soup(400, w, h, seed)
@@ -227,3 +254,24 @@ def test_binning_stress_full_parity():
     # repeatable with the grown scratch
     again = gs.render(sc.cameras[0], sc.views[0]).numpy()
     assert np.array_equal(again["depth"], got["depth"]) and np.array_equal(again["id"], got["id"])
+
+
+def test_depth_id_only_view_skips_shading():
+    """A view with neither RGBA nor normals outputs runs no kernel3; depth and
+    id are the same as with shading."""
+    import ctypes
+    from openclrenderer_gb300 import _native
+    from openclrenderer_gb300.pipeline import OutputSet, _Outs, _np_ptr, _stream_ptr
+    sc = scenes.plain_cubes()
+    gs = GpuScene(sc)
+    full = gs.render(sc.cameras[0], sc.views[0]).numpy()
+    before = gs.stats()["launches"]
+    o = OutputSet(800, 600)
+    outs = _Outs(o.depth.data_ptr(), o.id.data_ptr(), None, None)
+    cam = np.asarray(sc.cameras[0], S.CAMERA).reshape(1)
+    view = np.asarray(sc.views[0], S.VIEW).reshape(1)
+    _native.check(gs.L.gbr_render_view(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(outs), _stream_ptr(None)))
+    torch.cuda.synchronize()
+    assert gs.stats()["launches"] - before == 4  # setup, scan, fill, raster
+    got = o.numpy()
+    assert np.array_equal(got["depth"], full["depth"]) and np.array_equal(got["id"], full["id"])
