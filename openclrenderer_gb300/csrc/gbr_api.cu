@@ -144,6 +144,7 @@ void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector
   sh.nsurf = (uint32_t)surfs.size();
   sh.nfine = tb;
   sh.ncoarse = cb;
+  sh.tiles_per_surface = surfs.empty() ? 0u : (uint32_t)(surfs[0].tiles_x * surfs[0].tiles_y);  // cube faces
 }
 
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
@@ -192,7 +193,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(mark(2, geom));
   CU(launch_fill(ws, wm.surf.p, geom));
   CU(mark(3, geom));
-  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom));
+  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom, sh.tiles_per_surface));
   CU(mark(4, geom));
   if (split) {
     CU(cudaEventRecord(join, geom));

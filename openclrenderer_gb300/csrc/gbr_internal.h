@@ -150,8 +150,11 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
                                 const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
+// tiles_per_surface: the common tile count when every surface has the same
+// size (cube faces), else 0.
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,
-                          uint32_t ntiles, bool with_id, int threads, cudaStream_t st);
+                          uint32_t ntiles, bool with_id, int threads, cudaStream_t st,
+                          uint32_t tiles_per_surface = 0);
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                          const Surface* d_surf, uint32_t ntiles, const ShadeRec* srec,
                          cudaStream_t st);

@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __res
   }
 }
 
+// The surface owning a tile (binary search over tile_base, one thread).
 __device__ __forceinline__ uint32_t find_surface(const Surface* surfs, uint32_t nsurf, uint32_t tile) {
   uint32_t lo = 0, hi = nsurf - 1;
   while (lo < hi) {
@@ -488,6 +489,22 @@ __device__ __forceinline__ uint32_t find_surface(const Surface* surfs, uint32_t 
   }
   return lo;
 }
+
+// The surface owning a tile, found by one warp: surfaces are sorted by
+// tile_base, so one ballot over 32 of them finds the last one starting at or
+// before the tile.  Every lane of the warp must call it; all get the result.
+__device__ __forceinline__ uint32_t find_surface_warp(const Surface* surfs, uint32_t nsurf, uint32_t tile) {
+  const int lane = threadIdx.x & 31;
+  uint32_t owner = 0;
+  for (uint32_t b = 0; b < nsurf; b += 32) {
+    const uint32_t i = b + lane;
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, i < nsurf && __ldg(&surfs[i].tile_base) <= tile);
+    if (m) owner = b + 31 - __clz(m);
+    if (m != 0xFFFFFFFFu) break;
+  }
+  return owner;
+}
+
 
 // Coverage of a pixel known to lie inside the record's bbox: the reference
 // walk's skipped left-column pixels, then point_in_tri.
@@ -568,11 +585,12 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
   __shared__ uint32_t ssamples;
   __shared__ Surface S;
   __shared__ uint32_t lists[4];
-  if (ws.ctr->overflow) return;
-  const uint32_t tile = blockIdx.x;
+  // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
+  const uint32_t tile = gridDim.y > 1 ? surfs[blockIdx.y].tile_base + blockIdx.x : blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (ws.ctr->overflow) return;
   if (tid == 0) {
-    uint32_t s = find_surface(surfs, nsurf, tile);
+    const uint32_t s = gridDim.y > 1 ? blockIdx.y : find_surface(surfs, nsurf, tile);
     S = surfs[s];
     uint32_t lt = tile - S.tile_base;
     int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
@@ -770,8 +788,10 @@ __device__ __forceinline__ TexSlot tex_slot_pre(const SceneDev& sc, int which, i
 __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy) {
   cx = clampf_(cx, 0.001f, ts.width - 0.001f);
   cy = clampf_(cy, 0.001f, ts.width - 0.001f);
-  int ix = f2i_sat(fma_(ts.tnumx, ts.width, cx));
-  int iy = f2i_sat(fma_(ts.tnumy, ts.width, cy));
+  // in [0, 2048) and never NaN (the clamp maps NaN to 0.001): plain
+  // truncation equals the saturating convert_int
+  int ix = (int)fma_(ts.tnumx, ts.width, cx);
+  int iy = (int)fma_(ts.tnumy, ts.width, cy);
   const uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(ts.page) + ((size_t)iy * kTexPage + ix));
   f4 r; r.x = u8f(t & 0xFF); r.y = u8f((t >> 8) & 0xFF); r.z = u8f((t >> 16) & 0xFF); r.w = u8f(t >> 24);
   return r;
@@ -824,6 +844,14 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
   return r;
 }
 
+// How many of the thresholds t0 < t1 < t2 < t3 < t4 lie below d2, i.e.
+// (d2 > t0) + ... + (d2 > t4): the thresholds dep + z (z = -2..2, dep <=
+// 350000) are strictly increasing in float, so the predicates are monotone and
+// three comparisons find the count.
+__device__ __forceinline__ int ssao_count(float d2, float t0, float t1, float t2, float t3, float t4) {
+  return d2 > t2 ? (d2 > t4 ? 5 : (d2 > t3 ? 4 : 3)) : (d2 > t1 ? 2 : (d2 > t0 ? 1 : 0));
+}
+
 // generate_ssao (cl2.cl:2194-2260).  The 25 taps share 5 rows and 5
 // columns, so their rounded and clamped offsets are computed once; the depth
 // thresholds dep + z are computed once; and the count (at most 125, exact in
@@ -839,11 +867,12 @@ __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth,
   int wx[5];
 #pragma unroll
   for (int k = 0; k < 5; k++) wx[k] = (int)clampf_((float)x + roundf((float)(k - 2) * world_rad), 1.0f, (float)W - 2.0f);
+  const float t0 = dep + -2.0f, t1 = dep + -1.0f, t3 = dep + 1.0f, t4 = dep + 2.0f;
   int acc = 0;
   if (__all_sync(__activemask(), world_rad < 0.25f)) {
     const int wy = (int)clampf_((float)y, 1.0f, (float)H - 2.0f);
     const float d2 = depth_to_dist(__ldg(depth + (size_t)wy * W + wx[2]));
-    acc = 25 * ((d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f));
+    acc = 25 * ssao_count(d2, t0, t1, dep, t3, t4);
   } else {
 #pragma unroll 1
     for (int yy = -2; yy <= 2; yy++) {
@@ -852,7 +881,7 @@ __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth,
 #pragma unroll
       for (int xx = 0; xx < 5; xx++) {
         const float d2 = depth_to_dist(__ldg(row + wx[xx]));
-        acc += (d2 > dep + -2.0f) + (d2 > dep + -1.0f) + (d2 > dep) + (d2 > dep + 1.0f) + (d2 > dep + 2.0f);
+        acc += ssao_count(d2, t0, t1, dep, t3, t4);
       }
     }
   }
@@ -987,8 +1016,11 @@ struct SLight {
 };
 
 // kernel3 (cl2.cl:5792-6408) for one pixel of a view.
+// colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
+// 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
 __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
-                            const ShadeRec* __restrict__ srec, const SLight* __restrict__ lights, int x, int y) {
+                            const ShadeRec* __restrict__ srec, const SLight* __restrict__ lights, int x, int y,
+                            const float* __restrict__ colx, const float* __restrict__ rowy) {
   const int W = S.width, H = S.height;
   const size_t p = (size_t)y * W + x;
   const uint32_t d = S.depth[p];
@@ -1066,9 +1098,9 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     plane_const(depths, xpv, ypv, rconst, &DA, &DB, &DC);
     float dmx = fma_(DA, fx + 1.0f, fma_(DB, fy, DC));
     float dmy = fma_(DA, fx, fma_(DB, fy + 1.0f, DC));
-    float hw = (float)W / 2.0f, hh = (float)H / 2.0f;
-    f3 lmx = mk3(fdiv((fx + 1.0f) - hw, fov), fdiv(fy - hh, fov), 1.0f);
-    f3 lmy = mk3(fdiv(fx - hw, fov), fdiv((fy + 1.0f) - hh, fov), 1.0f);
+    const int lx = x & (kTile - 1), ly = y & (kTile - 1);
+    f3 lmx = mk3(colx[lx + 1], rowy[ly], 1.0f);  // fdiv((fx + 1) - hw, fov), fdiv(fy - hh, fov)
+    f3 lmy = mk3(colx[lx], rowy[ly + 1], 1.0f);  // fdiv(fx - hw, fov), fdiv((fy + 1) - hh, fov)
     lmx = mk3(fdiv(lmx.x, dmx), fdiv(lmx.y, dmx), fdiv(lmx.z, dmx));
     lmy = mk3(fdiv(lmy.x, dmy), fdiv(lmy.y, dmy), fdiv(lmy.z, dmy));
     f3 gmx = rot_quat_n(sub3(add3(back_rot_cs(lmx, zero, cc, cs), cpos), wpos), qi);
@@ -1186,7 +1218,11 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
                                                const ShadeRec* __restrict__ srec) {
   __shared__ uint32_t s_id;
   __shared__ SLight slights[kMaxLights];
-  if (threadIdx.x == 0) s_id = find_surface(surfs, nviews, blockIdx.x);
+  __shared__ float colx[kTile + 1], rowy[kTile + 1];
+  if (threadIdx.x < 32) {
+    const uint32_t sid = find_surface_warp(surfs, nviews, blockIdx.x);
+    if (threadIdx.x == 0) s_id = sid;
+  }
   __syncthreads();
   const Surface& S = surfs[s_id];
   for (uint32_t i = threadIdx.x; i < sc.nlights; i += blockDim.x) {
@@ -1204,11 +1240,20 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
     l.cr = c.x; l.cg = c.y; l.cb = c.z;
     slights[i] = l;
   }
-  __syncthreads();
   const uint32_t lt = blockIdx.x - S.tile_base;
-  const int x = (lt % S.tiles_x) * kTile + (threadIdx.x & (kTile - 1));
-  const int y = (lt / S.tiles_x) * kTile + (threadIdx.x / kTile);
-  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, slights, x, y);
+  const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
+  if (threadIdx.x < 2 * (kTile + 1)) {
+    const int i = threadIdx.x % (kTile + 1);
+    const float fov = views[s_id].fov;
+    if (threadIdx.x <= kTile)
+      colx[i] = fdiv((float)(x0 + i) - (float)S.width / 2.0f, fov);
+    else
+      rowy[i] = fdiv((float)(y0 + i) - (float)S.height / 2.0f, fov);
+  }
+  __syncthreads();
+  const int x = x0 + (threadIdx.x & (kTile - 1));
+  const int y = y0 + (threadIdx.x / kTile);
+  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, slights, x, y, colx, rowy);
 }
 
 // ---- texture atlas ----------------------------------------------------------------
@@ -1349,16 +1394,19 @@ cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t
 }
 
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, uint32_t ntiles,
-                          bool with_id, int threads, cudaStream_t st) {
+                          bool with_id, int threads, cudaStream_t st, uint32_t tiles_per_surface) {
   if (!ntiles) return cudaSuccess;
   const int wid = with_id ? 1 : 0;
+  // surfaces of equal size: one grid row per surface, no search for the owner
+  const dim3 grid = (tiles_per_surface && nsurf > 1 && nsurf <= 65535 && tiles_per_surface * nsurf == ntiles)
+                        ? dim3(tiles_per_surface, nsurf) : dim3(ntiles);
   switch (threads * 2 + wid) {
-    case 256: k_raster<128, false><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf); break;
-    case 257: k_raster<128, true><<<ntiles, 128, 0, st>>>(ws, d_surf, nsurf); break;
-    case 1024: k_raster<512, false><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf); break;
-    case 1025: k_raster<512, true><<<ntiles, 512, 0, st>>>(ws, d_surf, nsurf); break;
-    case 513: k_raster<256, true><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf); break;
-    default: k_raster<256, false><<<ntiles, 256, 0, st>>>(ws, d_surf, nsurf); break;
+    case 256: k_raster<128, false><<<grid, 128, 0, st>>>(ws, d_surf, nsurf); break;
+    case 257: k_raster<128, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf); break;
+    case 1024: k_raster<512, false><<<grid, 512, 0, st>>>(ws, d_surf, nsurf); break;
+    case 1025: k_raster<512, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf); break;
+    case 513: k_raster<256, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf); break;
+    default: k_raster<256, false><<<grid, 256, 0, st>>>(ws, d_surf, nsurf); break;
   }
   return cudaGetLastError();
 }

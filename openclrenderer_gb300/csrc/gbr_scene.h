@@ -108,6 +108,7 @@ struct PassShape {
   uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
   size_t npix = 0;
   bool shade = true;  // views: some view wants RGBA or normals (else depth / id only)
+  uint32_t tiles_per_surface = 0;  // every surface has this many fine tiles (cube faces), else 0
 };
 
 void euler_cs(const float ang[3], float c[3], float s[3]);
