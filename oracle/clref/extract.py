@@ -1,6 +1,6 @@
 """Extract the triangle-pipeline kernels of the reference's cl2.cl as C++.
 
-TEST INFRASTRUCTURE ONLY (the checker's checker).  Reads cl2.cl where it lies
+TEST INFRASTRUCTURE ONLY (it pins the oracle).  Reads cl2.cl where it lies
 in the reference checkout, runs the C preprocessor with the reference's own
 build defines (ocl.h:227-240, main.cpp:79-85, engine.cpp:474-477), keeps the
 dependency closure of the hot kernels, and rewrites the OpenCL C forms that C++
