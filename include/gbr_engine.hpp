@@ -17,17 +17,18 @@
 //   w.generate_realtime_shadowing(*ctx.fetch());   engine.cpp:1601
 //   w.draw_bulk_objs_n(*ctx.fetch());              engine.cpp:1794 (render_tris)
 //
-// Differences, all on the host side: geometry comes as triangle arrays
-// (OBJ loading is not part of this path), textures as RGBA8 pixel arrays,
-// object rotation as a quaternion, errors as gbr_status (never exit), and the
-// screen is a device framebuffer (gbr_framebuffer) instead of a GL surface.
-// Header-only; link with libgbr.so.
+// Differences, all on the host side: geometry comes as triangle arrays or, with
+// gbr_obj.hpp, as OBJ files through set_file + load_active; textures as RGBA8
+// pixel arrays or image files; object rotation as a quaternion; errors as
+// gbr_status (never exit); and the screen is a device framebuffer
+// (gbr_framebuffer) instead of a GL surface.  Header-only; link with libgbr.so.
 #ifndef GBR_ENGINE_HPP
 #define GBR_ENGINE_HPP
 
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -94,6 +95,9 @@ struct object {
 struct objects_container {
   std::vector<object> objs;
   bool isactive = false;
+  bool isloaded = false;
+  std::string file;             // set_file: loaded by object_context::load_active
+  float requested_scale = 1.f;  // applied to positions at load (obj_load.cpp:437)
   float4 pos;
   float4 rot_quat{0, 0, 0, 1};
   float dynamic_scale = 1.f;
@@ -128,6 +132,8 @@ struct objects_container {
     add_object(tris, tex);
     set_two_sided(true);
   }
+  void set_file(const std::string& f) { file = f; isloaded = false; }
+  void request_scale(float s) { requested_scale = s; }
   void set_pos(float4 p) { pos = p; for (auto& o : objs) o.pos = p; }
   void offset_pos(float4 d) { set_pos(float4{pos.x + d.x, pos.y + d.y, pos.z + d.z, pos.w}); }
   void set_rot_quat(float4 q) { rot_quat = q; for (auto& o : objs) o.rot_quat = q; }
@@ -194,7 +200,25 @@ struct object_context {
                                      [&](const std::unique_ptr<objects_container>& u) { return u.get() == c; }),
                      containers.end());
   }
-  void load_active() {}  // geometry is already in memory
+  // Loader of objects_container::set_file (gbr_obj.hpp installs obj_load):
+  // (container, textures, file, scale, error) -> ok
+  std::function<bool(objects_container*, texture_context&, const std::string&, float, std::string*)> file_loader;
+  std::string load_error;
+
+  // object_context::load_active: load the files of active containers that
+  // have not been loaded (the reference's obj_load / load funcs)
+  gbr_status load_active() {
+    for (auto& c : containers) {
+      if (!c->isactive || c->isloaded || c->file.empty()) continue;
+      if (!file_loader || !file_loader(c.get(), tex_ctx, c->file, c->requested_scale, &load_error))
+        return gpu_dat.status = GBR_INVALID_ARG;
+      c->isloaded = true;
+      c->set_pos(c->pos);
+      c->set_rot_quat(c->rot_quat);
+      c->set_dynamic_scale(c->dynamic_scale);
+    }
+    return GBR_OK;
+  }
   void set_clear_colour(float4 c) {
     gpu_dat.clear_col[0] = c.x; gpu_dat.clear_col[1] = c.y; gpu_dat.clear_col[2] = c.z; gpu_dat.clear_col[3] = c.w;
   }
