@@ -100,8 +100,15 @@ typedef struct gbr_view {
   float hfov_deg;      /* horizontal FOV in degrees, used when fov_const <= 0 */
   float clear_col[4];  /* RGBA written where nothing is drawn */
   uint32_t use_linear; /* TEST_LINEAR sRGB approximations on (reference default 1) */
-  uint32_t reserved;
+  uint32_t flags;      /* kernel3's optional switches, GBR_VIEW_* below (reference: -D defines) */
 } gbr_view;
+
+/* ENABLE_NORMAL_MAPPING (cl2.cl:5987-6027): objects whose descriptor rid is a
+ * texture id (not 0xFFFFFFFF) take their normal from that tangent-space map. */
+#define GBR_VIEW_NORMAL_MAPPING 1u
+/* CAN_OUTLINE (cl2.cl:6368-6373): objects with feature flag 4 get the depth
+ * outline of generate_outline (cl2.cl:2315-2362) added to their colour. */
+#define GBR_VIEW_OUTLINE 2u
 
 /* Device output buffers of one view, row-major W*H.  Any may be NULL. */
 typedef struct gbr_outputs {

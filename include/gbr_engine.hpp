@@ -90,6 +90,7 @@ struct object {
   float dynamic_scale = 1.f;
   float specular = 0.9f, spec_mult = 1.f, diffuse = 1.f;  // object.cpp:72-74
   int32_t feature_flag = 0;
+  texture* normal_map = nullptr;  // descriptor rid (obj.rid / normal_map, obj_load.cpp:544-556)
 };
 
 struct objects_container {
@@ -143,6 +144,8 @@ struct objects_container {
   void set_spec_mult(float s) { for (auto& o : objs) o.spec_mult = s; }
   void set_diffuse(float d) { for (auto& o : objs) o.diffuse = d; }
   void set_children_texture_id(texture* t) { for (auto& o : objs) o.tex = t; }
+  void set_normal_map(texture* t) { for (auto& o : objs) o.normal_map = t; }
+  void set_outline(bool on) { set_flag(FLAG_OUTLINE, on); }
   void set_flag(int32_t bit, bool on) {
     for (auto& o : objs) o.feature_flag = on ? (o.feature_flag | bit) : (o.feature_flag & ~bit);
   }
@@ -243,7 +246,7 @@ struct object_context {
         std::memcpy(g.old_world_rot_quat_2, q, 16);
         g.scale = o.dynamic_scale;
         g.tid = (uint32_t)tex_ctx.get_gpu_position_id(o.tex);
-        g.rid = 0xFFFFFFFFu;
+        g.rid = o.normal_map ? (uint32_t)tex_ctx.get_gpu_position_id(o.normal_map) : 0xFFFFFFFFu;
         g.ssid = 0xFFFFFFFFu;
         g.specular = o.specular;
         g.spec_mult = o.spec_mult;
@@ -360,6 +363,7 @@ struct engine {
   int width = 0, height = 0;
   float4 c_pos, c_rot;                  // camera position, extrinsic XYZ Euler angles
   float horizontal_fov_degrees = 120.f;  // engine.hpp:115
+  uint32_t view_flags = 0;              // GBR_VIEW_*: kernel3's optional -D switches
   void* stream = nullptr;               // cudaStream_t; null = the default stream
   const light_gpu* lights = nullptr;
   gbr_scene* lights_uploaded_to = nullptr;
@@ -372,6 +376,7 @@ struct engine {
   void set_camera_pos(float4 p) { c_pos = p; }
   void set_camera_rot(float4 r) { c_rot = r; }
   void set_fov(float hfov_deg) { horizontal_fov_degrees = hfov_deg; }
+  void set_view_flags(uint32_t flags) { view_flags = flags; }
   void set_light_data(const light_gpu& l) { lights = &l; lights_uploaded_to = nullptr; }
   gbr_status set_object_data(object_context_data& dat) { return dat.ensure_screen_buffers(width, height); }
 
@@ -391,6 +396,7 @@ struct engine {
     v.hfov_deg = horizontal_fov_degrees;
     std::memcpy(v.clear_col, dat.clear_col, 16);
     v.use_linear = dat.use_linear_rendering;
+    v.flags = view_flags;
     return v;
   }
   gbr_status sync_lights(object_context_data& dat) {

@@ -64,6 +64,8 @@ gbr_status check_indices(gbr_scene* s, bool shading) {
     return fail(GBR_INVALID_ARG, "triangle object_id %u but only %u descriptors", s->max_object_id, s->ndescs);
   if (shading && s->ntris && s->max_tid >= s->mipmap_start)
     return fail(GBR_INVALID_ARG, "descriptor tid %u but only %u textures", s->max_tid, s->mipmap_start);
+  if (shading && s->ntris && s->has_rid && s->max_rid >= s->mipmap_start)
+    return fail(GBR_INVALID_ARG, "descriptor rid %u but only %u textures", s->max_rid, s->mipmap_start);
   return GBR_OK;
 }
 
@@ -109,6 +111,7 @@ void fill_view_params(const gbr_camera& cam, const gbr_view& v, const gbr_output
   V.fov = v.fov_const > 0 ? v.fov_const : gbr_fov_const_from_hfov(v.hfov_deg, v.width);
   V.surface = surface;
   V.use_linear = v.use_linear;
+  V.flags = v.flags;
   memcpy(V.clear, v.clear_col, 16);
   V.rgba = o.rgba;
   V.normals = o.normals;
@@ -201,7 +204,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   }
   if (view && sh.shade) {
     CU(mark(6, st));
-    CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st));
+    CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st, sh.features));
     CU(mark(5, st));
   }
   CU(cudaMemcpyAsync(host_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -487,9 +490,18 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
   if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
   TRY(s->descs.reserve(n));
   if (n) CU(cudaMemcpy(s->descs.p, d, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyHostToDevice));
-  uint32_t mt = 0;
-  for (uint32_t i = 0; i < n; i++) mt = std::max(mt, d[i].tid);
+  uint32_t mt = 0, mr = 0;
+  bool has_rid = false;
+  for (uint32_t i = 0; i < n; i++) {
+    mt = std::max(mt, d[i].tid);
+    if (d[i].rid != 0xFFFFFFFFu) {
+      mr = std::max(mr, d[i].rid);
+      has_rid = true;
+    }
+  }
   s->max_tid = mt;
+  s->max_rid = mr;
+  s->has_rid = has_rid;
   s->ndescs = n;
   s->static_dirty = true;
   s->world_dirty = true;
@@ -712,8 +724,10 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   sh.ncoarse = cb;
   sh.npix = npix;
   sh.shade = false;
-  for (uint32_t i = 0; i < n; i++)
+  for (uint32_t i = 0; i < n; i++) {
     if (outs[i].rgba || outs[i].normals) sh.shade = true;
+    if (views[i].flags) sh.features = true;
+  }
   for (int attempt = 0; attempt < 8; attempt++) {
     TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
     CU(cudaStreamSynchronize(st));

@@ -93,8 +93,10 @@ gbr_status capture(gbr_batch* b) {
   b->vshape.ncoarse = cb;
   b->vshape.npix = npix;
   b->vshape.shade = false;
-  for (uint32_t i = 0; i < b->n; i++)
+  for (uint32_t i = 0; i < b->n; i++) {
     if (b->outs[i].rgba || b->outs[i].normals) b->vshape.shade = true;
+    if (b->views[i].flags) b->vshape.features = true;
+  }
   if (b->wv.rec_target == 0) {
     b->wv.rec_target = std::max(s->ws_view.rec_target, s->ntris + 1024u);
     b->wv.bin_target = std::max(s->ws_view.bin_target, 4u * b->wv.rec_target);

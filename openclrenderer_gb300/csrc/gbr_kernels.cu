@@ -1016,8 +1016,57 @@ struct SLight {
 };
 
 // kernel3 (cl2.cl:5792-6408) for one pixel of a view.
+// ENABLE_NORMAL_MAPPING (cl2.cl:5987-6027): the tangent-space normal from the
+// object's normal map, in object space through the triangle's tangent frame,
+// then rotated into world space.  It feeds the shadow bias, so it keeps the
+// IEEE contract (normalize as fast_normalize).
+__device__ __forceinline__ f3 normal_map(const SceneDev& sc, f2 vt, f2 vtdiff, uint32_t rid, f3 p1, f3 p2, f3 p3,
+                                      f2 vt1, f2 vt2, f2 vt3, f3 model_normal, f4 qn) {
+  const f4 t4 = texture_filter_diff(sc, vt, vtdiff, (int)rid);
+  f3 tn = mk3(2.0f * t4.x - 1.0f, 2.0f * t4.y - 1.0f, 2.0f * t4.z - 1.0f);
+  tn = fast_normalize3(tn);
+  const f3 dp1 = sub3(p2, p1), dp2 = sub3(p3, p1);
+  const f2 duv1 = mk2(vt2.x - vt1.x, vt2.y - vt1.y), duv2 = mk2(vt3.x - vt1.x, vt3.y - vt1.y);
+  const float r = fdiv(1.0f, duv1.x * duv2.y - duv1.y * duv2.x);
+  f3 tangent = mk3((dp1.x * duv2.y - dp2.x * duv1.y) * r, (dp1.y * duv2.y - dp2.y * duv1.y) * r,
+                   (dp1.z * duv2.y - dp2.z * duv1.y) * r);
+  f3 bitangent = mk3((dp2.x * duv1.x - dp1.x * duv2.x) * r, (dp2.y * duv1.x - dp1.y * duv2.x) * r,
+                     (dp2.z * duv1.x - dp1.z * duv2.x) * r);
+  tangent = fast_normalize3(tangent);
+  bitangent = fast_normalize3(bitangent);
+  tangent = fast_normalize3(sub3(tangent, mul3s(model_normal, dot3(model_normal, tangent))));
+  if (dot3(cross3(model_normal, tangent), bitangent) < 0.0f) tangent = mul3s(tangent, -1.0f);
+  const f3 ms = mk3((tangent.x * tn.x + bitangent.x * tn.y) + model_normal.x * tn.z,
+                    (tangent.y * tn.x + bitangent.y * tn.y) + model_normal.y * tn.z,
+                    (tangent.z * tn.x + bitangent.z * tn.y) + model_normal.z * tn.z);
+  return rot_quat_n(ms, qn);
+}
+
+// generate_outline (cl2.cl:2315-2362): the largest depth step to the four
+// neighbours, over 100, at most 1.
+__device__ __forceinline__ float generate_outline(int x, int y, const uint32_t* __restrict__ depth, int W, int H) {
+  const float d0 = depth_to_dist(__ldg(depth + (size_t)y * W + x));
+  float furthest = d0;
+  for (int xx = -1; xx <= 1; xx++) {
+    const int px = x + xx;
+    if (px < 0 || px >= W) continue;
+    const float nd = depth_to_dist(__ldg(depth + (size_t)y * W + px));
+    if (nd > furthest) furthest = nd;
+  }
+  for (int yy = -1; yy <= 1; yy++) {
+    const int py = y + yy;
+    if (py < 0 || py >= H) continue;
+    const uint32_t d = __ldg(depth + (size_t)py * W + x);
+    const float nd = depth_to_dist(d);
+    if (fabsf(nd - d0) > fabsf(furthest - d0) && nd > kDepthCutoff && d != 0) furthest = nd;
+  }
+  return fmin_(fdiv(fabsf(furthest - d0), 100.0f), 1.0f);
+}
+
 // colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
 // 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
+// FEAT: kernel3's optional switches (view flags) compiled in.
+template <bool FEAT>
 __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
                             const ShadeRec* __restrict__ srec, const SLight* __restrict__ lights, int x, int y,
                             const float* __restrict__ colx, const float* __restrict__ rowy) {
@@ -1076,17 +1125,15 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f2 vt = mk2(fma_(vt1.x, l1, fma_(vt2.x, l2, vt3.x * l3)), fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
   f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
                   fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
+  const f3 model_normal = normal;
   normal = rot_quat_n(normal, qn);
 
   f4 col;
   const uint32_t vc0 = __float_as_uint(vc0v.w);
-  if (vc0 != 0) {
-    f4 c0 = vertex_col(vc0), c1 = vertex_col(__float_as_uint(vc1v.w)), c2 = vertex_col(__float_as_uint(vc2v.w));
-    col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
-    col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
-    col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
-    col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
-  } else {
+  // normal map of the object (ENABLE_NORMAL_MAPPING), 0xFFFFFFFF if none
+  const uint32_t rid = (FEAT && (V.flags & GBR_VIEW_NORMAL_MAPPING)) ? __ldg(&G->rid) : 0xFFFFFFFFu;
+  f2 vtdiff = mk2(0.0f, 0.0f);
+  if (vc0 == 0 || rid != 0xFFFFFFFFu) {
     // get_vtdiff (cl2.cl:5691-5760).  The 1/z plane extrapolated to the
     // neighbouring pixels is ill-conditioned for triangles seen edge-on (it
     // can cross zero), so this stays in IEEE arithmetic: rounding differences
@@ -1111,8 +1158,20 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     f2 vtx = mk2(fma_(vt1.x, lx1, fma_(vt2.x, lx2, vt3.x * lx3)), fma_(vt1.y, lx1, fma_(vt2.y, lx2, vt3.y * lx3)));
     f2 vty = mk2(fma_(vt1.x, ly1, fma_(vt2.x, ly2, vt3.x * ly3)), fma_(vt1.y, ly1, fma_(vt2.y, ly2, vt3.y * ly3)));
     const float mip_bias = 1.0f / kMipBias;
-    f2 vtdiff = mk2((fabsf(vtx.x - vt.x) + fabsf(vty.x - vt.x)) * mip_bias,
-                    (fabsf(vtx.y - vt.y) + fabsf(vty.y - vt.y)) * mip_bias);
+    vtdiff = mk2((fabsf(vtx.x - vt.x) + fabsf(vty.x - vt.x)) * mip_bias,
+                 (fabsf(vtx.y - vt.y) + fabsf(vty.y - vt.y)) * mip_bias);
+  }
+  // (the reference replaces the normal after its colour and jitter seeds,
+  // neither of which reads it)
+  if (FEAT && rid != 0xFFFFFFFFu)
+    normal = normal_map(sc, vt, vtdiff, rid, p1, p2, p3, vt1, vt2, vt3, model_normal, qn);
+  if (vc0 != 0) {
+    f4 c0 = vertex_col(vc0), c1 = vertex_col(__float_as_uint(vc1v.w)), c2 = vertex_col(__float_as_uint(vc2v.w));
+    col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
+    col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
+    col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
+    col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
+  } else {
     col = texture_filter_diff(sc, vt, vtdiff, (int)__ldg(&G->tid));
   }
   if (V.use_linear) {
@@ -1199,6 +1258,10 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 sp2 = mul3s(ssum, 1.0f - rsc);
   f3 fin = mk3(fma_(colclamp.x, dsum.x, sp2.x), fma_(colclamp.y, dsum.y, sp2.y), fma_(colclamp.z, dsum.z, sp2.z));
   if (V.use_linear) fin = mk3(c_gamma_inv(fin.x), c_gamma_inv(fin.y), c_gamma_inv(fin.z));
+  if (FEAT && (V.flags & GBR_VIEW_OUTLINE) && (ff & kFlagOutline) > 0) {
+    const float o = generate_outline(x, y, S.depth, W, H);
+    fin = mk3(fin.x + o, fin.y + o, fin.z + o);
+  }
   if (out) out[p] = pack_rgba(fin.x, fin.y, fin.z, col.w);
   if (V.normals) {
     // encode_normal (cl2.cl:5618-5628)
@@ -1213,6 +1276,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
+template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec) {
@@ -1253,7 +1317,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   __syncthreads();
   const int x = x0 + (threadIdx.x & (kTile - 1));
   const int y = y0 + (threadIdx.x / kTile);
-  if (x < S.width && y < S.height) shade_pixel(sc, views[s_id], S, srec, slights, x, y, colx, rowy);
+  if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, views[s_id], S, srec, slights, x, y, colx, rowy);
 }
 
 // ---- texture atlas ----------------------------------------------------------------
@@ -1412,9 +1476,12 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
 }
 
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
-                         uint32_t ntiles, const ShadeRec* srec, cudaStream_t st) {
+                         uint32_t ntiles, const ShadeRec* srec, cudaStream_t st, bool features) {
   if (!ntiles) return cudaSuccess;
-  k_shade<<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
+  if (features)
+    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
+  else
+    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
   return cudaGetLastError();
 }
 

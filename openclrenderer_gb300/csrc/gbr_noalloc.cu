@@ -153,6 +153,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   V.fov = fov;
   V.surface = 0;
   V.use_linear = view->use_linear;
+  V.flags = view->flags;
   memcpy(V.clear, view->clear_col, 16);
   V.rgba = out->rgba;
   V.normals = out->normals;
@@ -210,7 +211,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   NA_CU(launch_scan(ws, s), "scan launch failed");
   NA_CU(launch_fill(ws, d_surf, s), "fill launch failed");
   NA_CU(launch_raster(ws, d_surf, 1, nfine, true, kRasterThreads, s), "raster launch failed");
-  NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws.srec, s), "shade launch failed");
+  NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws.srec, s, view->flags != 0), "shade launch failed");
   Counters c{};
   NA_CU(cudaMemcpyAsync(&c, ws.ctr, sizeof c, cudaMemcpyDeviceToHost, s), "counter read-back failed");
   NA_CU(cudaStreamSynchronize(s), "stream synchronisation failed");

@@ -109,6 +109,7 @@ struct PassShape {
   size_t npix = 0;
   bool shade = true;  // views: some view wants RGBA or normals (else depth / id only)
   uint32_t tiles_per_surface = 0;  // every surface has this many fine tiles (cube faces), else 0
+  bool features = false;            // views: some view has gbr_view.flags set
 };
 
 void euler_cs(const float ang[3], float c[3], float s[3]);
@@ -133,7 +134,8 @@ struct gbr_scene {
   uint32_t npages = 0;
   gbr::DevBuf<uint32_t> shadow_dyn, shadow_static;
   uint32_t n_dyn = 0, n_static = 0;
-  uint32_t max_object_id = 0, max_tid = 0;
+  uint32_t max_object_id = 0, max_tid = 0, max_rid = 0;
+  bool has_rid = false;  // some descriptor names a normal map (rid != 0xFFFFFFFF)
   bool static_dirty = true;
   gbr::WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
   gbr::HostBuf staging;         // counters read back: view at 0, shadow at 256

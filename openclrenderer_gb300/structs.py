@@ -28,7 +28,7 @@ LIGHT = np.dtype([
 CAMERA = np.dtype([("pos", "<f4", 4), ("rot", "<f4", 4)])
 VIEW = np.dtype([
     ("width", "<i4"), ("height", "<i4"), ("fov_const", "<f4"), ("hfov_deg", "<f4"),
-    ("clear_col", "<f4", 4), ("use_linear", "<u4"), ("reserved", "<u4"),
+    ("clear_col", "<f4", 4), ("use_linear", "<u4"), ("flags", "<u4"),
 ])
 STATS = np.dtype([
     ("view_records", "<u8"), ("view_bin_entries", "<u8"), ("shadow_records", "<u8"),
@@ -129,8 +129,13 @@ def make_camera(pos=(0, 0, 0), rot=(0, 0, 0)):
     return c
 
 
-def make_view(width, height, hfov_deg=90.0, fov_const=0.0, clear=(0, 0, 0, 1), use_linear=1):
+VIEW_NORMAL_MAPPING = 1
+VIEW_OUTLINE = 2
+
+
+def make_view(width, height, hfov_deg=90.0, fov_const=0.0, clear=(0, 0, 0, 1), use_linear=1, flags=0):
     v = np.zeros((), VIEW)
+    v["flags"] = flags
     v["width"] = width
     v["height"] = height
     v["hfov_deg"] = hfov_deg

@@ -16,36 +16,51 @@ ORACLE = os.path.dirname(HERE)
 REF_DIR = os.path.join(ORACLE, "_ref")
 KERNELS = os.path.join(REF_DIR, "cl2_hot.cpp")
 LIB = os.path.join(REF_DIR, "libclref.so")
+# the same kernels with kernel3's optional switches on (normal mapping, outline)
+KERNELS_F3 = os.path.join(REF_DIR, "cl2_hot_f3.cpp")
+LIB_F3 = os.path.join(REF_DIR, "libclref_f3.so")
 REFERENCE_CL = os.environ.get("GBR_REFERENCE_CL", "/root/reference/cl2.cl")
 
 
-def build(force=False):
-    os.makedirs(REF_DIR, exist_ok=True)
+def _build_one(kernels, lib, extra, force):
     if os.path.exists(REFERENCE_CL):
         sys.path.insert(0, HERE)
         import extract
-        extract.extract(REFERENCE_CL, KERNELS + ".tmp")
-        if not os.path.exists(KERNELS) or open(KERNELS).read() != open(KERNELS + ".tmp").read():
-            os.replace(KERNELS + ".tmp", KERNELS)
+        extract.extract(REFERENCE_CL, kernels + ".tmp", extra)
+        if not os.path.exists(kernels) or open(kernels).read() != open(kernels + ".tmp").read():
+            os.replace(kernels + ".tmp", kernels)
         else:
-            os.remove(KERNELS + ".tmp")
-    if not os.path.exists(KERNELS):
+            os.remove(kernels + ".tmp")
+    if not os.path.exists(kernels):
         raise FileNotFoundError("reference kernels not extracted (cl2.cl not found)")
-    deps = [KERNELS, os.path.join(HERE, "harness.cpp"), os.path.join(HERE, "shim.hpp"),
+    deps = [kernels, os.path.join(HERE, "harness.cpp"), os.path.join(HERE, "shim.hpp"),
             os.path.join(ORACLE, "..", "openclrenderer_gb300", "csrc", "gbr_math.h")]
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
-        return LIB
+    if not force and os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(d) for d in deps):
+        return lib
     cmd = ["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fno-strict-aliasing", "-fwrapv", "-Wno-narrowing",
-           "-w", "-fPIC", "-shared", "-pthread", f'-DCLREF_KERNELS="{KERNELS}"', "-o", LIB + ".tmp",
+           "-w", "-fPIC", "-shared", "-pthread", f'-DCLREF_KERNELS="{kernels}"', "-o", lib + ".tmp",
            os.path.join(HERE, "harness.cpp")]
     subprocess.run(cmd, check=True)
-    os.replace(LIB + ".tmp", LIB)
-    return LIB
+    os.replace(lib + ".tmp", lib)
+    return lib
+
+
+def build(force=False, features=False):
+    """Build the reference kernels library (features: with kernel3's optional
+    normal-mapping and outline switches); returns its path."""
+    os.makedirs(REF_DIR, exist_ok=True)
+    if features:
+        sys.path.insert(0, HERE)
+        import extract
+        return _build_one(KERNELS_F3, LIB_F3, extract.FEATURE_DEFINES, force)
+    return _build_one(KERNELS, LIB, (), force)
 
 
 def build_if_available():
     try:
-        return build()
+        lib = build()
+        build(features=True)
+        return lib
     except FileNotFoundError:
         return None
 

@@ -28,8 +28,13 @@ DEFINES = ["SCREENWIDTH=gbr_ref_W", "SCREENHEIGHT=gbr_ref_H", "FOV_CONST=gbr_ref
 IDENT = re.compile(r"[A-Za-z_][A-Za-z0-9_]*")
 
 
-def preprocess(src):
-    cmd = ["cpp", "-P", "-x", "c", "-undef", "-nostdinc"] + ["-D" + d for d in DEFINES] + [src]
+# kernel3's optional switches (cl2.cl:5987, 6368): normal mapping and the
+# per-object outline; the second build of the kernels has them on
+FEATURE_DEFINES = ["ENABLE_NORMAL_MAPPING", "CAN_OUTLINE"]
+
+
+def preprocess(src, extra=()):
+    cmd = ["cpp", "-P", "-x", "c", "-undef", "-nostdinc"] + ["-D" + d for d in DEFINES + list(extra)] + [src]
     return subprocess.run(cmd, check=True, capture_output=True, text=True).stdout
 
 
@@ -123,8 +128,8 @@ def rewrite(code):
     return "".join(out)
 
 
-def extract(cl_path, out_path):
-    items = top_level_items(preprocess(cl_path))
+def extract(cl_path, out_path, extra_defines=()):
+    items = top_level_items(preprocess(cl_path, extra_defines))
     need = closure(items, ROOTS)
     missing = [r for r in ROOTS if r not in need]
     if missing:

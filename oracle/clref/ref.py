@@ -8,7 +8,7 @@ import numpy as np
 
 from . import build_ref
 
-_lib = None
+_libs = {}
 P = ctypes.c_void_p
 
 
@@ -16,11 +16,12 @@ def available():
     return os.path.exists(build_ref.LIB) or os.path.exists(build_ref.REFERENCE_CL)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        build_ref.build()
-        L = ctypes.CDLL(build_ref.LIB)
+def lib(features=False):
+    """The reference kernels; features: the build with kernel3's optional
+    normal-mapping and outline switches on."""
+    if features not in _libs:
+        path = build_ref.build(features=features)
+        L = ctypes.CDLL(path)
         L.ref_render.restype = ctypes.c_int64
         L.ref_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32, P, P, P,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P, P, P, P, P,
@@ -29,8 +30,8 @@ def lib():
         L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int, ctypes.c_int]
         L.ref_textures.restype = None
         L.ref_textures.argtypes = [ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32]
-        _lib = L
-    return _lib
+        _libs[features] = L
+    return _libs[features]
 
 
 def _p(a):
@@ -65,7 +66,7 @@ def shadow(scene, nthreads=None, ordered=True):
 
 
 def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_dyn=None, shadow_static=None,
-           nthreads=None, ordered=True):
+           nthreads=None, ordered=True, features=False):
     nthreads = nthreads or (os.cpu_count() or 1)
     W, H = int(view["width"]), int(view["height"])
     if shadow_dyn is None:
@@ -80,7 +81,7 @@ def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_
     normals = np.empty((H, W, 2), np.uint16)
     nums = np.ascontiguousarray(nums, np.uint32)
     page_sizes = np.ascontiguousarray(page_sizes, np.uint32)
-    nf = lib().ref_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
+    nf = lib(features).ref_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
                           _p(atlas), _p(nums), _p(page_sizes), mipmap_start, _p(shadow_dyn), _p(shadow_static),
                           _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
                           _p(rgba), _p(normals), nthreads, 1 if ordered else 0)

@@ -131,6 +131,7 @@ struct alignas(8) int2 {
   int2(const int2& o) { memcpy(s, o.s, sizeof s); }
   int2& operator=(const int2& o) { memcpy(s, o.s, sizeof s); return *this; }
 };
+inline int2 operator+(int2 a, int2 b) { return int2(a.x + b.x, a.y + b.y); }
 
 struct alignas(16) int4 {
   union {
@@ -204,7 +205,8 @@ struct alignas(4) ushort2 {
   inline V native_cos(V a) { V r; for (int i = 0; i < N; i++) r.s[i] = (float)std::cos((double)a.s[i]); return r; } \
   inline V native_sin(V a) { V r; for (int i = 0; i < N; i++) r.s[i] = (float)std::sin((double)a.s[i]); return r; } \
   inline float fast_length(V a) { return sqrtf(dot(a, a)); }                                          \
-  inline V fast_normalize(V a) { float l = sqrtf(dot(a, a)); V r; for (int i = 0; i < N; i++) r.s[i] = a.s[i] / l; return r; }
+  inline V fast_normalize(V a) { float l = sqrtf(dot(a, a)); V r; for (int i = 0; i < N; i++) r.s[i] = a.s[i] / l; return r; } \
+  inline V normalize(V a) { float l = sqrtf(dot(a, a)); V r; for (int i = 0; i < N; i++) r.s[i] = a.s[i] / l; return r; }
 
 GBR_VEC_OPS(float2, 2)
 GBR_VEC_OPS(float3, 3)

@@ -358,6 +358,7 @@ struct ShadeView {
   float fov;
   f3 cpos, crot_c, crot_s;
   f3 crot;  // the Euler angles themselves (the FP64 shading takes exact cos / sin)
+  uint32_t flags = 0;  // gbr_view.flags: kernel3's optional switches
   f3 face_c[6], face_s[6];
   uint32_t use_linear;
   f4 clear;
@@ -421,6 +422,28 @@ float generate_ssao(int x, int y, const uint32_t* depth, const ShadeView& v) {
   }
   acc = fdiv(acc, 125.0f);
   return 1.0f - fdiv(1.0f - acc, kSsaoDiv);
+}
+
+// generate_outline (cl2.cl:2315-2362)
+float generate_outline(int x, int y, const uint32_t* depth_buffer, const ShadeView& v) {
+  float depth = depth_to_dist(depth_buffer[(size_t)y * v.W + x]);
+  float furthest = depth;
+  const int rad = 1;
+  for (int xx = -rad; xx <= rad; xx++) {
+    int px = x + xx, py = y;
+    if (px < 0 || px >= v.W || py < 0 || py >= v.H) continue;
+    float new_depth = depth_to_dist(depth_buffer[(size_t)py * v.W + px]);
+    if (new_depth > furthest) furthest = new_depth;
+  }
+  for (int yy = -rad; yy <= rad; yy++) {
+    int px = x, py = y + yy;
+    if (px < 0 || px >= v.W || py < 0 || py >= v.H) continue;
+    uint32_t d = depth_buffer[(size_t)py * v.W + px];
+    float new_depth = depth_to_dist(d);
+    if (fabsf(new_depth - depth) > fabsf(furthest - depth) && new_depth > kDepthCutoff && d != 0) furthest = new_depth;
+  }
+  float diff = fabsf(furthest - depth);
+  return fmin_(fdiv(diff, 100.f), 1.f);
 }
 
 float bilinear_interpolate(float cx, float cy, const float val[4]) {
@@ -520,9 +543,15 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
               fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
   f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
                   fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
+  const f3 model_normal = normal;
   normal = rot_quat(normal, q);
   f4 col;
   bool has_col = T.vertices[0].vertex_col != 0;
+  // kernel3 computes vtdiff for every pixel; the texture and the normal map read it
+  const bool normal_mapped = (v.flags & GBR_VIEW_NORMAL_MAPPING) && G.rid != 0xFFFFFFFFu;
+  f2 vtdiff = mk2(0.0f, 0.0f);
+  if (!has_col || normal_mapped)
+    vtdiff = get_vtdiff(ct.p, (float)x, (float)y, v, G, vt, p1, p2, p3, vt1, vt2, vt3, rconst);
   if (has_col) {
     f4 c0 = vertex_col(T.vertices[0].vertex_col), c1 = vertex_col(T.vertices[1].vertex_col),
        c2 = vertex_col(T.vertices[2].vertex_col);
@@ -531,7 +560,6 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
     col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
     col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
   } else {
-    f2 vtdiff = get_vtdiff(ct.p, (float)x, (float)y, v, G, vt, p1, p2, p3, vt1, vt2, vt3, rconst);
     col = texture_filter_diff(vt, vtdiff, (int)G.tid, in.atlas);
   }
   if (v.use_linear) {
@@ -545,6 +573,25 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
   uint32_t seed4 = rand_xorshift(seed3);
   f3 rseed = mk3((fdiv((float)seed2, kMulInt) - 0.5f) * 2.0f, (fdiv((float)seed3, kMulInt) - 0.5f) * 2.0f,
                  (fdiv((float)seed4, kMulInt) - 0.5f) * 2.0f);
+  if (normal_mapped) {
+    // ENABLE_NORMAL_MAPPING (cl2.cl:5987-6027)
+    f4 t4 = texture_filter_diff(vt, vtdiff, (int)G.rid, in.atlas);
+    f3 t_normal = mk3(2.f * t4.x - 1.f, 2.f * t4.y - 1.f, 2.f * t4.z - 1.f);
+    t_normal = fast_normalize3(t_normal);  // normalize, pinned as fast_normalize
+    f3 deltaPos1 = sub3(p2, p1), deltaPos2 = sub3(p3, p1);
+    f2 deltaUV1 = mk2(vt2.x - vt1.x, vt2.y - vt1.y), deltaUV2 = mk2(vt3.x - vt1.x, vt3.y - vt1.y);
+    float r = fdiv(1.0f, deltaUV1.x * deltaUV2.y - deltaUV1.y * deltaUV2.x);
+    f3 tangent = mul3s(sub3(mul3s(deltaPos1, deltaUV2.y), mul3s(deltaPos2, deltaUV1.y)), r);
+    f3 bitangent = mul3s(sub3(mul3s(deltaPos2, deltaUV1.x), mul3s(deltaPos1, deltaUV2.x)), r);
+    tangent = fast_normalize3(tangent);
+    bitangent = fast_normalize3(bitangent);
+    tangent = fast_normalize3(sub3(tangent, mul3s(model_normal, dot3(model_normal, tangent))));
+    if (dot3(cross3(model_normal, tangent), bitangent) < 0.0f) tangent = mul3s(tangent, -1.0f);
+    f3 model_space = mk3(tangent.x * t_normal.x + bitangent.x * t_normal.y + model_normal.x * t_normal.z,
+                         tangent.y * t_normal.x + bitangent.y * t_normal.y + model_normal.y * t_normal.z,
+                         tangent.z * t_normal.x + bitangent.z * t_normal.y + model_normal.z * t_normal.z);
+    normal = rot_quat(model_space, q);
+  }
   f3 l2p = fast_normalize3(sub3(v.cpos, gpos));
   int ff = G.feature_flag;
   bool two = (ff & kFlagTwoSided) > 0;
@@ -619,6 +666,11 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
   f3 fin = mk3(fma_(colclamp.x, diffuse_sum.x, sp2.x), fma_(colclamp.y, diffuse_sum.y, sp2.y),
                fma_(colclamp.z, diffuse_sum.z, sp2.z));
   if (v.use_linear) fin = mk3(gamma_inv(fin.x), gamma_inv(fin.y), gamma_inv(fin.z));
+  if ((v.flags & GBR_VIEW_OUTLINE) && (ff & kFlagOutline) > 0) {
+    // CAN_OUTLINE (cl2.cl:6368-6373)
+    float outline = generate_outline(x, y, depth, v);
+    fin = mk3(fin.x + outline, fin.y + outline, fin.z + outline);
+  }
   put(fin.x, fin.y, fin.z, col.w);
   if (normals) {
     float nx = normal.x, ny = normal.y, nz = normal.z;
@@ -1192,7 +1244,7 @@ int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
   kernel2(S, (float)W, (float)H, depth, reinterpret_cast<std::atomic<uint32_t>*>(ids), W, nthreads);
   if (!rgba) return 0;
   ShadeView v;
-  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot;
+  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot; v.flags = view->flags;
   euler_cs(crot, &v.crot_c, &v.crot_s);
   for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &v.face_c[f], &v.face_s[f]);
   v.use_linear = view->use_linear;
@@ -1222,7 +1274,7 @@ int oracle_render_fp64(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_des
   kernel1(S, (float)W, (float)H, reinterpret_cast<std::atomic<uint32_t>*>(depth.data()), W, nthreads);
   kernel2(S, (float)W, (float)H, depth.data(), reinterpret_cast<std::atomic<uint32_t>*>(ids.data()), W, nthreads);
   ShadeView v;
-  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot;
+  v.W = W; v.H = H; v.fov = fov; v.cpos = cpos; v.crot = crot; v.flags = view->flags;
   euler_cs(crot, &v.crot_c, &v.crot_s);
   for (int f = 0; f < 6; f++) euler_cs(face_angles(f), &v.face_c[f], &v.face_s[f]);
   v.use_linear = view->use_linear;

@@ -30,8 +30,10 @@ def sha(a):
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def main():
+def main(only=None):
     for name, make in golden_cases.CASES.items():
+        if only and name not in only:
+            continue
         sc, opts = make()
         tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
         atlas = R.textures(sc.tex_sizes, sc.tex_pixels, tex.nums, tex.sizes, tex.mipmap_start)
@@ -45,7 +47,8 @@ def main():
         for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
             fov = float(view["fov_const"]) if view["fov_const"] > 0 else O.fov_const(float(view["hfov_deg"]),
                                                                                  int(view["width"]))
-            r = R.render(sc, atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov, dyn, sta)
+            r = R.render(sc, atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov, dyn, sta,
+                         features=bool(opts.get("features")))
             arrays[f"depth{k}"] = r["depth"]
             arrays[f"id{k}"] = r["id"]
             arrays[f"rgba{k}"] = r["rgba"]
@@ -59,4 +62,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -78,5 +78,28 @@ def wide_boxes():
     return sc, {}
 
 
+def features():
+    """kernel3's optional switches: normal maps (descriptor rid) and the
+    per-object outline, with a shadow light; views with both flags on."""
+    sc = scenes.plain_cubes()
+    rng = np.random.default_rng(41)
+    sc.tex_sizes = [128, 64]
+    sc.tex_pixels = [sc.tex_pixels[0], rng.integers(0, 256, (64, 64, 4), dtype=np.uint8)]
+    descs = sc.descs.copy()
+    for i in range(len(descs)):
+        if i % 3 == 0:
+            descs[i]["rid"] = 1
+        if i % 4 == 0:
+            descs[i]["feature_flag"] = S.FLAG_TWO_SIDED | S.FLAG_OUTLINE
+    sc.descs = descs
+    sc.lights = np.stack([S.make_light((-150, 120, 300), (1, 0.9, 0.8), radius=6000.0, shadow=1),
+                          S.make_light((200, -100, 50), (0.5, 0.6, 1.0), radius=8000.0)])
+    flags = S.VIEW_NORMAL_MAPPING | S.VIEW_OUTLINE
+    sc.views = [S.make_view(800, 600, 90.0, flags=flags)]
+    sc.cameras.append(S.make_camera((-60.0, 40.0, 150.0), (-0.1, 0.25, 0.0)))
+    sc.views.append(S.make_view(512, 384, hfov_deg=80.0, flags=flags))
+    return sc, {"shadows": True, "normals": True, "features": True}
+
+
 CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
-         "wide_boxes": wide_boxes}
+         "wide_boxes": wide_boxes, "features": features}

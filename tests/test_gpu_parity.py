@@ -117,6 +117,30 @@ def test_multiple_and_static_shadow_lights():
     assert_parity(got, ref, "multi_shadow")
 
 
+def test_optional_kernel3_features_parity():
+    """Normal maps and the per-object outline (ENABLE_NORMAL_MAPPING,
+    CAN_OUTLINE; gbr_view.flags) against the oracle, which the reference's
+    own kernels built with those switches pin (tests/golden/features.npz)."""
+    from tests import golden_cases
+    sc, _ = golden_cases.features()
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    dyn, sta = O.shadow(sc)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        got = gs.render(cam, view, normals=True).numpy()
+        ref = O.render(sc, tex, cam, view, dyn, sta, normals=True)
+        assert_parity(got, ref, f"features view {k}")
+        assert np.array_equal(got["normals"], ref["normals"]), f"features view {k}: normals"
+    # a normal-map id beyond the textures is rejected when the switch is on
+    bad = sc.descs.copy()
+    bad[0]["rid"] = 7
+    gs.set_descriptors(bad)
+    from openclrenderer_gb300._native import GbrError
+    with pytest.raises(GbrError):
+        gs.render(sc.cameras[0], sc.views[0])
+
+
 def test_random_soup_parity():
     for seed, (w, h) in zip((1, 2, 3), ((640, 480), (333, 197), (1024, 768))):
         sc = random_soup(400, w, h, seed)
