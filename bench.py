@@ -167,13 +167,35 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(stage):
-    """dram__bytes_read.sum + dram__bytes_write.sum per launch of `stage` from
-    the committed ncu summary, when one exists for this workload."""
+def load_profile():
+    """Per-launch figures of the committed ncu capture of this workload:
+    DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) and warp
+    instructions (smsp__inst_executed.sum) per stage."""
     p = os.path.join(ROOT, "profiles", "traffic_terrain_1080p.json")
-    if os.path.exists(p):
-        return json.load(open(p)).get(stage)
-    return None
+    return json.load(open(p)) if os.path.exists(p) else {}
+
+
+def load_traffic(stage):
+    return load_profile().get(stage)
+
+
+def issue_roofline(stage, launch_ms, sm_mhz):
+    """The issue-rate bound of an instruction-bound kernel: its warp
+    instructions per launch (ncu) over the live launch time, against one warp
+    instruction per clock on each of the 4 schedulers of every SM."""
+    inst = load_profile().get("warp_inst", {}).get(stage)
+    if not inst or not launch_ms or not sm_mhz:
+        return None
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    except Exception:
+        sms = 152
+    achieved = inst / (launch_ms * 1e-3)
+    peak = sms * 4 * sm_mhz * 1e6
+    return {"achieved_warp_inst_per_s": round(achieved, 0), "peak_warp_inst_per_s": round(peak, 0),
+            "frac": round(achieved / peak, 4), "warp_inst_per_launch": inst, "sms": sms, "sm_mhz": sm_mhz,
+            "source": "smsp__inst_executed.sum of the committed ncu capture / live launch time"}
 
 
 # ---- CPU baseline --------------------------------------------------------------
@@ -430,7 +452,8 @@ def main():
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / peak, 5) if achieved else None,
             "algorithmic_bytes_per_launch": alg, "launch_ms": round(per_call[dom], 4),
-            "traffic": load_traffic(dom)}
+            "traffic": load_traffic(dom),
+            "issue": issue_roofline(dom, per_call[dom], clk.get("sm_mhz") if clk else None)}
 
     # end to end through the host-buffer C ABI call
     pin = torch.empty(P * 12, dtype=torch.uint8, pin_memory=True).numpy()

@@ -540,31 +540,31 @@ __device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py
 // kept in registers.
 constexpr int kRasterCache = 8;
 
+// Exclusive block scan with a single barrier: each warp scans its lanes,
+// publishes its total, and after the barrier every thread adds up the totals
+// of the warps before its own (and of all warps, the block total).
 template <int NT>
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* swarp, uint32_t* total) {
+__device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t incl = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
     if (lane >= o) incl += t;
   }
   if (lane == 31) swarp[warp] = incl;
   __syncthreads();
-  if (warp == 0) {
-    uint32_t w = lane < (NT / 32) ? swarp[lane] : 0;
-    uint32_t wi = w;
+  uint32_t before = 0, all = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xFFFFFFFFu, wi, o);
-      if (lane >= o) wi += t;
-    }
-    if (lane < (NT / 32)) swarp[lane] = wi - w;
-    if (lane == (NT / 32) - 1) *total = wi;
+  for (int w = 0; w < NT / 32; w++) {
+    const uint32_t t = swarp[w];
+    all += t;
+    if (w < warp) before += t;
   }
-  __syncthreads();
-  return swarp[warp] + incl - v;
+  *total = all;
+  return before + incl - v;
 }
+
 
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
 // (views) or only the depth (cube faces).
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
     for (uint32_t c0 = 0; c0 < ntotal; c0 += NT) {
       const uint32_t m = min((uint32_t)NT, ntotal - c0);
       if (!(resident && pass == 1)) {
-        __syncthreads();
+        if (pass != 0 || c0 != 0) __syncthreads();  // the previous chunk's readers are done
         uint32_t area = 0, r = 0, geo = 0;
         float4 q0, q1, q2, q3;
         if ((uint32_t)tid < m) {
@@ -640,7 +640,8 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
           }
         }
         const uint32_t word = area ? (area | (1u << kCountShift)) : 0u;
-        const uint32_t off = block_excl_scan<NT>(word, swarp, &sscan);
+        uint32_t tot = 0;
+        const uint32_t off = block_excl_scan1<NT>(word, swarp, &tot);
         if (area) {
           const uint32_t slot = off >> kCountShift;
           srec[slot][0] = q0;
@@ -651,7 +652,10 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
           sgeo[slot] = geo;
           soff[slot] = off & ((1u << kCountShift) - 1);
         }
-        if (tid == 0) soff[sscan >> kCountShift] = sscan & ((1u << kCountShift) - 1);
+        if (tid == 0) {
+          soff[tot >> kCountShift] = tot & ((1u << kCountShift) - 1);
+          sscan = tot;
+        }
         __syncthreads();
       }
       const uint32_t nstaged = sscan >> kCountShift;
