@@ -597,6 +597,28 @@ def main():
     if not args.no_extra and not args.no_serve:
         serving = run_serving(args, stream)
 
+    # engine::draw_godrays over the measured 1080p frame: two shaft lights
+    post = None
+    if not args.no_extra:
+        glights = sc.lights.copy()
+        glights["godray_intensity"][:2] = 1.0
+        gs.set_lights(glights)
+        gout = torch.empty_like(out.rgba)
+        for _ in range(3):
+            gs.post_godrays(cam, view, out, rgba_out=gout, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(10):
+            gs.post_godrays(cam, view, out, rgba_out=gout, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        gms = e0.elapsed_time(e1) / 10
+        post = {"pass": "screenspace_godrays", "lights": 2, "ms": round(gms, 4),
+                "value": round(P / (gms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                "note": "out of place over the frame's depth / RGBA8 (8 MB, L2-resident between launches)"}
+        gs.set_lights(sc.lights)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -626,6 +648,7 @@ def main():
                     "note": "covered pixel-samples (point_in_tri passes) resolved per second by the raster kernels "
                             "with shared-memory atomics; no measured atomic peak is available for a fraction"},
                 "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "serving": serving,
+                "post_godrays": post,
                 "impl": "gbr",
                 "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],
                            "view_bin_entries": st["view_bin_entries"], "shadow_records": st["shadow_records"]}}

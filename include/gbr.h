@@ -229,6 +229,17 @@ gbr_status gbr_framebuffer_outputs(gbr_framebuffer* fb, gbr_outputs* out, int32_
 gbr_status gbr_framebuffer_read(gbr_framebuffer* fb, int32_t which, void* host, size_t bytes);
 gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb);
 
+/* engine::draw_godrays (engine.cpp:1463-1482) -> screenspace_godrays
+ * (cl2.cl:1792-1917): a post pass over a rendered view.  Adds the light shafts
+ * of the scene's lights with godray_intensity > 0, marched over the view's
+ * depth, to the view's RGBA8 and writes RGBA8 to rgba_out (device buffers, W*H).
+ * rgba_out == rgba_in works in place, as the reference's call does, but every
+ * pixel reads the unmodified input (through a scene-owned scratch image); a
+ * partial overlap is rejected.  The input is read with the bilinear filter the
+ * reference's image sampler applies, pinned to float weights. */
+gbr_status gbr_post_godrays(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
+                            const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
+
 /* Counters of the last render / shadow pass on this scene. */
 gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
 

@@ -429,6 +429,23 @@ struct engine {
     if (st == GBR_OK) st = gbr_render_view(dat.scene, &c, &v, &o, stream);
     return dat.status = st;
   }
+  // engine::draw_godrays (engine.cpp:1463-1482): light shafts added to the
+  // RGBA8 screen of the last draw_bulk_objs_n, in place; nothing to do when no
+  // light has godray_intensity > 0 (the reference's any_godray check)
+  gbr_status draw_godrays(object_context_data& dat) {
+    bool any = false;
+    if (lights)
+      for (const gbr_light& l : lights->lights) any = any || l.godray_intensity > 0;
+    if (!any) return GBR_OK;
+    gbr_status st = sync_lights(dat);
+    if (st == GBR_OK) st = dat.ensure_screen_buffers(width, height);
+    gbr_outputs o;
+    if (st == GBR_OK) st = gbr_framebuffer_outputs(dat.fb, &o, nullptr, nullptr);
+    const gbr_camera c = camera();
+    const gbr_view v = view(dat);
+    if (st == GBR_OK) st = gbr_post_godrays(dat.scene, &c, &v, o.depth, o.rgba, o.rgba, stream);
+    return dat.status = st;
+  }
   // engine::generate_depth_buffer (engine.cpp:1540): depth only
   gbr_status generate_depth_buffer(object_context_data& dat) {
     gbr_status st = dat.ensure_screen_buffers(width, height);

@@ -109,6 +109,7 @@ SIGNATURES = {
     "gbr_batch_get_info": (ctypes.c_int, [_P, _P]),
     "gbr_batch_destroy": (ctypes.c_int, [_P]),
     "gbr_render_view_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+    "gbr_post_godrays": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "gbr_server_create": (ctypes.c_int, [_P, _U32, _P, _P]),
     "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),
     "gbr_server_poll": (ctypes.c_int, [_P, _P, _U32, _P, ctypes.c_int32]),

@@ -452,6 +452,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->ws_view.release();
   s->ws_shadow.release();
   s->ws_host.release();
+  s->post_scratch.release();
   s->world.release();
   s->objq.release();
   s->staging.release();
@@ -465,6 +466,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
 }
 
 gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint32_t n) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   s->version++;  // captured batches re-capture
   if (n && !tris) return fail(GBR_INVALID_ARG, "null triangles");
@@ -485,6 +487,7 @@ gbr_status gbr_scene_set_triangles(gbr_scene* s, const gbr_triangle* tris, uint3
 }
 
 gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d, uint32_t n) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   s->version++;  // captured batches re-capture
   if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
@@ -509,6 +512,7 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
 }
 
 gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   s->version++;  // captured batches re-capture
   if (n && !l) return fail(GBR_INVALID_ARG, "null lights");
@@ -536,6 +540,7 @@ gbr_status gbr_scene_set_lights(gbr_scene* s, const gbr_light* l, uint32_t n) {
 }
 
 gbr_status gbr_scene_set_textures(gbr_scene* s, uint32_t n, const int32_t* sizes, const uint8_t* const* rgba) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   s->version++;  // captured batches re-capture
   if (n && (!sizes || !rgba)) return fail(GBR_INVALID_ARG, "null texture arrays");
@@ -585,6 +590,7 @@ gbr_status gbr_scene_set_textures(gbr_scene* s, uint32_t n, const int32_t* sizes
 
 gbr_status gbr_scene_texture_layout(gbr_scene* s, uint32_t* nums, uint32_t* n_nums, uint32_t* sizes,
                                     uint32_t* n_sizes, uint32_t* mipmap_start) {
+  GBR_SCENE_LOCK(s);
   if (!s || !n_nums || !n_sizes) return fail(GBR_INVALID_ARG, "null argument");
   uint32_t cn = *n_nums, cs = *n_sizes;
   *n_nums = (uint32_t)s->host_nums.size();
@@ -596,6 +602,7 @@ gbr_status gbr_scene_texture_layout(gbr_scene* s, uint32_t* nums, uint32_t* n_nu
 }
 
 gbr_status gbr_scene_buffer(gbr_scene* s, int32_t which, const void** ptr, size_t* bytes) {
+  GBR_SCENE_LOCK(s);
   if (!s || !ptr || !bytes) return fail(GBR_INVALID_ARG, "null argument");
   const size_t face = (size_t)kLightBufferDim * kLightBufferDim;
   switch (which) {
@@ -607,6 +614,7 @@ gbr_status gbr_scene_buffer(gbr_scene* s, int32_t which, const void** ptr, size_
 }
 
 gbr_status gbr_scene_read_buffer(gbr_scene* s, int32_t which, void* dst, size_t offset, size_t bytes) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   TRY(settle_shadow_quiet(s));
   const void* p = nullptr;
@@ -631,6 +639,7 @@ gbr_status gbr_texture_pack(uint32_t n, const int32_t* sizes, uint32_t* nums, ui
 }
 
 gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   cudaStream_t st = (cudaStream_t)stream;
   TRY(settle_shadow_quiet(s));
@@ -741,16 +750,19 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
 
 gbr_status gbr_render_view(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const gbr_outputs* out,
                            void* stream) {
+  GBR_SCENE_LOCK(s);
   return render_views(s, 1, cam, view, out, (cudaStream_t)stream);
 }
 
 gbr_status gbr_render_batch(gbr_scene* s, uint32_t n, const gbr_camera* cams, const gbr_view* views,
                             const gbr_outputs* outs, void* stream) {
+  GBR_SCENE_LOCK(s);
   return render_views(s, n, cams, views, outs, (cudaStream_t)stream);
 }
 
 gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, uint32_t* depth,
                                 uint32_t* id, uint8_t* rgba, void* stream) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   TRY(validate_view(view));
   cudaStream_t st = (cudaStream_t)stream;
@@ -768,7 +780,34 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   return GBR_OK;
 }
 
+gbr_status gbr_post_godrays(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
+                            const uint8_t* rgba_in, uint8_t* rgba_out, void* stream) {
+  GBR_SCENE_LOCK(s);
+  TRY(check_scene(s));
+  TRY(validate_view(view));
+  if (!cam || !depth || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  const size_t P = (size_t)view->width * view->height * 4;
+  const bool in_place = rgba_out == rgba_in;
+  if (!in_place && rgba_out < rgba_in + P && rgba_in < rgba_out + P)
+    return fail(GBR_INVALID_ARG, "rgba_out partly overlaps rgba_in");
+  float cc[3], cs[3];
+  euler_cs(cam->rot, cc, cs);
+  const float fov = view->fov_const > 0 ? view->fov_const : gbr_fov_const_from_hfov(view->hfov_deg, view->width);
+  uint8_t* dst = rgba_out;
+  if (in_place) {
+    TRY(s->post_scratch.reserve(P));
+    dst = s->post_scratch.p;
+  }
+  const cudaStream_t st = (cudaStream_t)stream;
+  CU(launch_godrays(depth, rgba_in, dst, view->width, view->height, fov, s->lights.p,
+                    (uint32_t)s->host_lights.size(), cam->pos, cc, cs, st));
+  if (in_place) CU(cudaMemcpyAsync(rgba_out, dst, P, cudaMemcpyDeviceToDevice, st));
+  s->stats.launches += 1;
+  return GBR_OK;
+}
+
 gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   if (enable && !s->ev[0])
     for (auto& e : s->ev) CU(cudaEventCreate(&e));
@@ -850,6 +889,7 @@ gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb) {
 }
 
 gbr_status gbr_scene_set_tuning(gbr_scene* s, int32_t pass, const gbr_tuning* t) {
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   if (pass != GBR_PASS_SHADOW && pass != GBR_PASS_VIEW) return fail(GBR_INVALID_ARG, "pass %d", pass);
   Tuning tu;
@@ -860,6 +900,7 @@ gbr_status gbr_scene_set_tuning(gbr_scene* s, int32_t pass, const gbr_tuning* t)
 }
 
 gbr_status gbr_scene_get_tuning(gbr_scene* s, int32_t pass, gbr_tuning* t) {
+  GBR_SCENE_LOCK(s);
   if (!s || !t) return fail(GBR_INVALID_ARG, "null argument");
   if (pass != GBR_PASS_SHADOW && pass != GBR_PASS_VIEW) return fail(GBR_INVALID_ARG, "pass %d", pass);
   tuning_to_abi(s->tune[pass], t);
@@ -867,6 +908,7 @@ gbr_status gbr_scene_get_tuning(gbr_scene* s, int32_t pass, gbr_tuning* t) {
 }
 
 gbr_status gbr_scene_stats(gbr_scene* s, gbr_stats* out) {
+  GBR_SCENE_LOCK(s);
   if (!s || !out) return fail(GBR_INVALID_ARG, "null argument");
   TRY(check_scene(s));
   TRY(settle_shadow_quiet(s));

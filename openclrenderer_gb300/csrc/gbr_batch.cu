@@ -240,6 +240,7 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
                             int32_t flags, gbr_batch** out) {
   if (!out) return fail(GBR_INVALID_ARG, "null out");
   *out = nullptr;
+  GBR_SCENE_LOCK(s);
   TRY(check_scene(s));
   if (!n || !views || !outs) return fail(GBR_INVALID_ARG, "a batch needs n > 0 views and outputs");
   if (flags & ~GBR_BATCH_WITH_SHADOW) return fail(GBR_INVALID_ARG, "unknown batch flags %d", flags);
@@ -266,6 +267,7 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
 }
 
 gbr_status gbr_batch_launch(gbr_batch* b, const gbr_camera* cams, void* stream) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b || !cams) return fail(GBR_INVALID_ARG, "null argument");
   TRY(check_scene(b->s));
   TRY(wait_frame(b));
@@ -276,17 +278,20 @@ gbr_status gbr_batch_launch(gbr_batch* b, const gbr_camera* cams, void* stream) 
 }
 
 gbr_status gbr_batch_wait(gbr_batch* b) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b) return fail(GBR_INVALID_ARG, "null batch");
   TRY(check_scene(b->s));
   return wait_frame(b);
 }
 
 gbr_status gbr_batch_render(gbr_batch* b, const gbr_camera* cams, void* stream) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   TRY(gbr_batch_launch(b, cams, stream));
   return wait_frame(b);
 }
 
 gbr_status gbr_batch_set_tuning(gbr_batch* b, int32_t pass, const gbr_tuning* t) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b) return fail(GBR_INVALID_ARG, "null batch");
   TRY(check_pass_arg(pass));
   Tuning tu;
@@ -299,6 +304,7 @@ gbr_status gbr_batch_set_tuning(gbr_batch* b, int32_t pass, const gbr_tuning* t)
 }
 
 gbr_status gbr_batch_get_tuning(gbr_batch* b, int32_t pass, gbr_tuning* t) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b || !t) return fail(GBR_INVALID_ARG, "null argument");
   TRY(check_pass_arg(pass));
   tuning_to_abi(b->tune[pass], t);
@@ -307,6 +313,7 @@ gbr_status gbr_batch_get_tuning(gbr_batch* b, int32_t pass, gbr_tuning* t) {
 
 gbr_status gbr_batch_autotune(gbr_batch* b, const gbr_camera* cams, void* stream, int32_t reps,
                               gbr_tuning* view_pick, gbr_tuning* shadow_pick, float* best_ms) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b || !cams) return fail(GBR_INVALID_ARG, "null argument");
   if (reps < 1 || reps > 1000) return fail(GBR_INVALID_ARG, "reps %d: must be in 1..1000", reps);
   TRY(check_scene(b->s));
@@ -388,6 +395,7 @@ gbr_status gbr_batch_autotune(gbr_batch* b, const gbr_camera* cams, void* stream
 }
 
 gbr_status gbr_batch_get_info(gbr_batch* b, gbr_batch_info* out) {
+  GBR_SCENE_LOCK(b ? b->s : nullptr);
   if (!b || !out) return fail(GBR_INVALID_ARG, "null argument");
   out->views = b->n;
   out->graph_nodes = (uint32_t)b->nodes;

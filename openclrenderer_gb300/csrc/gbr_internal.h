@@ -168,6 +168,10 @@ cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* siz
                         uint32_t mipmap_start, const int32_t* tsizes, uint32_t ntex,
                         int32_t max_size, cudaStream_t st);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
+// screenspace_godrays over a rendered view (RGBA8 in / out, distinct buffers).
+cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* out, int W, int H, float fov,
+                           const gbr_light* lights, uint32_t nlights, const float cpos[3], const float cc[3],
+                           const float cs[3], cudaStream_t st);
 
 // Sets the message gbr_last_error_string() returns on this thread (gbr_api.cu).
 void set_last_error(const char* msg);

@@ -488,6 +488,30 @@ GBR_HD uint32_t quant8(float v) {
   return (uint32_t)floorf(v * 255.0f + 0.5f);
 }
 
+// ---- post passes -----------------------------------------------------------
+// Bilinear read of an RGBA8 image at unnormalised float coordinates with
+// clamp-to-edge: OpenCL 1.2 section 8.2's linear filter (i0 = floor(x - 0.5),
+// a = frac(x - 0.5)) with float weights, the device precision pinned.
+GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy) {
+  const float u = cx - 0.5f, v = cy - 0.5f;
+  const float fi = floorf(u), fj = floorf(v);
+  const float a = u - fi, b = v - fj;
+  const int i0 = (int)fi, j0 = (int)fj;
+  const int xs[2] = {i0 < 0 ? 0 : (i0 >= W ? W - 1 : i0), i0 + 1 < 0 ? 0 : (i0 + 1 >= W ? W - 1 : i0 + 1)};
+  const int ys[2] = {j0 < 0 ? 0 : (j0 >= H ? H - 1 : j0), j0 + 1 < 0 ? 0 : (j0 + 1 >= H ? H - 1 : j0 + 1)};
+  float t[4][4];
+  for (int k = 0; k < 4; k++) {
+    const uint8_t* p = img + ((size_t)ys[k >> 1] * W + xs[k & 1]) * 4;
+    for (int c = 0; c < 4; c++) t[k][c] = fdiv((float)p[c], 255.0f);
+  }
+  f4 r;
+  float* rc = &r.x;
+  for (int c = 0; c < 4; c++)
+    rc[c] = ((((1.0f - a) * (1.0f - b)) * t[0][c] + (a * (1.0f - b)) * t[1][c]) + ((1.0f - a) * b) * t[2][c]) +
+            (a * b) * t[3][c];
+  return r;
+}
+
 // Six cube-face Euler rotations (cl2.cl:4487-4511, 2538-2558) as float
 // angles; their cosines and sines are rounded from double on the host.
 GBR_HD f3 face_angles(int face) {

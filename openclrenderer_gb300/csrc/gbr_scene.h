@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 #include <vector>
 
 #include "../../include/gbr.h"
@@ -117,6 +118,9 @@ void euler_cs(const float ang[3], float c[3], float s[3]);
 }  // namespace gbr
 
 struct gbr_scene {
+  // Calls on one scene are serialised (the C ABI is thread-safe per handle);
+  // recursive because entry points call each other.
+  std::recursive_mutex mu;
   int device = 0;
   gbr::DevBuf<gbr_triangle> tris;
   uint32_t ntris = 0;
@@ -138,6 +142,7 @@ struct gbr_scene {
   bool has_rid = false;  // some descriptor names a normal map (rid != 0xFFFFFFFF)
   bool static_dirty = true;
   gbr::WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
+  gbr::DevBuf<uint8_t> post_scratch;         // in-place post passes write here first
   gbr::HostBuf staging;         // counters read back: view at 0, shadow at 256
   bool shadow_pending = false;  // a shadow pass whose counters are not checked yet
   cudaStream_t shadow_stream = nullptr;
@@ -183,6 +188,11 @@ struct gbr_scene {
 };
 
 namespace gbr {
+
+// Holds the scene's lock for the rest of the calling entry point.
+#define GBR_SCENE_LOCK(s)                            \
+  std::unique_lock<std::recursive_mutex> scene_lock_; \
+  if (s) scene_lock_ = std::unique_lock<std::recursive_mutex>((s)->mu)
 
 gbr_status check_scene(gbr_scene* s);
 // Every index the kernels follow must stay inside its table.

@@ -189,6 +189,17 @@ class GpuScene:
                                                   _np_ptr(ids), _np_ptr(rgba), _stream_ptr(stream)))
         return {"depth": depth, "id": ids, "rgba": rgba}
 
+    def post_godrays(self, cam, view, out, rgba_out=None, stream=None):
+        """engine::draw_godrays over a rendered OutputSet: RGBA8 with light shafts."""
+        import torch
+        cam = np.asarray(cam, S.CAMERA).reshape(1)
+        view = np.asarray(view, S.VIEW).reshape(1)
+        if rgba_out is None:
+            rgba_out = torch.empty_like(out.rgba)
+        _native.check(self.L.gbr_post_godrays(self.h, _np_ptr(cam), _np_ptr(view), _t_ptr(out.depth),
+                                              _t_ptr(out.rgba), _t_ptr(rgba_out), _stream_ptr(stream)))
+        return rgba_out
+
     def stats(self):
         st = np.zeros(1, S.STATS)
         _native.check(self.L.gbr_scene_stats(self.h, _np_ptr(st)))

@@ -110,7 +110,7 @@ def make_descriptor(world_pos=(0, 0, 0), quat=(0, 0, 0, 1), scale=1.0, tid=0,
 
 
 def make_light(pos, col=(1, 1, 1), brightness=1.0, radius=20000.0, shadow=0, diffuse=1.0,
-               is_static=0):
+               is_static=0, godray_intensity=0.0):
     l = np.zeros((), LIGHT)
     l["pos"][:3] = pos
     l["col"][:3] = col
@@ -119,6 +119,7 @@ def make_light(pos, col=(1, 1, 1), brightness=1.0, radius=20000.0, shadow=0, dif
     l["radius"] = radius
     l["diffuse"] = diffuse
     l["is_static"] = is_static
+    l["godray_intensity"] = godray_intensity
     return l
 
 

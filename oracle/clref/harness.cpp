@@ -208,6 +208,27 @@ void ref_shadow(const void* tris_in, uint32_t ntris, const void* descs, const vo
   }
 }
 
+// screenspace_godrays (cl2.cl:1792-1917) over a rendered view: depth u32 and
+// RGBA8 in, RGBA8 out (quantised as the product does).  cam = pos[4], rot[4].
+void ref_godrays(const uint32_t* depth, const uint8_t* rgba_in, int W, int H, float fov, const void* lights_in,
+                 uint32_t nlights, const float* cam, uint8_t* rgba_out, int nthreads) {
+  gbr_ref_W = W;
+  gbr_ref_H = H;
+  gbr_ref_FOV = fov;
+  const size_t P = (size_t)W * H;
+  std::vector<float> out(P * 4, 0.f);
+  image2d_t in{const_cast<uint8_t*>(rgba_in), W, H, 1}, o{out.data(), W, H, 2};
+  uint lnum = nlights;
+  float4 c_pos(cam[0], cam[1], cam[2], cam[3]), c_rot(cam[4], cam[5], cam[6], cam[7]);
+  par_for((int64_t)P, nthreads, [&](int64_t p) {
+    gbr_ref_gid[0] = (size_t)(p % W);
+    gbr_ref_gid[1] = (size_t)(p / W);
+    screenspace_godrays(const_cast<uint*>(depth), in, o, &lnum, (struct light*)const_cast<void*>(lights_in), c_pos,
+                        c_rot);
+  });
+  for (size_t i = 0; i < P * 4; i++) rgba_out[i] = (uint8_t)gbr::quant8(out[i]);
+}
+
 // update_gpu_tex (flip 1) + generate_mips + generate_mip_mips for every
 // texture, into an atlas already laid out by the page packing (nums, sizes).
 void ref_textures(uint32_t n, const int32_t* tsizes, const uint8_t* const* rgba, uint8_t* atlas, uint32_t* nums,

@@ -28,6 +28,9 @@ def lib(features=False):
                                  ctypes.c_int, ctypes.c_int]
         L.ref_shadow.restype = None
         L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int, ctypes.c_int]
+        L.ref_godrays.restype = None
+        L.ref_godrays.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_float, P, ctypes.c_uint32, P, P,
+                                  ctypes.c_int]
         L.ref_textures.restype = None
         L.ref_textures.argtypes = [ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32]
         _libs[features] = L
@@ -86,3 +89,15 @@ def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_
                           _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
                           _p(rgba), _p(normals), nthreads, 1 if ordered else 0)
     return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "fragments": int(nf)}
+
+
+def godrays(depth, rgba, lights, cam, fov, nthreads=None):
+    """screenspace_godrays of the reference over (depth, RGBA8): RGBA8 out."""
+    nthreads = nthreads or (os.cpu_count() or 1)
+    H, W = depth.shape
+    out = np.empty((H, W, 4), np.uint8)
+    c = np.concatenate([np.asarray(cam["pos"], np.float32), np.asarray(cam["rot"], np.float32)])
+    lights = np.ascontiguousarray(lights)
+    lib().ref_godrays(_p(np.ascontiguousarray(depth, np.uint32)), _p(np.ascontiguousarray(rgba, np.uint8)), W, H,
+                      fov, _p(lights), len(lights), _p(c), _p(out), nthreads)
+    return out

@@ -67,6 +67,11 @@ struct swz {
     for (int k = 0; k < (int)sizeof...(I); k++) v[idx[k]] = v[idx[k]] / s;
     return *this;
   }
+  swz& operator+=(const V& o) {
+    const int idx[] = {I...};
+    for (int k = 0; k < (int)sizeof...(I); k++) v[idx[k]] = v[idx[k]] + o.s[k];
+    return *this;
+  }
 };
 
 struct float2;
@@ -132,6 +137,10 @@ struct alignas(8) int2 {
   int2& operator=(const int2& o) { memcpy(s, o.s, sizeof s); return *this; }
 };
 inline int2 operator+(int2 a, int2 b) { return int2(a.x + b.x, a.y + b.y); }
+// vector relational operators (-1 where true) and any() (cl2.cl screenspace_godrays)
+inline int2 operator<(float2 a, float b) { return int2(a.x < b ? -1 : 0, a.y < b ? -1 : 0); }
+inline int2 operator>=(float2 a, float2 b) { return int2(a.x >= b.x ? -1 : 0, a.y >= b.y ? -1 : 0); }
+inline int any(int2 v) { return (v.x < 0 || v.y < 0) ? 1 : 0; }
 
 struct alignas(16) int4 {
   union {
@@ -288,6 +297,8 @@ typedef int sampler_t;
 #define CLK_NORMALIZED_COORDS_FALSE 0
 #define CLK_ADDRESS_NONE 0
 #define CLK_FILTER_NEAREST 0
+#define CLK_ADDRESS_CLAMP_TO_EDGE 2
+#define CLK_FILTER_LINEAR 16
 inline int2 get_image_dim(image2d_t im) { return int2(im.w, im.h); }
 inline uint4 read_imageui(image2d_t im, sampler_t, int2 c) {
   return uint4(static_cast<uint*>(im.data)[(size_t)c.y * im.w + c.x], 0, 0, 1);
@@ -298,6 +309,25 @@ inline void write_imageui(image2d_t im, int2 c, uint4 v) {
 inline float4 read_imagef(image2d_t im, sampler_t, int2 c) {
   const uchar* p = static_cast<uchar*>(im.data) + ((size_t)c.y * im.w + c.x) * 4;
   return float4(p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f, p[3] / 255.0f);
+}
+// Unnormalised float coordinates: nearest, or (CLK_FILTER_LINEAR) bilinear
+// with clamp-to-edge as OpenCL 1.2 section 8.2 defines it -- i0 = floor(x -
+// 0.5), a = frac(x - 0.5) -- with the weights in float (the precision OpenCL
+// leaves to the device, pinned).
+inline float4 read_imagef(image2d_t im, sampler_t s, float2 c) {
+  if (!(s & CLK_FILTER_LINEAR)) return read_imagef(im, s, int2((int)floorf(c.x), (int)floorf(c.y)));
+  const float u = c.x - 0.5f, v = c.y - 0.5f;
+  const float fi = floorf(u), fj = floorf(v);
+  const float a = u - fi, b = v - fj;
+  auto cl = [](int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); };
+  const int i0 = cl((int)fi, im.w), i1 = cl((int)fi + 1, im.w), j0 = cl((int)fj, im.h), j1 = cl((int)fj + 1, im.h);
+  const float4 t00 = read_imagef(im, s, int2(i0, j0)), t10 = read_imagef(im, s, int2(i1, j0));
+  const float4 t01 = read_imagef(im, s, int2(i0, j1)), t11 = read_imagef(im, s, int2(i1, j1));
+  float4 r;
+  for (int k = 0; k < 4; k++)
+    r.s[k] = ((((1.0f - a) * (1.0f - b)) * t00.s[k] + (a * (1.0f - b)) * t10.s[k]) + ((1.0f - a) * b) * t01.s[k]) +
+             (a * b) * t11.s[k];
+  return r;
 }
 inline void write_imagef(image2d_t im, int2 c, float4 v) {
   if (!im.data) return;

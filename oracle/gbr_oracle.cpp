@@ -1058,6 +1058,73 @@ void shadow_light(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
 
 }  // namespace
 
+// ---- screenspace_godrays (cl2.cl:1792-1917, engine.cpp:1463-1482) ----------
+// The sampler of the reference's screen image: unnormalised coordinates,
+// clamp to edge, bilinear (OpenCL 1.2 section 8.2), float weights.
+f4 sample_bilinear(const uint8_t* img, int W, int H, float x, float y) {
+  const float u = x - 0.5f, v = y - 0.5f;
+  const float fu = floorf(u), fv = floorf(v);
+  const float a = u - fu, b = v - fv;
+  auto cl = [](int i, int n) { return std::min(std::max(i, 0), n - 1); };
+  const int x0 = cl((int)fu, W), x1 = cl((int)fu + 1, W), y0 = cl((int)fv, H), y1 = cl((int)fv + 1, H);
+  auto texel = [&](int xx, int yy, int c) { return fdiv((float)img[((size_t)yy * W + xx) * 4 + c], 255.0f); };
+  float o[4];
+  for (int c = 0; c < 4; c++) {
+    const float w00 = (1.0f - a) * (1.0f - b), w10 = a * (1.0f - b), w01 = (1.0f - a) * b, w11 = a * b;
+    o[c] = w00 * texel(x0, y0, c) + w10 * texel(x1, y0, c);
+    o[c] = o[c] + w01 * texel(x0, y1, c);
+    o[c] = o[c] + w11 * texel(x1, y1, c);
+  }
+  return v4(o);
+}
+
+// One pixel: every light with godray_intensity > 0 marches up to 80 steps of
+// 400/80 pixels from the pixel towards the light's screen position (mirrored
+// through the pixel when the light is behind the camera), adding the light's
+// colour where the depth buffer holds something more than 5 units nearer than
+// the pixel; the march stops at the first step off screen.
+void godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* in, int W, int H, float fov,
+                   const gbr_light* lights, uint32_t nl, f3 cpos, f3 cc, f3 cs, uint8_t* out) {
+  f4 acc = sample_bilinear(in, W, H, (float)x - 0.25f, (float)y - 0.25f);
+  const float here = depth_to_dist(depth[(size_t)y * W + x]);
+  for (uint32_t l = 0; l < nl; l++) {
+    const gbr_light& L = lights[l];
+    if (L.godray_intensity <= 0) continue;
+    const f3 sl = depth_project1(rot_cs(v3(L.pos), cpos, cc, cs), (float)W, (float)H, fov);
+    f3 cur = mk3((float)x, (float)y, here);
+    const f3 to = sl.z < 0 ? add3(sub3(cur, sl), cur) : sl;
+    const float dx = std::fabs(cur.x - to.x), dy = std::fabs(cur.y - to.y);
+    const float steps = dx > dy ? dx : dy;
+    f3 d = sub3(to, cur);
+    d = mk3(fdiv(d.x, steps) * 5.0f, fdiv(d.y, steps) * 5.0f, fdiv(d.z, steps) * 5.0f);
+    float decay = 1.0f, sx = 0, sy = 0, sz = 0;
+    for (int j = 0; (float)j < steps && j < 80; j++) {
+      if (cur.x < 0 || cur.y < 0 || cur.x >= (float)(W - 1) || cur.y >= (float)(H - 1)) break;
+      const uint32_t cd = depth[(size_t)(int)cur.y * W + (int)cur.x];
+      float r = 0, g = 0, b = 0;
+      if (cd != kDepthClear && depth_to_dist(cd) < here - 5.0f) {
+        decay = decay * 0.9f;
+        r = L.col[0] * L.godray_intensity;
+        g = L.col[1] * L.godray_intensity;
+        b = L.col[2] * L.godray_intensity;
+      }
+      sx += (r * decay) * 0.01f;
+      sy += (g * decay) * 0.01f;
+      sz += (b * decay) * 0.01f;
+      decay = decay * 0.97f;
+      cur = add3(cur, d);
+    }
+    acc.x += sx;
+    acc.y += sy;
+    acc.z += sz;
+  }
+  const size_t p = ((size_t)y * W + x) * 4;
+  out[p + 0] = (uint8_t)quant8(acc.x * 0.99f);
+  out[p + 1] = (uint8_t)quant8(acc.y * 0.99f);
+  out[p + 2] = (uint8_t)quant8(acc.z * 0.99f);
+  out[p + 3] = (uint8_t)quant8(1.0f * 0.99f);
+}
+
 extern "C" {
 
 // engine.cpp:119-133 then the std::to_string / -D FOV_CONST round trip (engine.cpp:474-477).
@@ -1297,6 +1364,20 @@ int oracle_walk(const float* tp9, float ew, float eh, int chunk, uint32_t distan
     n++;
   });
   return n;
+}
+
+// engine::draw_godrays over a rendered view (depth, RGBA8): RGBA8 out.
+int oracle_godrays(const uint32_t* depth, const uint8_t* rgba_in, const gbr_light* lights, uint32_t nl,
+                   const gbr_camera* cam, const gbr_view* view, uint8_t* rgba_out, int nthreads) {
+  const int W = view->width, H = view->height;
+  const float fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
+  f3 cc, cs;
+  euler_cs(v3(cam->rot), &cc, &cs);
+  const f3 cpos = v3(cam->pos);
+  parallel_for((int64_t)W * H, nthreads, [&](int64_t p) {
+    godrays_pixel((int)(p % W), (int)(p / W), depth, rgba_in, W, H, fov, lights, nl, cpos, cc, cs, rgba_out);
+  });
+  return 0;
 }
 
 }  // extern "C"

@@ -47,6 +47,8 @@ def lib():
         L.oracle_render_fp64.restype = ctypes.c_int
         L.oracle_render_fp64.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32,
                                          P, P, P, P, P, ctypes.c_int, ctypes.c_int]
+        L.oracle_godrays.restype = ctypes.c_int
+        L.oracle_godrays.argtypes = [P, P, P, ctypes.c_uint32, P, P, P, ctypes.c_int]
         L.oracle_walk.restype = ctypes.c_int
         L.oracle_walk.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
                                   P, ctypes.c_int]
@@ -127,6 +129,19 @@ def render(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, shade=Tru
         out["rgba"] = rgba
     if nrm is not None:
         out["normals"] = nrm
+    return out
+
+
+def godrays(depth, rgba, lights, cam, view, nthreads=None):
+    """screenspace_godrays over a rendered view: (H, W, 4) RGBA8 out."""
+    nthreads = nthreads or default_threads()
+    H, W = depth.shape
+    out = np.empty((H, W, 4), np.uint8)
+    lights = np.ascontiguousarray(lights)
+    cam = np.asarray(cam).reshape(1)
+    view = np.asarray(view).reshape(1)
+    lib().oracle_godrays(_p(np.ascontiguousarray(depth, np.uint32)), _p(np.ascontiguousarray(rgba, np.uint8)),
+                         _p(lights), len(lights), _p(cam), _p(view), _p(out), nthreads)
     return out
 
 

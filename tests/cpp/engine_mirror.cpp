@@ -100,7 +100,7 @@ int main(int argc, char** argv) {
   window.set_light_data(lights);
   if (window.set_object_data(*ctx.fetch()) != GBR_OK ||
       window.generate_realtime_shadowing(*ctx.fetch()) != GBR_OK ||
-      window.draw_bulk_objs_n(*ctx.fetch()) != GBR_OK) {
+      window.draw_bulk_objs_n(*ctx.fetch()) != GBR_OK || window.draw_godrays(*ctx.fetch()) != GBR_OK) {
     fprintf(stderr, "frame: %s\n", gbr_last_error_string());
     return 5;
   }

@@ -61,5 +61,25 @@ def main(only=None):
               f"fragments {[meta[k] for k in meta if k.startswith('fragments')]}")
 
 
+def main_godrays():
+    """screenspace_godrays of the reference over the depth / RGBA8 stored in
+    the cubes fixture, with tests.golden_cases.godray_lights()."""
+    src = np.load(os.path.join(OUT, f"{golden_cases.POST['godrays']}.npz"))
+    sc, _ = golden_cases.CASES[golden_cases.POST["godrays"]]()
+    lights = golden_cases.godray_lights()
+    arrays = {}
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        fov = O.fov_const(float(view["hfov_deg"]), int(view["width"]))
+        arrays[f"rgba{k}"] = R.godrays(src[f"depth{k}"], src[f"rgba{k}"], lights, cam, fov)
+    path = os.path.join(OUT, "godrays.npz")
+    np.savez_compressed(path, **arrays)
+    print(f"godrays: {os.path.getsize(path) / 1e3:.0f} kB, views {len(arrays)}")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:] or None)
+    args = sys.argv[1:]
+    cases = [a for a in args if a != "godrays"]
+    if cases or not args:
+        main(cases or None)
+    if not args or "godrays" in args:
+        main_godrays()

@@ -101,5 +101,20 @@ def features():
     return sc, {"shadows": True, "normals": True, "features": True}
 
 
+def godray_lights():
+    """Lights of the screenspace_godrays fixture over the cubes views: one
+    beyond the cubes, one behind the camera (mirrored march), one off to the
+    side, one with no shafts."""
+    return np.stack([
+        S.make_light((30, -20, 2600), (1.0, 0.9, 0.7), godray_intensity=1.0),
+        S.make_light((100, 50, -500), (0.3, 0.5, 1.0), godray_intensity=0.5),
+        S.make_light((2000, 0, 500), (0.9, 0.2, 0.2), godray_intensity=0.8),
+        S.make_light((0, 0, 1000), (1.0, 1.0, 1.0), godray_intensity=0.0),
+    ])
+
+
+# post passes over the views of a rendered case: fixture name -> source case
+POST = {"godrays": "cubes"}
+
 CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
          "wide_boxes": wide_boxes, "features": features}

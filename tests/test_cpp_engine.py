@@ -29,8 +29,15 @@ def _multi_shadow_cubes():
     return sc
 
 
+def _godray_cubes():
+    from tests import golden_cases
+    sc = scenes.plain_cubes()
+    sc.lights = np.concatenate([sc.lights, golden_cases.godray_lights()])
+    return sc
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["cubes", "cubes_shadows", "terrain_small"])
+@pytest.mark.parametrize("name", ["cubes", "cubes_shadows", "terrain_small", "cubes_godrays"])
 def test_engine_mirror_matches_c_abi(tmp_path, name):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():  # pragma: no cover
@@ -38,7 +45,8 @@ def test_engine_mirror_matches_c_abi(tmp_path, name):
     from openclrenderer_gb300.pipeline import GpuScene
     sc = {"cubes": scenes.plain_cubes, "cubes_shadows": _multi_shadow_cubes,
           "terrain_small": lambda: scenes.terrain(nx=128, nz=64, width=640, height=360, n_lights=4,
-                                                  n_textures=4, tex_size=128)}[name]()
+                                                  n_textures=4, tex_size=128),
+          "cubes_godrays": _godray_cubes}[name]()
     view = sc.views[0]
     W, H = int(view["width"]), int(view["height"])
     exe = M.build(str(tmp_path))
@@ -46,7 +54,10 @@ def test_engine_mirror_matches_c_abi(tmp_path, name):
     got = M.run(exe, str(tmp_path / "scene.bin"), str(tmp_path / "out.bin"), W, H)
     gs = GpuScene(sc)
     gs.shadow_pass()
-    ref = gs.render(sc.cameras[0], view).numpy()
+    out = gs.render(sc.cameras[0], view)
+    if name == "cubes_godrays":  # engine::draw_godrays after the frame, in place
+        gs.post_godrays(sc.cameras[0], view, out, rgba_out=out.rgba)
+    ref = out.numpy()
     gs.close()
     for k in ("depth", "id", "rgba"):
         assert np.array_equal(got[k], ref[k]), f"{name}: {k} differs ({np.count_nonzero(got[k] != ref[k])})"

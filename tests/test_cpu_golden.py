@@ -79,3 +79,36 @@ def test_oracle_matches_reference_kernels_random(seed):
     assert got["fragments"] == ref["fragments"]
     for key in ("depth", "id", "rgba", "normals"):
         assert np.array_equal(got[key], ref[key]), key
+
+
+def test_oracle_godrays_matches_reference_fixture():
+    """screenspace_godrays (cl2.cl:1792-1917) over the cubes fixture's views."""
+    src = np.load(os.path.join(GOLDEN, f"{golden_cases.POST['godrays']}.npz"))
+    fx = np.load(os.path.join(GOLDEN, "godrays.npz"))
+    sc, _ = golden_cases.CASES[golden_cases.POST["godrays"]]()
+    lights = golden_cases.godray_lights()
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        got = O.godrays(src[f"depth{k}"], src[f"rgba{k}"], lights, cam, view)
+        bad = np.count_nonzero(got != fx[f"rgba{k}"])
+        assert bad == 0, f"godrays view {k}: {bad} values differ from the reference kernel"
+
+
+@pytest.mark.parametrize("seed", [201, 202])
+def test_oracle_godrays_matches_reference_kernel_random(seed):
+    """Random depth / RGBA8 with clear-depth holes, lights in front of,
+    behind and beside the camera, some with no shafts."""
+    R = _ref_or_skip()
+    from openclrenderer_gb300 import structs as S
+    rng = np.random.default_rng(seed)
+    W, H = int(rng.integers(40, 300)), int(rng.integers(30, 200))
+    depth = rng.integers(0, 2**32, (H, W), dtype=np.uint64).astype(np.uint32) >> int(rng.integers(0, 8))
+    depth[rng.random((H, W)) < 0.3] = 0xFFFFFFFF
+    rgba = rng.integers(0, 256, (H, W, 4), dtype=np.uint8)
+    lights = np.stack([S.make_light(rng.uniform(-3000, 3000, 3), rng.uniform(0, 1, 3),
+                                    godray_intensity=float(rng.choice([0.0, -1.0, 0.3, 1.5])))
+                       for _ in range(5)])
+    cam = S.make_camera(rng.uniform(-50, 50, 3), rng.uniform(-0.5, 0.5, 3))
+    view = S.make_view(W, H, float(rng.uniform(60, 120)))
+    ref = R.godrays(depth, rgba, lights, cam, O.fov_const(float(view["hfov_deg"]), W))
+    got = O.godrays(depth, rgba, lights, cam, view)
+    assert np.array_equal(got, ref)
