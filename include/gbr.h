@@ -164,6 +164,28 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* scene, const gbr_obj_g_descripto
 
 /* light::build (light.cpp:145-276): active lights and the shadow cubemaps
  * (6 * 1024^2 u32 per shadow-casting light, dynamic and static). Host array. */
+/* Reads the scene's n (= the count last set) descriptors back from the device,
+ * with the pose history the motion-blur pass keeps in them (synchronous). */
+gbr_status gbr_scene_get_descriptors(gbr_scene* scene, gbr_obj_g_descriptor* descs, uint32_t n);
+
+/* One object's state as object::g_flush writes it (object.cpp:652-860):
+ * position, rotation quaternion, scale, texture id and feature flags of
+ * descriptor `index`.  The descriptor's other fields -- the motion-blur pose
+ * history above all -- stay as they are on the device. */
+typedef struct gbr_object_flush {
+  uint32_t index;
+  uint32_t tid;
+  float scale;
+  int32_t feature_flag;
+  float world_pos[4];
+  float world_rot_quat[4];
+} gbr_object_flush;
+
+/* object_context::flush_locations (object_context.cpp:819-830): writes the
+ * listed objects' state into the scene's descriptors (synchronous, like
+ * gbr_scene_set_descriptors). */
+gbr_status gbr_scene_flush_objects(gbr_scene* scene, const gbr_object_flush* objs, uint32_t n);
+
 gbr_status gbr_scene_set_lights(gbr_scene* scene, const gbr_light* lights, uint32_t n); /* n <= 256 */
 
 /* texture_context::alloc_gpu (texture_context.cpp:350-517): pack n square RGBA8
@@ -239,6 +261,29 @@ gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb);
  * reference's image sampler applies, pinned to float weights. */
 gbr_status gbr_post_godrays(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
                             const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
+
+/* engine::do_pseudo_aa (engine.cpp:1513-1516) -> do_pseudo_aa
+ * (cl2.cl:6437-6657): edge pixels -- where the neighbourhood's depth jumps by
+ * more than 100 or its normal turns by more than 20 degrees along exactly one
+ * row and one column -- get a weighted mix of the two sides' colours.  Reads
+ * the view's depth, id, normals (as gbr_outputs.normals) and RGBA8. */
+gbr_status gbr_post_pseudo_aa(gbr_scene* scene, const gbr_view* view, const uint32_t* depth, const uint32_t* id,
+                              const uint16_t* normals, const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
+
+/* engine::do_motion_blur (engine.cpp:1518-1536) -> do_motion_blur
+ * (cl2.cl:6714-6860): every drawn pixel is blurred along its screen motion
+ * since the previous frame -- its object's previous pose (descriptor history
+ * slot 1 when frame_id is even, 2 when odd) and the previous camera cam_old --
+ * mixed with the motion under this frame's camera by camera_contribution and
+ * scaled by strength (at most 50 taps).  Updates the history: objects with a
+ * pixel on screen get their current pose in the other slot, as the
+ * reference's kernel does.  frame_id and cam_old are object_context_data's
+ * frame_id (incremented after each render) and c_pos_old / c_rot_old (set by
+ * swap_buffers). */
+gbr_status gbr_post_motion_blur(gbr_scene* scene, const gbr_camera* cam, const gbr_camera* cam_old,
+                                const gbr_view* view, uint32_t frame_id, float strength, float camera_contribution,
+                                const uint32_t* depth, const uint32_t* id, const uint8_t* rgba_in, uint8_t* rgba_out,
+                                void* stream);
 
 /* Counters of the last render / shadow pass on this scene. */
 gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);

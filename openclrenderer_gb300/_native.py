@@ -13,8 +13,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libgbr.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
-SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_server.cu"]
-HEADERS = ["gbr_math.h", "gbr_internal.h", "gbr_scene.h"]
+SOURCES = ["gbr_kernels.cu", "gbr_api.cu", "gbr_batch.cu", "gbr_noalloc.cu", "gbr_server.cu", "gbr_post.cu"]
+HEADERS = ["gbr_math.h", "gbr_internal.h", "gbr_scene.h", "gbr_post.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE]
@@ -110,6 +110,11 @@ SIGNATURES = {
     "gbr_batch_destroy": (ctypes.c_int, [_P]),
     "gbr_render_view_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "gbr_post_godrays": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "gbr_post_pseudo_aa": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
+    "gbr_post_motion_blur": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P,
+                                            _P]),
+    "gbr_scene_flush_objects": (ctypes.c_int, [_P, _P, _U32]),
+    "gbr_scene_get_descriptors": (ctypes.c_int, [_P, _P, _U32]),
     "gbr_server_create": (ctypes.c_int, [_P, _U32, _P, _P]),
     "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),
     "gbr_server_poll": (ctypes.c_int, [_P, _P, _U32, _P, ctypes.c_int32]),

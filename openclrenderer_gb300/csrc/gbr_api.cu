@@ -453,6 +453,8 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->ws_shadow.release();
   s->ws_host.release();
   s->post_scratch.release();
+  s->post_seen.release();
+  s->flush_buf.release();
   s->world.release();
   s->objq.release();
   s->staging.release();
@@ -495,7 +497,11 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
   if (n) CU(cudaMemcpy(s->descs.p, d, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyHostToDevice));
   uint32_t mt = 0, mr = 0;
   bool has_rid = false;
+  s->host_tid.resize(n);
+  s->host_flags.resize(n);
   for (uint32_t i = 0; i < n; i++) {
+    s->host_tid[i] = d[i].tid;
+    s->host_flags[i] = d[i].feature_flag;
     mt = std::max(mt, d[i].tid);
     if (d[i].rid != 0xFFFFFFFFu) {
       mr = std::max(mr, d[i].rid);
@@ -508,6 +514,42 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
   s->ndescs = n;
   s->static_dirty = true;
   s->world_dirty = true;
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_get_descriptors(gbr_scene* s, gbr_obj_g_descriptor* d, uint32_t n) {
+  GBR_SCENE_LOCK(s);
+  TRY(check_scene(s));
+  if (n != s->ndescs) return fail(GBR_INVALID_ARG, "%u descriptors asked, the scene has %u", n, s->ndescs);
+  if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
+  CU(cudaDeviceSynchronize());
+  if (n) CU(cudaMemcpy(d, s->descs.p, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyDeviceToHost));
+  return GBR_OK;
+}
+
+gbr_status gbr_scene_flush_objects(gbr_scene* s, const gbr_object_flush* f, uint32_t n) {
+  GBR_SCENE_LOCK(s);
+  TRY(check_scene(s));
+  if (n && !f) return fail(GBR_INVALID_ARG, "null objects");
+  for (uint32_t i = 0; i < n; i++)
+    if (f[i].index >= s->ndescs) return fail(GBR_INVALID_ARG, "object %u: index %u of %u descriptors", i, f[i].index,
+                                            s->ndescs);
+  if (!n) return GBR_OK;
+  s->version++;  // captured batches re-capture
+  bool statics = false;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t o = f[i].index;
+    statics = statics || ((s->host_flags[o] | f[i].feature_flag) & 8) != 0;
+    s->host_tid[o] = f[i].tid;
+    s->host_flags[o] = f[i].feature_flag;
+  }
+  s->max_tid = s->host_tid.empty() ? 0 : *std::max_element(s->host_tid.begin(), s->host_tid.end());
+  TRY(s->flush_buf.reserve(n));
+  CU(cudaMemcpy(s->flush_buf.p, f, sizeof(gbr_object_flush) * n, cudaMemcpyHostToDevice));
+  CU(launch_flush_objects(s->descs.p, s->flush_buf.p, n, 0));
+  CU(cudaStreamSynchronize(0));
+  s->world_dirty = true;
+  if (statics) s->static_dirty = true;
   return GBR_OK;
 }
 
@@ -777,32 +819,6 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, st));
   if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
   CU(cudaStreamSynchronize(st));
-  return GBR_OK;
-}
-
-gbr_status gbr_post_godrays(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
-                            const uint8_t* rgba_in, uint8_t* rgba_out, void* stream) {
-  GBR_SCENE_LOCK(s);
-  TRY(check_scene(s));
-  TRY(validate_view(view));
-  if (!cam || !depth || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
-  const size_t P = (size_t)view->width * view->height * 4;
-  const bool in_place = rgba_out == rgba_in;
-  if (!in_place && rgba_out < rgba_in + P && rgba_in < rgba_out + P)
-    return fail(GBR_INVALID_ARG, "rgba_out partly overlaps rgba_in");
-  float cc[3], cs[3];
-  euler_cs(cam->rot, cc, cs);
-  const float fov = view->fov_const > 0 ? view->fov_const : gbr_fov_const_from_hfov(view->hfov_deg, view->width);
-  uint8_t* dst = rgba_out;
-  if (in_place) {
-    TRY(s->post_scratch.reserve(P));
-    dst = s->post_scratch.p;
-  }
-  const cudaStream_t st = (cudaStream_t)stream;
-  CU(launch_godrays(depth, rgba_in, dst, view->width, view->height, fov, s->lights.p,
-                    (uint32_t)s->host_lights.size(), cam->pos, cc, cs, st));
-  if (in_place) CU(cudaMemcpyAsync(rgba_out, dst, P, cudaMemcpyDeviceToDevice, st));
-  s->stats.launches += 1;
   return GBR_OK;
 }
 

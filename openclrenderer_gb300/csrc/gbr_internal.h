@@ -169,6 +169,15 @@ cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* siz
                         int32_t max_size, cudaStream_t st);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 // screenspace_godrays over a rendered view (RGBA8 in / out, distinct buffers).
+cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_flush* objs, uint32_t n,
+                                 cudaStream_t st);
+cudaError_t launch_pseudo_aa(const uint32_t* depth, const uint32_t* ids, const uint16_t* normals, const uint8_t* in,
+                             uint8_t* out, int W, int H, cudaStream_t st);
+cudaError_t launch_motion_blur(const gbr_triangle* tris, uint32_t ntris, gbr_obj_g_descriptor* descs, uint32_t ndescs,
+                               const uint32_t* depth, const uint32_t* ids, const uint8_t* in, uint8_t* out, int W,
+                               int H, float fov, const float cpos[3], const float cc[3], const float cs[3],
+                               const float opos[3], const float oc[3], const float os[3], uint32_t frame_id,
+                               float strength, float camera_contribution, uint32_t* seen, cudaStream_t st);
 cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* out, int W, int H, float fov,
                            const gbr_light* lights, uint32_t nlights, const float cpos[3], const float cc[3],
                            const float cs[3], cudaStream_t st);

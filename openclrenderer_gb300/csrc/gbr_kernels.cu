@@ -1324,72 +1324,6 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, views[s_id], S, srec, slights, x, y, colx, rowy);
 }
 
-// screenspace_godrays (cl2.cl:1792-1917) for pixel (x, y) of a view: light
-// shafts of every light with godray_intensity > 0, marched from the pixel
-// towards the light's screen position over the depth buffer.  cc / cs: the
-// camera's cosines and sines.  Returns the RGBA colour before quantisation.
-__device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* rgba_in, int W, int H, float fov,
-                        const gbr_light* __restrict__ lights, uint32_t nlights, f3 cpos, f3 cc, f3 cs) {
-  const float samples = 80.f;
-  const uint32_t my_depth = depth[(size_t)y * W + x];
-  f4 my_col = read_linear_rgba8(rgba_in, W, H, (float)x - 0.25f, (float)y - 0.25f);
-  const float decay_factor = 0.97f, weight = 0.01f;
-  const float step = 400.f / samples;  // max_length / samples
-  for (uint32_t i = 0; i < nlights; i++) {
-    const gbr_light& L = lights[i];
-    const float ray_intensity = L.godray_intensity;
-    if (ray_intensity <= 0) continue;
-    float idecay = 1.f;
-    f3 iter_col = mk3(0, 0, 0);
-    const f3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
-    const f3 slpos = depth_project1(rot_cs(lpos, cpos, cc, cs), (float)W, (float)H, fov);
-    f3 current = mk3((float)x, (float)y, fdiv((float)my_depth, kMulInt) * kDepthFar);
-    f3 dest = slpos;
-    const f3 original = current;
-    if (slpos.z < 0) dest = add3(sub3(current, dest), current);
-    const float vx = fabsf(current.x - dest.x), vy = fabsf(current.y - dest.y);
-    const float mnum = vx > vy ? vx : vy;
-    f3 dir = sub3(dest, current);
-    dir = mk3(fdiv(dir.x, mnum), fdiv(dir.y, mnum), fdiv(dir.z, mnum));
-    dir = mul3s(dir, step);
-    const f3 col = mk3(L.col[0], L.col[1], L.col[2]);
-    for (int j = 0; (float)j < mnum && (float)j < samples; j++) {
-      // the reference skips the rest of the march once it leaves the screen
-      if (current.x < 0 || current.y < 0 || current.x >= (float)W - 1.0f || current.y >= (float)H - 1.0f) break;
-      const uint32_t cdepth = depth[(size_t)((int)current.y) * W + (int)current.x];
-      const float fdepth = fdiv((float)cdepth, kMulInt) * kDepthFar;
-      f3 val = mk3(0, 0, 0);
-      if (fdepth < original.z - 5.0f && cdepth != 0xFFFFFFFFu) {
-        idecay *= 0.9f;
-        val = mul3s(col, ray_intensity);
-      }
-      val = mul3s(mul3s(val, idecay), weight);
-      iter_col = add3(iter_col, val);
-      idecay *= decay_factor;
-      current = add3(current, dir);
-    }
-    my_col.x += iter_col.x;
-    my_col.y += iter_col.y;
-    my_col.z += iter_col.z;
-  }
-  my_col.w = 1.0f;
-  const float exposure = 0.99f;
-  f4 r;
-  r.x = my_col.x * exposure; r.y = my_col.y * exposure; r.z = my_col.z * exposure; r.w = my_col.w * exposure;
-  return r;
-}
-
-// engine::draw_godrays (engine.cpp:1463-1482): one thread per pixel.
-__global__ void __launch_bounds__(256) k_godrays(const uint32_t* __restrict__ depth, const uint8_t* __restrict__ in,
-                                                 uint8_t* __restrict__ out, int W, int H, float fov,
-                                                 const gbr_light* __restrict__ lights, uint32_t nlights, f3 cpos,
-                                                 f3 cc, f3 cs) {
-  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
-  if (x >= W || y >= H) return;
-  const f4 c = godrays_pixel(x, y, depth, in, W, H, fov, lights, nlights, cpos, cc, cs);
-  reinterpret_cast<uint32_t*>(out)[(size_t)y * W + x] = pack_rgba(c.x, c.y, c.z, c.w);
-}
-
 // ---- texture atlas ----------------------------------------------------------------
 // Slot origin of texture descriptor tid as write_tex_array computes it
 // (cl2.cl:856-889).
@@ -1475,6 +1409,22 @@ __global__ void k_mip(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes
   uchar4 c = make_uchar4((unsigned char)f2u_sat(a0), (unsigned char)f2u_sat(a1), (unsigned char)f2u_sat(a2),
                          (unsigned char)f2u_sat(a3));
   write_tex(atlas, nums, sizes, dst, yx0, yx1, c);
+}
+
+// object::g_flush's writes (object.cpp:652-860): pose, scale, texture id and
+// feature flags of the listed descriptors.
+__global__ void k_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_flush* objs, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const gbr_object_flush f = objs[i];
+  gbr_obj_g_descriptor* G = descs + f.index;
+  for (int k = 0; k < 4; k++) {
+    G->world_pos[k] = f.world_pos[k];
+    G->world_rot_quat[k] = f.world_rot_quat[k];
+  }
+  G->scale = f.scale;
+  G->tid = f.tid;
+  G->feature_flag = f.feature_flag;
 }
 
 __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
@@ -1576,12 +1526,10 @@ cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* siz
   return cudaSuccess;
 }
 
-cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* out, int W, int H, float fov,
-                           const gbr_light* lights, uint32_t nlights, const float cpos[3], const float cc[3],
-                           const float cs[3], cudaStream_t st) {
-  dim3 grid((W + 15) / 16, (H + 15) / 16);
-  k_godrays<<<grid, 256, 0, st>>>(depth, in, out, W, H, fov, lights, nlights, mk3(cpos[0], cpos[1], cpos[2]),
-                                  mk3(cc[0], cc[1], cc[2]), mk3(cs[0], cs[1], cs[2]));
+cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_flush* objs, uint32_t n,
+                                 cudaStream_t st) {
+  if (!n) return cudaSuccess;
+  k_flush_objects<<<(n + 255) / 256, 256, 0, st>>>(descs, objs, n);
   return cudaGetLastError();
 }
 
@@ -1592,3 +1540,7 @@ cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st) 
 }
 
 }  // namespace gbr
+
+// Post passes over a rendered view (godrays, pseudo-AA, motion blur,
+// reflections): they share the device helpers above.
+#include "gbr_post.cuh"

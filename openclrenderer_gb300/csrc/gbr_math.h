@@ -512,6 +512,23 @@ GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy
   return r;
 }
 
+// short_to_float + decode_normal (cl2.cl:5597-5642): the ushort2 of the
+// normals buffer back to a unit vector; xy carry the direction, their length
+// the z component.
+GBR_HD f3 decode_normal(uint32_t sx, uint32_t sy) {
+  const float vx = fdiv((float)sx, 65535.0f) * 2.0f - 1.0f;
+  const float vy = fdiv((float)sy, 65535.0f) * 2.0f - 1.0f;
+  const float z = (vx * vx + vy * vy) * 2.0f - 1.0f;
+  const float l = fsqrt(vx * vx + vy * vy);
+  const float g = fsqrt(fmax_(1.0f - z * z, 0.0f));
+  return mk3(fdiv(vx, l) * g, fdiv(vy, l) * g, z);
+}
+
+// do_pseudo_aa's edge angle: cos(20.f * 2 * M_PI / 360.f) with the float
+// M_PI of cl2.cl, the argument rounded in float and the cosine rounded from
+// double (0.9396926f).
+constexpr float kAACos = 0x1.e11f64p-1f;
+
 // Six cube-face Euler rotations (cl2.cl:4487-4511, 2538-2558) as float
 // angles; their cosines and sines are rounded from double on the host.
 GBR_HD f3 face_angles(int face) {

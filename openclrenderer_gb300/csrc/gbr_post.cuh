@@ -1,0 +1,285 @@
+// gbr_post.cuh -- post passes over a rendered view: the reference's
+// screenspace_godrays, do_pseudo_aa, do_motion_blur and
+// screenspace_reflections (cl2.cl:1792-1917, 6437-7356), behind
+// engine::draw_godrays / do_pseudo_aa / do_motion_blur /
+// draw_screenspace_reflections (engine.cpp:1463-1536).  Included at the end
+// of gbr_kernels.cu, whose device helpers they use.  Every pass reads one
+// RGBA8 image and writes another; a pixel the reference leaves unwritten keeps
+// its input colour.
+#pragma once
+
+namespace gbr {
+
+// screenspace_godrays (cl2.cl:1792-1917) for pixel (x, y) of a view: light
+// shafts of every light with godray_intensity > 0, marched from the pixel
+// towards the light's screen position over the depth buffer.  cc / cs: the
+// camera's cosines and sines.  Returns the RGBA colour before quantisation.
+__device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* rgba_in, int W, int H, float fov,
+                        const gbr_light* __restrict__ lights, uint32_t nlights, f3 cpos, f3 cc, f3 cs) {
+  const float samples = 80.f;
+  const uint32_t my_depth = depth[(size_t)y * W + x];
+  f4 my_col = read_linear_rgba8(rgba_in, W, H, (float)x - 0.25f, (float)y - 0.25f);
+  const float decay_factor = 0.97f, weight = 0.01f;
+  const float step = 400.f / samples;  // max_length / samples
+  for (uint32_t i = 0; i < nlights; i++) {
+    const gbr_light& L = lights[i];
+    const float ray_intensity = L.godray_intensity;
+    if (ray_intensity <= 0) continue;
+    float idecay = 1.f;
+    f3 iter_col = mk3(0, 0, 0);
+    const f3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
+    const f3 slpos = depth_project1(rot_cs(lpos, cpos, cc, cs), (float)W, (float)H, fov);
+    f3 current = mk3((float)x, (float)y, fdiv((float)my_depth, kMulInt) * kDepthFar);
+    f3 dest = slpos;
+    const f3 original = current;
+    if (slpos.z < 0) dest = add3(sub3(current, dest), current);
+    const float vx = fabsf(current.x - dest.x), vy = fabsf(current.y - dest.y);
+    const float mnum = vx > vy ? vx : vy;
+    f3 dir = sub3(dest, current);
+    dir = mk3(fdiv(dir.x, mnum), fdiv(dir.y, mnum), fdiv(dir.z, mnum));
+    dir = mul3s(dir, step);
+    const f3 col = mk3(L.col[0], L.col[1], L.col[2]);
+    for (int j = 0; (float)j < mnum && (float)j < samples; j++) {
+      // the reference skips the rest of the march once it leaves the screen
+      if (current.x < 0 || current.y < 0 || current.x >= (float)W - 1.0f || current.y >= (float)H - 1.0f) break;
+      const uint32_t cdepth = depth[(size_t)((int)current.y) * W + (int)current.x];
+      const float fdepth = fdiv((float)cdepth, kMulInt) * kDepthFar;
+      f3 val = mk3(0, 0, 0);
+      if (fdepth < original.z - 5.0f && cdepth != 0xFFFFFFFFu) {
+        idecay *= 0.9f;
+        val = mul3s(col, ray_intensity);
+      }
+      val = mul3s(mul3s(val, idecay), weight);
+      iter_col = add3(iter_col, val);
+      idecay *= decay_factor;
+      current = add3(current, dir);
+    }
+    my_col.x += iter_col.x;
+    my_col.y += iter_col.y;
+    my_col.z += iter_col.z;
+  }
+  my_col.w = 1.0f;
+  const float exposure = 0.99f;
+  f4 r;
+  r.x = my_col.x * exposure; r.y = my_col.y * exposure; r.z = my_col.z * exposure; r.w = my_col.w * exposure;
+  return r;
+}
+
+// engine::draw_godrays (engine.cpp:1463-1482): one thread per pixel.
+__global__ void __launch_bounds__(256) k_godrays(const uint32_t* __restrict__ depth, const uint8_t* __restrict__ in,
+                                                 uint8_t* __restrict__ out, int W, int H, float fov,
+                                                 const gbr_light* __restrict__ lights, uint32_t nlights, f3 cpos,
+                                                 f3 cc, f3 cs) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+  if (x >= W || y >= H) return;
+  const f4 c = godrays_pixel(x, y, depth, in, W, H, fov, lights, nlights, cpos, cc, cs);
+  reinterpret_cast<uint32_t*>(out)[(size_t)y * W + x] = pack_rgba(c.x, c.y, c.z, c.w);
+}
+
+cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* out, int W, int H, float fov,
+                           const gbr_light* lights, uint32_t nlights, const float cpos[3], const float cc[3],
+                           const float cs[3], cudaStream_t st) {
+  dim3 grid((W + 15) / 16, (H + 15) / 16);
+  k_godrays<<<grid, 256, 0, st>>>(depth, in, out, W, H, fov, lights, nlights, mk3(cpos[0], cpos[1], cpos[2]),
+                                  mk3(cc[0], cc[1], cc[2]), mk3(cs[0], cs[1], cs[2]));
+  return cudaGetLastError();
+}
+
+// ---- do_pseudo_aa (cl2.cl:6437-6657) ---------------------------------------
+// Pixel (x, y) is an edge when exactly one horizontal and one vertical
+// neighbour, and at least one diagonal, differ from it: by more than 100 depth
+// units (test 0), or by more than 20 degrees of normal (test 1).  The first
+// test that finds an edge replaces the colour with 0.65 x the mean of the
+// similar neighbours + 0.35 x the mean of the differing ones.
+__device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int H, const uint32_t* __restrict__ depth,
+                                                const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
+                                                f3* out) {
+  const size_t p = (size_t)y * W + x;
+  const float here = fdiv((float)depth[p], kMulInt) * kDepthFar;
+  const ushort2 np = nrm[p];
+  const f3 n0 = fast_normalize3(decode_normal(np.x, np.y));
+  int horiz[2] = {0, 0}, vert[2] = {0, 0}, diag[2] = {0, 0};
+  f3 same[2] = {mk3(0, 0, 0), mk3(0, 0, 0)}, other[2] = {mk3(0, 0, 0), mk3(0, 0, 0)};
+  float nsame[2] = {0, 0}, nother[2] = {0, 0};
+#pragma unroll
+  for (int dy = -1; dy <= 1; dy++) {
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      const size_t q = (size_t)(y + dy) * W + (x + dx);
+      const float d = fdiv((float)depth[q], kMulInt) * kDepthFar;
+      const ushort2 nq = nrm[q];
+      const f3 n = decode_normal(nq.x, nq.y);
+      const uchar4 t = in[q];
+      const f3 c = mk3(fdiv((float)t.x, 255.0f), fdiv((float)t.y, 255.0f), fdiv((float)t.z, 255.0f));
+      const bool edge[2] = {fabsf(d - here) > 100.0f, dot3(n0, n) < kAACos};
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        if (edge[k]) {
+          if (dx == dy || dx == -dy) diag[k]++;
+          else if (dx != 0) horiz[k]++;
+          else vert[k]++;
+          other[k] = add3(other[k], c);
+          nother[k] += 1.0f;
+        } else {
+          same[k] = add3(same[k], c);
+          nsame[k] += 1.0f;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 2; k++) {
+    if (horiz[k] == 1 && vert[k] == 1 && diag[k] >= 1) {
+      const f3 m = mk3(fdiv(same[k].x, nsame[k]), fdiv(same[k].y, nsame[k]), fdiv(same[k].z, nsame[k]));
+      const f3 o = mk3(fdiv(other[k].x, nother[k]), fdiv(other[k].y, nother[k]), fdiv(other[k].z, nother[k]));
+      *out = add3(mul3s(m, 0.65f), mul3s(o, 0.35f));
+      return true;
+    }
+  }
+  return false;
+}
+
+// engine::do_pseudo_aa (engine.cpp:1513-1516): one thread per pixel.
+__global__ void __launch_bounds__(256) k_pseudo_aa(const uint32_t* __restrict__ depth, const uint32_t* __restrict__ ids,
+                                                   const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
+                                                   uchar4* __restrict__ out, int W, int H) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  f3 c;
+  const bool inner = x >= 1 && y >= 1 && x < W - 1 && y < H - 1;
+  if (inner && depth[p] != kDepthClear && ids[p] != kNoId && pseudo_aa_pixel(x, y, W, H, depth, nrm, in, &c)) {
+    reinterpret_cast<uint32_t*>(out)[p] = pack_rgba(c.x, c.y, c.z, 1.0f);
+  } else {
+    out[p] = in[p];
+  }
+}
+
+cudaError_t launch_pseudo_aa(const uint32_t* depth, const uint32_t* ids, const uint16_t* normals, const uint8_t* in,
+                             uint8_t* out, int W, int H, cudaStream_t st) {
+  dim3 grid((W + 15) / 16, (H + 15) / 16);
+  k_pseudo_aa<<<grid, 256, 0, st>>>(depth, ids, reinterpret_cast<const ushort2*>(normals),
+                                    reinterpret_cast<const uchar4*>(in), reinterpret_cast<uchar4*>(out), W, H);
+  return cudaGetLastError();
+}
+
+// ---- do_motion_blur (cl2.cl:6714-6860) ---------------------------------------
+// The pixel's surface point, in its object's frame, is carried through the
+// object's pose of the previous frame (history slot 1 on even frame ids, 2 on
+// odd) and projected with this frame's and the previous frame's camera; the
+// blend of the two screen motions (camera_contribution), times strength and
+// capped at 50 px, is averaged over that many bilinear taps centred on the
+// pixel.  Objects with a pixel on screen are marked in seen[] for the history
+// update.
+struct MotionCam {
+  f3 cpos, cc, cs, opos, oc, os;
+  float fov, strength, cam_w;
+  uint32_t frame_id;
+};
+
+__global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restrict__ tris,
+                                                     const gbr_obj_g_descriptor* __restrict__ descs,
+                                                     const uint32_t* __restrict__ depth,
+                                                     const uint32_t* __restrict__ ids, const uint8_t* __restrict__ in,
+                                                     uint8_t* __restrict__ out, int W, int H, MotionCam a,
+                                                     uint32_t* __restrict__ seen, uint32_t ntris) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  const uint32_t d = depth[p], id = ids[p];
+  uint32_t* o32 = reinterpret_cast<uint32_t*>(out);
+  if (d == kDepthClear || id == kNoId || (id >> 1) >= ntris) {  // (an id past the triangles: left as it is)
+    o32[p] = reinterpret_cast<const uint32_t*>(in)[p];
+    return;
+  }
+  const uint32_t obj = __ldg(&tris[id >> 1].vertices[0].object_id);
+  if (!seen[obj]) seen[obj] = 1u;
+  const gbr_obj_g_descriptor* G = descs + obj;
+  const float dist = fdiv((float)d, kMulInt) * kDepthFar;
+  const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, a.fov), fdiv(((float)y - (float)H / 2.0f) * dist, a.fov),
+                       dist);
+  const f3 world = add3(back_rot_cs(local, mk3(0, 0, 0), a.cc, a.cs), a.cpos);
+  const f3 objl = back_rot_quat(sub3(world, ld3(G->world_pos)), ld4(G->world_rot_quat));
+  const bool even = (a.frame_id & 1u) == 0;
+  const f3 opos = ld3(even ? G->old_world_pos_1 : G->old_world_pos_2);
+  const f4 oq = ld4(even ? G->old_world_rot_quat_1 : G->old_world_rot_quat_2);
+  const f3 last = add3(rot_quat(objl, oq), opos);
+  const f3 nocam = depth_project1(rot_cs(last, a.cpos, a.cc, a.cs), (float)W, (float)H, a.fov);
+  const f3 prev = depth_project1(rot_cs(last, a.opos, a.oc, a.os), (float)W, (float)H, a.fov);
+  f4 acc;
+  if (prev.z < 20.0f) {
+    acc = read_linear_rgba8(in, W, H, (float)x + 0.5f, (float)y + 0.5f);
+  } else {
+    float mx = (float)x - prev.x, my = (float)y - prev.y;
+    const float nx = (float)x - nocam.x, ny = (float)y - nocam.y;
+    mx = a.cam_w * mx + (1.0f - a.cam_w) * nx;
+    my = a.cam_w * my + (1.0f - a.cam_w) * ny;
+    mx = mx * a.strength;
+    my = my * a.strength;
+    int n = f2i_sat(fmax_(fabsf(mx), fabsf(my)) + 1.0f);
+    if (n > 50) {
+      mx = fdiv(mx, (float)n) * 50.0f;
+      my = fdiv(my, (float)n) * 50.0f;
+      n = 50;
+    }
+    float sx = 0.0f, sy = 0.0f;
+    if (n != 0) {
+      sx = fdiv(mx, (float)n);
+      sy = fdiv(my, (float)n);
+    }
+    float cx = (float)x - fdiv(mx, 2.0f), cy = (float)y - fdiv(my, 2.0f);
+    acc.x = acc.y = acc.z = acc.w = 0.0f;
+    float cnt = 0.0f;
+    for (int i = 0; i < n; i++, cx += sx, cy += sy) {
+      if (cx < 0 || cx >= (float)W || cy < 0 || cy >= (float)H) continue;
+      const f4 c = read_linear_rgba8(in, W, H, cx + 0.5f, cy + 0.5f);
+      acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+      cnt += 1.0f;
+    }
+    if (cnt != 0.0f) {
+      acc.x = fdiv(acc.x, cnt); acc.y = fdiv(acc.y, cnt); acc.z = fdiv(acc.z, cnt); acc.w = fdiv(acc.w, cnt);
+    }
+  }
+  o32[p] = pack_rgba(acc.x, acc.y, acc.z, acc.w);
+}
+
+// The pose-history writes of do_motion_blur (cl2.cl:6771-6786): every object
+// with a pixel on screen stores its current pose in the slot the next frame
+// reads (2 on even frame ids, 1 on odd); the marks are cleared.
+__global__ void k_motion_history(gbr_obj_g_descriptor* descs, uint32_t* seen, uint32_t n, uint32_t frame_id) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n || !seen[o]) return;
+  seen[o] = 0;
+  gbr_obj_g_descriptor* G = descs + o;
+  float* pos = (frame_id & 1u) == 0 ? G->old_world_pos_2 : G->old_world_pos_1;
+  float* q = (frame_id & 1u) == 0 ? G->old_world_rot_quat_2 : G->old_world_rot_quat_1;
+  for (int k = 0; k < 3; k++) pos[k] = G->world_pos[k];
+  for (int k = 0; k < 4; k++) q[k] = G->world_rot_quat[k];
+}
+
+cudaError_t launch_motion_blur(const gbr_triangle* tris, uint32_t ntris, gbr_obj_g_descriptor* descs, uint32_t ndescs,
+                               const uint32_t* depth, const uint32_t* ids, const uint8_t* in, uint8_t* out, int W,
+                               int H, float fov, const float cpos[3], const float cc[3], const float cs[3],
+                               const float opos[3], const float oc[3], const float os[3], uint32_t frame_id,
+                               float strength, float camera_contribution, uint32_t* seen, cudaStream_t st) {
+  MotionCam a;
+  a.cpos = mk3(cpos[0], cpos[1], cpos[2]);
+  a.cc = mk3(cc[0], cc[1], cc[2]);
+  a.cs = mk3(cs[0], cs[1], cs[2]);
+  a.opos = mk3(opos[0], opos[1], opos[2]);
+  a.oc = mk3(oc[0], oc[1], oc[2]);
+  a.os = mk3(os[0], os[1], os[2]);
+  a.fov = fov;
+  a.strength = strength;
+  a.cam_w = camera_contribution;
+  a.frame_id = frame_id;
+  dim3 grid((W + 15) / 16, (H + 15) / 16);
+  k_motion_blur<<<grid, 256, 0, st>>>(tris, descs, depth, ids, in, out, W, H, a, seen, ntris);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !ndescs) return e;
+  k_motion_history<<<(ndescs + 255) / 256, 256, 0, st>>>(descs, seen, ndescs, frame_id);
+  return cudaGetLastError();
+}
+
+}  // namespace gbr

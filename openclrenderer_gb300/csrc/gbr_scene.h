@@ -129,6 +129,9 @@ struct gbr_scene {
   bool world_dirty = true;    // triangles or descriptors changed since k_world ran
   gbr::DevBuf<gbr_obj_g_descriptor> descs;
   uint32_t ndescs = 0;
+  std::vector<uint32_t> host_tid;      // per descriptor, for the texture-id bound
+  std::vector<int32_t> host_flags;     // per descriptor feature flags
+  gbr::DevBuf<gbr_object_flush> flush_buf;
   gbr::DevBuf<gbr_light> lights;
   std::vector<gbr_light> host_lights;
   gbr::DevBuf<uchar4> atlas;
@@ -143,6 +146,7 @@ struct gbr_scene {
   bool static_dirty = true;
   gbr::WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host
   gbr::DevBuf<uint8_t> post_scratch;         // in-place post passes write here first
+  gbr::DevBuf<uint32_t> post_seen;           // motion blur: objects on screen (cleared after use)
   gbr::HostBuf staging;         // counters read back: view at 0, shadow at 256
   bool shadow_pending = false;  // a shadow pass whose counters are not checked yet
   cudaStream_t shadow_stream = nullptr;

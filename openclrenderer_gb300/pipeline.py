@@ -111,6 +111,12 @@ class GpuScene:
         descs = np.ascontiguousarray(descs, S.OBJ_DESC)
         _native.check(self.L.gbr_scene_set_descriptors(self.h, _np_ptr(descs), len(descs)))
 
+    def flush_objects(self, objs):
+        """object_context::flush_locations: pose / scale / tid / flags of the
+        listed descriptors (S.OBJECT_FLUSH records); the history slots stay."""
+        objs = np.ascontiguousarray(objs, S.OBJECT_FLUSH)
+        _native.check(self.L.gbr_scene_flush_objects(self.h, _np_ptr(objs), len(objs)))
+
     def set_lights(self, lights):
         lights = np.ascontiguousarray(lights, S.LIGHT)
         _native.check(self.L.gbr_scene_set_lights(self.h, _np_ptr(lights), len(lights)))
@@ -199,6 +205,38 @@ class GpuScene:
         _native.check(self.L.gbr_post_godrays(self.h, _np_ptr(cam), _np_ptr(view), _t_ptr(out.depth),
                                               _t_ptr(out.rgba), _t_ptr(rgba_out), _stream_ptr(stream)))
         return rgba_out
+
+    def post_pseudo_aa(self, view, out, rgba_out=None, stream=None):
+        """engine::do_pseudo_aa over a rendered OutputSet (normals required)."""
+        import torch
+        view = np.asarray(view, S.VIEW).reshape(1)
+        if rgba_out is None:
+            rgba_out = torch.empty_like(out.rgba)
+        _native.check(self.L.gbr_post_pseudo_aa(self.h, _np_ptr(view), _t_ptr(out.depth), _t_ptr(out.id),
+                                                _t_ptr(out.normals), _t_ptr(out.rgba), _t_ptr(rgba_out),
+                                                _stream_ptr(stream)))
+        return rgba_out
+
+    def post_motion_blur(self, cam, cam_old, view, out, frame_id, strength=1.0, camera_contribution=1.0,
+                         rgba_out=None, stream=None):
+        """engine::do_motion_blur over a rendered OutputSet; updates the pose history."""
+        import torch
+        cam = np.asarray(cam, S.CAMERA).reshape(1)
+        cam_old = np.asarray(cam_old, S.CAMERA).reshape(1)
+        view = np.asarray(view, S.VIEW).reshape(1)
+        if rgba_out is None:
+            rgba_out = torch.empty_like(out.rgba)
+        _native.check(self.L.gbr_post_motion_blur(self.h, _np_ptr(cam), _np_ptr(cam_old), _np_ptr(view),
+                                                  int(frame_id), float(strength), float(camera_contribution),
+                                                  _t_ptr(out.depth), _t_ptr(out.id), _t_ptr(out.rgba),
+                                                  _t_ptr(rgba_out), _stream_ptr(stream)))
+        return rgba_out
+
+    def descriptors(self, n):
+        """The scene's n descriptors as they are on the device."""
+        d = np.zeros(n, S.OBJ_DESC)
+        _native.check(self.L.gbr_scene_get_descriptors(self.h, _np_ptr(d), n))
+        return d
 
     def stats(self):
         st = np.zeros(1, S.STATS)

@@ -26,6 +26,9 @@ LIGHT = np.dtype([
     ("is_static", "<i4"), ("pad_", "<u4", 2),
 ])
 CAMERA = np.dtype([("pos", "<f4", 4), ("rot", "<f4", 4)])
+# gbr_object_flush: what object::g_flush writes (48 bytes)
+OBJECT_FLUSH = np.dtype([("index", "<u4"), ("tid", "<u4"), ("scale", "<f4"), ("feature_flag", "<i4"),
+                         ("world_pos", "<f4", 4), ("world_rot_quat", "<f4", 4)])
 VIEW = np.dtype([
     ("width", "<i4"), ("height", "<i4"), ("fov_const", "<f4"), ("hfov_deg", "<f4"),
     ("clear_col", "<f4", 4), ("use_linear", "<u4"), ("flags", "<u4"),

@@ -19,7 +19,8 @@ import subprocess
 import sys
 
 ROOTS = ["prearrange", "prearrange_realtime_shadowing", "kernel1", "kernel1_realtime_shadowing",
-         "kernel2", "kernel3", "update_gpu_tex", "generate_mips", "generate_mip_mips", "screenspace_godrays"]
+         "kernel2", "kernel3", "update_gpu_tex", "generate_mips", "generate_mip_mips", "screenspace_godrays",
+         "do_pseudo_aa", "do_motion_blur", "screenspace_reflections"]
 
 DEFINES = ["SCREENWIDTH=gbr_ref_W", "SCREENHEIGHT=gbr_ref_H", "FOV_CONST=gbr_ref_FOV",
            "LIGHTBUFFERDIM=1024", "SHADOWBIAS=50", "depth_icutoff=20", "AMBIENT=0.2f",

@@ -70,6 +70,16 @@ struct Lazy {
   }
 };
 
+// The reference's own per-frame buffers, kept for a post pass.
+struct Frame {
+  Lazy frags{(size_t)1 << 36};
+  std::vector<float4> cut;
+  std::vector<uint> b_before;   // first cutdown slot of each triangle
+  std::vector<uint> raw_ids;    // kernel2's id image: fragment indices
+  std::vector<ushort2> nrm;
+  uint nfrag = 0;
+};
+
 }  // namespace
 
 extern "C" {
@@ -77,22 +87,26 @@ extern "C" {
 // One view: prearrange -> kernel1 -> kernel2 -> kernel3.  cam = pos[4], rot[4].
 // Outputs: depth u32, canonical id u32, rgba u8 (quantised as the product does),
 // normals ushort2 (may be null).  Returns the fragment count, or -1.
-int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const void* lights, uint32_t nlights,
-                   const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
-                   const uint32_t* shadow_dyn, const uint32_t* shadow_static, const float* cam, int W, int H,
-                   float fov, uint32_t use_linear, const float* clear, uint32_t* depth, uint32_t* ids,
-                   uint8_t* rgba, uint16_t* normals, int nthreads, int ordered) {
+int64_t ref_render_frame(const void* tris_in, uint32_t ntris, const void* descs, const void* lights,
+                         uint32_t nlights, const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes,
+                         uint32_t mipmap_start, const uint32_t* shadow_dyn, const uint32_t* shadow_static,
+                         const float* cam, int W, int H, float fov, uint32_t use_linear, const float* clear,
+                         uint32_t* depth, uint32_t* ids, uint8_t* rgba, uint16_t* normals, int nthreads, int ordered,
+                         Frame* keep) {
   gbr_ref_W = W;
   gbr_ref_H = H;
   gbr_ref_FOV = fov;
   auto* tris = (struct triangle*)const_cast<void*>(tris_in);
   auto* gobj = (struct obj_g_descriptor*)const_cast<void*>(descs);
   const size_t P = (size_t)W * H;
-  Lazy fragbuf((size_t)1 << 36);
-  if (!fragbuf.p) return -1;
-  uint* frags = (uint*)fragbuf.p;
-  std::vector<float4> cut((size_t)ntris * 6 + 6);
-  std::vector<uint> b_before(ntris);
+  Frame local_frame;
+  Frame& F = keep ? *keep : local_frame;
+  if (!F.frags.p) return -1;
+  uint* frags = (uint*)F.frags.p;
+  std::vector<float4>& cut = F.cut;
+  cut.assign((size_t)ntris * 6 + 6, float4(0.f));
+  std::vector<uint>& b_before = F.b_before;
+  b_before.assign(ntris, 0);
   uint tri_num = ntris, maxlen = 0xFFFFFFFFu, frag_count = 0, cut_count = 0;
   float4 c_pos(cam[0], cam[1], cam[2], cam[3]), c_rot(cam[4], cam[5], cam[6], cam[7]);
   if (ordered) {
@@ -114,6 +128,7 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
     });
   }
   const uint nfrag = frag_count;
+  F.nfrag = nfrag;
   for (size_t p = 0; p < P; p++) depth[p] = 0xFFFFFFFFu;
   image2d_t idimg{ids, W, H, 0};
   for (size_t p = 0; p < P; p++) ids[p] = 0xFFFFFFFFu;
@@ -128,7 +143,8 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
   });
   std::vector<float> screen(P * 4, 0.f);
   std::vector<uint> to_clear(P);
-  std::vector<ushort2> nrm(P);
+  std::vector<ushort2>& nrm = F.nrm;
+  nrm.assign(P, ushort2{0, 0});
   image2d_t scr{screen.data(), W, H, 2}, backup{nullptr, W, H, 2}, blend{nullptr, W, H, 2};
   uint lnum = nlights;
   float4 clear_col(clear[0], clear[1], clear[2], clear[3]);
@@ -147,12 +163,14 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
             const_cast<uint*>(shadow_dyn), const_cast<uint*>(shadow_static), to_clear.data(), frags, cut.data(),
             clear_col, 0, nrm.data(), 0, nullptr, blend, mipmap_start, use_linear);
   });
+  if (keep) F.raw_ids.assign(ids, ids + P);
   for (size_t p = 0; p < P; p++) {
     for (int k = 0; k < 4; k++) rgba[p * 4 + k] = (uint8_t)gbr::quant8(screen[p * 4 + k]);
+    bool drawn = depth[p] != 0xFFFFFFFFu && ids[p] != 0xFFFFFFFFu;
+    if (!drawn) nrm[p] = ushort2{0, 0};
     if (normals) {
-      bool drawn = depth[p] != 0xFFFFFFFFu && ids[p] != 0xFFFFFFFFu;
-      normals[p * 2] = drawn ? nrm[p].x : 0;
-      normals[p * 2 + 1] = drawn ? nrm[p].y : 0;
+      normals[p * 2] = nrm[p].x;
+      normals[p * 2 + 1] = nrm[p].y;
     }
     if (ordered && ids[p] != 0xFFFFFFFFu) {
       uint f = ids[p];
@@ -162,6 +180,78 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
     }
   }
   return (int64_t)nfrag;
+}
+
+int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const void* lights, uint32_t nlights,
+                   const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                   const uint32_t* shadow_dyn, const uint32_t* shadow_static, const float* cam, int W, int H,
+                   float fov, uint32_t use_linear, const float* clear, uint32_t* depth, uint32_t* ids,
+                   uint8_t* rgba, uint16_t* normals, int nthreads, int ordered) {
+  return ref_render_frame(tris_in, ntris, descs, lights, nlights, atlas, nums, sizes, mipmap_start, shadow_dyn,
+                          shadow_static, cam, W, H, fov, use_linear, clear, depth, ids, rgba, normals, nthreads,
+                          ordered, nullptr);
+}
+
+// A post pass over one rendered frame, with the reference's own fragment
+// records, cutdown triangles and kernel2 id image (engine.cpp:1463-1531):
+//   kind 0 do_pseudo_aa, 1 do_motion_blur, 2 screenspace_reflections.
+// in_screen is the frame's RGBA8 (as the product keeps it); the output image
+// starts as a copy of it, so pixels the pass leaves unwritten keep the input.
+// Pixels with depth but no id (kernel2's test failed everywhere) would read a
+// stale id in the reference; they are left unwritten.  descs is updated by
+// do_motion_blur's pose-history writes.  params: frame_id, strength,
+// camera_contribution; cam_old = pos[4], rot[4] of the previous frame.
+// Outputs: rgba (the frame), rgba_post.
+int64_t ref_post(int kind, const void* tris_in, uint32_t ntris, void* descs, const void* lights, uint32_t nlights,
+                 const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                 const uint32_t* shadow_dyn, const uint32_t* shadow_static, const float* cam, const float* cam_old,
+                 int W, int H, float fov, uint32_t use_linear, const float* clear, uint32_t frame_id, float strength,
+                 float camera_contribution, uint32_t* depth, uint32_t* ids, uint8_t* rgba, uint16_t* normals,
+                 uint8_t* rgba_post) {
+  Frame F;
+  const int64_t nf = ref_render_frame(tris_in, ntris, descs, lights, nlights, atlas, nums, sizes, mipmap_start,
+                                      shadow_dyn, shadow_static, cam, W, H, fov, use_linear, clear, depth, ids, rgba,
+                                      normals, 1, 1, &F);
+  if (nf < 0) return nf;
+  auto* tris = (struct triangle*)const_cast<void*>(tris_in);
+  auto* gobj = (struct obj_g_descriptor*)descs;
+  const size_t P = (size_t)W * H;
+  // the id image the post kernels read: fragment indices; pixels without one
+  // point at fragment 0 (read by do_pseudo_aa, its value unused)
+  std::vector<uint> raw(F.raw_ids);
+  for (size_t p = 0; p < P; p++)
+    if (raw[p] == 0xFFFFFFFFu) raw[p] = 0;
+  uint zero_frag[5] = {0, 0, 0, 0, 0};
+  uint* frags = F.nfrag ? (uint*)F.frags.p : zero_frag;
+  image2d_t idimg{raw.data(), W, H, 0};
+  image2d_t in{rgba, W, H, 1};
+  std::vector<float> out(P * 4), front(P * 4);
+  for (size_t i = 0; i < P * 4; i++) out[i] = front[i] = rgba[i] / 255.0f;
+  image2d_t o{out.data(), W, H, 2}, fr{front.data(), W, H, 2};
+  float4 c_pos(cam[0], cam[1], cam[2], cam[3]), c_rot(cam[4], cam[5], cam[6], cam[7]);
+  float4 c_pos_old(cam_old[0], cam_old[1], cam_old[2], cam_old[3]);
+  float4 c_rot_old(cam_old[4], cam_old[5], cam_old[6], cam_old[7]);
+  // one thread: do_motion_blur's pose-history writes from every pixel of an
+  // object store the same values
+  for (size_t p = 0; p < P; p++) {
+    if (depth[p] != 0xFFFFFFFFu && F.raw_ids[p] == 0xFFFFFFFFu) continue;
+    gbr_ref_gid[0] = p % W;
+    gbr_ref_gid[1] = p / W;
+    if (kind == 0)
+      do_pseudo_aa(idimg, frags, in, o, fr, F.cut.data(), depth, F.nrm.data());
+    else if (kind == 1)
+      do_motion_blur(idimg, frags, in, o, F.cut.data(), depth, gobj, frame_id, c_pos, c_rot, c_pos_old, c_rot_old,
+                     strength, camera_contribution);
+    else
+      screenspace_reflections(0, tris, idimg, frags, in, o, F.cut.data(), depth, gobj, frame_id, c_pos, c_rot,
+                              c_pos_old, c_rot_old, (uchar4*)atlas, const_cast<uint*>(nums),
+                              const_cast<uint*>(sizes), mipmap_start);
+  }
+  for (size_t i = 0; i < P * 4; i++) rgba_post[i] = (uint8_t)gbr::quant8(out[i]);
+  if (kind == 0)
+    for (size_t i = 0; i < P * 4; i++)
+      if (out[i] != front[i]) return -2;  // the two screens must agree
+  return nf;
 }
 
 // Cubemaps of every shadow light (dynamic: lights with shadow == 1; static:

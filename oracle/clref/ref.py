@@ -26,6 +26,10 @@ def lib(features=False):
         L.ref_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32, P, P, P,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P, P, P, P, P,
                                  ctypes.c_int, ctypes.c_int]
+        L.ref_post.restype = ctypes.c_int64
+        L.ref_post.argtypes = [ctypes.c_int, P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32,
+                               P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P,
+                               ctypes.c_uint32, ctypes.c_float, ctypes.c_float, P, P, P, P, P]
         L.ref_shadow.restype = None
         L.ref_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int, ctypes.c_int]
         L.ref_godrays.restype = None
@@ -89,6 +93,43 @@ def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_
                           _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
                           _p(rgba), _p(normals), nthreads, 1 if ordered else 0)
     return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "fragments": int(nf)}
+
+
+POST_KINDS = {"pseudo_aa": 0, "motion_blur": 1, "reflections": 2}
+
+
+def post(kind, scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_dyn=None, shadow_static=None,
+         cam_old=None, frame_id=0, strength=1.0, camera_contribution=1.0):
+    """One reference frame followed by a post pass (do_pseudo_aa,
+    do_motion_blur or screenspace_reflections) over the reference's own
+    fragment buffers.  Returns the frame (depth, id, rgba, normals), the pass's
+    RGBA8 ("post") and the descriptors after the pass ("descs")."""
+    W, H = int(view["width"]), int(view["height"])
+    if shadow_dyn is None:
+        shadow_dyn = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    if shadow_static is None:
+        shadow_static = np.full((1, 6, 1024, 1024), 0xFFFFFFFF, np.uint32)
+    c = np.concatenate([np.asarray(cam["pos"], np.float32), np.asarray(cam["rot"], np.float32)])
+    co = c if cam_old is None else np.concatenate([np.asarray(cam_old["pos"], np.float32),
+                                                   np.asarray(cam_old["rot"], np.float32)])
+    clear = np.asarray(view["clear_col"], np.float32)
+    descs = np.array(scene.descs, copy=True)
+    depth = np.empty((H, W), np.uint32)
+    ids = np.empty((H, W), np.uint32)
+    rgba = np.empty((H, W, 4), np.uint8)
+    normals = np.empty((H, W, 2), np.uint16)
+    out = np.empty((H, W, 4), np.uint8)
+    nums = np.ascontiguousarray(nums, np.uint32)
+    page_sizes = np.ascontiguousarray(page_sizes, np.uint32)
+    nf = lib().ref_post(POST_KINDS[kind], _p(scene.tris), len(scene.tris), _p(descs), _p(scene.lights),
+                        len(scene.lights), _p(atlas), _p(nums), _p(page_sizes), mipmap_start, _p(shadow_dyn),
+                        _p(shadow_static), _p(c), _p(co), W, H, float(fov), int(view["use_linear"]), _p(clear),
+                        int(frame_id), float(strength), float(camera_contribution), _p(depth), _p(ids), _p(rgba),
+                        _p(normals), _p(out))
+    if nf < 0:
+        raise RuntimeError(f"ref_post failed ({nf})")
+    return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "post": out, "descs": descs,
+            "fragments": int(nf)}
 
 
 def godrays(depth, rgba, lights, cam, fov, nthreads=None):

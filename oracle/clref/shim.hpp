@@ -264,6 +264,7 @@ inline uint4 convert_uint4(uchar4 a) { return uint4(a.x, a.y, a.z, a.w); }
 inline uchar4 convert_uchar4(uint4 a) { return uchar4{(uchar)a.x, (uchar)a.y, (uchar)a.z, (uchar)a.w}; }
 inline float4 convert_float4(uint4 a) { return float4((float)a.x, (float)a.y, (float)a.z, (float)a.w); }
 inline float2 convert_float2(int2 a) { return float2((float)a.x, (float)a.y); }
+inline float2 convert_float2(ushort2 a) { return float2((float)a.x, (float)a.y); }
 inline ushort2 convert_ushort2(float2 a) {
   return ushort2{(ushort)(gbr_ref_f2u(a.x) > 65535u ? 65535u : gbr_ref_f2u(a.x)),
                  (ushort)(gbr_ref_f2u(a.y) > 65535u ? 65535u : gbr_ref_f2u(a.y))};

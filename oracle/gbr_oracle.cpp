@@ -1125,6 +1125,116 @@ void godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* in, int W
   out[p + 3] = (uint8_t)quant8(1.0f * 0.99f);
 }
 
+// ---- do_pseudo_aa (cl2.cl:6437-6657, engine.cpp:1513-1516) -----------------
+// An edge pixel -- exactly one of its horizontal and one of its vertical
+// neighbours, and at least one diagonal, differ from it by more than 100 depth
+// units (test 0) or 20 degrees of normal (test 1) -- becomes 0.65 x the mean
+// of its similar neighbours + 0.35 x the mean of the differing ones; the first
+// test that finds an edge decides.  Every other pixel keeps its colour.
+bool pseudo_aa_pixel(int x, int y, int W, int H, const uint32_t* depth, const uint16_t* nrm,
+                     const uint8_t* in, float out[3]) {
+  if (x < 1 || y < 1 || x >= W - 1 || y >= H - 1) return false;
+  const size_t p = (size_t)y * W + x;
+  if (depth[p] == kDepthClear) return false;
+  const float here = depth_to_dist(depth[p]);
+  const f3 n0 = fast_normalize3(decode_normal(nrm[2 * p], nrm[2 * p + 1]));
+  int horiz[2] = {0, 0}, vert[2] = {0, 0}, diag[2] = {0, 0};
+  float same[2][3] = {}, other[2][3] = {}, nsame[2] = {0, 0}, nother[2] = {0, 0};
+  for (int dy = -1; dy <= 1; dy++)
+    for (int dx = -1; dx <= 1; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      const size_t q = (size_t)(y + dy) * W + (x + dx);
+      const float d = depth_to_dist(depth[q]);
+      const f3 n = decode_normal(nrm[2 * q], nrm[2 * q + 1]);
+      float c[3];
+      for (int k = 0; k < 3; k++) c[k] = (float)in[4 * q + k] / 255.0f;
+      const bool edge[2] = {std::fabs(d - here) > 100.0f, dot3(n0, n) < kAACos};
+      for (int t = 0; t < 2; t++) {
+        if (edge[t]) {
+          if (dx == dy || dx == -dy) diag[t]++;
+          else if (dx != 0) horiz[t]++;
+          else vert[t]++;
+          for (int k = 0; k < 3; k++) other[t][k] += c[k];
+          nother[t] += 1.0f;
+        } else {
+          for (int k = 0; k < 3; k++) same[t][k] += c[k];
+          nsame[t] += 1.0f;
+        }
+      }
+    }
+  for (int t = 0; t < 2; t++) {
+    if (horiz[t] == 1 && vert[t] == 1 && diag[t] >= 1) {
+      for (int k = 0; k < 3; k++) out[k] = (same[t][k] / nsame[t]) * 0.65f + (other[t][k] / nother[t]) * 0.35f;
+      return true;
+    }
+  }
+  return false;
+}
+
+// ---- do_motion_blur (cl2.cl:6714-6860, engine.cpp:1518-1536) ----------------
+// The pixel's surface point is carried back through its object's pose of the
+// previous frame (descriptor history slot 1 on even frames, 2 on odd) and
+// projected with this frame's camera and with last frame's; the blend of the
+// two screen-space motions (camera_contribution), scaled by strength and
+// capped at 50 px, is averaged over n bilinear taps centred on the pixel.
+struct MotionArgs {
+  f3 cpos, cc, cs, opos, oc, os;
+  float fov, strength, cam_w;
+  uint32_t frame_id;
+};
+bool motion_blur_pixel(int x, int y, int W, int H, const gbr_triangle* tris, const gbr_obj_g_descriptor* descs,
+                       const uint32_t* depth, const uint32_t* ids, const uint8_t* in, const MotionArgs& a,
+                       float out[4], uint32_t* obj) {
+  const size_t p = (size_t)y * W + x;
+  if (depth[p] == kDepthClear || ids[p] == kNoId) return false;
+  const uint32_t o = tris[ids[p] >> 1].vertices[0].object_id;
+  *obj = o;
+  const gbr_obj_g_descriptor& G = descs[o];
+  const float dist = depth_to_dist(depth[p]);
+  const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, a.fov), fdiv(((float)y - (float)H / 2.0f) * dist, a.fov),
+                       dist);
+  const f3 world = add3(back_rot_cs(local, mk3(0, 0, 0), a.cc, a.cs), a.cpos);
+  const f3 objl = back_rot_quat(sub3(world, v3(G.world_pos)), v4(G.world_rot_quat));
+  const bool even = (a.frame_id & 1u) == 0;
+  const f3 opos = v3(even ? G.old_world_pos_1 : G.old_world_pos_2);
+  const f4 oq = v4(even ? G.old_world_rot_quat_1 : G.old_world_rot_quat_2);
+  const f3 last = add3(rot_quat(objl, oq), opos);
+  const f3 nocam = depth_project1(rot_cs(last, a.cpos, a.cc, a.cs), (float)W, (float)H, a.fov);
+  const f3 prev = depth_project1(rot_cs(last, a.opos, a.oc, a.os), (float)W, (float)H, a.fov);
+  if (prev.z < 20.0f) {
+    const f4 c = sample_bilinear(in, W, H, (float)x + 0.5f, (float)y + 0.5f);
+    out[0] = c.x; out[1] = c.y; out[2] = c.z; out[3] = c.w;
+    return true;
+  }
+  float mx = (float)x - prev.x, my = (float)y - prev.y;
+  const float nx = (float)x - nocam.x, ny = (float)y - nocam.y;
+  mx = a.cam_w * mx + (1.0f - a.cam_w) * nx;
+  my = a.cam_w * my + (1.0f - a.cam_w) * ny;
+  mx = mx * a.strength;
+  my = my * a.strength;
+  int n = f2i_sat(fmax_(std::fabs(mx), std::fabs(my)) + 1.0f);
+  if (n > 50) {
+    mx = (mx / (float)n) * 50.0f;
+    my = (my / (float)n) * 50.0f;
+    n = 50;
+  }
+  float sx = 0.0f, sy = 0.0f;
+  if (n != 0) {
+    sx = mx / (float)n;
+    sy = my / (float)n;
+  }
+  float cx = (float)x - mx / 2.0f, cy = (float)y - my / 2.0f;
+  float acc[4] = {0, 0, 0, 0}, cnt = 0.0f;
+  for (int i = 0; i < n; i++, cx += sx, cy += sy) {
+    if (cx < 0 || cx >= (float)W || cy < 0 || cy >= (float)H) continue;
+    const f4 c = sample_bilinear(in, W, H, cx + 0.5f, cy + 0.5f);
+    acc[0] += c.x; acc[1] += c.y; acc[2] += c.z; acc[3] += c.w;
+    cnt += 1.0f;
+  }
+  for (int k = 0; k < 4; k++) out[k] = cnt != 0.0f ? acc[k] / cnt : acc[k];
+  return true;
+}
+
 extern "C" {
 
 // engine.cpp:119-133 then the std::to_string / -D FOV_CONST round trip (engine.cpp:474-477).
@@ -1377,6 +1487,57 @@ int oracle_godrays(const uint32_t* depth, const uint8_t* rgba_in, const gbr_ligh
   parallel_for((int64_t)W * H, nthreads, [&](int64_t p) {
     godrays_pixel((int)(p % W), (int)(p / W), depth, rgba_in, W, H, fov, lights, nl, cpos, cc, cs, rgba_out);
   });
+  return 0;
+}
+
+// do_pseudo_aa over a rendered view: rgba_out = rgba_in with edge pixels
+// replaced.  Pixels with depth but no id are left as they are.
+int oracle_pseudo_aa(const uint32_t* depth, const uint32_t* ids, const uint16_t* normals, const uint8_t* rgba_in,
+                     int W, int H, uint8_t* rgba_out, int nthreads) {
+  parallel_for((int64_t)W * H, nthreads, [&](int64_t p) {
+    const int x = (int)(p % W), y = (int)(p / W);
+    float c[3];
+    const bool edge = ids[p] != kNoId && pseudo_aa_pixel(x, y, W, H, depth, normals, rgba_in, c);
+    for (int k = 0; k < 4; k++)
+      rgba_out[4 * p + k] = edge ? (uint8_t)quant8(k < 3 ? c[k] : 1.0f) : rgba_in[4 * p + k];
+  });
+  return 0;
+}
+
+// do_motion_blur over a rendered view.  descs is updated with the pose
+// history: every object with a pixel on screen gets its current pose in slot
+// 2 (even frame_id) or 1 (odd).
+int oracle_motion_blur(const gbr_triangle* tris, gbr_obj_g_descriptor* descs, uint32_t ndescs, const uint32_t* depth,
+                       const uint32_t* ids, const uint8_t* rgba_in, const gbr_camera* cam, const gbr_camera* cam_old,
+                       const gbr_view* view, uint32_t frame_id, float strength, float camera_contribution,
+                       uint8_t* rgba_out, int nthreads) {
+  const int W = view->width, H = view->height;
+  MotionArgs a;
+  a.fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
+  a.cpos = v3(cam->pos);
+  euler_cs(v3(cam->rot), &a.cc, &a.cs);
+  a.opos = v3(cam_old->pos);
+  euler_cs(v3(cam_old->rot), &a.oc, &a.os);
+  a.strength = strength;
+  a.cam_w = camera_contribution;
+  a.frame_id = frame_id;
+  std::vector<std::atomic<uint8_t>> seen(ndescs);
+  for (auto& f : seen) f.store(0);
+  parallel_for((int64_t)W * H, nthreads, [&](int64_t p) {
+    float c[4];
+    uint32_t o = 0;
+    const bool hit = motion_blur_pixel((int)(p % W), (int)(p / W), W, H, tris, descs, depth, ids, rgba_in, a, c, &o);
+    if (hit) seen[o].store(1);
+    for (int k = 0; k < 4; k++) rgba_out[4 * p + k] = hit ? (uint8_t)quant8(c[k]) : rgba_in[4 * p + k];
+  });
+  for (uint32_t o = 0; o < ndescs; o++) {
+    if (!seen[o].load()) continue;
+    gbr_obj_g_descriptor& G = descs[o];
+    float* pos = (frame_id & 1u) == 0 ? G.old_world_pos_2 : G.old_world_pos_1;
+    float* q = (frame_id & 1u) == 0 ? G.old_world_rot_quat_2 : G.old_world_rot_quat_1;
+    for (int k = 0; k < 3; k++) pos[k] = G.world_pos[k];
+    for (int k = 0; k < 4; k++) q[k] = G.world_rot_quat[k];
+  }
   return 0;
 }
 

@@ -49,6 +49,11 @@ def lib():
                                          P, P, P, P, P, ctypes.c_int, ctypes.c_int]
         L.oracle_godrays.restype = ctypes.c_int
         L.oracle_godrays.argtypes = [P, P, P, ctypes.c_uint32, P, P, P, ctypes.c_int]
+        L.oracle_pseudo_aa.restype = ctypes.c_int
+        L.oracle_pseudo_aa.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
+        L.oracle_motion_blur.restype = ctypes.c_int
+        L.oracle_motion_blur.argtypes = [P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_uint32, ctypes.c_float,
+                                         ctypes.c_float, P, ctypes.c_int]
         L.oracle_walk.restype = ctypes.c_int
         L.oracle_walk.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
                                   P, ctypes.c_int]
@@ -143,6 +148,31 @@ def godrays(depth, rgba, lights, cam, view, nthreads=None):
     lib().oracle_godrays(_p(np.ascontiguousarray(depth, np.uint32)), _p(np.ascontiguousarray(rgba, np.uint8)),
                          _p(lights), len(lights), _p(cam), _p(view), _p(out), nthreads)
     return out
+
+
+def pseudo_aa(depth, ids, normals, rgba, nthreads=None):
+    """do_pseudo_aa over a rendered view: (H, W, 4) RGBA8."""
+    H, W = depth.shape
+    out = np.empty((H, W, 4), np.uint8)
+    lib().oracle_pseudo_aa(_p(np.ascontiguousarray(depth, np.uint32)), _p(np.ascontiguousarray(ids, np.uint32)),
+                           _p(np.ascontiguousarray(normals, np.uint16)), _p(np.ascontiguousarray(rgba, np.uint8)),
+                           W, H, _p(out), nthreads or default_threads())
+    return out
+
+
+def motion_blur(scene, descs, depth, ids, rgba, cam, cam_old, view, frame_id, strength, camera_contribution,
+                nthreads=None):
+    """do_motion_blur over a rendered view: (RGBA8, descriptors with the pose
+    history updated)."""
+    H, W = depth.shape
+    out = np.empty((H, W, 4), np.uint8)
+    d = np.array(descs, copy=True)
+    lib().oracle_motion_blur(_p(scene.tris), _p(d), len(d), _p(np.ascontiguousarray(depth, np.uint32)),
+                             _p(np.ascontiguousarray(ids, np.uint32)), _p(np.ascontiguousarray(rgba, np.uint8)),
+                             _p(np.asarray(cam).reshape(1)), _p(np.asarray(cam_old).reshape(1)),
+                             _p(np.asarray(view).reshape(1)), int(frame_id), float(strength),
+                             float(camera_contribution), _p(out), nthreads or default_threads())
+    return out, d
 
 
 def render_fp64(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, exact_acos=False, nthreads=None):

@@ -76,10 +76,41 @@ def main_godrays():
     print(f"godrays: {os.path.getsize(path) / 1e3:.0f} kB, views {len(arrays)}")
 
 
+def main_post():
+    """do_pseudo_aa and do_motion_blur of the reference, run over its own
+    frame of each cubes view (the frame equals tests/golden/cubes.npz); SHA-256
+    digests of the RGBA8 results and of the pose history after the pass."""
+    name = golden_cases.POST["post"]
+    src = np.load(os.path.join(OUT, f"{name}.npz"))
+    sc, _ = golden_cases.CASES[name]()
+    sc.descs = golden_cases.motion_descs(sc.descs)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    meta = {}
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        fov = O.fov_const(float(view["hfov_deg"]), int(view["width"]))
+        r = R.post("pseudo_aa", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov)
+        for key in ("depth", "id", "rgba", "normals"):
+            assert np.array_equal(r[key], src[f"{key}{k}"]), f"frame {k} differs from the {name} fixture: {key}"
+        meta[f"aa{k}"] = sha(r["post"])
+        meta[f"aa_changed{k}"] = int(np.count_nonzero(np.any(r["post"] != r["rgba"], axis=-1)))
+        for fid, strength, cw in golden_cases.MOTION:
+            r = R.post("motion_blur", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov,
+                       cam_old=golden_cases.motion_cameras(cam), frame_id=fid, strength=strength,
+                       camera_contribution=cw)
+            meta[f"mb{k}_{fid}"] = sha(r["post"])
+            meta[f"mb_descs{k}_{fid}"] = sha(r["descs"])
+            meta[f"mb_changed{k}_{fid}"] = int(np.count_nonzero(np.any(r["post"] != r["rgba"], axis=-1)))
+    path = os.path.join(OUT, "post.npz")
+    np.savez_compressed(path, meta=np.array(json.dumps(meta)))
+    print("post:", {k: v for k, v in meta.items() if "changed" in k})
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
-    cases = [a for a in args if a != "godrays"]
+    cases = [a for a in args if a not in ("godrays", "post")]
     if cases or not args:
         main(cases or None)
     if not args or "godrays" in args:
         main_godrays()
+    if not args or "post" in args:
+        main_post()

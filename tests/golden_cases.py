@@ -113,8 +113,34 @@ def godray_lights():
     ])
 
 
+def motion_descs(descs):
+    """The cubes' descriptors with a pose history: every object was a little
+    elsewhere and turned in each of the two previous frames."""
+    d = np.array(descs, copy=True)
+    rng = np.random.default_rng(51)
+    for i in range(len(d)):
+        for slot in ("1", "2"):
+            d[i][f"old_world_pos_{slot}"][:3] = d[i]["world_pos"][:3] + rng.uniform(-12, 12, 3)
+            axis = rng.normal(size=3)
+            axis /= np.linalg.norm(axis)
+            half = rng.uniform(-0.08, 0.08)
+            d[i][f"old_world_rot_quat_{slot}"] = np.float32([*(np.sin(half) * axis), np.cos(half)])
+    return d
+
+
+def motion_cameras(cam):
+    """The previous frame's camera for a view: moved and turned a little."""
+    c = np.array(cam, S.CAMERA)
+    c["pos"][:3] += np.float32([6.0, -4.0, 15.0])
+    c["rot"][:3] += np.float32([0.012, -0.02, 0.005])
+    return c
+
+
+# motion blur settings of the post fixture: (frame_id, strength, camera_contribution)
+MOTION = [(0, 0.75, 0.6), (1, 1.5, 0.25)]
+
 # post passes over the views of a rendered case: fixture name -> source case
-POST = {"godrays": "cubes"}
+POST = {"godrays": "cubes", "post": "cubes"}
 
 CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
          "wide_boxes": wide_boxes, "features": features}

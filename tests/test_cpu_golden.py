@@ -112,3 +112,58 @@ def test_oracle_godrays_matches_reference_kernel_random(seed):
     ref = R.godrays(depth, rgba, lights, cam, O.fov_const(float(view["hfov_deg"]), W))
     got = O.godrays(depth, rgba, lights, cam, view)
     assert np.array_equal(got, ref)
+
+
+def _post_inputs():
+    name = golden_cases.POST["post"]
+    src = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    meta = json.loads(str(np.load(os.path.join(GOLDEN, "post.npz"))["meta"]))
+    sc, _ = golden_cases.CASES[name]()
+    sc.descs = golden_cases.motion_descs(sc.descs)
+    return sc, src, meta
+
+
+def test_oracle_pseudo_aa_matches_reference_fixture():
+    """do_pseudo_aa (cl2.cl:6437-6657) over the cubes fixture's frames."""
+    sc, src, meta = _post_inputs()
+    for k in range(len(sc.views)):
+        got = O.pseudo_aa(src[f"depth{k}"], src[f"id{k}"], src[f"normals{k}"], src[f"rgba{k}"])
+        assert int(np.count_nonzero(np.any(got != src[f"rgba{k}"], axis=-1))) == meta[f"aa_changed{k}"]
+        assert sha(got) == meta[f"aa{k}"], f"view {k}: pseudo-AA differs from the reference kernel"
+
+
+def test_oracle_motion_blur_matches_reference_fixture():
+    """do_motion_blur (cl2.cl:6714-6860): colours and the pose history it writes."""
+    sc, src, meta = _post_inputs()
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        for fid, strength, cw in golden_cases.MOTION:
+            got, descs = O.motion_blur(sc, sc.descs, src[f"depth{k}"], src[f"id{k}"], src[f"rgba{k}"], cam,
+                                       golden_cases.motion_cameras(cam), view, fid, strength, cw)
+            assert sha(got) == meta[f"mb{k}_{fid}"], f"view {k} frame {fid}: motion blur differs"
+            assert sha(descs) == meta[f"mb_descs{k}_{fid}"], f"view {k} frame {fid}: pose history differs"
+
+
+@pytest.mark.parametrize("seed", [301, 302])
+def test_oracle_post_passes_match_reference_kernels_random(seed):
+    """Random soups with moving objects: the reference's own frame, then its
+    pseudo-AA and motion-blur kernels over its own fragment buffers."""
+    R = _ref_or_skip()
+    from openclrenderer_gb300 import structs as S
+    rng = np.random.default_rng(seed)
+    w, h = int(rng.integers(64, 400)), int(rng.integers(48, 300))
+    sc = random_soup(int(rng.integers(100, 600)), w, h, seed, two_sided=True)
+    sc.descs = golden_cases.motion_descs(sc.descs)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    cam, view = sc.cameras[0], sc.views[0]
+    fov = O.fov_const(float(view["hfov_deg"]), w)
+    r = R.post("pseudo_aa", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov)
+    assert np.array_equal(O.pseudo_aa(r["depth"], r["id"], r["normals"], r["rgba"]), r["post"])
+    old = S.make_camera(np.asarray(cam["pos"][:3]) + rng.uniform(-20, 20, 3),
+                        np.asarray(cam["rot"][:3]) + rng.uniform(-0.05, 0.05, 3))
+    for fid in (int(rng.integers(0, 100)) * 2, 7):
+        strength, cw = float(rng.uniform(0.2, 3.0)), float(rng.uniform(0, 1))
+        r = R.post("motion_blur", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov, cam_old=old,
+                   frame_id=fid, strength=strength, camera_contribution=cw)
+        got, descs = O.motion_blur(sc, sc.descs, r["depth"], r["id"], r["rgba"], cam, old, view, fid, strength, cw)
+        assert np.array_equal(got, r["post"]), f"frame {fid}: {np.count_nonzero(got != r['post'])} values differ"
+        assert descs.tobytes() == r["descs"].tobytes()
