@@ -597,7 +597,7 @@ def main():
     if not args.no_extra and not args.no_serve:
         serving = run_serving(args, stream)
 
-    # engine::draw_godrays over the measured 1080p frame: two shaft lights
+    # post passes over the measured 1080p frame (godrays with two shaft lights)
     post = None
     if not args.no_extra:
         glights = sc.lights.copy()
@@ -614,10 +614,36 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         gms = e0.elapsed_time(e1) / 10
-        post = {"pass": "screenspace_godrays", "lights": 2, "ms": round(gms, 4),
-                "value": round(P / (gms * 1e-3) / 1e6, 1), "unit": "Mpix/s",
-                "note": "out of place over the frame's depth / RGBA8 (8 MB, L2-resident between launches)"}
+        post = {"godrays": {"lights": 2, "ms": round(gms, 4), "value": round(P / (gms * 1e-3) / 1e6, 1),
+                            "unit": "Mpix/s"},
+                "note": "each pass out of place over the measured frame's buffers (L2-resident between launches)"}
         gs.set_lights(sc.lights)
+
+        def time_pass(fn, reps=10):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / reps
+            return {"ms": round(t, 4), "value": round(P / (t * 1e-3) / 1e6, 1), "unit": "Mpix/s"}
+
+        nout = gs.render(cam, view, normals=True, stream=stream)
+        post["pseudo_aa"] = time_pass(lambda: gs.post_pseudo_aa(view, nout, rgba_out=gout, stream=stream))
+        prev = np.array(cam, S.CAMERA)
+        prev["pos"][:3] += np.float32([4.0, 1.0, -6.0])
+        prev["rot"][:2] += np.float32([0.004, -0.006])
+        post["motion_blur"] = time_pass(lambda: gs.post_motion_blur(cam, prev, view, out, 2, 1.0, 0.5,
+                                                                    rgba_out=gout, stream=stream))
+        rdescs = sc.descs.copy()
+        rdescs["feature_flag"] |= 1
+        gs.set_descriptors(rdescs)
+        post["reflections"] = time_pass(lambda: gs.post_reflections(cam, view, out, rgba_out=gout, stream=stream))
+        post["reflections"]["note"] = "every object reflective"
+        gs.set_descriptors(sc.descs)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -648,7 +674,7 @@ def main():
                     "note": "covered pixel-samples (point_in_tri passes) resolved per second by the raster kernels "
                             "with shared-memory atomics; no measured atomic peak is available for a fraction"},
                 "batched": batched, "binning_stress": stress, "batched_mixed": mixed, "serving": serving,
-                "post_godrays": post,
+                "post_passes": post,
                 "impl": "gbr",
                 "counts": {"visible_records": T_vis, "covered_px": P_cov, "reference_fragments": st["fragments_ref"],
                            "view_bin_entries": st["view_bin_entries"], "shadow_records": st["shadow_records"]}}

@@ -262,6 +262,15 @@ gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb);
 gbr_status gbr_post_godrays(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
                             const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
 
+/* engine::draw_screenspace_reflections (engine.cpp:1483-1511) ->
+ * screenspace_reflections (cl2.cl:6906-7355): pixels of objects with feature
+ * flag 1 (FEATURE_FLAG_SS_REFLECTIVE) mix in the colour found by marching the
+ * mirrored eye ray over the depth buffer, faded by distance and screen edge
+ * and scaled by the object's reflection map (descriptor ssid, a texture id;
+ * 0xFFFFFFFF: none).  Background pixels become 0, as the reference writes. */
+gbr_status gbr_post_reflections(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
+                                const uint32_t* id, const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
+
 /* engine::do_pseudo_aa (engine.cpp:1513-1516) -> do_pseudo_aa
  * (cl2.cl:6437-6657): edge pixels -- where the neighbourhood's depth jumps by
  * more than 100 or its normal turns by more than 20 degrees along exactly one

@@ -42,7 +42,13 @@ struct float4 {
 };
 
 // feature_flag bits of obj_g_descriptor (cl2.cl:90-97)
-enum : int32_t { FLAG_TWO_SIDED = 2, FLAG_OUTLINE = 4, FLAG_IS_STATIC = 8, FLAG_NO_DYN_SHADOWS = 16 };
+enum : int32_t {
+  FLAG_SS_REFLECTIVE = 1,
+  FLAG_TWO_SIDED = 2,
+  FLAG_OUTLINE = 4,
+  FLAG_IS_STATIC = 8,
+  FLAG_NO_DYN_SHADOWS = 16
+};
 
 // ---- textures (texture_context.hpp:39-71) ---------------------------------------
 struct texture {
@@ -91,6 +97,7 @@ struct object {
   float specular = 0.9f, spec_mult = 1.f, diffuse = 1.f;  // object.cpp:72-74
   int32_t feature_flag = 0;
   texture* normal_map = nullptr;  // descriptor rid (obj.rid / normal_map, obj_load.cpp:544-556)
+  texture* ss_map = nullptr;      // descriptor ssid: the screen-space reflection map (object.cpp:106-109)
 };
 
 struct objects_container {
@@ -145,6 +152,9 @@ struct objects_container {
   void set_diffuse(float d) { for (auto& o : objs) o.diffuse = d; }
   void set_children_texture_id(texture* t) { for (auto& o : objs) o.tex = t; }
   void set_normal_map(texture* t) { for (auto& o : objs) o.normal_map = t; }
+  // objects_container::set_screenspace_map_id / set_ss_reflective (objects_container.cpp:28-35, 105-112)
+  void set_screenspace_map_id(texture* t) { for (auto& o : objs) o.ss_map = t; }
+  void set_ss_reflective(bool on) { set_flag(FLAG_SS_REFLECTIVE, on); }
   void set_outline(bool on) { set_flag(FLAG_OUTLINE, on); }
   void set_flag(int32_t bit, bool on) {
     for (auto& o : objs) o.feature_flag = on ? (o.feature_flag | bit) : (o.feature_flag & ~bit);
@@ -163,6 +173,12 @@ struct object_context_data {
   uint32_t use_linear_rendering = 1;
   uint32_t tri_num = 0, obj_num = 0;
   gbr_status status = GBR_OK;  // the last call's status
+  uint32_t frame_id = 0;       // increases monotonically, once per draw_bulk_objs_n
+  float4 c_pos_old, c_rot_old;  // the camera of the previous frame (swap_buffers)
+
+  // object_context_data::swap_buffers (object_context.cpp:17-25): end of a
+  // frame; the engine's camera becomes the previous camera
+  void swap_buffers();
 
   // object_context_data::ensure_screen_buffers
   gbr_status ensure_screen_buffers(int w, int h) {
@@ -247,7 +263,7 @@ struct object_context {
         g.scale = o.dynamic_scale;
         g.tid = (uint32_t)tex_ctx.get_gpu_position_id(o.tex);
         g.rid = o.normal_map ? (uint32_t)tex_ctx.get_gpu_position_id(o.normal_map) : 0xFFFFFFFFu;
-        g.ssid = 0xFFFFFFFFu;
+        g.ssid = o.ss_map ? (uint32_t)tex_ctx.get_gpu_position_id(o.ss_map) : 0xFFFFFFFFu;
         g.specular = o.specular;
         g.spec_mult = o.spec_mult;
         g.diffuse = o.diffuse;
@@ -291,10 +307,21 @@ struct object_context {
     gpu_dat.obj_num = (uint32_t)descs.size();
     return gpu_dat.status = st;
   }
-  // object_context::flush_locations: positions, rotations and materials only
+  // object_context::flush_locations -> object::g_flush (object.cpp:652-860):
+  // position, rotation, scale, texture id and feature flags of every object;
+  // the motion-blur pose history kept in the descriptors stays
   gbr_status flush_locations() {
     const auto descs = descriptors();
-    return gpu_dat.status = gbr_scene_set_descriptors(gpu_dat.scene, descs.data(), (uint32_t)descs.size());
+    std::vector<gbr_object_flush> f(descs.size());
+    for (size_t i = 0; i < descs.size(); i++) {
+      f[i].index = (uint32_t)i;
+      f[i].tid = descs[i].tid;
+      f[i].scale = descs[i].scale;
+      f[i].feature_flag = descs[i].feature_flag;
+      std::memcpy(f[i].world_pos, descs[i].world_pos, 16);
+      std::memcpy(f[i].world_rot_quat, descs[i].world_rot_quat, 16);
+    }
+    return gpu_dat.status = gbr_scene_flush_objects(gpu_dat.scene, f.data(), (uint32_t)f.size());
   }
   object_context_data* fetch() { return &gpu_dat; }
 };
@@ -361,7 +388,7 @@ struct light {
 // ---- engine (engine.hpp) ----------------------------------------------------------
 struct engine {
   int width = 0, height = 0;
-  float4 c_pos, c_rot;                  // camera position, extrinsic XYZ Euler angles
+  static inline float4 c_pos, c_rot;    // camera position, extrinsic XYZ Euler angles (static, engine.hpp)
   float horizontal_fov_degrees = 120.f;  // engine.hpp:115
   uint32_t view_flags = 0;              // GBR_VIEW_*: kernel3's optional -D switches
   void* stream = nullptr;               // cudaStream_t; null = the default stream
@@ -369,6 +396,7 @@ struct engine {
   gbr_scene* lights_uploaded_to = nullptr;
   size_t lights_uploaded_n = 0;
   std::vector<gbr_light> lights_uploaded;
+  object_context_data* last_dat = nullptr;  // the context of the last draw_bulk_objs_n (do_pseudo_aa's buffers)
 
   // engine::load: the screen size (the reference also builds the OpenCL
   // program with it compiled in; here it is a per-view parameter)
@@ -427,6 +455,47 @@ struct engine {
     const gbr_camera c = camera();
     const gbr_view v = view(dat);
     if (st == GBR_OK) st = gbr_render_view(dat.scene, &c, &v, &o, stream);
+    if (st == GBR_OK) {
+      dat.frame_id++;
+      last_dat = &dat;
+    }
+    return dat.status = st;
+  }
+  // engine::do_pseudo_aa (engine.cpp:1513-1516): over the last frame drawn, in place
+  gbr_status do_pseudo_aa() {
+    if (!last_dat) return GBR_INVALID_ARG;
+    object_context_data& dat = *last_dat;
+    gbr_outputs o;
+    gbr_status st = gbr_framebuffer_outputs(dat.fb, &o, nullptr, nullptr);
+    const gbr_view v = view(dat);
+    if (st == GBR_OK) st = gbr_post_pseudo_aa(dat.scene, &v, o.depth, o.id, o.normals, o.rgba, o.rgba, stream);
+    return dat.status = st;
+  }
+  // engine::do_motion_blur (engine.cpp:1518-1536): in place, with the
+  // context's frame id and previous camera
+  gbr_status do_motion_blur(object_context_data& dat, float strength, float camera_contribution) {
+    gbr_outputs o;
+    gbr_status st = gbr_framebuffer_outputs(dat.fb, &o, nullptr, nullptr);
+    const gbr_camera c = camera();
+    gbr_camera old;
+    const float p[4] = {dat.c_pos_old.x, dat.c_pos_old.y, dat.c_pos_old.z, dat.c_pos_old.w};
+    const float r[4] = {dat.c_rot_old.x, dat.c_rot_old.y, dat.c_rot_old.z, dat.c_rot_old.w};
+    std::memcpy(old.pos, p, 16);
+    std::memcpy(old.rot, r, 16);
+    const gbr_view v = view(dat);
+    if (st == GBR_OK)
+      st = gbr_post_motion_blur(dat.scene, &c, &old, &v, dat.frame_id, strength, camera_contribution, o.depth, o.id,
+                                o.rgba, o.rgba, stream);
+    return dat.status = st;
+  }
+  // engine::draw_screenspace_reflections (engine.cpp:1483-1511): in place over
+  // the context's last frame (the reference's tex argument is unused by the kernel)
+  gbr_status draw_screenspace_reflections(object_context_data& dat) {
+    gbr_outputs o;
+    gbr_status st = gbr_framebuffer_outputs(dat.fb, &o, nullptr, nullptr);
+    const gbr_camera c = camera();
+    const gbr_view v = view(dat);
+    if (st == GBR_OK) st = gbr_post_reflections(dat.scene, &c, &v, o.depth, o.id, o.rgba, o.rgba, stream);
     return dat.status = st;
   }
   // engine::draw_godrays (engine.cpp:1463-1482): light shafts added to the
@@ -459,6 +528,11 @@ struct engine {
     return dat.status = st;
   }
 };
+
+inline void object_context_data::swap_buffers() {
+  c_pos_old = engine::c_pos;
+  c_rot_old = engine::c_rot;
+}
 
 }  // namespace openclrenderer
 

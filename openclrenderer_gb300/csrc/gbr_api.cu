@@ -495,8 +495,8 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
   if (n && !d) return fail(GBR_INVALID_ARG, "null descriptors");
   TRY(s->descs.reserve(n));
   if (n) CU(cudaMemcpy(s->descs.p, d, sizeof(gbr_obj_g_descriptor) * n, cudaMemcpyHostToDevice));
-  uint32_t mt = 0, mr = 0;
-  bool has_rid = false;
+  uint32_t mt = 0, mr = 0, ms = 0;
+  bool has_rid = false, has_ssid = false;
   s->host_tid.resize(n);
   s->host_flags.resize(n);
   for (uint32_t i = 0; i < n; i++) {
@@ -507,10 +507,16 @@ gbr_status gbr_scene_set_descriptors(gbr_scene* s, const gbr_obj_g_descriptor* d
       mr = std::max(mr, d[i].rid);
       has_rid = true;
     }
+    if (d[i].ssid != 0xFFFFFFFFu) {
+      ms = std::max(ms, d[i].ssid);
+      has_ssid = true;
+    }
   }
   s->max_tid = mt;
   s->max_rid = mr;
   s->has_rid = has_rid;
+  s->max_ssid = ms;
+  s->has_ssid = has_ssid;
   s->ndescs = n;
   s->static_dirty = true;
   s->world_dirty = true;

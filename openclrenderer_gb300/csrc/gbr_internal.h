@@ -178,6 +178,9 @@ cudaError_t launch_motion_blur(const gbr_triangle* tris, uint32_t ntris, gbr_obj
                                int H, float fov, const float cpos[3], const float cc[3], const float cs[3],
                                const float opos[3], const float oc[3], const float os[3], uint32_t frame_id,
                                float strength, float camera_contribution, uint32_t* seen, cudaStream_t st);
+cudaError_t launch_reflections(const SceneDev& sc, const uint32_t* depth, const uint32_t* ids, const uint8_t* in,
+                               uint8_t* out, int W, int H, float fov, const float cpos[3], const float cc[3],
+                               const float cs[3], cudaStream_t st);
 cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* out, int W, int H, float fov,
                            const gbr_light* lights, uint32_t nlights, const float cpos[3], const float cc[3],
                            const float cs[3], cudaStream_t st);

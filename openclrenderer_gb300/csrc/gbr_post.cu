@@ -59,6 +59,27 @@ gbr_status gbr_post_godrays(gbr_scene* s, const gbr_camera* cam, const gbr_view*
   return post_finish(s, view, rgba_out, dst, st);
 }
 
+gbr_status gbr_post_reflections(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
+                                const uint32_t* id, const uint8_t* rgba_in, uint8_t* rgba_out, void* stream) {
+  GBR_SCENE_LOCK(s);
+  TRY(check_scene(s));
+  TRY(validate_view(view));
+  if (!cam || !depth || !id || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  if (s->ntris && s->max_object_id >= s->ndescs)
+    return fail(GBR_INVALID_ARG, "object id %u has no descriptor (%u)", s->max_object_id, s->ndescs);
+  if (s->has_ssid && s->max_ssid >= s->mipmap_start)
+    return fail(GBR_INVALID_ARG, "descriptor ssid %u but only %u textures", s->max_ssid, s->mipmap_start);
+  uint8_t* dst = nullptr;
+  TRY(post_target(s, view, rgba_in, rgba_out, &dst));
+  float cc[3], cs[3];
+  euler_cs(cam->rot, cc, cs);
+  const cudaStream_t st = (cudaStream_t)stream;
+  CU(launch_reflections(s->dev(), depth, id, rgba_in, dst, view->width, view->height, view_fov(view), cam->pos, cc, cs,
+                        st));
+  s->stats.launches += 1;
+  return post_finish(s, view, rgba_out, dst, st);
+}
+
 gbr_status gbr_post_pseudo_aa(gbr_scene* s, const gbr_view* view, const uint32_t* depth, const uint32_t* id,
                               const uint16_t* normals, const uint8_t* rgba_in, uint8_t* rgba_out, void* stream) {
   GBR_SCENE_LOCK(s);

@@ -282,4 +282,202 @@ cudaError_t launch_motion_blur(const gbr_triangle* tris, uint32_t ntris, gbr_obj
   return cudaGetLastError();
 }
 
+// ---- screenspace_reflections (cl2.cl:6862-7355) -----------------------------
+// interpolate_single_line_depth (cl2.cl:6862-6873): the point at parameter a
+// on the screen-space segment s -> f, depth interpolated in 1/z.
+__device__ __forceinline__ f3 line_depth_point(f3 s, f3 f, float a) {
+  s.z = rcp(s.z);
+  f.z = rcp(f.z);
+  const float b = 1.0f - a;
+  const f3 r = mk3(fma_(s.x, b, f.x * a), fma_(s.y, b, f.y * a), fma_(s.z, b, f.z * a));
+  return mk3(r.x, r.y, rcp(r.z));
+}
+
+struct ReflectCam {
+  f3 cpos, cc, cs;
+  float fov;
+};
+
+// A pixel of an object with FEATURE_FLAG_SS_REFLECTIVE: the eye ray mirrored
+// in the interpolated normal is marched in screen space from a point 10.5
+// units along it (at most 200 steps, until it passes more than 1 unit behind
+// the depth buffer), refined in tenths of a step, and the colour there mixed
+// in by a contact fade (400 units, fading towards the screen edge) times the
+// object's reflection map (ssid) when it has one.  Returns 0 when the pixel
+// keeps its colour.  Background pixels become 0.
+__device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, int y, int W, int H,
+                                const uint32_t* __restrict__ depth, const uint32_t* __restrict__ ids,
+                                const uint8_t* __restrict__ in, f4* out) {
+  const size_t p = (size_t)y * W + x;
+  const uint32_t d = depth[p];
+  if (d == kDepthClear) {
+    out->x = out->y = out->z = out->w = 0.0f;
+    return 1;
+  }
+  const uint32_t id = ids[p];
+  if (id == kNoId || (id >> 1) >= sc.ntris) return 0;
+  const uint32_t tri = id >> 1, sub = id & 1u;
+  const gbr_triangle* T = sc.tris + tri;
+  const uint32_t o_id = __ldg(&T->vertices[0].object_id);
+  const gbr_obj_g_descriptor* G = sc.descs + o_id;
+  if (!((__ldg(&G->feature_flag) & 1) > 0)) return 0;
+  const float dist = fdiv((float)d, kMulInt) * kDepthFar;
+  const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, v.fov), fdiv(((float)y - (float)H / 2.0f) * dist, v.fov),
+                       dist);
+  const f3 zero = mk3(0, 0, 0);
+  const f3 world = add3(back_rot_cs(local, zero, v.cc, v.cs), v.cpos);
+  const f3 ray = sub3(world, v.cpos);
+  const float scale = __ldg(&G->scale);
+  f3 pv[3], nv[3];
+  f2 tv[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    pv[k] = mul3s(ld3(T->vertices[k].pos), scale);
+    nv[k] = ld3(T->vertices[k].normal);
+    tv[k] = mk2(__ldg(&T->vertices[k].vt[0]), __ldg(&T->vertices[k].vt[1]));
+  }
+  const f4 q = ld4(G->world_rot_quat);
+  const f3 wpos = ld3(G->world_pos);
+  const BaryFrame bf = bary_frame(pv[0], pv[1], pv[2]);
+  float l1, l2, l3;
+  bary_exact(bf, back_rot_quat(sub3(world, wpos), q), &l1, &l2, &l3);
+  f3 normal = mk3(fma_(nv[0].x, l1, fma_(nv[1].x, l2, nv[2].x * l3)), fma_(nv[0].y, l1, fma_(nv[1].y, l2, nv[2].y * l3)),
+                  fma_(nv[0].z, l1, fma_(nv[1].z, l2, nv[2].z * l3)));
+  normal = fast_normalize3(rot_quat(normal, q));
+  const f2 vt = mk2(fma_(tv[0].x, l1, fma_(tv[1].x, l2, tv[2].x * l3)), fma_(tv[0].y, l1, fma_(tv[1].y, l2, tv[2].y * l3)));
+  float refl = 1.0f;
+  const uint32_t ssid = __ldg(&G->ssid);
+  if (ssid != 0xFFFFFFFFu) {
+    // the pixel's clip output, as prearrange wrote it to cutdown_tris
+    f3 w[3], o0[3], o1[3];
+    uint32_t oid;
+    load_world(sc, tri, w, &oid);
+    const int n = transform_clip(w, v.cpos, v.cc, v.cs, v.fov, (float)W, (float)H, o0, o1);
+    if ((int)sub >= n) return 0;
+    const f3* tp = sub ? o1 : o0;
+    const f3 xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
+    const f3 ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
+    const float rc = rconstant(xpv, ypv);
+    // get_vtdiff (cl2.cl:5691-5760), per pixel
+    const f3 depths = mk3(rcp(tp[0].z), rcp(tp[1].z), rcp(tp[2].z));
+    float DA, DB, DC;
+    plane_const(depths, xpv, ypv, rc, &DA, &DB, &DC);
+    const float fx = (float)x, fy = (float)y;
+    const float dmx = fma_(DA, fx + 1.0f, fma_(DB, fy, DC));
+    const float dmy = fma_(DA, fx, fma_(DB, fy + 1.0f, DC));
+    const float hw = (float)W / 2.0f, hh = (float)H / 2.0f;
+    f3 lmx = mk3(fdiv((fx + 1.0f) - hw, v.fov), fdiv(fy - hh, v.fov), 1.0f);
+    f3 lmy = mk3(fdiv(fx - hw, v.fov), fdiv((fy + 1.0f) - hh, v.fov), 1.0f);
+    lmx = mk3(fdiv(lmx.x, dmx), fdiv(lmx.y, dmx), fdiv(lmx.z, dmx));
+    lmy = mk3(fdiv(lmy.x, dmy), fdiv(lmy.y, dmy), fdiv(lmy.z, dmy));
+    const f3 gmx = back_rot_quat(sub3(add3(back_rot_cs(lmx, zero, v.cc, v.cs), v.cpos), wpos), q);
+    const f3 gmy = back_rot_quat(sub3(add3(back_rot_cs(lmy, zero, v.cc, v.cs), v.cpos), wpos), q);
+    float lx1, lx2, lx3, ly1, ly2, ly3;
+    bary_exact(bf, gmx, &lx1, &lx2, &lx3);
+    bary_exact(bf, gmy, &ly1, &ly2, &ly3);
+    const f2 vtx = mk2(fma_(tv[0].x, lx1, fma_(tv[1].x, lx2, tv[2].x * lx3)),
+                       fma_(tv[0].y, lx1, fma_(tv[1].y, lx2, tv[2].y * lx3)));
+    const f2 vty = mk2(fma_(tv[0].x, ly1, fma_(tv[1].x, ly2, tv[2].x * ly3)),
+                       fma_(tv[0].y, ly1, fma_(tv[1].y, ly2, tv[2].y * ly3)));
+    const float mip_bias = 1.0f / kMipBias;
+    const f2 vtdiff = mk2((fabsf(vtx.x - vt.x) + fabsf(vty.x - vt.x)) * mip_bias,
+                          (fabsf(vtx.y - vt.y) + fabsf(vty.y - vt.y)) * mip_bias);
+    refl = texture_filter_diff(sc, vt, vtdiff, (int)ssid).x;
+    if (refl < 0.1f) return 0;
+  }
+  // reflect (cl2.cl:169-176) normalises the normal once more
+  const f3 nn = fast_normalize3(normal);
+  const float k2 = 2.0f * dot3(ray, nn);
+  const f3 refd = fast_normalize3(sub3(ray, mul3s(nn, k2)));
+  const f3 jit = add3(world, mul3s(refd, 10.5f));
+  const f3 sj = depth_project1(rot_cs(jit, v.cpos, v.cc, v.cs), (float)W, (float)H, v.fov);
+  const f3 ss = depth_project1(rot_cs(world, v.cpos, v.cc, v.cs), (float)W, (float)H, v.fov);
+  const float dx = sj.x - ss.x, dy = sj.y - ss.y;
+  const float sdist = fsqrt(dx * dx + dy * dy);
+  const float back = 1.0f - fdiv(sdist - 3.0f, sdist);
+  f3 vprev = mk3(ss.x * back + sj.x * (1.0f - back), ss.y * back + sj.y * (1.0f - back),
+                 rcp(ss.z) * back + rcp(sj.z) * (1.0f - back));
+  vprev.z = rcp(vprev.z);
+  const f3 vstart = sj;
+  f3 cur = sj;
+  const float fw = (float)W, fh = (float)H;
+  if (cur.x < 0 || cur.y < 0 || cur.x >= fw || cur.y >= fh) return 0;
+  bool found = false;
+  float a = 1.0f;
+  for (int i = 0; i < 200; i++) {
+    if (cur.x < 0 || cur.y < 0 || cur.x >= fw || cur.y >= fh) return 0;
+    const uint32_t cd = depth[(size_t)f2i_sat(cur.y) * W + f2i_sat(cur.x)];
+    if (fdiv((float)cd, kMulInt) * kDepthFar < cur.z - 1.0f) {
+      found = true;
+      break;
+    }
+    a += 1.0f;
+    cur = line_depth_point(vprev, vstart, a);
+  }
+  if (!found) return 0;
+  // the refinement reads the depth where the march stopped on every try
+  const float stop = fdiv((float)depth[(size_t)f2i_sat(cur.y) * W + f2i_sat(cur.x)], kMulInt) * kDepthFar;
+  float ta = a;
+  f3 hit = cur;
+  bool ok = false;
+  for (int i = 0; i < 10; i++) {
+    hit = line_depth_point(vprev, vstart, ta);
+    if (stop < hit.z + 1.0f && stop > hit.z - 20.0f) {
+      ok = true;
+      break;
+    }
+    ta += fdiv(1.0f, 10.0f);
+  }
+  if (!ok) return 0;
+  const f3 te = line_depth_point(vstart, hit, 1.35f);
+  float fextra = 0.0f;
+  if (te.x < 0) fextra += fabsf(te.x);
+  if (te.y < 0) fextra += fabsf(te.y);
+  if (te.x >= fw) fextra += te.x - fw;
+  if (te.y >= fh) fextra += te.y - fh;
+  fextra = clampf_(fdiv(fextra, 200.0f), 0.0f, 1.0f);
+  f3 gl = mk3(fdiv((hit.x - fw / 2.0f) * hit.z, v.fov), fdiv((hit.y - fh / 2.0f) * hit.z, v.fov), hit.z);
+  gl = add3(back_rot_cs(gl, zero, v.cc, v.cs), v.cpos);
+  const float ray_len = fast_length3(sub3(gl, world));
+  float fade = 1.0f - fdiv(ray_len, 400.0f);
+  fade = fade - fextra;
+  fade = clampf_(fade, 0.0f, 1.0f) * refl;
+  const f4 fc = read_linear_rgba8(in, W, H, hit.x, hit.y);
+  const uchar4 t = reinterpret_cast<const uchar4*>(in)[p];
+  const float den = 1.0f + fade;
+  out->x = fdiv(fdiv((float)t.x, 255.0f) + fc.x * fade, den);
+  out->y = fdiv(fdiv((float)t.y, 255.0f) + fc.y * fade, den);
+  out->z = fdiv(fdiv((float)t.z, 255.0f) + fc.z * fade, den);
+  out->w = 1.0f;
+  return 1;
+}
+
+// engine::draw_screenspace_reflections (engine.cpp:1483-1511): one thread per pixel.
+__global__ void __launch_bounds__(256) k_reflections(SceneDev sc, ReflectCam v, const uint32_t* __restrict__ depth,
+                                                     const uint32_t* __restrict__ ids, const uint8_t* __restrict__ in,
+                                                     uint8_t* __restrict__ out, int W, int H) {
+  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+  if (x >= W || y >= H) return;
+  const size_t p = (size_t)y * W + x;
+  f4 c;
+  uint32_t* o32 = reinterpret_cast<uint32_t*>(out);
+  if (reflection_pixel(sc, v, x, y, W, H, depth, ids, in, &c))
+    o32[p] = pack_rgba(c.x, c.y, c.z, c.w);
+  else
+    o32[p] = reinterpret_cast<const uint32_t*>(in)[p];
+}
+
+cudaError_t launch_reflections(const SceneDev& sc, const uint32_t* depth, const uint32_t* ids, const uint8_t* in,
+                               uint8_t* out, int W, int H, float fov, const float cpos[3], const float cc[3],
+                               const float cs[3], cudaStream_t st) {
+  ReflectCam v;
+  v.cpos = mk3(cpos[0], cpos[1], cpos[2]);
+  v.cc = mk3(cc[0], cc[1], cc[2]);
+  v.cs = mk3(cs[0], cs[1], cs[2]);
+  v.fov = fov;
+  dim3 grid((W + 15) / 16, (H + 15) / 16);
+  k_reflections<<<grid, 256, 0, st>>>(sc, v, depth, ids, in, out, W, H);
+  return cudaGetLastError();
+}
+
 }  // namespace gbr

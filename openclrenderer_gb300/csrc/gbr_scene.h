@@ -141,7 +141,8 @@ struct gbr_scene {
   uint32_t npages = 0;
   gbr::DevBuf<uint32_t> shadow_dyn, shadow_static;
   uint32_t n_dyn = 0, n_static = 0;
-  uint32_t max_object_id = 0, max_tid = 0, max_rid = 0;
+  uint32_t max_object_id = 0, max_tid = 0, max_rid = 0, max_ssid = 0;
+  bool has_ssid = false;  // some descriptor names a reflection map (ssid != 0xFFFFFFFF)
   bool has_rid = false;  // some descriptor names a normal map (rid != 0xFFFFFFFF)
   bool static_dirty = true;
   gbr::WorkMem ws_view, ws_shadow, ws_host;  // ws_host: output buffers of gbr_render_view_host

@@ -206,6 +206,18 @@ class GpuScene:
                                               _t_ptr(out.rgba), _t_ptr(rgba_out), _stream_ptr(stream)))
         return rgba_out
 
+    def post_reflections(self, cam, view, out, rgba_out=None, stream=None):
+        """engine::draw_screenspace_reflections over a rendered OutputSet."""
+        import torch
+        cam = np.asarray(cam, S.CAMERA).reshape(1)
+        view = np.asarray(view, S.VIEW).reshape(1)
+        if rgba_out is None:
+            rgba_out = torch.empty_like(out.rgba)
+        _native.check(self.L.gbr_post_reflections(self.h, _np_ptr(cam), _np_ptr(view), _t_ptr(out.depth),
+                                                  _t_ptr(out.id), _t_ptr(out.rgba), _t_ptr(rgba_out),
+                                                  _stream_ptr(stream)))
+        return rgba_out
+
     def post_pseudo_aa(self, view, out, rgba_out=None, stream=None):
         """engine::do_pseudo_aa over a rendered OutputSet (normals required)."""
         import torch

@@ -1235,6 +1235,137 @@ bool motion_blur_pixel(int x, int y, int W, int H, const gbr_triangle* tris, con
   return true;
 }
 
+// ---- screenspace_reflections (cl2.cl:6862-7355, engine.cpp:1483-1511) -------
+// interpolate_single_line_depth (cl2.cl:6862-6873): a point on the screen-space
+// segment s -> f at parameter a, depth interpolated in 1/z.
+f3 line_depth_point(f3 s, f3 f, float a) {
+  s.z = rcp(s.z);
+  f.z = rcp(f.z);
+  const float b = 1.0f - a;
+  const f3 r = mk3(fma_(s.x, b, f.x * a), fma_(s.y, b, f.y * a), fma_(s.z, b, f.z * a));
+  return mk3(r.x, r.y, rcp(r.z));
+}
+
+// One pixel of a surface whose object has FEATURE_FLAG_SS_REFLECTIVE: the eye
+// ray is mirrored in the interpolated normal, marched over the depth buffer in
+// screen space from a point 10.5 units along it (200 steps, until it passes
+// behind the depth by more than 1), refined in tenths of a step, and the
+// colour found there is mixed in by a contact fade (400 units, fading towards
+// the screen edge) times the object's screen-space map (ssid) when it has one.
+// Returns 0: unchanged, 1: out written.  Background pixels become 0.
+int reflection_pixel(int x, int y, const ShadeView& v, const gbr_triangle* tris, const gbr_obj_g_descriptor* descs,
+                     const Atlas& at, const uint32_t* depth, const uint32_t* ids, const uint8_t* in, float out[4]) {
+  const int W = v.W, H = v.H;
+  const size_t p = (size_t)y * W + x;
+  if (depth[p] == kDepthClear) {
+    out[0] = out[1] = out[2] = out[3] = 0.0f;
+    return 1;
+  }
+  if (ids[p] == kNoId) return 0;
+  const uint32_t tri = ids[p] >> 1, sub = ids[p] & 1u;
+  const gbr_triangle& T = tris[tri];
+  const gbr_obj_g_descriptor& G = descs[T.vertices[0].object_id];
+  if (!((G.feature_flag & 1) > 0)) return 0;
+  const float dist = depth_to_dist(depth[p]);
+  const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, v.fov), fdiv(((float)y - (float)H / 2.0f) * dist, v.fov),
+                       dist);
+  const f3 zero = mk3(0, 0, 0);
+  const f3 world = add3(back_rot_cs(local, zero, v.crot_c, v.crot_s), v.cpos);
+  const f3 ray = sub3(world, v.cpos);
+  f3 pv[3], nv[3];
+  f2 tv[3];
+  for (int k = 0; k < 3; k++) {
+    pv[k] = mul3s(v3(T.vertices[k].pos), G.scale);
+    nv[k] = v3(T.vertices[k].normal);
+    tv[k] = mk2(T.vertices[k].vt[0], T.vertices[k].vt[1]);
+  }
+  const f4 q = v4(G.world_rot_quat);
+  const f3 objl = back_rot_quat(sub3(world, v3(G.world_pos)), q);
+  float l1, l2, l3;
+  barycentric(objl, pv[0], pv[1], pv[2], &l1, &l2, &l3);
+  f3 normal = mk3(fma_(nv[0].x, l1, fma_(nv[1].x, l2, nv[2].x * l3)), fma_(nv[0].y, l1, fma_(nv[1].y, l2, nv[2].y * l3)),
+                  fma_(nv[0].z, l1, fma_(nv[1].z, l2, nv[2].z * l3)));
+  normal = fast_normalize3(rot_quat(normal, q));
+  const f2 vt = mk2(fma_(tv[0].x, l1, fma_(tv[1].x, l2, tv[2].x * l3)), fma_(tv[0].y, l1, fma_(tv[1].y, l2, tv[2].y * l3)));
+  float refl = 1.0f;
+  if (G.ssid != 0xFFFFFFFFu) {
+    f3 outs[2][3];
+    const int n = project_tri(T, G, v.cpos, v.crot_c, v.crot_s, v.fov, (float)W, (float)H, outs);
+    if ((int)sub >= n) return 0;
+    const f3* tp = outs[sub];
+    const float rc = rconstant(mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x)),
+                               mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y)));
+    const f2 vtdiff = get_vtdiff(tp, (float)x, (float)y, v, G, vt, pv[0], pv[1], pv[2], tv[0], tv[1], tv[2], rc);
+    refl = texture_filter_diff(vt, vtdiff, (int)G.ssid, at).x;
+    if (refl < 0.1f) return 0;
+  }
+  // reflect (cl2.cl:169-176) normalises the normal once more
+  const f3 nn = fast_normalize3(normal);
+  const float k2 = 2.0f * dot3(ray, nn);
+  const f3 refd = fast_normalize3(sub3(ray, mul3s(nn, k2)));
+  const f3 jit = add3(world, mul3s(refd, 10.5f));
+  const f3 sj = depth_project1(rot_cs(jit, v.cpos, v.crot_c, v.crot_s), (float)W, (float)H, v.fov);
+  const f3 ss = depth_project1(rot_cs(world, v.cpos, v.crot_c, v.crot_s), (float)W, (float)H, v.fov);
+  const float dx = sj.x - ss.x, dy = sj.y - ss.y;
+  const float sdist = fsqrt(dx * dx + dy * dy);
+  const float back = 1.0f - fdiv(sdist - 3.0f, sdist);
+  f3 vprev = mk3(ss.x * back + sj.x * (1.0f - back), ss.y * back + sj.y * (1.0f - back),
+                 rcp(ss.z) * back + rcp(sj.z) * (1.0f - back));
+  vprev.z = rcp(vprev.z);
+  const f3 vstart = sj;
+  f3 cur = sj;
+  auto off = [&](f3 c) { return c.x < 0 || c.y < 0 || c.x >= (float)W || c.y >= (float)H; };
+  auto dist_at = [&](f3 c) { return depth_to_dist(depth[(size_t)f2i_sat(c.y) * W + f2i_sat(c.x)]); };
+  if (off(cur)) return 0;
+  bool found = false;
+  float a = 1.0f;
+  for (int i = 0; i < 200; i++) {
+    if (off(cur)) return 0;
+    if (dist_at(cur) < cur.z - 1.0f) {
+      found = true;
+      break;
+    }
+    a += 1.0f;
+    cur = line_depth_point(vprev, vstart, a);
+  }
+  if (!found) return 0;
+  // the refinement reads the depth where the march stopped on every try
+  const float stop = dist_at(cur);
+  float ta = a;
+  f3 hit = cur;
+  bool ok = false;
+  for (int i = 0; i < 10; i++) {
+    hit = line_depth_point(vprev, vstart, ta);
+    if (stop < hit.z + 1.0f && stop > hit.z - 20.0f) {
+      ok = true;
+      break;
+    }
+    ta += 1.0f / 10.0f;
+  }
+  if (!ok) return 0;
+  const f3 te = line_depth_point(vstart, hit, 1.35f);
+  float fextra = 0.0f;
+  if (te.x < 0) fextra += std::fabs(te.x);
+  if (te.y < 0) fextra += std::fabs(te.y);
+  if (te.x >= (float)W) fextra += te.x - (float)W;
+  if (te.y >= (float)H) fextra += te.y - (float)H;
+  fextra = clampf_(fextra / 200.0f, 0.0f, 1.0f);
+  f3 gl = mk3(fdiv((hit.x - (float)W / 2.0f) * hit.z, v.fov), fdiv((hit.y - (float)H / 2.0f) * hit.z, v.fov), hit.z);
+  gl = add3(back_rot_cs(gl, zero, v.crot_c, v.crot_s), v.cpos);
+  const float ray_len = fast_length3(sub3(gl, world));
+  float fade = 1.0f - ray_len / 400.0f;
+  fade = fade - fextra;
+  fade = clampf_(fade, 0.0f, 1.0f) * refl;
+  const f4 found_col = sample_bilinear(in, W, H, hit.x, hit.y);
+  const float fc[3] = {found_col.x, found_col.y, found_col.z};
+  for (int k = 0; k < 3; k++) {
+    const float c = (float)in[4 * p + k] / 255.0f;
+    out[k] = (c + fc[k] * fade) / (1.0f + fade);
+  }
+  out[3] = 1.0f;
+  return 1;
+}
+
 extern "C" {
 
 // engine.cpp:119-133 then the std::to_string / -D FOV_CONST round trip (engine.cpp:474-477).
@@ -1538,6 +1669,27 @@ int oracle_motion_blur(const gbr_triangle* tris, gbr_obj_g_descriptor* descs, ui
     for (int k = 0; k < 3; k++) pos[k] = G.world_pos[k];
     for (int k = 0; k < 4; k++) q[k] = G.world_rot_quat[k];
   }
+  return 0;
+}
+
+// screenspace_reflections over a rendered view (cl2.cl:6906-7355).
+int oracle_reflections(const gbr_triangle* tris, const gbr_obj_g_descriptor* descs, const uint8_t* atlas,
+                       const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start, const uint32_t* depth,
+                       const uint32_t* ids, const uint8_t* rgba_in, const gbr_camera* cam, const gbr_view* view,
+                       uint8_t* rgba_out, int nthreads) {
+  ShadeView v;
+  v.W = view->width;
+  v.H = view->height;
+  v.fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, v.W);
+  v.cpos = v3(cam->pos);
+  v.crot = v3(cam->rot);
+  euler_cs(v.crot, &v.crot_c, &v.crot_s);
+  const Atlas at{atlas, nums, sizes, mipmap_start};
+  parallel_for((int64_t)v.W * v.H, nthreads, [&](int64_t p) {
+    float c[4];
+    const int w = reflection_pixel((int)(p % v.W), (int)(p / v.W), v, tris, descs, at, depth, ids, rgba_in, c);
+    for (int k = 0; k < 4; k++) rgba_out[4 * p + k] = w ? (uint8_t)quant8(c[k]) : rgba_in[4 * p + k];
+  });
   return 0;
 }
 

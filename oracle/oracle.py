@@ -54,6 +54,8 @@ def lib():
         L.oracle_motion_blur.restype = ctypes.c_int
         L.oracle_motion_blur.argtypes = [P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_uint32, ctypes.c_float,
                                          ctypes.c_float, P, ctypes.c_int]
+        L.oracle_reflections.restype = ctypes.c_int
+        L.oracle_reflections.argtypes = [P, P, P, P, P, ctypes.c_uint32, P, P, P, P, P, P, ctypes.c_int]
         L.oracle_walk.restype = ctypes.c_int
         L.oracle_walk.argtypes = [P, ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_uint32,
                                   P, ctypes.c_int]
@@ -173,6 +175,18 @@ def motion_blur(scene, descs, depth, ids, rgba, cam, cam_old, view, frame_id, st
                              _p(np.asarray(view).reshape(1)), int(frame_id), float(strength),
                              float(camera_contribution), _p(out), nthreads or default_threads())
     return out, d
+
+
+def reflections(scene, descs, tex, depth, ids, rgba, cam, view, nthreads=None):
+    """screenspace_reflections over a rendered view: (H, W, 4) RGBA8."""
+    H, W = depth.shape
+    out = np.empty((H, W, 4), np.uint8)
+    d = np.ascontiguousarray(descs)
+    lib().oracle_reflections(_p(scene.tris), _p(d), _p(tex.atlas), _p(tex.nums), _p(tex.sizes), tex.mipmap_start,
+                             _p(np.ascontiguousarray(depth, np.uint32)), _p(np.ascontiguousarray(ids, np.uint32)),
+                             _p(np.ascontiguousarray(rgba, np.uint8)), _p(np.asarray(cam).reshape(1)),
+                             _p(np.asarray(view).reshape(1)), _p(out), nthreads or default_threads())
+    return out
 
 
 def render_fp64(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, exact_acos=False, nthreads=None):

@@ -9,8 +9,15 @@
 // f32 clear[4]; textures: i32 edge + edge*edge*4 bytes; objects: f32 pos[4],
 // f32 quat[4], f32 scale, specular, spec_mult, diffuse, i32 feature_flag,
 // i32 texture, u32 ntris, ntris * 144-byte triangles; lights: 64-byte lights.
+//
+// Optional third argument: "aa" runs engine::do_pseudo_aa after the frame;
+// "mb" draws a first frame from a camera moved by (6, -4, 15) and turned by
+// (0.012, -0.02, 0.005), swaps buffers, draws the frame from the scene's camera
+// and runs engine::do_motion_blur(0.75, 0.6); "ssr" runs
+// engine::draw_screenspace_reflections after the frame.
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "gbr_engine.hpp"
@@ -21,10 +28,11 @@ template <class T>
 static bool rd(FILE* f, T* v, size_t n = 1) { return fread(v, sizeof(T), n, f) == n; }
 
 int main(int argc, char** argv) {
-  if (argc != 3) {
-    fprintf(stderr, "usage: %s scene.bin out.bin\n", argv[0]);
+  if (argc != 3 && argc != 4) {
+    fprintf(stderr, "usage: %s scene.bin out.bin [aa|mb|ssr]\n", argv[0]);
     return 2;
   }
+  const std::string mode = argc == 4 ? argv[3] : "";
   FILE* f = fopen(argv[1], "rb");
   if (!f) return 2;
   char magic[4];
@@ -66,6 +74,9 @@ int main(int argc, char** argv) {
     c->set_two_sided((ff & FLAG_TWO_SIDED) != 0);
     c->set_is_static((ff & FLAG_IS_STATIC) != 0);
     c->set_does_not_receive_dynamic_shadows((ff & FLAG_NO_DYN_SHADOWS) != 0);
+    c->set_ss_reflective((ff & FLAG_SS_REFLECTIVE) != 0);
+    // an object that reflects, with a texture, uses that texture as its reflection map
+    if ((ff & FLAG_SS_REFLECTIVE) && tex >= 0 && (i % 2)) c->set_screenspace_map_id(texs[tex]);
     c->set_active(true);
   }
   for (uint32_t i = 0; i < nl; i++) {
@@ -98,10 +109,27 @@ int main(int argc, char** argv) {
   window.set_camera_pos(float4{cam[0], cam[1], cam[2], cam[3]});
   window.set_camera_rot(float4{cam[4], cam[5], cam[6], cam[7]});
   window.set_light_data(lights);
+  if (mode == "mb") {  // the previous frame
+    window.set_camera_pos(float4{cam[0] + 6.f, cam[1] - 4.f, cam[2] + 15.f, cam[3]});
+    window.set_camera_rot(float4{cam[4] + 0.012f, cam[5] - 0.02f, cam[6] + 0.005f, cam[7]});
+    if (window.set_object_data(*ctx.fetch()) != GBR_OK || window.draw_bulk_objs_n(*ctx.fetch()) != GBR_OK) {
+      fprintf(stderr, "frame 1: %s\n", gbr_last_error_string());
+      return 5;
+    }
+    ctx.fetch()->swap_buffers();
+    window.set_camera_pos(float4{cam[0], cam[1], cam[2], cam[3]});
+    window.set_camera_rot(float4{cam[4], cam[5], cam[6], cam[7]});
+  }
   if (window.set_object_data(*ctx.fetch()) != GBR_OK ||
       window.generate_realtime_shadowing(*ctx.fetch()) != GBR_OK ||
       window.draw_bulk_objs_n(*ctx.fetch()) != GBR_OK || window.draw_godrays(*ctx.fetch()) != GBR_OK) {
     fprintf(stderr, "frame: %s\n", gbr_last_error_string());
+    return 5;
+  }
+  if ((mode == "aa" && window.do_pseudo_aa() != GBR_OK) ||
+      (mode == "mb" && window.do_motion_blur(*ctx.fetch(), 0.75f, 0.6f) != GBR_OK) ||
+      (mode == "ssr" && window.draw_screenspace_reflections(*ctx.fetch()) != GBR_OK)) {
+    fprintf(stderr, "post: %s\n", gbr_last_error_string());
     return 5;
   }
   FILE* o = fopen(argv[2], "wb");

@@ -100,6 +100,17 @@ def main_post():
             meta[f"mb{k}_{fid}"] = sha(r["post"])
             meta[f"mb_descs{k}_{fid}"] = sha(r["descs"])
             meta[f"mb_changed{k}_{fid}"] = int(np.count_nonzero(np.any(r["post"] != r["rgba"], axis=-1)))
+    # screenspace_reflections with reflective objects (golden_cases.reflect_descs)
+    sc, _ = golden_cases.CASES[name]()
+    sc.descs = golden_cases.reflect_descs(sc.descs)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        fov = O.fov_const(float(view["hfov_deg"]), int(view["width"]))
+        r = R.post("reflections", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov)
+        for key in ("depth", "id", "rgba"):
+            assert np.array_equal(r[key], src[f"{key}{k}"]), f"frame {k} differs from the {name} fixture: {key}"
+        meta[f"ssr{k}"] = sha(r["post"])
+        drawn = src[f"depth{k}"] != 0xFFFFFFFF
+        meta[f"ssr_changed{k}"] = int(np.count_nonzero(np.any(r["post"] != r["rgba"], axis=-1) & drawn))
     path = os.path.join(OUT, "post.npz")
     np.savez_compressed(path, meta=np.array(json.dumps(meta)))
     print("post:", {k: v for k, v in meta.items() if "changed" in k})

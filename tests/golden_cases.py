@@ -128,6 +128,19 @@ def motion_descs(descs):
     return d
 
 
+def reflect_descs(descs):
+    """Descriptors with screen-space reflections (FEATURE_FLAG_SS_REFLECTIVE):
+    every third object plain mirror, every third with texture 0 as its
+    reflection map (ssid)."""
+    d = np.array(descs, copy=True)
+    for i in range(len(d)):
+        if i % 3 != 2:
+            d[i]["feature_flag"] |= 1
+        if i % 3 == 1:
+            d[i]["ssid"] = 0
+    return d
+
+
 def motion_cameras(cam):
     """The previous frame's camera for a view: moved and turned a little."""
     c = np.array(cam, S.CAMERA)

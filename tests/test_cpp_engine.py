@@ -37,6 +37,46 @@ def _godray_cubes():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["aa", "mb", "ssr"])
+def test_engine_mirror_post_passes(tmp_path, mode):
+    """engine::do_pseudo_aa / do_motion_blur in the engine's frame sequence
+    (frame ids, swap_buffers' previous camera) against the C ABI."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("no CUDA device")
+    from openclrenderer_gb300.pipeline import GpuScene
+    from tests import golden_cases
+    sc = scenes.plain_cubes()
+    if mode == "ssr":  # as the mirror sets them: odd objects use their texture as the reflection map
+        sc.descs = golden_cases.reflect_descs(sc.descs)
+        sc.descs["ssid"] = 0xFFFFFFFF
+        refl = (sc.descs["feature_flag"] & 1) != 0
+        odd = (np.arange(len(sc.descs)) % 2) == 1
+        sc.descs["ssid"][refl & odd] = sc.descs["tid"][refl & odd]
+    cam, view = sc.cameras[0], sc.views[0]
+    W, H = int(view["width"]), int(view["height"])
+    exe = M.build(str(tmp_path))
+    M.write_scene(str(tmp_path / "scene.bin"), sc)
+    got = M.run(exe, str(tmp_path / "scene.bin"), str(tmp_path / "out.bin"), W, H, mode)
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    out = gs.render(cam, view, normals=True)
+    if mode == "aa":
+        rgba = gs.post_pseudo_aa(view, out)
+    elif mode == "ssr":
+        rgba = gs.post_reflections(cam, view, out)
+    else:
+        old = golden_cases.motion_cameras(cam)
+        rgba = gs.post_motion_blur(cam, old, view, out, 2, 0.75, 0.6)
+    ref = out.numpy()
+    ref["rgba"] = rgba.cpu().numpy()
+    gs.close()
+    for k in ("depth", "id", "rgba"):
+        assert np.array_equal(got[k], ref[k]), f"{mode}: {k} differs ({np.count_nonzero(got[k] != ref[k])})"
+    assert np.count_nonzero(ref["rgba"] != out.rgba.cpu().numpy()) > 100
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", ["cubes", "cubes_shadows", "terrain_small", "cubes_godrays"])
 def test_engine_mirror_matches_c_abi(tmp_path, name):
     torch = pytest.importorskip("torch")

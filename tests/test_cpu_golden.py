@@ -167,3 +167,40 @@ def test_oracle_post_passes_match_reference_kernels_random(seed):
         got, descs = O.motion_blur(sc, sc.descs, r["depth"], r["id"], r["rgba"], cam, old, view, fid, strength, cw)
         assert np.array_equal(got, r["post"]), f"frame {fid}: {np.count_nonzero(got != r['post'])} values differ"
         assert descs.tobytes() == r["descs"].tobytes()
+
+
+def test_oracle_reflections_match_reference_fixture():
+    """screenspace_reflections (cl2.cl:6906-7355) over the cubes fixture's frames."""
+    name = golden_cases.POST["post"]
+    src = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    meta = json.loads(str(np.load(os.path.join(GOLDEN, "post.npz"))["meta"]))
+    sc, _ = golden_cases.CASES[name]()
+    descs = golden_cases.reflect_descs(sc.descs)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        got = O.reflections(sc, descs, tex, src[f"depth{k}"], src[f"id{k}"], src[f"rgba{k}"], cam, view)
+        drawn = src[f"depth{k}"] != 0xFFFFFFFF
+        assert int(np.count_nonzero(np.any(got != src[f"rgba{k}"], axis=-1) & drawn)) == meta[f"ssr_changed{k}"]
+        assert sha(got) == meta[f"ssr{k}"], f"view {k}: reflections differ from the reference kernel"
+
+
+@pytest.mark.parametrize("seed", [401, 402])
+def test_oracle_reflections_match_reference_kernel_random(seed):
+    """Terrain and soups with reflective objects, some with a reflection map."""
+    R = _ref_or_skip()
+    from openclrenderer_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    if seed % 2:
+        sc = scenes.terrain(nx=96, nz=48, width=int(rng.integers(160, 400)), height=int(rng.integers(120, 300)),
+                            n_lights=2, n_textures=3, tex_size=64)
+    else:
+        w, h = int(rng.integers(64, 400)), int(rng.integers(48, 300))
+        sc = random_soup(int(rng.integers(100, 600)), w, h, seed, two_sided=True)
+    sc.descs = golden_cases.reflect_descs(sc.descs)
+    sc.descs["ssid"][::2] = 0
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    cam, view = sc.cameras[0], sc.views[0]
+    fov = O.fov_const(float(view["hfov_deg"]), int(view["width"]))
+    r = R.post("reflections", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov)
+    got = O.reflections(sc, sc.descs, tex, r["depth"], r["id"], r["rgba"], cam, view)
+    assert np.array_equal(got, r["post"]), f"{np.count_nonzero(got != r['post'])} values differ"

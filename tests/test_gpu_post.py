@@ -122,3 +122,41 @@ def test_flush_objects_keeps_pose_history():
         bad = moved[:1].copy()
         bad["index"] = n
         gs.flush_objects(bad)
+
+
+def test_reflections_parity():
+    name = golden_cases.POST["post"]
+    src = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    meta = json.loads(str(np.load(os.path.join(GOLDEN, "post.npz"))["meta"]))
+    sc, _ = golden_cases.CASES[name]()
+    sc.descs = golden_cases.reflect_descs(sc.descs)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    gs = GpuScene(sc)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        f = Frame(src[f"depth{k}"], src[f"id{k}"], src[f"rgba{k}"])
+        got = gs.post_reflections(cam, view, f).cpu().numpy()
+        assert sha(got) == meta[f"ssr{k}"], f"view {k}: differs from the reference kernel"
+        out = gs.render(cam, view)
+        got = gs.post_reflections(cam, view, out).cpu().numpy()
+        h = out.numpy()
+        ref = O.reflections(sc, sc.descs, tex, h["depth"], h["id"], h["rgba"], cam, view)
+        assert np.array_equal(got, ref), f"view {k}: {np.count_nonzero(got != ref)} values differ from the oracle"
+
+
+def test_reflections_on_terrain_parity():
+    """A reflective terrain with a reflection map, and a world-space cache that
+    is stale (descriptors changed after the last pass)."""
+    from openclrenderer_gb300 import scenes
+    sc = scenes.terrain(nx=128, nz=64, width=480, height=270, n_lights=3, n_textures=3, tex_size=64)
+    sc.descs = golden_cases.reflect_descs(sc.descs)
+    sc.descs["ssid"][:] = 1
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    gs = GpuScene(sc)
+    cam, view = sc.cameras[0], sc.views[0]
+    out = gs.render(cam, view)
+    gs.set_descriptors(sc.descs)
+    got = gs.post_reflections(cam, view, out).cpu().numpy()
+    h = out.numpy()
+    ref = O.reflections(sc, sc.descs, tex, h["depth"], h["id"], h["rgba"], cam, view)
+    assert np.array_equal(got, ref), f"{np.count_nonzero(got != ref)} values differ from the oracle"
+    assert np.count_nonzero(np.any(got != h["rgba"], axis=-1) & (h["depth"] != 0xFFFFFFFF)) > 100
