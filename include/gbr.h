@@ -229,7 +229,17 @@ gbr_status gbr_shadow_pass(gbr_scene* scene, void* stream);
 gbr_status gbr_render_view(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
                            const gbr_outputs* out, void* stream);
 
-/* Same, with HOST output buffers (copied back before returning). */
+/* render_tris with object_context::set_blend_render_context
+ * (object_context.cpp:891-894, engine.cpp:1943-1988) and kernel3's
+ * CAN_INTEGRATED_BLEND switch (cl2.cl:5839-5851, 6339-6351): where the other
+ * context's depth (blend->depth) is nearer than this view's, its RGBA8
+ * (blend->rgba, alpha-weighted) is blended over the shaded colour, or over the
+ * clear colour, whose alpha then becomes the blended blue (the reference's
+ * .xyzz).  blend: device buffers of the same size as the view. */
+gbr_status gbr_render_view_blend(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
+                                 const gbr_outputs* out, const gbr_outputs* blend, void* stream);
+
+/* gbr_render_view with HOST output buffers (copied back before returning). */
 gbr_status gbr_render_view_host(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
                                 uint32_t* depth, uint32_t* id, uint8_t* rgba, void* stream);
 

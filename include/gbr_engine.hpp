@@ -174,6 +174,7 @@ struct object_context_data {
   uint32_t tri_num = 0, obj_num = 0;
   gbr_status status = GBR_OK;  // the last call's status
   uint32_t frame_id = 0;       // increases monotonically, once per draw_bulk_objs_n
+  const object_context_data* blend_render_context = nullptr;  // kernel3's integrated blend source
   float4 c_pos_old, c_rot_old;  // the camera of the previous frame (swap_buffers)
 
   // object_context_data::swap_buffers (object_context.cpp:17-25): end of a
@@ -324,6 +325,9 @@ struct object_context {
     return gpu_dat.status = gbr_scene_flush_objects(gpu_dat.scene, f.data(), (uint32_t)f.size());
   }
   object_context_data* fetch() { return &gpu_dat; }
+  // object_context::set_blend_render_context (object_context.cpp:891-894):
+  // this context's frames blend in the other's last frame where it is nearer
+  void set_blend_render_context(object_context& other) { gpu_dat.blend_render_context = &other.gpu_dat; }
 };
 
 // ---- lights (light.hpp:11-68) ----------------------------------------------------
@@ -454,7 +458,16 @@ struct engine {
     if (st == GBR_OK) st = gbr_framebuffer_outputs(dat.fb, &o, nullptr, nullptr);
     const gbr_camera c = camera();
     const gbr_view v = view(dat);
-    if (st == GBR_OK) st = gbr_render_view(dat.scene, &c, &v, &o, stream);
+    const object_context_data* b = dat.blend_render_context;
+    gbr_outputs bo;
+    if (st == GBR_OK && b && b->fb) {
+      // render_tris binds the other context's depth and screen (engine.cpp:1943-1988)
+      if (b->s_w != width || b->s_h != height) st = GBR_INVALID_ARG;
+      if (st == GBR_OK) st = gbr_framebuffer_outputs(b->fb, &bo, nullptr, nullptr);
+      if (st == GBR_OK) st = gbr_render_view_blend(dat.scene, &c, &v, &o, &bo, stream);
+    } else if (st == GBR_OK) {
+      st = gbr_render_view(dat.scene, &c, &v, &o, stream);
+    }
     if (st == GBR_OK) {
       dat.frame_id++;
       last_dat = &dat;

@@ -110,6 +110,7 @@ SIGNATURES = {
     "gbr_batch_destroy": (ctypes.c_int, [_P]),
     "gbr_render_view_noalloc": (ctypes.c_int, [_P, _P, _P, _P, _P]),
     "gbr_post_godrays": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "gbr_render_view_blend": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "gbr_post_pseudo_aa": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "gbr_post_reflections": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "gbr_post_motion_blur": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P,

@@ -115,6 +115,8 @@ void fill_view_params(const gbr_camera& cam, const gbr_view& v, const gbr_output
   memcpy(V.clear, v.clear_col, 16);
   V.rgba = o.rgba;
   V.normals = o.normals;
+  V.blend_depth = nullptr;
+  V.blend_rgba = nullptr;
 }
 
 void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector<ShadowJob>& jobs,
@@ -724,7 +726,7 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
 }
 
 static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams, const gbr_view* views,
-                               const gbr_outputs* outs, cudaStream_t st) {
+                               const gbr_outputs* outs, cudaStream_t st, const gbr_outputs* blend = nullptr) {
   TRY(check_scene(s));
   if (!n) return GBR_OK;
   if (!cams || !views || !outs) return fail(GBR_INVALID_ARG, "null camera/view/output array");
@@ -754,6 +756,10 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     S.rec = s->ws_view.pix_rec.p + off;
     S.chunk = kOpSize;
     fill_view_params(cams[i], v, outs[i], i, vp[i]);
+    if (blend) {
+      vp[i].blend_depth = blend[i].depth;
+      vp[i].blend_rgba = blend[i].rgba;
+    }
     off += (size_t)v.width * v.height;
   }
   TRY(check_indices(s, true));
@@ -783,7 +789,7 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   sh.shade = false;
   for (uint32_t i = 0; i < n; i++) {
     if (outs[i].rgba || outs[i].normals) sh.shade = true;
-    if (views[i].flags) sh.features = true;
+    if (views[i].flags || vp[i].blend_depth) sh.features = true;
   }
   for (int attempt = 0; attempt < 8; attempt++) {
     TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
@@ -794,6 +800,13 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     if (fit && !rerun) return GBR_OK;
   }
   return fail(GBR_INTERNAL, "scratch kept overflowing after 8 attempts");
+}
+
+gbr_status gbr_render_view_blend(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const gbr_outputs* out,
+                                 const gbr_outputs* blend, void* stream) {
+  GBR_SCENE_LOCK(s);
+  if (!blend || !blend->depth || !blend->rgba) return fail(GBR_INVALID_ARG, "blend source needs depth and rgba");
+  return render_views(s, 1, cam, view, out, (cudaStream_t)stream, blend);
 }
 
 gbr_status gbr_render_view(gbr_scene* s, const gbr_camera* cam, const gbr_view* view, const gbr_outputs* out,

@@ -75,6 +75,10 @@ struct ViewParams {
   float clear[4];
   uint8_t* rgba;
   uint16_t* normals;
+  // CAN_INTEGRATED_BLEND: another context's depth and RGBA8, blended in where
+  // nearer (null: no blend)
+  const uint32_t* blend_depth;
+  const uint8_t* blend_rgba;
 };
 
 // One cubemap render: a light, static or dynamic geometry, 6 surfaces.

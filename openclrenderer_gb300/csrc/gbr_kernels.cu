@@ -1067,6 +1067,15 @@ __device__ __forceinline__ float generate_outline(int x, int y, const uint32_t* 
   return fmin_(fdiv(fabsf(furthest - d0), 100.0f), 1.0f);
 }
 
+// One RGBA8 texel of the blend source as read_imagef returns it (c / 255).
+__device__ __forceinline__ f4 blend_texel(const uint8_t* __restrict__ rgba, size_t p) {
+  const uchar4 t = reinterpret_cast<const uchar4*>(rgba)[p];
+  f4 o;
+  o.x = fdiv((float)t.x, 255.0f); o.y = fdiv((float)t.y, 255.0f);
+  o.z = fdiv((float)t.z, 255.0f); o.w = fdiv((float)t.w, 255.0f);
+  return o;
+}
+
 // colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
 // 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
 // FEAT: kernel3's optional switches (view flags) compiled in.
@@ -1080,7 +1089,21 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const uint32_t r = S.rec[p];
   uint32_t* out = reinterpret_cast<uint32_t*>(V.rgba);
   if (d == kDepthClear || r == kNoId) {
-    if (out) out[p] = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
+    if (out) {
+      f4 c;
+      c.x = V.clear[0]; c.y = V.clear[1]; c.z = V.clear[2]; c.w = V.clear[3];
+      // CAN_INTEGRATED_BLEND (cl2.cl:5839-5851): the other context's colour
+      // over the clear colour where it has depth; its .xyzz swizzle gives
+      // alpha = blue
+      if (FEAT && V.blend_depth && V.blend_depth[p] < d) {
+        const f4 o = blend_texel(V.blend_rgba, p);
+        c.x = fma_(o.x, o.w, c.x * (1.0f - o.w));
+        c.y = fma_(o.y, o.w, c.y * (1.0f - o.w));
+        c.z = fma_(o.z, o.w, c.z * (1.0f - o.w));
+        c.w = c.z;
+      }
+      out[p] = pack_rgba(c.x, c.y, c.z, c.w);
+    }
     if (V.normals) reinterpret_cast<uint32_t*>(V.normals)[p] = 0;
     return;
   }
@@ -1261,6 +1284,13 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 colclamp = add3(add3(mk3(col.x, col.y, col.z), zero), mul3s(ssum, rsc));
   f3 sp2 = mul3s(ssum, 1.0f - rsc);
   f3 fin = mk3(fma_(colclamp.x, dsum.x, sp2.x), fma_(colclamp.y, dsum.y, sp2.y), fma_(colclamp.z, dsum.z, sp2.z));
+  // CAN_INTEGRATED_BLEND (cl2.cl:6339-6351): alpha_blend of the other
+  // context's colour where it is nearer, before the output gamma
+  if (FEAT && V.blend_depth && V.blend_depth[p] < d) {
+    const f4 o = blend_texel(V.blend_rgba, p);
+    fin = mk3(fma_(o.x, o.w, fin.x * (1.0f - o.w)), fma_(o.y, o.w, fin.y * (1.0f - o.w)),
+              fma_(o.z, o.w, fin.z * (1.0f - o.w)));
+  }
   if (V.use_linear) fin = mk3(c_gamma_inv(fin.x), c_gamma_inv(fin.y), c_gamma_inv(fin.z));
   if (FEAT && (V.flags & GBR_VIEW_OUTLINE) && (ff & kFlagOutline) > 0) {
     const float o = generate_outline(x, y, S.depth, W, H);

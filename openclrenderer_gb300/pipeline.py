@@ -159,14 +159,21 @@ class GpuScene:
     def shadow_pass(self, stream=None):
         _native.check(self.L.gbr_shadow_pass(self.h, _stream_ptr(stream)))
 
-    def render(self, cam, view, out=None, stream=None, normals=False):
+    def render(self, cam, view, out=None, stream=None, normals=False, blend=None):
+        """One view.  blend: an OutputSet (depth, rgba) of another render
+        context to blend in where nearer (kernel3's integrated blend)."""
         cam = np.asarray(cam, S.CAMERA).reshape(1)
         view = np.asarray(view, S.VIEW).reshape(1)
         if out is None:
             out = OutputSet(int(view[0]["width"]), int(view[0]["height"]), normals=normals)
         o = out.as_struct()
-        _native.check(self.L.gbr_render_view(self.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(o),
-                                             _stream_ptr(stream)))
+        if blend is None:
+            _native.check(self.L.gbr_render_view(self.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(o),
+                                                 _stream_ptr(stream)))
+        else:
+            b = _Outs(blend.depth.data_ptr(), None, blend.rgba.data_ptr(), None)
+            _native.check(self.L.gbr_render_view_blend(self.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(o),
+                                                       ctypes.byref(b), _stream_ptr(stream)))
         return out
 
     def render_batch(self, cams, views, outs=None, stream=None):

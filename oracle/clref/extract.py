@@ -29,9 +29,10 @@ DEFINES = ["SCREENWIDTH=gbr_ref_W", "SCREENHEIGHT=gbr_ref_H", "FOV_CONST=gbr_ref
 IDENT = re.compile(r"[A-Za-z_][A-Za-z0-9_]*")
 
 
-# kernel3's optional switches (cl2.cl:5987, 6368): normal mapping and the
-# per-object outline; the second build of the kernels has them on
-FEATURE_DEFINES = ["ENABLE_NORMAL_MAPPING", "CAN_OUTLINE"]
+# kernel3's optional switches (cl2.cl:5839, 5987, 6368): the blend with a
+# second render context, normal mapping and the per-object outline; the second
+# build of the kernels has them on
+FEATURE_DEFINES = ["ENABLE_NORMAL_MAPPING", "CAN_OUTLINE", "CAN_INTEGRATED_BLEND"]
 
 
 def preprocess(src, extra=()):

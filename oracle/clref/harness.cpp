@@ -92,7 +92,7 @@ int64_t ref_render_frame(const void* tris_in, uint32_t ntris, const void* descs,
                          uint32_t mipmap_start, const uint32_t* shadow_dyn, const uint32_t* shadow_static,
                          const float* cam, int W, int H, float fov, uint32_t use_linear, const float* clear,
                          uint32_t* depth, uint32_t* ids, uint8_t* rgba, uint16_t* normals, int nthreads, int ordered,
-                         Frame* keep) {
+                         Frame* keep, const uint32_t* blend_depth = nullptr, const uint8_t* blend_rgba = nullptr) {
   gbr_ref_W = W;
   gbr_ref_H = H;
   gbr_ref_FOV = fov;
@@ -145,15 +145,25 @@ int64_t ref_render_frame(const void* tris_in, uint32_t ntris, const void* descs,
   std::vector<uint> to_clear(P);
   std::vector<ushort2>& nrm = F.nrm;
   nrm.assign(P, ushort2{0, 0});
-  image2d_t scr{screen.data(), W, H, 2}, backup{nullptr, W, H, 2}, blend{nullptr, W, H, 2};
+  image2d_t scr{screen.data(), W, H, 2}, backup{nullptr, W, H, 2};
+  image2d_t blend{const_cast<uint8_t*>(blend_rgba), W, H, 1};
+  const int use_blend = blend_depth && blend_rgba ? 1 : 0;
   uint lnum = nlights;
   float4 clear_col(clear[0], clear[1], clear[2], clear[3]);
   par_for((int64_t)P, nthreads, [&](int64_t p) {
     const int x = (int)(p % W), y = (int)(p / W);
     if (depth[p] != 0xFFFFFFFFu && ids[p] == 0xFFFFFFFFu) {
       // depth without any fragment passing kernel2's test: the reference would
-      // read a stale id; the canonical rule shades it as background
-      memcpy(&screen[p * 4], clear_col.s, 16);
+      // read a stale id; the canonical rule shades it as background (kernel3's
+      // background path, blend included)
+      float4 c = clear_col;
+      if (use_blend && blend_depth[p] < depth[p]) {
+        const float4 o(blend_rgba[p * 4] / 255.0f, blend_rgba[p * 4 + 1] / 255.0f, blend_rgba[p * 4 + 2] / 255.0f,
+                       blend_rgba[p * 4 + 3] / 255.0f);
+        for (int k = 0; k < 3; k++) c.s[k] = fmaf(o.s[k], o.s[3], c.s[k] * (1.0f - o.s[3]));
+        c.s[3] = c.s[2];
+      }
+      memcpy(&screen[p * 4], c.s, 16);
       return;
     }
     gbr_ref_gid[0] = (size_t)x;
@@ -161,7 +171,7 @@ int64_t ref_render_frame(const void* tris_in, uint32_t ntris, const void* descs,
     kernel3(tris, c_pos, c_rot, depth, idimg, (uchar4*)atlas, scr, backup, const_cast<uint*>(nums),
             const_cast<uint*>(sizes), gobj, &lnum, (struct light*)const_cast<void*>(lights),
             const_cast<uint*>(shadow_dyn), const_cast<uint*>(shadow_static), to_clear.data(), frags, cut.data(),
-            clear_col, 0, nrm.data(), 0, nullptr, blend, mipmap_start, use_linear);
+            clear_col, 0, nrm.data(), use_blend, const_cast<uint*>(blend_depth), blend, mipmap_start, use_linear);
   });
   if (keep) F.raw_ids.assign(ids, ids + P);
   for (size_t p = 0; p < P; p++) {
@@ -186,10 +196,11 @@ int64_t ref_render(const void* tris_in, uint32_t ntris, const void* descs, const
                    const uint8_t* atlas, const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
                    const uint32_t* shadow_dyn, const uint32_t* shadow_static, const float* cam, int W, int H,
                    float fov, uint32_t use_linear, const float* clear, uint32_t* depth, uint32_t* ids,
-                   uint8_t* rgba, uint16_t* normals, int nthreads, int ordered) {
+                   uint8_t* rgba, uint16_t* normals, int nthreads, int ordered, const uint32_t* blend_depth,
+                   const uint8_t* blend_rgba) {
   return ref_render_frame(tris_in, ntris, descs, lights, nlights, atlas, nums, sizes, mipmap_start, shadow_dyn,
                           shadow_static, cam, W, H, fov, use_linear, clear, depth, ids, rgba, normals, nthreads,
-                          ordered, nullptr);
+                          ordered, nullptr, blend_depth, blend_rgba);
 }
 
 // A post pass over one rendered frame, with the reference's own fragment

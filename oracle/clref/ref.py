@@ -25,7 +25,7 @@ def lib(features=False):
         L.ref_render.restype = ctypes.c_int64
         L.ref_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32, P, P, P,
                                  ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P, P, P, P, P,
-                                 ctypes.c_int, ctypes.c_int]
+                                 ctypes.c_int, ctypes.c_int, P, P]
         L.ref_post.restype = ctypes.c_int64
         L.ref_post.argtypes = [ctypes.c_int, P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32,
                                P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_uint32, P,
@@ -73,7 +73,9 @@ def shadow(scene, nthreads=None, ordered=True):
 
 
 def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_dyn=None, shadow_static=None,
-           nthreads=None, ordered=True, features=False):
+           nthreads=None, ordered=True, features=False, blend=None):
+    """blend: (depth, rgba) of a blend context; needs features=True (the
+    build with CAN_INTEGRATED_BLEND)."""
     nthreads = nthreads or (os.cpu_count() or 1)
     W, H = int(view["width"]), int(view["height"])
     if shadow_dyn is None:
@@ -88,10 +90,12 @@ def render(scene, atlas, nums, page_sizes, mipmap_start, cam, view, fov, shadow_
     normals = np.empty((H, W, 2), np.uint16)
     nums = np.ascontiguousarray(nums, np.uint32)
     page_sizes = np.ascontiguousarray(page_sizes, np.uint32)
+    bd = None if blend is None else np.ascontiguousarray(blend[0], np.uint32)
+    br = None if blend is None else np.ascontiguousarray(blend[1], np.uint8)
     nf = lib(features).ref_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights), len(scene.lights),
                           _p(atlas), _p(nums), _p(page_sizes), mipmap_start, _p(shadow_dyn), _p(shadow_static),
                           _p(cam), W, H, float(fov), int(view["use_linear"]), _p(clear), _p(depth), _p(ids),
-                          _p(rgba), _p(normals), nthreads, 1 if ordered else 0)
+                          _p(rgba), _p(normals), nthreads, 1 if ordered else 0, _p(bd), _p(br))
     return {"depth": depth, "id": ids, "rgba": rgba, "normals": normals, "fragments": int(nf)}
 
 

@@ -362,7 +362,20 @@ struct ShadeView {
   f3 face_c[6], face_s[6];
   uint32_t use_linear;
   f4 clear;
+  // CAN_INTEGRATED_BLEND: the blend context's depth and RGBA8, or null
+  const uint32_t* blend_depth = nullptr;
+  const uint8_t* blend_rgba = nullptr;
 };
+
+// alpha_blend (cl2.cl:1721-1728) of the blend context's texel p over c, when
+// that context is nearer than depth d (cl2.cl:5839-5851, 6339-6351).
+bool blend_over(const ShadeView& v, size_t p, uint32_t d, float c[3]) {
+  if (!v.blend_depth || !(v.blend_depth[p] < d)) return false;
+  float o[4];
+  for (int k = 0; k < 4; k++) o[k] = fdiv((float)v.blend_rgba[4 * p + k], 255.0f);
+  for (int k = 0; k < 3; k++) c[k] = fma_(o[k], o[3], c[k] * (1.0f - o[3]));
+  return true;
+}
 
 f2 get_vtdiff(const f3 tp[3], float x, float y, const ShadeView& v,
               const gbr_obj_g_descriptor& G, f2 vt, f3 p1, f3 p2, f3 p3, f2 vt1, f2 vt2, f2 vt3,
@@ -513,7 +526,11 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
     rgba[p * 4 + 3] = (uint8_t)quant8(a);
   };
   if (d == kDepthClear || key == kNoId) {
-    put(v.clear.x, v.clear.y, v.clear.z, v.clear.w);
+    float c[3] = {v.clear.x, v.clear.y, v.clear.z};
+    if (blend_over(v, p, d, c))
+      put(c[0], c[1], c[2], c[2]);  // the reference's .xyzz: alpha = blue
+    else
+      put(v.clear.x, v.clear.y, v.clear.z, v.clear.w);
     if (normals) { normals[p * 2] = 0; normals[p * 2 + 1] = 0; }
     return;
   }
@@ -665,6 +682,10 @@ void kernel3_pixel(int x, int y, const ShadeView& v, const ShadeIn& in, const Se
   f3 sp2 = mul3s(specular_sum, 1.0f - rsc);
   f3 fin = mk3(fma_(colclamp.x, diffuse_sum.x, sp2.x), fma_(colclamp.y, diffuse_sum.y, sp2.y),
                fma_(colclamp.z, diffuse_sum.z, sp2.z));
+  {
+    float c[3] = {fin.x, fin.y, fin.z};
+    if (blend_over(v, p, d, c)) fin = mk3(c[0], c[1], c[2]);
+  }
   if (v.use_linear) fin = mk3(gamma_inv(fin.x), gamma_inv(fin.y), gamma_inv(fin.z));
   if ((v.flags & GBR_VIEW_OUTLINE) && (ff & kFlagOutline) > 0) {
     // CAN_OUTLINE (cl2.cl:6368-6373)
@@ -846,9 +867,18 @@ void kernel3_pixel_fp64(int x, int y, const ShadeView& v, const ShadeIn& in, con
   const size_t p = (size_t)y * v.W + x;
   const uint32_t d = depth[p], key = ids[p];
   double* o = out + p * 4;
+  auto blend_d = [&](double c[3]) {
+    if (!v.blend_depth || !(v.blend_depth[p] < d)) return false;
+    double b[4];
+    for (int k = 0; k < 4; k++) b[k] = v.blend_rgba[4 * p + k] / 255.0;
+    for (int k = 0; k < 3; k++) c[k] = b[k] * b[3] + c[k] * (1.0 - b[3]);
+    return true;
+  };
   if (d == kDepthClear || key == kNoId) {
-    o[0] = clampd(v.clear.x, 0, 1); o[1] = clampd(v.clear.y, 0, 1);
-    o[2] = clampd(v.clear.z, 0, 1); o[3] = clampd(v.clear.w, 0, 1);
+    double c[3] = {v.clear.x, v.clear.y, v.clear.z};
+    const bool bl = blend_d(c);
+    o[0] = clampd(c[0], 0, 1); o[1] = clampd(c[1], 0, 1);
+    o[2] = clampd(c[2], 0, 1); o[3] = clampd(bl ? c[2] : v.clear.w, 0, 1);
     return;
   }
   const uint32_t tri = key >> 1;
@@ -985,6 +1015,10 @@ void kernel3_pixel_fp64(int x, int y, const ShadeView& v, const ShadeIn& in, con
   dsum = dsum * ssao;
   D3 fin = d3((col.x + ssum.x * 0.7) * dsum.x + ssum.x * 0.3, (col.y + ssum.y * 0.7) * dsum.y + ssum.y * 0.3,
               (col.z + ssum.z * 0.7) * dsum.z + ssum.z * 0.3);
+  {
+    double c[3] = {fin.x, fin.y, fin.z};
+    if (blend_d(c)) fin = d3(c[0], c[1], c[2]);
+  }
   if (v.use_linear) fin = d3(gamma_inv_d(fin.x), gamma_inv_d(fin.y), gamma_inv_d(fin.z));
   o[0] = clampd(fin.x, 0, 1);
   o[1] = clampd(fin.y, 0, 1);
@@ -1538,7 +1572,8 @@ int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
                   const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
                   const uint32_t* shadow_dyn, const uint32_t* shadow_static,
                   const gbr_camera* cam, const gbr_view* view, uint32_t* depth, uint32_t* ids,
-                  uint8_t* rgba, uint16_t* normals, int nthreads, uint64_t* nfrags_out) {
+                  uint8_t* rgba, uint16_t* normals, int nthreads, uint64_t* nfrags_out,
+                  const uint32_t* blend_depth, const uint8_t* blend_rgba) {
   const int W = view->width, H = view->height;
   const float fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
   f3 cpos = v3(cam->pos), crot = v3(cam->rot);
@@ -1558,6 +1593,8 @@ int oracle_render(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_descript
   v.use_linear = view->use_linear;
   v.clear.x = view->clear_col[0]; v.clear.y = view->clear_col[1];
   v.clear.z = view->clear_col[2]; v.clear.w = view->clear_col[3];
+  v.blend_depth = blend_depth;
+  v.blend_rgba = blend_rgba;
   ShadeIn in{tris, descs, lights, nl, Atlas{atlas, nums, sizes, mipmap_start}, shadow_dyn, shadow_static};
   parallel_for((int64_t)P, nthreads, [&](int64_t p) {
     kernel3_pixel((int)(p % W), (int)(p / W), v, in, S, depth, ids, rgba, normals);
@@ -1571,7 +1608,8 @@ int oracle_render_fp64(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_des
                        const gbr_light* lights, uint32_t nl, const uint8_t* atlas, const uint32_t* nums,
                        const uint32_t* sizes, uint32_t mipmap_start, const uint32_t* shadow_dyn,
                        const uint32_t* shadow_static, const gbr_camera* cam, const gbr_view* view,
-                       double* rgba64, int exact_acos, int nthreads) {
+                       double* rgba64, int exact_acos, int nthreads, const uint32_t* blend_depth,
+                       const uint8_t* blend_rgba) {
   const int W = view->width, H = view->height;
   const float fov = view->fov_const > 0 ? view->fov_const : oracle_fov_const(view->hfov_deg, W);
   f3 cpos = v3(cam->pos), crot = v3(cam->rot);
@@ -1588,6 +1626,8 @@ int oracle_render_fp64(const gbr_triangle* tris, uint32_t n, const gbr_obj_g_des
   v.use_linear = view->use_linear;
   v.clear.x = view->clear_col[0]; v.clear.y = view->clear_col[1];
   v.clear.z = view->clear_col[2]; v.clear.w = view->clear_col[3];
+  v.blend_depth = blend_depth;
+  v.blend_rgba = blend_rgba;
   ShadeIn in{tris, descs, lights, nl, Atlas{atlas, nums, sizes, mipmap_start}, shadow_dyn, shadow_static};
   parallel_for((int64_t)P, nthreads, [&](int64_t p) {
     kernel3_pixel_fp64((int)(p % W), (int)(p / W), v, in, S, depth.data(), ids.data(), exact_acos != 0, rgba64);

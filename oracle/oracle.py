@@ -43,10 +43,10 @@ def lib():
         L.oracle_shadow.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, ctypes.c_int]
         L.oracle_render.restype = ctypes.c_int
         L.oracle_render.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P,
-                                    ctypes.c_uint32, P, P, P, P, P, P, P, P, ctypes.c_int, P]
+                                    ctypes.c_uint32, P, P, P, P, P, P, P, P, ctypes.c_int, P, P, P]
         L.oracle_render_fp64.restype = ctypes.c_int
         L.oracle_render_fp64.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_uint32, P, P, P, ctypes.c_uint32,
-                                         P, P, P, P, P, ctypes.c_int, ctypes.c_int]
+                                         P, P, P, P, P, ctypes.c_int, ctypes.c_int, P, P]
         L.oracle_godrays.restype = ctypes.c_int
         L.oracle_godrays.argtypes = [P, P, P, ctypes.c_uint32, P, P, P, ctypes.c_int]
         L.oracle_pseudo_aa.restype = ctypes.c_int
@@ -112,8 +112,9 @@ def shadow(scene, nthreads=None):
 
 
 def render(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, shade=True,
-           nthreads=None, normals=False):
-    """Returns dict(depth, id, rgba[, normals], fragments)."""
+           nthreads=None, normals=False, blend=None):
+    """Returns dict(depth, id, rgba[, normals], fragments).  blend: (depth,
+    rgba) of a blend context (kernel3's CAN_INTEGRATED_BLEND)."""
     nthreads = nthreads or default_threads()
     W, H = int(view["width"]), int(view["height"])
     depth = np.empty((H, W), np.uint32)
@@ -127,10 +128,12 @@ def render(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, shade=Tru
     cam = np.asarray(cam).reshape(1)
     view = np.asarray(view).reshape(1)
     nf = np.zeros(1, np.uint64)
+    bd = None if blend is None else np.ascontiguousarray(blend[0], np.uint32)
+    br = None if blend is None else np.ascontiguousarray(blend[1], np.uint8)
     lib().oracle_render(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights),
                         len(scene.lights), _p(tex.atlas), _p(tex.nums), _p(tex.sizes),
                         tex.mipmap_start, _p(shadow_dyn), _p(shadow_static), _p(cam), _p(view),
-                        _p(depth), _p(ids), _p(rgba), _p(nrm), nthreads, _p(nf))
+                        _p(depth), _p(ids), _p(rgba), _p(nrm), nthreads, _p(nf), _p(bd), _p(br))
     out = {"depth": depth, "id": ids, "fragments": int(nf[0])}
     if shade:
         out["rgba"] = rgba
@@ -204,7 +207,7 @@ def render_fp64(scene, tex, cam, view, shadow_dyn=None, shadow_static=None, exac
     lib().oracle_render_fp64(_p(scene.tris), len(scene.tris), _p(scene.descs), _p(scene.lights),
                              len(scene.lights), _p(tex.atlas), _p(tex.nums), _p(tex.sizes), tex.mipmap_start,
                              _p(shadow_dyn), _p(shadow_static), _p(cam), _p(view), _p(out),
-                             1 if exact_acos else 0, nthreads)
+                             1 if exact_acos else 0, nthreads, None, None)
     return out
 
 

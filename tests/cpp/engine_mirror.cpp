@@ -14,7 +14,10 @@
 // "mb" draws a first frame from a camera moved by (6, -4, 15) and turned by
 // (0.012, -0.02, 0.005), swaps buffers, draws the frame from the scene's camera
 // and runs engine::do_motion_blur(0.75, 0.6); "ssr" runs
-// engine::draw_screenspace_reflections after the frame.
+// engine::draw_screenspace_reflections after the frame; "blend other.bin"
+// loads a second context, draws it (its lights join the list, as the
+// reference's light list is global) from its own camera and renders this one
+// with object_context::set_blend_render_context(other).
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -27,25 +30,23 @@ using namespace openclrenderer;
 template <class T>
 static bool rd(FILE* f, T* v, size_t n = 1) { return fread(v, sizeof(T), n, f) == n; }
 
-int main(int argc, char** argv) {
-  if (argc != 3 && argc != 4) {
-    fprintf(stderr, "usage: %s scene.bin out.bin [aa|mb|ssr]\n", argv[0]);
-    return 2;
-  }
-  const std::string mode = argc == 4 ? argv[3] : "";
-  FILE* f = fopen(argv[1], "rb");
-  if (!f) return 2;
-  char magic[4];
+struct Header {
   uint32_t nobj = 0, ntex = 0, nl = 0, use_linear = 1;
   float cam[8], hfov = 90.f, clear[4];
   int32_t W = 0, H = 0;
-  if (!rd(f, magic, 4) || memcmp(magic, "GBRS", 4) || !rd(f, &nobj) || !rd(f, &ntex) || !rd(f, &nl) ||
-      !rd(f, cam, 8) || !rd(f, &W) || !rd(f, &H) || !rd(f, &hfov) || !rd(f, &use_linear) || !rd(f, clear, 4))
-    return 3;
+};
 
-  object_context ctx;
+// Reads a scene file into ctx (objects, textures) and the global light list.
+static int load(const char* path, object_context& ctx, Header& h) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return 2;
+  char magic[4];
+  if (!rd(f, magic, 4) || memcmp(magic, "GBRS", 4) || !rd(f, &h.nobj) || !rd(f, &h.ntex) || !rd(f, &h.nl) ||
+      !rd(f, h.cam, 8) || !rd(f, &h.W) || !rd(f, &h.H) || !rd(f, &h.hfov) || !rd(f, &h.use_linear) ||
+      !rd(f, h.clear, 4))
+    return 3;
   std::vector<texture*> texs;
-  for (uint32_t i = 0; i < ntex; i++) {
+  for (uint32_t i = 0; i < h.ntex; i++) {
     int32_t edge = 0;
     if (!rd(f, &edge)) return 3;
     std::vector<uint8_t> px((size_t)edge * edge * 4);
@@ -54,7 +55,7 @@ int main(int argc, char** argv) {
     t->set_pixels(edge, px.data());
     texs.push_back(t);
   }
-  for (uint32_t i = 0; i < nobj; i++) {
+  for (uint32_t i = 0; i < h.nobj; i++) {
     float pos[4], quat[4], scale, spec, spec_mult, diffuse;
     int32_t ff, tex;
     uint32_t nt;
@@ -79,7 +80,7 @@ int main(int argc, char** argv) {
     if ((ff & FLAG_SS_REFLECTIVE) && tex >= 0 && (i % 2)) c->set_screenspace_map_id(texs[tex]);
     c->set_active(true);
   }
-  for (uint32_t i = 0; i < nl; i++) {
+  for (uint32_t i = 0; i < h.nl; i++) {
     gbr_light g;
     if (!rd(f, &g)) return 3;
     light l;
@@ -94,13 +95,35 @@ int main(int argc, char** argv) {
     light::add_light(&l);
   }
   fclose(f);
-
   ctx.load_active();
-  ctx.set_clear_colour(float4{clear[0], clear[1], clear[2], clear[3]});
-  ctx.set_use_linear_rendering(use_linear);
+  ctx.set_clear_colour(float4{h.clear[0], h.clear[1], h.clear[2], h.clear[3]});
+  ctx.set_use_linear_rendering(h.use_linear);
   if (ctx.build(true) != GBR_OK) {
     fprintf(stderr, "build: %s\n", gbr_last_error_string());
     return 4;
+  }
+  return 0;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3 || argc > 5) {
+    fprintf(stderr, "usage: %s scene.bin out.bin [aa|mb|ssr|blend other.bin]\n", argv[0]);
+    return 2;
+  }
+  const std::string mode = argc >= 4 ? argv[3] : "";
+  object_context ctx;
+  Header h;
+  if (int e = load(argv[1], ctx, h)) return e;
+  const float* cam = h.cam;
+  const int32_t W = h.W, H = h.H;
+  const float hfov = h.hfov;
+  // "blend": a second context, drawn first from its own camera, blended into this one
+  object_context other;
+  Header oh;
+  if (mode == "blend") {
+    if (argc != 5) return 2;
+    if (int e = load(argv[4], other, oh)) return e;
+    ctx.set_blend_render_context(other);
   }
   light_gpu lights = light::build();
   engine window;
@@ -109,6 +132,16 @@ int main(int argc, char** argv) {
   window.set_camera_pos(float4{cam[0], cam[1], cam[2], cam[3]});
   window.set_camera_rot(float4{cam[4], cam[5], cam[6], cam[7]});
   window.set_light_data(lights);
+  if (mode == "blend") {
+    window.set_camera_pos(float4{oh.cam[0], oh.cam[1], oh.cam[2], oh.cam[3]});
+    window.set_camera_rot(float4{oh.cam[4], oh.cam[5], oh.cam[6], oh.cam[7]});
+    if (window.set_object_data(*other.fetch()) != GBR_OK || window.draw_bulk_objs_n(*other.fetch()) != GBR_OK) {
+      fprintf(stderr, "blend context: %s\n", gbr_last_error_string());
+      return 5;
+    }
+    window.set_camera_pos(float4{cam[0], cam[1], cam[2], cam[3]});
+    window.set_camera_rot(float4{cam[4], cam[5], cam[6], cam[7]});
+  }
   if (mode == "mb") {  // the previous frame
     window.set_camera_pos(float4{cam[0] + 6.f, cam[1] - 4.f, cam[2] + 15.f, cam[3]});
     window.set_camera_rot(float4{cam[4] + 0.012f, cam[5] - 0.02f, cam[6] + 0.005f, cam[7]});

@@ -43,8 +43,9 @@ def write_scene(path, sc):
         f.write(np.ascontiguousarray(sc.lights).tobytes())
 
 
-def run(exe, scene_path, out_path, W, H, mode=None):
-    r = subprocess.run([exe, scene_path, out_path] + ([mode] if mode else []), capture_output=True, text=True)
+def run(exe, scene_path, out_path, W, H, mode=None, extra=()):
+    r = subprocess.run([exe, scene_path, out_path] + ([mode] if mode else []) + list(extra), capture_output=True,
+                       text=True)
     assert r.returncode == 0, r.stderr
     raw = np.fromfile(out_path, np.uint8)
     P = W * H

@@ -116,12 +116,40 @@ def main_post():
     print("post:", {k: v for k, v in meta.items() if "changed" in k})
 
 
+def main_blend():
+    """kernel3 built with CAN_INTEGRATED_BLEND, each view of the
+    golden_cases.BLEND cases blended with golden_cases.blend_source: SHA-256
+    digests of the RGBA8 and the count of pixels the blend changed."""
+    meta = {}
+    for name in golden_cases.BLEND:
+        sc, opts = golden_cases.CASES[name]()
+        src = np.load(os.path.join(OUT, f"{name}.npz"))
+        tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+        dyn = sta = None
+        if opts.get("shadows"):
+            dyn, sta = R.shadow(sc)
+        for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+            W, H = int(view["width"]), int(view["height"])
+            fov = float(view["fov_const"]) if view["fov_const"] > 0 else O.fov_const(float(view["hfov_deg"]), W)
+            r = R.render(sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov, dyn, sta,
+                         features=True, blend=golden_cases.blend_source(W, H))
+            for key in ("depth", "id"):
+                assert np.array_equal(r[key], src[f"{key}{k}"]), f"{name} view {k}: {key} differs from the fixture"
+            meta[f"{name}{k}"] = sha(r["rgba"])
+            meta[f"{name}_changed{k}"] = int(np.count_nonzero(np.any(r["rgba"] != src[f"rgba{k}"], axis=-1)))
+    path = os.path.join(OUT, "blend.npz")
+    np.savez_compressed(path, meta=np.array(json.dumps(meta)))
+    print("blend:", {k: v for k, v in meta.items() if "changed" in k})
+
+
 if __name__ == "__main__":
     args = sys.argv[1:]
-    cases = [a for a in args if a not in ("godrays", "post")]
+    cases = [a for a in args if a not in ("godrays", "post", "blend")]
     if cases or not args:
         main(cases or None)
     if not args or "godrays" in args:
         main_godrays()
     if not args or "post" in args:
         main_post()
+    if not args or "blend" in args:
+        main_blend()

@@ -101,6 +101,17 @@ def features():
     return sc, {"shadows": True, "normals": True, "features": True}
 
 
+def blend_source(width, height, seed=61):
+    """A second render context's frame for kernel3's integrated blend: depth
+    (a third of it empty) spread over the scenes' depth range, RGBA8 with
+    every alpha."""
+    rng = np.random.default_rng(seed)
+    depth = (rng.random((height, width)) * 0.02 * 2**32).astype(np.uint32)
+    depth[rng.random((height, width)) < 0.33] = 0xFFFFFFFF
+    rgba = rng.integers(0, 256, (height, width, 4), dtype=np.uint8)
+    return depth, rgba
+
+
 def godray_lights():
     """Lights of the screenspace_godrays fixture over the cubes views: one
     beyond the cubes, one behind the camera (mirrored march), one off to the
@@ -154,6 +165,9 @@ MOTION = [(0, 0.75, 0.6), (1, 1.5, 0.25)]
 
 # post passes over the views of a rendered case: fixture name -> source case
 POST = {"godrays": "cubes", "post": "cubes"}
+
+# cases rendered again with an integrated blend source (blend_source)
+BLEND = ["cubes", "features"]
 
 CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
          "wide_boxes": wide_boxes, "features": features}

@@ -102,3 +102,36 @@ def test_engine_mirror_matches_c_abi(tmp_path, name):
     for k in ("depth", "id", "rgba"):
         assert np.array_equal(got[k], ref[k]), f"{name}: {k} differs ({np.count_nonzero(got[k] != ref[k])})"
     assert (ref["depth"] != 0xFFFFFFFF).sum() > 1000
+
+
+@pytest.mark.gpu
+def test_engine_mirror_blend_render_context(tmp_path):
+    """object_context::set_blend_render_context: the engine draws the other
+    context, then this one with its frame blended in (kernel3's integrated
+    blend), as gbr_render_view_blend does."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():  # pragma: no cover
+        pytest.skip("no CUDA device")
+    from openclrenderer_gb300 import structs as S
+    from openclrenderer_gb300.pipeline import GpuScene
+    sc = scenes.plain_cubes()
+    other = scenes.plain_cubes(seed=7)
+    other.lights = np.zeros(0, S.LIGHT)  # the light list is global: other renders with sc's lights
+    other.cameras = [S.make_camera((20.0, -10.0, -50.0), (0.02, 0.05, 0.0))]
+    cam, view = sc.cameras[0], sc.views[0]
+    W, H = int(view["width"]), int(view["height"])
+    exe = M.build(str(tmp_path))
+    M.write_scene(str(tmp_path / "scene.bin"), sc)
+    M.write_scene(str(tmp_path / "other.bin"), other)
+    got = M.run(exe, str(tmp_path / "scene.bin"), str(tmp_path / "out.bin"), W, H, "blend",
+                [str(tmp_path / "other.bin")])
+    go = GpuScene(other)
+    go.set_lights(sc.lights)
+    src = go.render(other.cameras[0], other.views[0])
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    ref = gs.render(cam, view, blend=src).numpy()
+    plain = gs.render(cam, view).numpy()
+    for k in ("depth", "id", "rgba"):
+        assert np.array_equal(got[k], ref[k]), f"{k} differs ({np.count_nonzero(got[k] != ref[k])})"
+    assert np.count_nonzero(np.any(ref["rgba"] != plain["rgba"], axis=-1)) > 1000

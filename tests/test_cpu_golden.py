@@ -204,3 +204,18 @@ def test_oracle_reflections_match_reference_kernel_random(seed):
     r = R.post("reflections", sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, cam, view, fov)
     got = O.reflections(sc, sc.descs, tex, r["depth"], r["id"], r["rgba"], cam, view)
     assert np.array_equal(got, r["post"]), f"{np.count_nonzero(got != r['post'])} values differ"
+
+
+def test_oracle_integrated_blend_matches_reference_fixture():
+    """kernel3 with CAN_INTEGRATED_BLEND (cl2.cl:5839-5851, 6339-6351)."""
+    meta = json.loads(str(np.load(os.path.join(GOLDEN, "blend.npz"))["meta"]))
+    for name in golden_cases.BLEND:
+        sc, opts = golden_cases.CASES[name]()
+        tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+        dyn = sta = None
+        if opts.get("shadows"):
+            dyn, sta = O.shadow(sc)
+        for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+            bl = golden_cases.blend_source(int(view["width"]), int(view["height"]))
+            got = O.render(sc, tex, cam, view, dyn, sta, blend=bl)
+            assert sha(got["rgba"]) == meta[f"{name}{k}"], f"{name} view {k}: blend differs from the reference"

@@ -377,3 +377,39 @@ def test_godrays_post_pass_parity():
     r.rgba = big[:n]
     with pytest.raises(Exception):  # output shifted by one pixel over the input
         gs.post_godrays(cam, view, r, rgba_out=big[4:])
+
+
+def test_integrated_blend_parity():
+    """kernel3's CAN_INTEGRATED_BLEND: a second context's depth / RGBA8 blended
+    in where nearer, against the oracle (which the reference kernels' digests
+    pin on the CPU)."""
+    import json
+    import os
+
+    from tests import golden_cases
+    from openclrenderer_gb300.pipeline import OutputSet
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    meta = json.loads(str(np.load(os.path.join(gold, "blend.npz"))["meta"]))
+    for name in golden_cases.BLEND:
+        sc, opts = golden_cases.CASES[name]()
+        gs = GpuScene(sc)
+        tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+        dyn = sta = None
+        if opts.get("shadows"):
+            gs.shadow_pass()
+            dyn, sta = O.shadow(sc)
+        for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+            W, H = int(view["width"]), int(view["height"])
+            bd, br = golden_cases.blend_source(W, H)
+            src = OutputSet(W, H)
+            src.depth.copy_(torch.from_numpy(bd.view(np.int32)))
+            src.rgba.copy_(torch.from_numpy(br))
+            got = gs.render(cam, view, blend=src).numpy()
+            ref = O.render(sc, tex, cam, view, dyn, sta, blend=(bd, br))
+            assert_parity(got, ref, f"{name} view {k}")
+            # the background path is IEEE throughout: exact
+            bg = got["depth"] == 0xFFFFFFFF
+            assert np.array_equal(got["rgba"][bg], ref["rgba"][bg])
+            changed = np.count_nonzero(np.any(ref["rgba"] != O.render(sc, tex, cam, view, dyn, sta)["rgba"], -1))
+            assert abs(changed - meta[f"{name}_changed{k}"]) < 0.01 * changed
+        gs.close()
