@@ -360,6 +360,10 @@ gbr_status gbr_batch_launch(gbr_batch* batch, const gbr_camera* cams, void* stre
 /* Wait for the last launch and check its scratch bounds (rendering it again
  * when they overflowed). */
 gbr_status gbr_batch_wait(gbr_batch* batch);
+/* gbr_batch_wait bounded by timeout_ms (< 0: unbounded): GBR_DEVICE_TIMEOUT
+ * when the frame is still running then; it stays in flight and a later wait
+ * completes it. */
+gbr_status gbr_batch_wait_for(gbr_batch* batch, int32_t timeout_ms);
 /* gbr_batch_launch + gbr_batch_wait. */
 gbr_status gbr_batch_render(gbr_batch* batch, const gbr_camera* cams, void* stream);
 /* Autotuner: times `reps` graph launches per candidate shape (coordinate
@@ -430,6 +434,9 @@ gbr_status gbr_server_poll(gbr_server* server, gbr_completion* out, uint32_t cap
                            int32_t wait_ms);
 /* Wait until every submitted request has completed. */
 gbr_status gbr_server_drain(gbr_server* server);
+/* gbr_server_drain bounded by timeout_ms (< 0: unbounded): GBR_DEVICE_TIMEOUT
+ * when requests are still in the system then. */
+gbr_status gbr_server_drain_for(gbr_server* server, int32_t timeout_ms);
 gbr_status gbr_server_stats_get(gbr_server* server, gbr_server_stats* out);
 gbr_status gbr_server_destroy(gbr_server* server);
 

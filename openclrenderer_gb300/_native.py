@@ -102,6 +102,7 @@ SIGNATURES = {
     "gbr_batch_create": (ctypes.c_int, [_P, _U32, _P, _P, ctypes.c_int32, _P]),
     "gbr_batch_launch": (ctypes.c_int, [_P, _P, _P]),
     "gbr_batch_wait": (ctypes.c_int, [_P]),
+    "gbr_batch_wait_for": (ctypes.c_int, [_P, ctypes.c_int32]),
     "gbr_batch_render": (ctypes.c_int, [_P, _P, _P]),
     "gbr_batch_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P, _P, _P]),
     "gbr_batch_set_tuning": (ctypes.c_int, [_P, ctypes.c_int32, _P]),
@@ -121,6 +122,7 @@ SIGNATURES = {
     "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),
     "gbr_server_poll": (ctypes.c_int, [_P, _P, _U32, _P, ctypes.c_int32]),
     "gbr_server_drain": (ctypes.c_int, [_P]),
+    "gbr_server_drain_for": (ctypes.c_int, [_P, ctypes.c_int32]),
     "gbr_server_stats_get": (ctypes.c_int, [_P, _P]),
     "gbr_server_destroy": (ctypes.c_int, [_P]),
 }

@@ -5,8 +5,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/gbr.h"
@@ -282,6 +284,25 @@ gbr_status gbr_batch_wait(gbr_batch* b) {
   if (!b) return fail(GBR_INVALID_ARG, "null batch");
   TRY(check_scene(b->s));
   return wait_frame(b);
+}
+
+gbr_status gbr_batch_wait_for(gbr_batch* b, int32_t timeout_ms) {
+  if (!b) return fail(GBR_INVALID_ARG, "null batch");
+  if (timeout_ms < 0) return gbr_batch_wait(b);
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+  for (;;) {
+    {
+      GBR_SCENE_LOCK(b->s);
+      TRY(check_scene(b->s));
+      if (!b->in_flight) return GBR_OK;
+      const cudaError_t e = cudaEventQuery(b->done);
+      if (e == cudaSuccess) return wait_frame(b);
+      if (e != cudaErrorNotReady) return fail(GBR_CUDA_ERROR, "batch event: %s", cudaGetErrorString(e));
+    }
+    if (std::chrono::steady_clock::now() >= deadline)
+      return fail(GBR_DEVICE_TIMEOUT, "batch still running after %d ms", timeout_ms);
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
 }
 
 gbr_status gbr_batch_render(gbr_batch* b, const gbr_camera* cams, void* stream) {

@@ -29,7 +29,7 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
     f3 iter_col = mk3(0, 0, 0);
     const f3 lpos = mk3(L.pos[0], L.pos[1], L.pos[2]);
     const f3 slpos = depth_project1(rot_cs(lpos, cpos, cc, cs), (float)W, (float)H, fov);
-    f3 current = mk3((float)x, (float)y, fdiv((float)my_depth, kMulInt) * kDepthFar);
+    f3 current = mk3((float)x, (float)y, depth_to_dist(my_depth));
     f3 dest = slpos;
     const f3 original = current;
     if (slpos.z < 0) dest = add3(sub3(current, dest), current);
@@ -38,21 +38,43 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
     f3 dir = sub3(dest, current);
     dir = mk3(fdiv(dir.x, mnum), fdiv(dir.y, mnum), fdiv(dir.z, mnum));
     dir = mul3s(dir, step);
-    const f3 col = mk3(L.col[0], L.col[1], L.col[2]);
-    for (int j = 0; (float)j < mnum && (float)j < samples; j++) {
-      // the reference skips the rest of the march once it leaves the screen
-      if (current.x < 0 || current.y < 0 || current.x >= (float)W - 1.0f || current.y >= (float)H - 1.0f) break;
-      const uint32_t cdepth = depth[(size_t)((int)current.y) * W + (int)current.x];
-      const float fdepth = fdiv((float)cdepth, kMulInt) * kDepthFar;
-      f3 val = mk3(0, 0, 0);
-      if (fdepth < original.z - 5.0f && cdepth != 0xFFFFFFFFu) {
-        idecay *= 0.9f;
-        val = mul3s(col, ray_intensity);
+    const f3 cval = mul3s(mk3(L.col[0], L.col[1], L.col[2]), ray_intensity);
+    const float thr = original.z - 5.0f;
+    const float xmax = (float)W - 1.0f, ymax = (float)H - 1.0f;
+    // steps j with (float)j < mnum and j < samples
+    const int n = mnum > 0.0f ? (int)fminf(ceilf(mnum), samples) : 0;
+    float cx = current.x, cy = current.y;
+    // Eight steps at a time: their positions (the same running sums as the
+    // reference's current += dir), then their depth loads in flight together,
+    // then the decay chain in order.  The reference skips the rest of the
+    // march once it leaves the screen; an unoccluded step adds exactly 0.
+    for (int j0 = 0; j0 < n; j0 += 8) {
+      float px[8], py[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        px[k] = cx;
+        py[k] = cy;
+        cx += dir.x;
+        cy += dir.y;
       }
-      val = mul3s(mul3s(val, idecay), weight);
-      iter_col = add3(iter_col, val);
-      idecay *= decay_factor;
-      current = add3(current, dir);
+      int m = 8;
+#pragma unroll
+      for (int k = 7; k >= 0; k--)
+        if (j0 + k >= n || px[k] < 0 || py[k] < 0 || px[k] >= xmax || py[k] >= ymax) m = k;
+      uint32_t dv[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) dv[k] = k < m ? __ldg(depth + (size_t)((int)py[k]) * W + (int)px[k]) : 0u;
+#pragma unroll
+      for (int k = 0; k < 8; k++) {
+        if (k < m) {
+          if (depth_to_dist(dv[k]) < thr && dv[k] != kDepthClear) {
+            idecay *= 0.9f;
+            iter_col = add3(iter_col, mul3s(mul3s(cval, idecay), weight));
+          }
+          idecay *= decay_factor;
+        }
+      }
+      if (m < 8) break;
     }
     my_col.x += iter_col.x;
     my_col.y += iter_col.y;
@@ -95,7 +117,7 @@ __device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int H, cons
                                                 const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
                                                 f3* out) {
   const size_t p = (size_t)y * W + x;
-  const float here = fdiv((float)depth[p], kMulInt) * kDepthFar;
+  const float here = depth_to_dist(depth[p]);
   const ushort2 np = nrm[p];
   const f3 n0 = fast_normalize3(decode_normal(np.x, np.y));
   int horiz[2] = {0, 0}, vert[2] = {0, 0}, diag[2] = {0, 0};
@@ -107,7 +129,7 @@ __device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int H, cons
     for (int dx = -1; dx <= 1; dx++) {
       if (dx == 0 && dy == 0) continue;
       const size_t q = (size_t)(y + dy) * W + (x + dx);
-      const float d = fdiv((float)depth[q], kMulInt) * kDepthFar;
+      const float d = depth_to_dist(depth[q]);
       const ushort2 nq = nrm[q];
       const f3 n = decode_normal(nq.x, nq.y);
       const uchar4 t = in[q];
@@ -196,7 +218,7 @@ __global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restr
   const uint32_t obj = __ldg(&tris[id >> 1].vertices[0].object_id);
   if (!seen[obj]) seen[obj] = 1u;
   const gbr_obj_g_descriptor* G = descs + obj;
-  const float dist = fdiv((float)d, kMulInt) * kDepthFar;
+  const float dist = depth_to_dist(d);
   const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, a.fov), fdiv(((float)y - (float)H / 2.0f) * dist, a.fov),
                        dist);
   const f3 world = add3(back_rot_cs(local, mk3(0, 0, 0), a.cc, a.cs), a.cpos);
@@ -321,7 +343,7 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
   const uint32_t o_id = __ldg(&T->vertices[0].object_id);
   const gbr_obj_g_descriptor* G = sc.descs + o_id;
   if (!((__ldg(&G->feature_flag) & 1) > 0)) return 0;
-  const float dist = fdiv((float)d, kMulInt) * kDepthFar;
+  const float dist = depth_to_dist(d);
   const f3 local = mk3(fdiv(((float)x - (float)W / 2.0f) * dist, v.fov), fdiv(((float)y - (float)H / 2.0f) * dist, v.fov),
                        dist);
   const f3 zero = mk3(0, 0, 0);
@@ -399,24 +421,50 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
                  rcp(ss.z) * back + rcp(sj.z) * (1.0f - back));
   vprev.z = rcp(vprev.z);
   const f3 vstart = sj;
-  f3 cur = sj;
   const float fw = (float)W, fh = (float)H;
-  if (cur.x < 0 || cur.y < 0 || cur.x >= fw || cur.y >= fh) return 0;
+  if (sj.x < 0 || sj.y < 0 || sj.x >= fw || sj.y >= fh) return 0;
+  // The march: step i at sj (i = 0) or line_depth_point(vprev, vstart, 1 + i),
+  // until the depth buffer is more than 1 unit in front of the ray.  Four
+  // steps at a time: positions first (they do not depend on the loads), then
+  // their depth loads in flight together, then the tests in order.
+  const float ipz = rcp(vprev.z), isz = rcp(vstart.z);  // line_depth_point's reciprocals, loop-invariant
+  f3 cur = sj;
+  float a = 1.0f, stop = 0.0f;
   bool found = false;
-  float a = 1.0f;
-  for (int i = 0; i < 200; i++) {
-    if (cur.x < 0 || cur.y < 0 || cur.x >= fw || cur.y >= fh) return 0;
-    const uint32_t cd = depth[(size_t)f2i_sat(cur.y) * W + f2i_sat(cur.x)];
-    if (fdiv((float)cd, kMulInt) * kDepthFar < cur.z - 1.0f) {
-      found = true;
-      break;
+  for (int i0 = 0; i0 < 200 && !found; i0 += 4) {
+    f3 pt[4];
+    int m = 4;  // the first step off screen
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int i = i0 + k;
+      if (i == 0) {
+        pt[k] = sj;
+      } else {
+        const float ai = 1.0f + (float)i, b = 1.0f - ai;
+        pt[k] = mk3(fma_(vprev.x, b, vstart.x * ai), fma_(vprev.y, b, vstart.y * ai),
+                    rcp(fma_(ipz, b, isz * ai)));
+      }
     }
-    a += 1.0f;
-    cur = line_depth_point(vprev, vstart, a);
+#pragma unroll
+    for (int k = 3; k >= 0; k--)
+      if (pt[k].x < 0 || pt[k].y < 0 || pt[k].x >= fw || pt[k].y >= fh) m = k;
+    uint32_t dv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) dv[k] = k < m ? __ldg(depth + (size_t)f2i_sat(pt[k].y) * W + f2i_sat(pt[k].x)) : 0u;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (found) break;
+      if (k >= m) return 0;  // off screen before the ray met anything
+      const float dd = depth_to_dist(dv[k]);
+      if (dd < pt[k].z - 1.0f) {
+        found = true;
+        cur = pt[k];
+        a = 1.0f + (float)(i0 + k);
+        stop = dd;  // the refinement reads the depth where the march stopped on every try
+      }
+    }
   }
   if (!found) return 0;
-  // the refinement reads the depth where the march stopped on every try
-  const float stop = fdiv((float)depth[(size_t)f2i_sat(cur.y) * W + f2i_sat(cur.x)], kMulInt) * kDepthFar;
   float ta = a;
   f3 hit = cur;
   bool ok = false;

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/gbr.h"
+#include "gbr_scene.h"
 #include "gbr_internal.h"
 
 namespace {
@@ -314,6 +315,16 @@ gbr_status gbr_server_drain(gbr_server* s) {
   if (!s) return GBR_INVALID_ARG;
   std::unique_lock<std::mutex> lk(s->mu);
   s->cv_done.wait(lk, [&] { return s->in_system == 0; });
+  return GBR_OK;
+}
+
+gbr_status gbr_server_drain_for(gbr_server* s, int32_t timeout_ms) {
+  if (!s) return GBR_INVALID_ARG;
+  if (timeout_ms < 0) return gbr_server_drain(s);
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return s->in_system == 0; }))
+    return gbr::fail(GBR_DEVICE_TIMEOUT, "%llu requests still in the system after %d ms",
+                (unsigned long long)s->in_system, timeout_ms);
   return GBR_OK;
 }
 

@@ -316,8 +316,13 @@ class Batch:
         self._pending = self._cams(cams)
         _native.check(self.L.gbr_batch_launch(self.h, _np_ptr(self._pending), _stream_ptr(stream)))
 
-    def wait(self):
-        _native.check(self.L.gbr_batch_wait(self.h))
+    def wait(self, timeout_ms=None):
+        """Wait for the launched frame; with timeout_ms, GbrError
+        GBR_DEVICE_TIMEOUT if it is still running then (it stays in flight)."""
+        if timeout_ms is None:
+            _native.check(self.L.gbr_batch_wait(self.h))
+        else:
+            _native.check(self.L.gbr_batch_wait_for(self.h, int(timeout_ms)))
         return self.outs
 
     def autotune(self, cams, reps=3, stream=None):
@@ -395,8 +400,11 @@ class Server:
             self._keep.pop(int(r), None)
         return done
 
-    def drain(self):
-        _native.check(self.L.gbr_server_drain(self.h))
+    def drain(self, timeout_ms=None):
+        if timeout_ms is None:
+            _native.check(self.L.gbr_server_drain(self.h))
+        else:
+            _native.check(self.L.gbr_server_drain_for(self.h, int(timeout_ms)))
 
     def stats(self):
         st = np.zeros(1, S.SERVER_STATS)

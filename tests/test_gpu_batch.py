@@ -156,3 +156,26 @@ def test_autotune_picks_a_valid_shape():
     ref = [o.numpy() for o in gs.render_batch(sc.cameras, sc.views)]
     for i in range(len(ref)):
         same(ref[i], got[i], f"tuned view {i}")
+
+
+def test_bounded_batch_wait():
+    """gbr_batch_wait_for: GBR_DEVICE_TIMEOUT while the frame still runs, the
+    frame stays in flight, and a later wait completes it with the right
+    results."""
+    sc = scenes.spheres_batch(n_spheres=300, n_views=32)
+    gs = GpuScene(sc)
+    b = Batch(gs, sc.views)
+    ref = [o.numpy() for o in b.render(sc.cameras)]
+    timeouts = 0
+    for _ in range(5):
+        b.launch(sc.cameras)
+        try:
+            b.wait(timeout_ms=0)
+        except _native.GbrError as e:
+            assert e.status == "GBR_DEVICE_TIMEOUT"
+            timeouts += 1
+        b.wait(timeout_ms=60000)
+        got = [o.numpy() for o in b.outs]
+        for i in range(len(ref)):
+            same(ref[i], got[i], f"view {i}")
+    assert timeouts >= 1

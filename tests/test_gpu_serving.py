@@ -98,3 +98,23 @@ def test_serving_rejects_oversized_and_overlaps_scenes():
     assert st["p99_ms"] >= st["p50_ms"] > 0
     assert wall < 30
     assert any(int(b[..., 3].max()) > 0 for b in bufs)
+
+
+def test_bounded_drain():
+    """gbr_server_drain_for: GBR_DEVICE_TIMEOUT while requests are in the
+    system; an unbounded drain then completes them all."""
+    scs = _scenes()
+    gss = [GpuScene(sc) for sc in scs]
+    rng = np.random.default_rng(7)
+    reqs = _requests(60, rng)
+    srv = Server(gss, hbm_budget_bytes=2 * 1280 * 720 * 46)
+    for k, (s, cam, view) in enumerate(reqs):
+        W, H = int(view["width"]), int(view["height"])
+        srv.submit(s, cam, view, np.zeros((H, W), np.uint32), None, np.zeros((H, W, 4), np.uint8), tag=k)
+    with pytest.raises(_native.GbrError) as e:
+        srv.drain(timeout_ms=0)
+    assert e.value.status == "GBR_DEVICE_TIMEOUT"
+    srv.drain(timeout_ms=120000)
+    done = srv.poll(cap=1024)
+    assert len(done) == len(reqs) and all(c["status"] == 0 for c in done)
+    srv.close()
