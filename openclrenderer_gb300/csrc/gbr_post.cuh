@@ -63,7 +63,9 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
         if (j0 + k >= n || px[k] < 0 || py[k] < 0 || px[k] >= xmax || py[k] >= ymax) m = k;
       uint32_t dv[8];
 #pragma unroll
-      for (int k = 0; k < 8; k++) dv[k] = k < m ? __ldg(depth + (size_t)((int)py[k]) * W + (int)px[k]) : 0u;
+      // (cvt.rzi: truncation, NaN -> 0, so a NaN march stays in bounds as in the oracle)
+      for (int k = 0; k < 8; k++)
+        dv[k] = k < m ? __ldg(depth + (size_t)__float2int_rz(py[k]) * W + __float2int_rz(px[k])) : 0u;
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         if (k < m) {

@@ -1134,7 +1134,7 @@ void godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* in, int W
     float decay = 1.0f, sx = 0, sy = 0, sz = 0;
     for (int j = 0; (float)j < steps && j < 80; j++) {
       if (cur.x < 0 || cur.y < 0 || cur.x >= (float)(W - 1) || cur.y >= (float)(H - 1)) break;
-      const uint32_t cd = depth[(size_t)(int)cur.y * W + (int)cur.x];
+      const uint32_t cd = depth[(size_t)f2i_sat(cur.y) * W + f2i_sat(cur.x)];  // (NaN -> 0, as the GPU converts)
       float r = 0, g = 0, b = 0;
       if (cd != kDepthClear && depth_to_dist(cd) < here - 5.0f) {
         decay = decay * 0.9f;

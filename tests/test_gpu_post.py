@@ -160,3 +160,39 @@ def test_reflections_on_terrain_parity():
     ref = O.reflections(sc, sc.descs, tex, h["depth"], h["id"], h["rgba"], cam, view)
     assert np.array_equal(got, ref), f"{np.count_nonzero(got != ref)} values differ from the oracle"
     assert np.count_nonzero(np.any(got != h["rgba"], axis=-1) & (h["depth"] != 0xFFFFFFFF)) > 100
+
+
+@pytest.mark.parametrize("size", [(1, 1), (2, 3), (3, 2), (17, 5), (64, 48)])
+def test_post_passes_on_small_and_ragged_views(size):
+    """Every post pass on views from 1x1 up, with random depth (a third empty),
+    ids (some with depth but no id) and colours, against the oracle."""
+    W, H = size
+    sc = golden_cases.CASES["cubes"]()[0]
+    sc.descs = golden_cases.reflect_descs(golden_cases.motion_descs(sc.descs))
+    sc.descs["ssid"][1::3] = 0
+    lights = golden_cases.godray_lights()
+    sc.lights = lights
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    gs = GpuScene(sc)
+    rng = np.random.default_rng(W * 100 + H)
+    depth = (rng.random((H, W)) * 0.01 * 2**32).astype(np.uint32)
+    depth[rng.random((H, W)) < 0.33] = 0xFFFFFFFF
+    ids = rng.integers(0, 2 * len(sc.tris), (H, W)).astype(np.uint32)
+    ids[(depth == 0xFFFFFFFF) | (rng.random((H, W)) < 0.1)] = 0xFFFFFFFF
+    rgba = rng.integers(0, 256, (H, W, 4), dtype=np.uint8)
+    normals = rng.integers(0, 65536, (H, W, 2), dtype=np.uint16)
+    cam = S.make_camera((3.0, -2.0, -10.0), (0.05, -0.04, 0.0))
+    view = S.make_view(W, H, 90.0)
+    f = Frame(depth, ids, rgba, normals)
+    got = gs.post_godrays(cam, view, f).cpu().numpy()
+    assert np.array_equal(got, O.godrays(depth, rgba, lights, cam, view))
+    got = gs.post_pseudo_aa(view, f).cpu().numpy()
+    assert np.array_equal(got, O.pseudo_aa(depth, ids, normals, rgba))
+    old = golden_cases.motion_cameras(cam)
+    got = gs.post_motion_blur(cam, old, view, f, 3, 1.7, 0.3).cpu().numpy()
+    ref, ref_descs = O.motion_blur(sc, sc.descs, depth, ids, rgba, cam, old, view, 3, 1.7, 0.3)
+    assert np.array_equal(got, ref)
+    assert gs.descriptors(len(sc.descs)).tobytes() == ref_descs.tobytes()
+    gs.set_descriptors(sc.descs)
+    got = gs.post_reflections(cam, view, f).cpu().numpy()
+    assert np.array_equal(got, O.reflections(sc, sc.descs, tex, depth, ids, rgba, cam, view))
