@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -200,6 +201,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(mark(3, geom));
   CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom, sh.tiles_per_surface));
   CU(mark(4, geom));
+  if (view && s->mark_raster) CU(cudaEventRecord(s->raster_done, geom));
   if (split) {
     CU(cudaEventRecord(join, geom));
     CU(cudaStreamWaitEvent(st, join, 0));
@@ -465,6 +467,9 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   if (s->pre_shadow) cudaEventDestroy(s->pre_shadow);
   if (s->geom_done) cudaEventDestroy(s->geom_done);
   if (s->aux) cudaStreamDestroy(s->aux);
+  if (s->raster_done) cudaEventDestroy(s->raster_done);
+  if (s->copies_done) cudaEventDestroy(s->copies_done);
+  if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
   delete s;
   return GBR_OK;
 }
@@ -725,8 +730,11 @@ gbr_status gbr_shadow_pass(gbr_scene* s, void* stream) {
   return GBR_OK;
 }
 
+// after_enqueue, when given, runs after each attempt's pass is queued and
+// before the stream is synchronised (gbr_render_view_host queues its copies).
 static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams, const gbr_view* views,
-                               const gbr_outputs* outs, cudaStream_t st, const gbr_outputs* blend = nullptr) {
+                               const gbr_outputs* outs, cudaStream_t st, const gbr_outputs* blend = nullptr,
+                               const std::function<gbr_status()>* after_enqueue = nullptr) {
   TRY(check_scene(s));
   if (!n) return GBR_OK;
   if (!cams || !views || !outs) return fail(GBR_INVALID_ARG, "null camera/view/output array");
@@ -793,6 +801,7 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   }
   for (int attempt = 0; attempt < 8; attempt++) {
     TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
+    if (after_enqueue) TRY((*after_enqueue)());
     CU(cudaStreamSynchronize(st));
     bool rerun = false;
     TRY(settle_shadow(s, true, &rerun));  // same stream: already complete
@@ -833,10 +842,28 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   TRY(hw.pix_id.reserve(P));
   TRY(hw.pix_rgba.reserve(P * 4));
   gbr_outputs o{hw.pix_depth.p, hw.pix_id.p, hw.pix_rgba.p, nullptr};
-  TRY(render_views(s, 1, cam, view, &o, st));
-  if (depth) CU(cudaMemcpyAsync(depth, o.depth, P * 4, cudaMemcpyDeviceToHost, st));
-  if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, st));
-  if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
+  if (!s->copy_stream) {
+    CU(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&s->raster_done, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&s->copies_done, cudaEventDisableTiming));
+  }
+  // depth and id are final once the raster has run: they travel to the host
+  // on the copy stream while kernel3 shades; RGBA8 follows kernel3 on st.
+  // Each attempt queues its own copies (a re-run after an overflow
+  // overwrites them); st waits for the copy stream before it is synchronised.
+  const std::function<gbr_status()> copies = [&]() -> gbr_status {
+    CU(cudaStreamWaitEvent(s->copy_stream, s->raster_done, 0));
+    if (depth) CU(cudaMemcpyAsync(depth, o.depth, P * 4, cudaMemcpyDeviceToHost, s->copy_stream));
+    if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, s->copy_stream));
+    CU(cudaEventRecord(s->copies_done, s->copy_stream));
+    if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamWaitEvent(st, s->copies_done, 0));
+    return GBR_OK;
+  };
+  s->mark_raster = true;
+  const gbr_status r = render_views(s, 1, cam, view, &o, st, nullptr, &copies);
+  s->mark_raster = false;
+  TRY(r);
   CU(cudaStreamSynchronize(st));
   return GBR_OK;
 }

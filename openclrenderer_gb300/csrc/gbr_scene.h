@@ -165,6 +165,11 @@ struct gbr_scene {
   bool pre_shadow_valid = false;  // pre_shadow marks the pending shadow pass's start
   bool overlap = true;
   bool view_shaded = true;  // the last view pass ran kernel3
+  // gbr_render_view_host: depth and id leave for the host on copy_stream as
+  // soon as the raster has written them (raster_done), while kernel3 runs
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t raster_done = nullptr, copies_done = nullptr;
+  bool mark_raster = false;  // record raster_done in the next view pass
   uint64_t version = 1;  // bumped whenever a device pointer or table a pass reads changes
 
   gbr::SceneDev dev() const {
