@@ -153,8 +153,9 @@ def test_walk_rule_matches_literal_walk(tmp_path):
 
 
 def test_walk_boundaries_are_at_most_one_late(tmp_path):
-    """The premise of the walk rule, exhaustively for every width <= 800 and top row < 600
-    (the full 3840x2160 run is recorded in the design doc)."""
+    """The premise of the walk rule, exhaustively for every width <= 800 and top row < 600.
+    (Run with arguments 3840 2160, the same program covers every width <= 3840 and
+    top row < 2160: no early boundary and none two steps late there either.)"""
     exe = tmp_path / "wbc"
     subprocess.run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-o", str(exe),
                     os.path.join(ROOT, "tests", "cpp", "walk_boundary_check.c"), "-lm"], check=True)
