@@ -190,10 +190,13 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(cudaMemsetAsync(ws.coarse_count, 0, sizeof(uint32_t) * std::max<uint32_t>(sh.ncoarse, 1), geom));
   auto mark = [&](int k, cudaStream_t on) -> cudaError_t { return ev ? cudaEventRecord(ev[k], on) : cudaSuccess; };
   CU(mark(0, geom));
-  if (view)
+  if (view) {
     CU(launch_setup_views(sd, wm.views.p, sh.nitems, wm.surf.p, ws, geom));
-  else
+  } else {
+    // the setup writes small triangles straight into the faces
+    CU(launch_clear_surfaces(wm.surf.p, sh.nsurf, geom));
     CU(launch_setup_shadow(sd, wm.jobs.p, sh.nitems, wm.surf.p, ws, geom));
+  }
   CU(mark(1, geom));
   CU(launch_scan(ws, geom));
   CU(mark(2, geom));
@@ -271,7 +274,7 @@ gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream
 bool check_pass(gbr_scene* s, bool view) {
   const Counters c = *counter_slot(s, view);
   if (s->profile) {
-    const int sb = view ? 4 : 0, nst = (int)pass_kernels(view);
+    const int sb = view ? 4 : 0, nst = (int)pass_stages(view);
     for (int k = 0; k < nst; k++) {
       if (view && k == 4 && !s->view_shaded) continue;
       float ms = 0.f;

@@ -171,6 +171,8 @@ cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uin
 cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
                         uint32_t mipmap_start, const int32_t* tsizes, uint32_t ntex,
                         int32_t max_size, cudaStream_t st);
+// depth-only passes: every surface's depth to UINT_MAX (16-byte aligned buffers)
+cudaError_t launch_clear_surfaces(const Surface* d_surf, uint32_t nsurf, cudaStream_t st);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 // screenspace_godrays over a rendered view (RGBA8 in / out, distinct buffers).
 cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_flush* objs, uint32_t n,

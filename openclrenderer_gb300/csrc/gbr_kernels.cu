@@ -136,6 +136,21 @@ __device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr, const Worksp
   return f;
 }
 
+// Coverage of a pixel known to lie inside the record's bbox: the reference
+// walk's skipped left-column pixels, then point_in_tri.
+__device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py, int chunk) {
+  const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
+  if (px == minx && py > miny &&
+      !walk_visits(0, py - miny, (int)(xr >> 16) - minx, (int)(yr >> 16) - miny, (float)miny, chunk))
+    return false;
+  float fx = (float)px, fy = (float)py;
+  float sgn = q[1].w;
+  float s = ((q[1].x + q[1].y * fx) + q[1].z * fy) * sgn;
+  float t = ((q[2].x + q[2].y * fx) + q[2].z * fy) * sgn;
+  return s > -0.0001f && t > -0.0001f && (s + t) < q[0].w;
+}
+
 // One candidate as a record (and shade record for views); returns its tile footprint.
 __device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t surface, const Workspace& ws, bool view,
                                          Foot* foot) {
@@ -152,25 +167,64 @@ __device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t sur
   return foot_count(*foot);
 }
 
+// Depth-only passes (cube faces): a candidate whose bbox has at most this
+// many pixels is rasterised by its setup thread straight into the face with
+// global atomicMin -- the same coverage tests and depths as the tile raster,
+// and a minimum does not depend on order -- instead of becoming a record.
+constexpr float kDirectArea = 32.0f;
+
+__device__ __forceinline__ bool direct_cand(const Cand& c) {
+  return (c.mm[1] - c.mm[0]) * (c.mm[3] - c.mm[2]) <= kDirectArea;
+}
+
+// kernel1 of one small candidate into its surface's depth; returns the
+// covered pixel count.
+__device__ uint32_t direct_raster(const Cand& c, uint32_t surface, const Surface& S) {
+  RasterRec R;
+  make_rec(c, surface, R);
+  const float4 q[4] = {make_float4(R.A, R.B, R.C, R.bound), make_float4(R.s0, R.sa, R.sb, R.sign),
+                       make_float4(R.t0, R.ta, R.tb, __uint_as_float(R.key)),
+                       make_float4(__uint_as_float(R.xr), __uint_as_float(R.yr), 0.0f, 0.0f)};
+  const int x0 = (int)(R.xr & 0xFFFF), x1 = (int)(R.xr >> 16), y0 = (int)(R.yr & 0xFFFF), y1 = (int)(R.yr >> 16);
+  uint32_t hits = 0;
+  for (int y = y0; y < y1; y++)
+    for (int x = x0; x < x1; x++)
+      if (covers_in_bbox(q, x, y, S.chunk)) {
+        atomicMin(S.depth + (size_t)y * S.width + x, depth_at(R.A, R.B, R.C, (float)x, (float)y));
+        hits++;
+      }
+  return hits;
+}
+
 // Append this lane's candidates (n = 0, 1 or 2: c0, then c1) as records and
-// count their bins.  Every lane of the warp must call it.  Returns this lane's
-// reference fragment count (sum of ceil(area / chunk)).
+// count their bins (depth-only passes rasterise small ones directly).  Every
+// lane of the warp must call it.  Returns this lane's reference fragment count
+// (sum of ceil(area / chunk)).
 __device__ unsigned long long emit(const Cand& c0, const Cand& c1, int n, uint32_t surface, const Surface* surfs,
                                    const Workspace& ws, bool view) {
-  const uint32_t base = warp_alloc(&ws.ctr->nrec, (uint32_t)n);
+  const bool d0 = !view && n > 0 && direct_cand(c0), d1 = !view && n > 1 && direct_cand(c1);
+  const uint32_t nr = (uint32_t)(n > 0 && !d0) + (uint32_t)(n > 1 && !d1);
+  const uint32_t base = warp_alloc(&ws.ctr->nrec, nr);
   unsigned long long frags = 0;
   const Surface& S = surfs[surface];
   Foot f0{0, 0, 0, 0, false}, f1{0, 0, 0, 0, false};
   int n0 = 0, n1 = 0;
+  uint32_t slot = base, hits = 0;
   if (n > 0) {
     frags += (unsigned long long)ceilf(fdiv((c0.mm[1] - c0.mm[0]) * (c0.mm[3] - c0.mm[2]), (float)S.chunk));
-    if (base < ws.rec_cap) n0 = write_rec(c0, base, surface, ws, view, &f0);
+    if (d0) hits += direct_raster(c0, surface, S);
+    else if (slot < ws.rec_cap) n0 = write_rec(c0, slot++, surface, ws, view, &f0);
     else atomicOr(&ws.ctr->overflow, 1u);
   }
   if (n > 1) {
     frags += (unsigned long long)ceilf(fdiv((c1.mm[1] - c1.mm[0]) * (c1.mm[3] - c1.mm[2]), (float)S.chunk));
-    if (base + 1 < ws.rec_cap) n1 = write_rec(c1, base + 1, surface, ws, view, &f1);
+    if (d1) hits += direct_raster(c1, surface, S);
+    else if (slot < ws.rec_cap) n1 = write_rec(c1, slot++, surface, ws, view, &f1);
     else atomicOr(&ws.ctr->overflow, 1u);
+  }
+  if (!view) {
+    hits = __reduce_add_sync(0xFFFFFFFFu, hits);
+    if ((threadIdx.x & 31) == 0 && hits) atomicAdd(&ws.ctr->samples, (unsigned long long)hits);
   }
   // tile counts, aggregated across the warp (neighbouring triangles usually
   // share tiles): iterate over this lane's (record, tile) pairs in lockstep
@@ -506,20 +560,6 @@ __device__ __forceinline__ uint32_t find_surface_warp(const Surface* surfs, uint
 }
 
 
-// Coverage of a pixel known to lie inside the record's bbox: the reference
-// walk's skipped left-column pixels, then point_in_tri.
-__device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py, int chunk) {
-  const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
-  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
-  if (px == minx && py > miny &&
-      !walk_visits(0, py - miny, (int)(xr >> 16) - minx, (int)(yr >> 16) - miny, (float)miny, chunk))
-    return false;
-  float fx = (float)px, fy = (float)py;
-  float sgn = q[1].w;
-  float s = ((q[1].x + q[1].y * fx) + q[1].z * fy) * sgn;
-  float t = ((q[2].x + q[2].y * fx) + q[2].z * fy) * sgn;
-  return s > -0.0001f && t > -0.0001f && (s + t) < q[0].w;
-}
 
 // kernel1 + kernel2 for one 16x16 tile: depth min, then the canonical id.
 //
@@ -601,13 +641,24 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
     lists[3] = ws.coarse_count[ct];
     ssamples = 0;
   }
-  for (int p = tid; p < kTilePixels; p += NT) {
-    sdepth[p] = kDepthClear;
-    sid[p] = ~0ull;
+  if (with_id) {
+    for (int p = tid; p < kTilePixels; p += NT) {
+      sdepth[p] = kDepthClear;
+      sid[p] = ~0ull;
+    }
   }
   __syncthreads();
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
+  if (!with_id) {
+    // depth-only passes: the surface was cleared and holds the small
+    // triangles the setup rasterised; a tile without records keeps it as is
+    if (lists[1] + lists[3] == 0) return;
+    for (int p = tid; p < kTilePixels; p += NT) {
+      const int px = tx0 + (p & (kTile - 1)), py = ty0 + p / kTile;
+      sdepth[p] = (px < S.width && py < S.height) ? S.depth[(size_t)py * S.width + px] : kDepthClear;
+    }
+  }
   const int chunk = S.chunk;
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
@@ -1457,6 +1508,18 @@ __global__ void k_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_fl
   G->feature_flag = f.feature_flag;
 }
 
+// Clear every surface of a depth-only pass to UINT_MAX before its setup
+// rasterises small candidates into them (blockIdx.y = surface).
+__global__ void __launch_bounds__(256) k_clear_surfaces(const Surface* __restrict__ surfs) {
+  const Surface& S = surfs[blockIdx.y];
+  const size_t n = (size_t)S.width * S.height;
+  uint4* d4 = reinterpret_cast<uint4*>(S.depth);
+  const uint4 v = make_uint4(kDepthClear, kDepthClear, kDepthClear, kDepthClear);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 4; i += (size_t)gridDim.x * blockDim.x)
+    d4[i] = v;
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) S.depth[(n & ~(size_t)3) + threadIdx.x] = kDepthClear;
+}
+
 __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     p[i] = v;
@@ -1560,6 +1623,12 @@ cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_f
                                  cudaStream_t st) {
   if (!n) return cudaSuccess;
   k_flush_objects<<<(n + 255) / 256, 256, 0, st>>>(descs, objs, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clear_surfaces(const Surface* d_surf, uint32_t nsurf, cudaStream_t st) {
+  if (!nsurf) return cudaSuccess;
+  k_clear_surfaces<<<dim3(64, nsurf), 256, 0, st>>>(d_surf);
   return cudaGetLastError();
 }
 

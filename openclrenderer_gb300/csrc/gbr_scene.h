@@ -232,8 +232,12 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view);
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
                        Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom = nullptr,
                        cudaEvent_t join = nullptr);
-// Kernel launches of one pass (for the launch statistics).
-inline uint32_t pass_kernels(bool view) { return view ? 5u : 4u; }
+// Kernel launches of one pass (for the launch statistics): views setup, scan,
+// fill, raster, shade; depth-only passes clear, setup, scan, fill, raster.
+inline uint32_t pass_kernels(bool view) { return view ? 5u : 5u; }
+// Timed stages of one pass (stage_ms): setup (a depth-only pass's clear
+// included), scan, fill, raster and, for views, shade.
+inline uint32_t pass_stages(bool view) { return view ? 5u : 4u; }
 // Record a finished pass's counters in the scene's statistics; on overflow
 // grow the memory's targets by the tuning's headroom and return false.
 bool absorb_counters(gbr_scene* s, const Counters& c, WorkMem& w, float headroom, bool view);
