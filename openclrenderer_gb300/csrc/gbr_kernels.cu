@@ -171,7 +171,7 @@ __device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t sur
 // many pixels is rasterised by its setup thread straight into the face with
 // global atomicMin -- the same coverage tests and depths as the tile raster,
 // and a minimum does not depend on order -- instead of becoming a record.
-constexpr float kDirectArea = 32.0f;
+constexpr float kDirectArea = 64.0f;
 
 __device__ __forceinline__ bool direct_cand(const Cand& c) {
   return (c.mm[1] - c.mm[0]) * (c.mm[3] - c.mm[2]) <= kDirectArea;
@@ -179,7 +179,7 @@ __device__ __forceinline__ bool direct_cand(const Cand& c) {
 
 // kernel1 of one small candidate into its surface's depth; returns the
 // covered pixel count.
-__device__ uint32_t direct_raster(const Cand& c, uint32_t surface, const Surface& S) {
+__device__ __noinline__ uint32_t direct_raster(const Cand& c, uint32_t surface, const Surface& S) {
   RasterRec R;
   make_rec(c, surface, R);
   const float4 q[4] = {make_float4(R.A, R.B, R.C, R.bound), make_float4(R.s0, R.sa, R.sb, R.sign),
