@@ -503,7 +503,7 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
 }
 
 // engine::draw_screenspace_reflections (engine.cpp:1483-1511): one thread per pixel.
-__global__ void __launch_bounds__(256) k_reflections(SceneDev sc, ReflectCam v, const uint32_t* __restrict__ depth,
+__global__ void __launch_bounds__(256, 4) k_reflections(SceneDev sc, ReflectCam v, const uint32_t* __restrict__ depth,
                                                      const uint32_t* __restrict__ ids, const uint8_t* __restrict__ in,
                                                      uint8_t* __restrict__ out, int W, int H) {
   const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
