@@ -304,6 +304,12 @@ gbr_status gbr_post_motion_blur(gbr_scene* scene, const gbr_camera* cam, const g
                                 const uint32_t* depth, const uint32_t* id, const uint8_t* rgba_in, uint8_t* rgba_out,
                                 void* stream);
 
+/* Diagnostics: the device's 32-bit atomicMin rate, measured on the current
+ * device (ops per second; shared_mode 1: shared memory, conflict-free; 0:
+ * global words spread over an L2-resident 16 MB array).  The peak the raster
+ * kernels' atomics are compared with.  Synchronous. */
+gbr_status gbr_atomic_rate(int32_t shared_mode, double* ops_per_s);
+
 /* Counters of the last render / shadow pass on this scene. */
 gbr_status gbr_scene_stats(gbr_scene* scene, gbr_stats* out);
 

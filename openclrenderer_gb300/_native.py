@@ -117,6 +117,7 @@ SIGNATURES = {
     "gbr_post_motion_blur": (ctypes.c_int, [_P, _P, _P, _P, _U32, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P,
                                             _P]),
     "gbr_scene_flush_objects": (ctypes.c_int, [_P, _P, _U32]),
+    "gbr_atomic_rate": (ctypes.c_int, [ctypes.c_int32, _P]),
     "gbr_scene_get_descriptors": (ctypes.c_int, [_P, _P, _U32]),
     "gbr_server_create": (ctypes.c_int, [_P, _U32, _P, _P]),
     "gbr_server_submit": (ctypes.c_int, [_P, _P, _P]),

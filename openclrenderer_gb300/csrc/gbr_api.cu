@@ -871,6 +871,35 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   return GBR_OK;
 }
 
+gbr_status gbr_atomic_rate(int32_t shared_mode, double* ops_per_s) {
+  if (!ops_per_s) return fail(GBR_INVALID_ARG, "null output");
+  int dev = 0, sms = 0;
+  CU(cudaGetDevice(&dev));
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint32_t nwords = 4u << 20;  // 16 MB: L2-resident
+  const int iters = shared_mode ? 512 : 64;
+  const uint32_t blocks = (uint32_t)std::max(sms, 1) * 8u;
+  uint32_t* g = nullptr;
+  CU(cudaMalloc(&g, nwords * sizeof(uint32_t)));
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaMemset(g, 0xFF, nwords * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = launch_atomic_rate(g, nwords, iters, shared_mode, blocks, 0);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(a, 0);
+  for (int r = 0; r < 5 && e == cudaSuccess; r++) e = launch_atomic_rate(g, nwords, iters, shared_mode, blocks, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(b, 0);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(g);
+  if (e != cudaSuccess) return fail(GBR_CUDA_ERROR, "atomic-rate probe: %s", cudaGetErrorString(e));
+  *ops_per_s = 5.0 * (double)blocks * 256.0 * (double)iters / ((double)ms * 1e-3);
+  return GBR_OK;
+}
+
 gbr_status gbr_scene_profile(gbr_scene* s, int32_t enable) {
   GBR_SCENE_LOCK(s);
   TRY(check_scene(s));

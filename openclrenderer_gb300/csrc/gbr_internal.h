@@ -173,6 +173,8 @@ cudaError_t launch_mips(uchar4* atlas, const uint32_t* nums, const uint32_t* siz
                         int32_t max_size, cudaStream_t st);
 // depth-only passes: every surface's depth to UINT_MAX (16-byte aligned buffers)
 cudaError_t launch_clear_surfaces(const Surface* d_surf, uint32_t nsurf, cudaStream_t st);
+cudaError_t launch_atomic_rate(uint32_t* g, uint32_t nwords, int iters, int shared_mode, uint32_t blocks,
+                               cudaStream_t st);
 cudaError_t launch_fill_u32(uint32_t* p, uint32_t v, size_t n, cudaStream_t st);
 // screenspace_godrays over a rendered view (RGBA8 in / out, distinct buffers).
 cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_flush* objs, uint32_t n,

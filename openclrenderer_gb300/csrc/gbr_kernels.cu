@@ -1520,6 +1520,25 @@ __global__ void __launch_bounds__(256) k_clear_surfaces(const Surface* __restric
   if (blockIdx.x == 0 && threadIdx.x < (n & 3)) S.depth[(n & ~(size_t)3) + threadIdx.x] = kDepthClear;
 }
 
+// Atomic-rate probe (diagnostics): every thread issues `iters` 32-bit
+// atomicMin.  Shared mode: each lane its own word of the block's 256 (a lane
+// XOR keeps a warp's 32 words distinct, in 32 banks).  Global mode: words
+// spread over an L2-resident array of nwords.
+__global__ void __launch_bounds__(256) k_atomic_rate(uint32_t* g, uint32_t nwords, int iters, int shared_mode) {
+  __shared__ uint32_t s[256];
+  s[threadIdx.x] = 0xFFFFFFFFu;
+  __syncthreads();
+  const uint32_t v = blockIdx.x * 256u + threadIdx.x;
+  if (shared_mode) {
+    for (int i = 0; i < iters; i++) atomicMin(&s[threadIdx.x ^ (uint32_t)(i & 31)], v - (uint32_t)i);
+    __syncthreads();
+    if (s[threadIdx.x] == 0x12345u) g[0] = 0;  // keeps the shared result live
+  } else {
+    const uint32_t base = v % nwords;
+    for (int i = 0; i < iters; i++) atomicMin(g + (base + (uint32_t)i * 4099u) % nwords, v - (uint32_t)i);
+  }
+}
+
 __global__ void k_fill_u32(uint32_t* p, uint32_t v, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     p[i] = v;
@@ -1629,6 +1648,12 @@ cudaError_t launch_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_f
 cudaError_t launch_clear_surfaces(const Surface* d_surf, uint32_t nsurf, cudaStream_t st) {
   if (!nsurf) return cudaSuccess;
   k_clear_surfaces<<<dim3(64, nsurf), 256, 0, st>>>(d_surf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_atomic_rate(uint32_t* g, uint32_t nwords, int iters, int shared_mode, uint32_t blocks,
+                               cudaStream_t st) {
+  k_atomic_rate<<<blocks, 256, 0, st>>>(g, nwords, iters, shared_mode);
   return cudaGetLastError();
 }
 

@@ -179,3 +179,17 @@ def test_bounded_batch_wait():
         for i in range(len(ref)):
             same(ref[i], got[i], f"view {i}")
     assert timeouts >= 1
+
+
+def test_atomic_rate_probe():
+    """gbr_atomic_rate: the measured 32-bit atomicMin rates are positive and
+    shared memory is faster than spread global words."""
+    import ctypes
+    L = _native.load()
+    rates = []
+    for mode in (1, 0):
+        r = ctypes.c_double(0.0)
+        _native.check(L.gbr_atomic_rate(mode, ctypes.byref(r)))
+        rates.append(r.value)
+    assert rates[0] > 1e11 and rates[1] > 1e9, rates
+    assert rates[0] > rates[1]
