@@ -418,7 +418,6 @@ def main():
     depth = out.depth.cpu().numpy().view(np.uint32)
     P_cov = int(np.count_nonzero(depth != 0xFFFFFFFF))
     launches0 = gs.stats()["launches"]
-    gs.profile(True)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -432,13 +431,19 @@ def main():
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
-    st = gs.stats()
-    gs.profile(False)
-    launches = st["launches"] - launches0
+    launches = gs.stats()["launches"] - launches0
     ms = max_over_ranks(ms, world, "cuda")
     if world > 1:
         dist.barrier()
     value = job_mpix_per_s(P, world, ms)
+    # stage times: the same frames again, after the timed region, with the
+    # scene's per-stage CUDA events on (they add event records of their own)
+    gs.profile(True)
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    st = gs.stats()
+    gs.profile(False)
 
     # per-stage device time and the roofline of the dominant kernel
     per_call = {k: st["stage_ms"][k] / max(st["stage_calls"][k], 1) for k in S.STAGES}
