@@ -413,3 +413,22 @@ def test_integrated_blend_parity():
             changed = np.count_nonzero(np.any(ref["rgba"] != O.render(sc, tex, cam, view, dyn, sta)["rgba"], -1))
             assert abs(changed - meta[f"{name}_changed{k}"]) < 0.01 * changed
         gs.close()
+
+
+@pytest.mark.parametrize("seed", [501, 502, 503])
+def test_cube_faces_random_soups_bit_exact(seed):
+    """Cube faces of shadow lights placed inside random soups: triangles of
+    every size around each light (the small ones rasterised by the setup, the
+    larger ones binned), near and across face boundaries; faces bit-exact."""
+    rng = np.random.default_rng(seed)
+    sc = random_soup(int(rng.integers(800, 2500)), 640, 480, seed, zmin=5.0, zmax=3000.0, max_px=200.0)
+    pos = [rng.uniform(-200, 200, 3) + np.float64([0, 0, 800]),      # inside the cloud: large triangles
+           rng.uniform(-2000, 2000, 3) + np.float64([0, 0, 6000]),    # far: small triangles
+           rng.uniform(-1000, 1000, 3) + np.float64([0, 0, 1500])]
+    sc.lights = np.stack([S.make_light(p, (1, 1, 1), radius=5000.0, shadow=1) for p in pos])
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    got = gs.cubemaps()
+    dyn, _ = O.shadow(sc)
+    assert np.array_equal(got, dyn[:3]), f"{np.count_nonzero(got != dyn[:3])} texels differ"
+    assert np.count_nonzero(dyn[:3] != 0xFFFFFFFF) > 10000
