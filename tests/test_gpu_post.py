@@ -196,3 +196,49 @@ def test_post_passes_on_small_and_ragged_views(size):
     gs.set_descriptors(sc.descs)
     got = gs.post_reflections(cam, view, f).cpu().numpy()
     assert np.array_equal(got, O.reflections(sc, sc.descs, tex, depth, ids, rgba, cam, view))
+
+
+def test_post_and_new_entry_points_reject_bad_arguments():
+    """Null pointers, bad views, out-of-range reflection maps and wrong counts
+    come back as GBR_INVALID_ARG before any launch."""
+    import ctypes
+
+    from openclrenderer_gb300 import _native
+    from openclrenderer_gb300.pipeline import _np_ptr
+    sc, _ = golden_cases.CASES["cubes"]()
+    gs = GpuScene(sc)
+    L = gs.L
+    cam = np.asarray(sc.cameras[0], S.CAMERA).reshape(1)
+    view = np.asarray(sc.views[0], S.VIEW).reshape(1)
+    bad_view = view.copy()
+    bad_view["width"] = 0
+    out = gs.render(sc.cameras[0], sc.views[0], normals=True)
+    d, i, n, c = (out.depth.data_ptr(), out.id.data_ptr(), out.normals.data_ptr(), out.rgba.data_ptr())
+    dst = torch.empty_like(out.rgba).data_ptr()
+    INVALID = 1
+
+    def status(r):
+        return int(r)
+
+    assert status(L.gbr_post_pseudo_aa(gs.h, _np_ptr(view), d, i, None, c, dst, None)) == INVALID
+    assert status(L.gbr_post_pseudo_aa(gs.h, _np_ptr(bad_view), d, i, n, c, dst, None)) == INVALID
+    assert status(L.gbr_post_godrays(gs.h, None, _np_ptr(view), d, c, dst, None)) == INVALID
+    assert status(L.gbr_post_motion_blur(gs.h, _np_ptr(cam), None, _np_ptr(view), 0, ctypes.c_float(1.0),
+                                         ctypes.c_float(0.5), d, i, c, dst, None)) == INVALID
+    assert status(L.gbr_post_reflections(gs.h, _np_ptr(cam), _np_ptr(view), d, None, c, dst, None)) == INVALID
+    descs = sc.descs.copy()
+    descs["ssid"][0] = 7  # one texture only
+    gs.set_descriptors(descs)
+    assert status(L.gbr_post_reflections(gs.h, _np_ptr(cam), _np_ptr(view), d, i, c, dst, None)) == INVALID
+    gs.set_descriptors(sc.descs)
+    o = (ctypes.c_void_p * 4)(d, i, c, None)
+    assert status(L.gbr_render_view_blend(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.cast(o, ctypes.c_void_p), None,
+                                          None)) == INVALID
+    buf = np.zeros(len(sc.descs) + 1, S.OBJ_DESC)
+    assert status(L.gbr_scene_get_descriptors(gs.h, _np_ptr(buf), len(buf))) == INVALID
+    assert status(L.gbr_batch_wait_for(None, 10)) == INVALID
+    assert status(L.gbr_scene_flush_objects(gs.h, None, 3)) == INVALID
+    # the scene still renders afterwards
+    again = gs.render(sc.cameras[0], sc.views[0]).numpy()
+    assert np.array_equal(again["depth"], out.numpy()["depth"])
+    assert _native.load() is L
