@@ -954,7 +954,7 @@ __device__ __forceinline__ float bilinear_interpolate(float cx, float cy, float 
 }
 
 // generate_hard_occlusion (cl2.cl:2536-2701), SMOOTH_SHADOWS
-__device__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 normal, f3 ptl, const uint32_t* buf,
+__device__ __noinline__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 normal, f3 ptl, const uint32_t* buf,
                                 int face, f3 gpos, int shnum) {
   ptl = fast_normalize3(ptl);
   f3 c = mk3(sc.face_cos[face][0], sc.face_cos[face][1], sc.face_cos[face][2]);
