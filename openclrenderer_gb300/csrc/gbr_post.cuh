@@ -69,7 +69,9 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
 #pragma unroll
       for (int k = 0; k < 8; k++) {
         if (k < m) {
-          if (depth_to_dist(dv[k]) < thr && dv[k] != kDepthClear) {
+          // (the reference also requires cdepth != UINT_MAX; an empty pixel is at
+          // 350000, never below thr = the pixel's own distance - 5 <= 349995)
+          if (depth_to_dist(dv[k]) < thr) {
             idecay *= 0.9f;
             iter_col = add3(iter_col, mul3s(mul3s(cval, idecay), weight));
           }
