@@ -44,6 +44,13 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
     // steps j with (float)j < mnum and j < samples
     const int n = mnum > 0.0f ? (int)fminf(ceilf(mnum), samples) : 0;
     float cx = current.x, cy = current.y;
+    // A march whose whole segment, one step past its end, keeps 0.05 px inside
+    // the screen needs no bounds tests: the positions move monotonically along
+    // dir, and 80 float additions below 4096 stray from the exact line by less
+    // than 0.01 px.  (Every comparison fails on NaN.)
+    const float ex = cx + (float)n * dir.x, ey = cy + (float)n * dir.y;
+    const bool inside = cx >= 0.05f && ex >= 0.05f && cx <= xmax - 0.05f && ex <= xmax - 0.05f &&
+                        cy >= 0.05f && ey >= 0.05f && cy <= ymax - 0.05f && ey <= ymax - 0.05f;
     // Eight steps at a time: their positions (the same running sums as the
     // reference's current += dir), then their depth loads in flight together,
     // then the decay chain in order.  The reference skips the rest of the
@@ -57,10 +64,12 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
         cx += dir.x;
         cy += dir.y;
       }
-      int m = 8;
+      int m = min(8, n - j0);
+      if (!inside) {
 #pragma unroll
-      for (int k = 7; k >= 0; k--)
-        if (j0 + k >= n || px[k] < 0 || py[k] < 0 || px[k] >= xmax || py[k] >= ymax) m = k;
+        for (int k = 7; k >= 0; k--)
+          if (px[k] < 0 || py[k] < 0 || px[k] >= xmax || py[k] >= ymax) m = min(m, k);
+      }
       uint32_t dv[8];
 #pragma unroll
       // (cvt.rzi: truncation, NaN -> 0, so a NaN march stays in bounds as in the oracle)
