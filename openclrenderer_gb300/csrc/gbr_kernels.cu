@@ -663,8 +663,10 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
   const bool resident = ntotal <= (uint32_t)NT;
-  // covered tests of pass 0 (resident case): depth, and pixel | staged record << 8 | 1 << 31
+  // the covered tests of pass 0 (resident tiles), up to kRasterCache per
+  // thread: depth, and pixel | staged record << 8 | 1 << 31; nh counts them
   uint32_t cache_d[kRasterCache], cache_m[kRasterCache];
+  uint32_t nh = 0;
   bool cached = false;
   for (int pass = 0; pass < passes; pass++) {
     for (uint32_t c0 = 0; c0 < ntotal; c0 += NT) {
@@ -727,11 +729,10 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
       // this warp's contiguous range of the test list, in windows of 32
       const uint32_t per = ((total + NW * 32 - 1) / (NW * 32)) * 32;
       const uint32_t start = min(total, (uint32_t)warp * per), end = min(total, start + per);
-      const bool keep = resident && pass == 0 && with_id && per <= 32u * kRasterCache;
+      const bool keep = resident && pass == 0 && with_id;
       if (keep) {
 #pragma unroll
         for (int g = 0; g < kRasterCache; g++) cache_m[g] = 0;
-        cached = true;
       }
       if (start < end) {
         // first record: the last staged record with soff <= start (warp-uniform)
@@ -741,7 +742,7 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
           if (soff[mid] <= start) rec = mid; else hi = mid - 1;
         }
 #pragma unroll 1
-        for (uint32_t base = start, g = 0; base < end; base += 32, g++) {
+        for (uint32_t base = start; base < end; base += 32) {
           // record starts inside (base, base + 32): at most 32 records
           const uint32_t nxt = (uint32_t)rec + 1 + lane;
           const uint32_t pos = nxt < nstaged ? soff[nxt] - base : 32u;
@@ -767,10 +768,11 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
                 if (keep) {
 #pragma unroll
                   for (int k = 0; k < kRasterCache; k++)
-                    if (k == (int)g) {
+                    if (k == (int)nh) {
                       cache_d[k] = d;
                       cache_m[k] = (uint32_t)p | (lo << 8) | (1u << 31);
                     }
+                  nh++;
                 }
               } else {
                 const uint32_t fd = sdepth[p];
@@ -789,7 +791,12 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
         }
       }
     }
-    __syncthreads();
+    // a resident tile's id pass reads pass 0's kept tests when every thread's
+    // fit (block-uniform)
+    if (resident && with_id && pass == 0)
+      cached = __syncthreads_or(nh > (uint32_t)kRasterCache) == 0;
+    else
+      __syncthreads();
   }
   if (tid == 0 && ssamples) atomicAdd(&ws.ctr->samples, (unsigned long long)ssamples);
   for (int lp = tid; lp < kTilePixels; lp += NT) {
