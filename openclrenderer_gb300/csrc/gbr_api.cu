@@ -844,14 +844,25 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   TRY(hw.pix_depth.reserve(P));
   TRY(hw.pix_id.reserve(P));
   TRY(hw.pix_rgba.reserve(P * 4));
-  gbr_outputs o{hw.pix_depth.p, hw.pix_id.p, hw.pix_rgba.p, nullptr};
+  // RGBA8 into pinned (page-locked, mapped) host memory is written by kernel3
+  // itself through the buffer's device address: nothing to copy after shading
+  uint8_t* rgba_dev = nullptr;
+  if (rgba && (reinterpret_cast<uintptr_t>(rgba) & 3) == 0) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, rgba) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+      rgba_dev = static_cast<uint8_t*>(at.devicePointer);
+    else
+      cudaGetLastError();
+  }
+  gbr_outputs o{hw.pix_depth.p, hw.pix_id.p, rgba_dev ? rgba_dev : hw.pix_rgba.p, nullptr};
   if (!s->copy_stream) {
     CU(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
     CU(cudaEventCreateWithFlags(&s->raster_done, cudaEventDisableTiming));
     CU(cudaEventCreateWithFlags(&s->copies_done, cudaEventDisableTiming));
   }
   // depth and id are final once the raster has run: they travel to the host
-  // on the copy stream while kernel3 shades; RGBA8 follows kernel3 on st.
+  // on the copy stream while kernel3 shades; RGBA8 follows kernel3 on st
+  // (unless kernel3 wrote it to the host directly).
   // Each attempt queues its own copies (a re-run after an overflow
   // overwrites them); st waits for the copy stream before it is synchronised.
   const std::function<gbr_status()> copies = [&]() -> gbr_status {
@@ -859,7 +870,7 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
     if (depth) CU(cudaMemcpyAsync(depth, o.depth, P * 4, cudaMemcpyDeviceToHost, s->copy_stream));
     if (id) CU(cudaMemcpyAsync(id, o.id, P * 4, cudaMemcpyDeviceToHost, s->copy_stream));
     CU(cudaEventRecord(s->copies_done, s->copy_stream));
-    if (rgba) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
+    if (rgba && !rgba_dev) CU(cudaMemcpyAsync(rgba, o.rgba, P * 4, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamWaitEvent(st, s->copies_done, 0));
     return GBR_OK;
   };

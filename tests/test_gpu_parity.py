@@ -225,6 +225,20 @@ def test_render_host_matches_device():
     host = gs.render_host(sc.cameras[0], sc.views[0])
     for k in ("depth", "id", "rgba"):
         assert np.array_equal(dev[k], host[k])
+    # pinned host buffers: kernel3 writes RGBA8 into them directly
+    W, H = int(sc.views[0]["width"]), int(sc.views[0]["height"])
+    pin = torch.empty(W * H * 12, dtype=torch.uint8, pin_memory=True).numpy()
+    hd, hi, hr = pin[:4 * W * H].view(np.uint32), pin[4 * W * H:8 * W * H].view(np.uint32), pin[8 * W * H:]
+    hr[:] = 7
+    for _ in range(2):
+        gs.render_host(sc.cameras[0], sc.views[0], hd, hi, hr)
+        assert np.array_equal(hd.reshape(H, W), dev["depth"]) and np.array_equal(hi.reshape(H, W), dev["id"])
+        assert np.array_equal(hr.reshape(H, W, 4), dev["rgba"])
+    # an unaligned pinned RGBA buffer takes the copy path
+    big = torch.empty(W * H * 4 + 1, dtype=torch.uint8, pin_memory=True).numpy()
+    odd = big[1:].reshape(H, W, 4)
+    gs.render_host(sc.cameras[0], sc.views[0], False, False, odd)
+    assert np.array_equal(odd, dev["rgba"])
 
 
 def test_concurrent_calls_on_one_scene():
