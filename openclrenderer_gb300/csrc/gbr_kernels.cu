@@ -952,13 +952,6 @@ __device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth,
   return 1.0f - (1.0f - facc) * (1.0f / kSsaoDiv);
 }
 
-__device__ __forceinline__ float bilinear_interpolate(float cx, float cy, float v0, float v1, float v2,
-                                                      float v3) {
-  float mx = cx - 0.5f, my = cy - 0.5f;
-  float ux = mx - floorf(mx), uy = my - floorf(my);
-  float bx = 1.0f - ux, by = 1.0f - uy;
-  return (v0 * bx + v1 * ux) * by + (v2 * bx + v3 * ux) * uy;
-}
 
 // generate_hard_occlusion (cl2.cl:2536-2701), SMOOTH_SHADOWS
 __device__ __noinline__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 normal, f3 ptl, const uint32_t* buf,
@@ -983,17 +976,23 @@ __device__ __noinline__ float hard_occlusion(const SceneDev& sc, f3 lpos, f3 nor
       float ldp = depth_to_dist(__ldg(map + (iy + yy) * kLightBufferDim + ix + xx));
       if (dpth > ldp + bias) cond |= 1u << ((yy + 1) * 4 + xx + 1);
     }
-  float shadow = 0.0f;
-#pragma unroll
-  for (int yy = -1; yy <= 1; yy++)
-#pragma unroll
-    for (int xx = -1; xx <= 1; xx++) {
-      int b = (yy + 1) * 4 + xx + 1;
-      shadow += bilinear_interpolate((px + 0.5f) + (float)xx, (py + 0.5f) + (float)yy,
-                                     (float)((cond >> b) & 1u), (float)((cond >> (b + 1)) & 1u),
-                                     (float)((cond >> (b + 4)) & 1u), (float)((cond >> (b + 5)) & 1u));
-    }
-  return fdiv(shadow, 9.0f);
+  // The 3x3 bilinear blend of the 4x4 tests: every tap has the same
+  // fractional offsets (ux, uy), so the sum of the nine bilinear_interpolate
+  // calls is separable, with column weights (1 - ux, 1, 1, ux) and row
+  // weights (1 - uy, 1, 1, uy).  The occlusion scales the colour only.
+  const float mx = (px + 0.5f) - 0.5f, my = (py + 0.5f) - 0.5f;
+  const float ux = mx - floorf(mx), uy = my - floorf(my);
+  const float by = 1.0f - uy;
+  // per column group (left, middle two, right): tests of the top row, the
+  // middle two rows and the bottom row
+  auto rows = [&](uint32_t top, uint32_t mid, uint32_t bot) {
+    return fma_(uy, (float)__popc(cond & bot), fma_(by, (float)__popc(cond & top), (float)__popc(cond & mid)));
+  };
+  const float sl = rows(0x0001u, 0x0110u, 0x1000u);
+  const float sm = rows(0x0006u, 0x0660u, 0x6000u);
+  const float sr = rows(0x0008u, 0x0880u, 0x8000u);
+  const float shadow = fma_(ux, sr, fma_(1.0f - ux, sl, sm));
+  return shadow * (1.0f / 9.0f);
 }
 
 // Vertex colour channels (colour path: multiplication by 1/255).
@@ -1012,15 +1011,19 @@ __device__ __forceinline__ f4 vertex_col(uint32_t c) {
 // continuously (no comparison, rounding or index depends on it), so the
 // approximate division is covered by the 1/255 colour tolerance.
 __device__ __forceinline__ float cdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float crcp(float b) { return __fdividef(1.0f, b); }
 __device__ __forceinline__ f3 cnormalize(f3 a) {
   float r = rsqrtf(dot3(a, a));
   return mk3(a.x * r, a.y * r, a.z * r);
 }
+// Colour-path dot product with contraction.
+__device__ __forceinline__ float cdot3(f3 a, f3 b) { return fma_(a.z, b.z, fma_(a.y, b.y, a.x * b.x)); }
+// rational_acos (cl2.cl:1919-1936) in Horner form: x (a + b x^2) / (1 + c x^2 + d x^4) + pi/2.
 __device__ __forceinline__ float c_rational_acos(float x) {
   const float a = -0.939115566365855f, b = 0.9217841528914573f, c = -1.2845906244690837f,
               d = 0.295624144969963174f;
-  float x2 = x * x;
-  return kPi / 2.0f + cdiv(a * x + ((b * x) * x) * x, (1.0f + (c * x) * x) + d * (x2 * x2));
+  const float x2 = x * x;
+  return fma_(x * fma_(b, x2, a), crcp(fma_(x2, fma_(d, x2, c), 1.0f)), kPi / 2.0f);
 }
 
 __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
@@ -1280,6 +1283,11 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
   const float g_diffuse = __ldg(&G->diffuse), g_spec_mult = __ldg(&G->spec_mult);
   const float rough = clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f);
+  // per-pixel factors of the light loop (colour only)
+  const float ndv = fmax_(0.0f, cdot3(normal, l2p));
+  const float r_pndv = crcp(kPi * ndv);  // spec / (pi ndv)
+  const float nr2 = -crcp(rough * rough);  // Gaussian exponent -alpha^2 / rough^2
+  const float spec_k = 0.4f * g_spec_mult;
   f3 dsum = mk3(0, 0, 0), ssum = mk3(0, 0, 0);
   int shnum = 0, static_num = 0;
   for (uint32_t i = 0; i < sc.nlights; i++) {
@@ -1314,27 +1322,26 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
       shnum++;
     }
     ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
-    float light = fmax_(dot3(ptl, lnormal) * occlusion, 0.0f);
-    float diffuse = (1.0f - ambient) * light;
-    float dscale = (((diffuse + ambient) * L.diffuse) * g_diffuse) * illum;
-    dsum = add3(dsum, mul3s(lcol, dscale));
-    f3 Hv = cnormalize(add3(l2p, ptl));
-    float ndh = fmax_(0.0f, dot3(normal, Hv));
-    float ndv = fmax_(0.0f, dot3(normal, l2p));
-    float vdh = fmax_(0.0f, dot3(l2p, Hv));
-    float ndl = fmax_(0.0f, dot3(normal, ptl));
-    const float F0 = 0.4f;
-    float omv = 1.0f - vdh, omv2 = omv * omv;
-    float fresnel = F0 + (1.0f - F0) * ((omv2 * omv2) * omv);
-    float alpha = c_rational_acos(ndh);
-    float microfacet = 0.8346f * __expf(cdiv((-alpha) * alpha, rough * rough));
-    float sv = cdiv(2.0f * ndh, vdh);
-    float geometric = min3f(1.0f, sv * ndv, sv * ndl);
-    float spec = cdiv((fresnel * microfacet) * geometric, kPi * ndv);
-    float sscale = (spec * 0.4f) * illum;
-    ssum = add3(ssum, mul3s(mul3s(lcol, sscale), g_spec_mult));
-    ssum = mk3(fmax_(ssum.x, 0.0f), fmax_(ssum.y, 0.0f), fmax_(ssum.z, 0.0f));
-    ssum = mul3s(ssum, occlusion);
+    // Lambert + ambient
+    const float light = fmax_(cdot3(ptl, lnormal) * occlusion, 0.0f);
+    const float dscale = fma_(1.0f - ambient, light, ambient) * ((L.diffuse * g_diffuse) * illum);
+    dsum = mk3(fma_(lcol.x, dscale, dsum.x), fma_(lcol.y, dscale, dsum.y), fma_(lcol.z, dscale, dsum.z));
+    // Cook-Torrance: F0 0.4, Gaussian microfacet 0.8346, geometric term
+    const f3 Hv = cnormalize(add3(l2p, ptl));
+    const float ndh = fmax_(0.0f, cdot3(normal, Hv));
+    const float vdh = fmax_(0.0f, cdot3(l2p, Hv));
+    const float ndl = fmax_(0.0f, cdot3(normal, ptl));
+    const float omv = 1.0f - vdh, omv2 = omv * omv;
+    const float fresnel = fma_(0.6f, (omv2 * omv2) * omv, 0.4f);
+    const float alpha = c_rational_acos(ndh);
+    const float microfacet = 0.8346f * __expf((alpha * alpha) * nr2);
+    const float sv = (2.0f * ndh) * crcp(vdh);
+    const float geometric = min3f(1.0f, sv * ndv, sv * ndl);
+    const float spec = ((fresnel * microfacet) * geometric) * r_pndv;
+    const float sscale = spec * (spec_k * illum);
+    ssum = mk3(fmax_(fma_(lcol.x, sscale, ssum.x), 0.0f) * occlusion,
+               fmax_(fma_(lcol.y, sscale, ssum.y), 0.0f) * occlusion,
+               fmax_(fma_(lcol.z, sscale, ssum.z), 0.0f) * occlusion);
   }
   ssum = mul3s(ssum, ssao);
   dsum = mul3s(dsum, ssao);
