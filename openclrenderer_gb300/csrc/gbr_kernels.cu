@@ -920,11 +920,13 @@ __device__ __forceinline__ int ssao_count(float d2, float t0, float t1, float t2
 // float) is kept in an integer.  Far from the camera (world_rad < 0.25) every
 // offset rounds to 0 and all 25 taps read the same pixel; when that holds for
 // the whole warp, the pixel is read once and its count taken 25 times.
-__device__ float generate_ssao(int x, int y, const uint32_t* __restrict__ depth, int W, int H, float fov) {
-  uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)W * (uint32_t)H * (uint32_t)y));
+// seed2 = rand_xorshift(wang_hash(x + W*H*y)), the pixel's first random
+// number, which kernel3's normal jitter also draws.
+__device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* __restrict__ depth, int W, int H,
+                               float fov) {
   float foffset = (float)seed2 * kInvMulInt;
   float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
-  float rad = kSsaoRad + fdiv(foffset, 2.0f);
+  float rad = kSsaoRad + foffset * 0.5f;  // foffset / 2, exact
   float world_rad = fdiv(rad * fov, dep);
   int wx[5];
 #pragma unroll
@@ -1077,7 +1079,7 @@ struct SLight {
   float diffuse;
   uint32_t shadow;
   int32_t is_static;
-  uint32_t pad;
+  float rradius;  // approximate 1 / radius, for the colour-only cutoff of unshadowed lights
 };
 
 // kernel3 (cl2.cl:5792-6408) for one pixel of a view.
@@ -1277,7 +1279,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const bool two = (ff & kFlagTwoSided) > 0;
   const bool recv_dyn = !((ff & kFlagNoDynShadows) > 0);
   if (!backface_front(tp[0], tp[1], tp[2]) && two) normal = neg3(normal);
-  const float ssao = generate_ssao(x, y, S.depth, W, H, fov);
+  const float ssao = generate_ssao(x, y, seed2, S.depth, W, H, fov);
   normal = fast_normalize3(normal);
   const f3 lnormal = cnormalize(add3(normal, mk3(rseed.x * 0.01f, rseed.y * 0.01f, rseed.z * 0.01f)));
   const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
@@ -1304,12 +1306,19 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     }
     // The distance only feeds the colour, except through the cutoff below,
     // which for a shadow light also decides which cubemap later shadow lights
-    // read (shnum): exact for shadow lights, approximate otherwise.
+    // read (shnum): IEEE arithmetic for shadow lights (a warp-uniform branch),
+    // approximate otherwise.
     const float d2 = dot3(ptl, ptl);
     const float rinv = rsqrtf(d2);
-    const float distance = (!lshadow && d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
-    float tt = cdiv(distance, L.radius) + 1.0f;
-    float illum = cdiv(L.brightness, tt * tt);
+    float illum;
+    if (lshadow) {
+      const float tt = fdiv(fsqrt(d2), L.radius) + 1.0f;
+      illum = fdiv(L.brightness, tt * tt);
+    } else {
+      const float distance = (d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
+      const float tt = fma_(distance, L.rradius, 1.0f);
+      illum = L.brightness * crcp(tt * tt);
+    }
     const float cutoff = 0.1f;
     illum -= cutoff;
     illum *= 1.0f / (1.0f - cutoff);
@@ -1397,7 +1406,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
     l.diffuse = L->diffuse;
     l.shadow = L->shadow;
     l.is_static = L->is_static;
-    l.pad = 0;
+    l.rradius = crcp(l.radius);
     f3 c = mk3(L->col[0], L->col[1], L->col[2]);
     if (views[s_id].use_linear) c = mk3(gamma_fwd(c.x), gamma_fwd(c.y), gamma_fwd(c.z));
     l.cr = c.x; l.cg = c.y; l.cb = c.z;
