@@ -859,6 +859,10 @@ __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy
   return r;
 }
 
+// COLOUR: the result only scales the colour (the texel colour), so the blend
+// may contract; the normal map's fetch, which feeds the exact normal, keeps
+// the plain products.
+template <bool COLOUR>
 __device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, int slice, float width) {
   const TexSlot ts = tex_slot_pre(sc, which, slice, width);
   float posx = floorf(mx), posy = floorf(my);
@@ -869,14 +873,22 @@ __device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, in
   float ux = mx - posx, uy = my - posy;
   float bx = 1.0f - ux, by = 1.0f - uy;
   f4 r;
-  r.x = fma_(c0.x, bx, c1.x * ux) * by + fma_(c2.x, bx, c3.x * ux) * uy;
-  r.y = fma_(c0.y, bx, c1.y * ux) * by + fma_(c2.y, bx, c3.y * ux) * uy;
-  r.z = fma_(c0.z, bx, c1.z * ux) * by + fma_(c2.z, bx, c3.z * ux) * uy;
-  r.w = fma_(c0.w, bx, c1.w * ux) * by + fma_(c2.w, bx, c3.w * ux) * uy;
+  if (COLOUR) {
+    r.x = fma_(fma_(c2.x, bx, c3.x * ux), uy, fma_(c0.x, bx, c1.x * ux) * by);
+    r.y = fma_(fma_(c2.y, bx, c3.y * ux), uy, fma_(c0.y, bx, c1.y * ux) * by);
+    r.z = fma_(fma_(c2.z, bx, c3.z * ux), uy, fma_(c0.z, bx, c1.z * ux) * by);
+    r.w = fma_(fma_(c2.w, bx, c3.w * ux), uy, fma_(c0.w, bx, c1.w * ux) * by);
+  } else {
+    r.x = fma_(c0.x, bx, c1.x * ux) * by + fma_(c2.x, bx, c3.x * ux) * uy;
+    r.y = fma_(c0.y, bx, c1.y * ux) * by + fma_(c2.y, bx, c3.y * ux) * uy;
+    r.z = fma_(c0.z, bx, c1.z * ux) * by + fma_(c2.z, bx, c3.z * ux) * uy;
+    r.w = fma_(c0.w, bx, c1.w * ux) * by + fma_(c2.w, bx, c3.w * ux) * uy;
+  }
   return r;
 }
 
-// texture_filter_diff (cl2.cl:1511-1573)
+// texture_filter_diff (cl2.cl:1511-1573); COLOUR as for bilinear_pre
+template <bool COLOUR>
 __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2) {
   uint32_t nv = __ldg(sc.nums + tid2);
   int slice = (int)(nv >> 16);
@@ -895,14 +907,21 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
   uint32_t lnv = __ldg(sc.nums + tid_lower), hnv = __ldg(sc.nums + tid_higher);
   int sl = (int)(lnv >> 16), sh = (int)(hnv >> 16);
   float szl = (float)__ldg(sc.sizes + sl), szh = (float)__ldg(sc.sizes + sh);
-  f4 c1 = bilinear_pre(sc, vtm.x * szl, vtm.y * szl, (int)(lnv & 0xFFFF), sl, szl);
-  f4 c2 = bilinear_pre(sc, vtm.x * szh, vtm.y * szh, (int)(hnv & 0xFFFF), sh, szh);
+  f4 c1 = bilinear_pre<COLOUR>(sc, vtm.x * szl, vtm.y * szl, (int)(lnv & 0xFFFF), sl, szl);
+  f4 c2 = bilinear_pre<COLOUR>(sc, vtm.x * szh, vtm.y * szh, (int)(hnv & 0xFFFF), sh, szh);
   const float i255 = 1.0f / 255.0f;
   f4 r;
-  r.x = (c1.x + (c2.x - c1.x) * fmd) * i255;
-  r.y = (c1.y + (c2.y - c1.y) * fmd) * i255;
-  r.z = (c1.z + (c2.z - c1.z) * fmd) * i255;
-  r.w = (c1.w + (c2.w - c1.w) * fmd) * i255;
+  if (COLOUR) {
+    r.x = fma_(c2.x - c1.x, fmd, c1.x) * i255;
+    r.y = fma_(c2.y - c1.y, fmd, c1.y) * i255;
+    r.z = fma_(c2.z - c1.z, fmd, c1.z) * i255;
+    r.w = fma_(c2.w - c1.w, fmd, c1.w) * i255;
+  } else {
+    r.x = (c1.x + (c2.x - c1.x) * fmd) * i255;
+    r.y = (c1.y + (c2.y - c1.y) * fmd) * i255;
+    r.z = (c1.z + (c2.z - c1.z) * fmd) * i255;
+    r.w = (c1.w + (c2.w - c1.w) * fmd) * i255;
+  }
   return r;
 }
 
@@ -1067,7 +1086,11 @@ __device__ __forceinline__ float c_gamma_inv(float c) {
   float s1 = csqrt(c);
   float s2 = csqrt(s1);
   float s3 = csqrt(s2);
-  return (0.585122381f * s1 + 0.783140355f * s2) - 0.368262736f * s3;
+  return fma_(-0.368262736f, s3, fma_(0.783140355f, s2, 0.585122381f * s1));
+}
+// gamma_fwd (cl2.cl:5763-5770) in Horner form, for colours
+__device__ __forceinline__ float c_gamma_fwd(float c) {
+  return c * fma_(fma_(0.305306011f, c, 0.682171111f), c, 0.012522878f);
 }
 
 // A light as the shade loop reads it, staged once per CTA in shared memory;
@@ -1089,7 +1112,7 @@ struct SLight {
 // IEEE contract (normalize as fast_normalize).
 __device__ __forceinline__ f3 normal_map(const SceneDev& sc, f2 vt, f2 vtdiff, uint32_t rid, f3 p1, f3 p2, f3 p3,
                                       f2 vt1, f2 vt2, f2 vt3, f3 model_normal, f4 qn) {
-  const f4 t4 = texture_filter_diff(sc, vt, vtdiff, (int)rid);
+  const f4 t4 = texture_filter_diff<false>(sc, vt, vtdiff, (int)rid);
   f3 tn = mk3(2.0f * t4.x - 1.0f, 2.0f * t4.y - 1.0f, 2.0f * t4.z - 1.0f);
   tn = fast_normalize3(tn);
   const f3 dp1 = sub3(p2, p1), dp2 = sub3(p3, p1);
@@ -1262,12 +1285,12 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
     col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
   } else {
-    col = texture_filter_diff(sc, vt, vtdiff, (int)__ldg(&G->tid));
+    col = texture_filter_diff<true>(sc, vt, vtdiff, (int)__ldg(&G->tid));
   }
   if (V.use_linear) {
-    col.x = gamma_fwd(col.x);
-    col.y = gamma_fwd(col.y);
-    col.z = gamma_fwd(col.z);
+    col.x = c_gamma_fwd(col.x);
+    col.y = c_gamma_fwd(col.y);
+    col.z = c_gamma_fwd(col.z);
   }
   uint32_t seed2 = rand_xorshift(wang_hash((uint32_t)x + (uint32_t)y * (uint32_t)W * (uint32_t)H));
   uint32_t seed3 = rand_xorshift(seed2);

@@ -417,7 +417,7 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
     const float mip_bias = 1.0f / kMipBias;
     const f2 vtdiff = mk2((fabsf(vtx.x - vt.x) + fabsf(vty.x - vt.x)) * mip_bias,
                           (fabsf(vtx.y - vt.y) + fabsf(vty.y - vt.y)) * mip_bias);
-    refl = texture_filter_diff(sc, vt, vtdiff, (int)ssid).x;
+    refl = texture_filter_diff<false>(sc, vt, vtdiff, (int)ssid).x;
     if (refl < 0.1f) return 0;
   }
   // reflect (cl2.cl:169-176) normalises the normal once more
