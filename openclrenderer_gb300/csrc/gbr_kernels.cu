@@ -1031,7 +1031,6 @@ __device__ __forceinline__ f4 vertex_col(uint32_t c) {
 // Colour-only arithmetic of the light loop: every use below feeds the colour
 // continuously (no comparison, rounding or index depends on it), so the
 // approximate division is covered by the 1/255 colour tolerance.
-__device__ __forceinline__ float cdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ float crcp(float b) { return __fdividef(1.0f, b); }
 __device__ __forceinline__ f3 cnormalize(f3 a) {
   float r = rsqrtf(dot3(a, a));
