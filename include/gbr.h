@@ -239,7 +239,9 @@ gbr_status gbr_render_view(gbr_scene* scene, const gbr_camera* cam, const gbr_vi
 gbr_status gbr_render_view_blend(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
                                  const gbr_outputs* out, const gbr_outputs* blend, void* stream);
 
-/* gbr_render_view with HOST output buffers (copied back before returning). */
+/* gbr_render_view with HOST output buffers, filled before returning.  A
+ * pinned, mapped, 4-byte aligned rgba buffer is written by kernel3 itself;
+ * other buffers are copied back. */
 gbr_status gbr_render_view_host(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view,
                                 uint32_t* depth, uint32_t* id, uint8_t* rgba, void* stream);
 
