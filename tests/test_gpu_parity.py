@@ -90,6 +90,21 @@ def test_terrain_1080p_full_parity():
     assert_parity(got, ref, "terrain_1080p")
 
 
+def test_maximum_sizes_parity():
+    """The largest sizes the path takes in one view: 3840x2160 of the
+    1,048,576-triangle terrain with its shadow cubemap, textured from a 2048^2
+    texture (a whole atlas page with its mips) beside 16^2 and 512^2 ones."""
+    sc = scenes.terrain(width=3840, height=2160, n_textures=3, tex_size=16)
+    sc.tex_sizes = [2048, 16, 512]
+    sc.tex_pixels = [np.random.default_rng(60 + i).integers(0, 256, (s, s, 4), dtype=np.uint8)
+                     for i, s in enumerate(sc.tex_sizes)]
+    gs, got, ref = run_both(sc, shadows=True)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    assert np.array_equal(gs.atlas(), tex.atlas)
+    assert (ref["depth"] != 0xFFFFFFFF).mean() > 0.9
+    assert_parity(got, ref, "terrain_4k")
+
+
 def test_multiple_and_static_shadow_lights():
     """Three dynamic shadow lights (one also static), a plain light, static
     objects (drawn only into the static cubemaps, dynamic ones only into the
