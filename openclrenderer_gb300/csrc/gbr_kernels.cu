@@ -333,10 +333,13 @@ __device__ __forceinline__ int transform_clip(const f3 w[3], f3 cpos, f3 c, f3 s
                                               float height, f3 o0[3], f3 o1[3]) {
   f3 t0[3], t1[3];
   const int n = clip_tri_reg(rot_cs(w[0], cpos, c, s), rot_cs(w[1], cpos, c, s), rot_cs(w[2], cpos, c, s), t0, t1);
+  if (n > 0) {
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    o0[k] = depth_project1(t0[k], width, height, fov);
-    o1[k] = depth_project1(t1[k], width, height, fov);
+    for (int k = 0; k < 3; k++) o0[k] = depth_project1(t0[k], width, height, fov);
+  }
+  if (n > 1) {  // only a triangle with one vertex behind the near plane splits
+#pragma unroll
+    for (int k = 0; k < 3; k++) o1[k] = depth_project1(t1[k], width, height, fov);
   }
   return n;
 }
