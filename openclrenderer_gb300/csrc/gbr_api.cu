@@ -37,6 +37,15 @@ thread_local std::string g_err;
 
 namespace gbr {
 
+uint8_t* mapped_host_alias(void* p) {
+  if (!p || (reinterpret_cast<uintptr_t>(p) & 3) != 0) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+    return static_cast<uint8_t*>(at.devicePointer);
+  cudaGetLastError();
+  return nullptr;
+}
+
 gbr_status fail(gbr_status s, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -846,14 +855,7 @@ gbr_status gbr_render_view_host(gbr_scene* s, const gbr_camera* cam, const gbr_v
   TRY(hw.pix_rgba.reserve(P * 4));
   // RGBA8 into pinned (page-locked, mapped) host memory is written by kernel3
   // itself through the buffer's device address: nothing to copy after shading
-  uint8_t* rgba_dev = nullptr;
-  if (rgba && (reinterpret_cast<uintptr_t>(rgba) & 3) == 0) {
-    cudaPointerAttributes at;
-    if (cudaPointerGetAttributes(&at, rgba) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
-      rgba_dev = static_cast<uint8_t*>(at.devicePointer);
-    else
-      cudaGetLastError();
-  }
+  uint8_t* rgba_dev = mapped_host_alias(rgba);
   gbr_outputs o{hw.pix_depth.p, hw.pix_id.p, rgba_dev ? rgba_dev : hw.pix_rgba.p, nullptr};
   if (!s->copy_stream) {
     CU(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));

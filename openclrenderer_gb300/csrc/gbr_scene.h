@@ -18,6 +18,10 @@ namespace gbr {
 // Records the message for gbr_last_error_string() and returns s.
 gbr_status fail(gbr_status s, const char* fmt, ...);
 
+// The device address of a pinned, mapped host buffer that is 4-byte aligned
+// (kernel3 writes RGBA8 as 32-bit words), or nullptr for any other buffer.
+uint8_t* mapped_host_alias(void* p);
+
 #define CU(call)                                                                                  \
   do {                                                                                            \
     cudaError_t e_ = (call);                                                                      \

@@ -163,13 +163,16 @@ void worker_loop(gbr_server* s, Worker* w) {
     std::vector<gbr_camera> cams(batch.size());
     std::vector<gbr_view> views(batch.size());
     std::vector<gbr_outputs> outs(batch.size());
+    // a pinned, mapped RGBA buffer is written by kernel3 itself (no copy)
+    std::vector<uint8_t*> direct(batch.size(), nullptr);
     for (size_t i = 0; i < batch.size() && st == GBR_OK; i++) {
       const size_t P = (size_t)batch[i].r.view.width * batch[i].r.view.height;
       uint8_t* b = pl.p + offs[i];
       cams[i] = batch[i].r.cam;
       views[i] = batch[i].r.view;
-      outs[i] = gbr_outputs{reinterpret_cast<uint32_t*>(b), reinterpret_cast<uint32_t*>(b + 4 * P), b + 8 * P,
-                            nullptr};
+      direct[i] = gbr::mapped_host_alias(batch[i].r.rgba);
+      outs[i] = gbr_outputs{reinterpret_cast<uint32_t*>(b), reinterpret_cast<uint32_t*>(b + 4 * P),
+                            direct[i] ? direct[i] : b + 8 * P, nullptr};
     }
     if (st == GBR_OK)
       st = gbr_render_batch(w->scene, (uint32_t)batch.size(), cams.data(), views.data(), outs.data(), w->stream);
@@ -181,7 +184,8 @@ void worker_loop(gbr_server* s, Worker* w) {
           st = GBR_CUDA_ERROR;
         if (r.id && cudaMemcpyAsync(r.id, outs[i].id, 4 * P, cudaMemcpyDeviceToHost, w->stream) != cudaSuccess)
           st = GBR_CUDA_ERROR;
-        if (r.rgba && cudaMemcpyAsync(r.rgba, outs[i].rgba, 4 * P, cudaMemcpyDeviceToHost, w->stream) != cudaSuccess)
+        if (r.rgba && !direct[i] &&
+            cudaMemcpyAsync(r.rgba, outs[i].rgba, 4 * P, cudaMemcpyDeviceToHost, w->stream) != cudaSuccess)
           st = GBR_CUDA_ERROR;
       }
     }

@@ -49,11 +49,18 @@ def test_serving_results_identical_alone_and_in_mix():
     # in the mix: all submitted at once; a budget that holds only a few views
     budget = 4 * 1280 * 720 * 46
     srv = Server(gss, hbm_budget_bytes=budget)
-    outs = []
+    outs, keep = [], []
     for k, (s, cam, view) in enumerate(reqs):
         W, H = int(view["width"]), int(view["height"])
         o = {"depth": np.zeros((H, W), np.uint32), "id": np.zeros((H, W), np.uint32),
              "rgba": np.zeros((H, W, 4), np.uint8)}
+        if k % 3 != 2:
+            # pinned RGBA buffers: kernel3 writes them itself when 4-byte
+            # aligned; one in five sits one byte off and is copied instead
+            off = 1 if k % 5 == 0 else 0
+            t = torch.zeros(W * H * 4 + 4, dtype=torch.uint8, pin_memory=True)
+            keep.append(t)
+            o["rgba"] = t.numpy()[off:off + W * H * 4].reshape(H, W, 4)
         outs.append(o)
         srv.submit(s, cam, view, o["depth"], o["id"], o["rgba"], tag=k)
     srv.drain()
