@@ -308,11 +308,16 @@ def run_serving(args, stream):
             w, h = res[int(rng.integers(0, len(res)))]
             reqs.append((int(rng.integers(0, len(sizes))), scenes.random_pose(rng), S.make_view(int(w), int(h))))
         srv = Server(gss, hbm_budget_bytes=budget)
-        # warm the scenes' scratch and the workers' output pools (largest views first)
-        for s_i, cam, view in sorted(reqs, key=lambda r: -int(r[2]["width"]) * int(r[2]["height"]))[:16]:
-            srv.submit(s_i, cam, view, rgba=pool[0][:int(view["width"]) * int(view["height"]) * 4], tag=0)
+        # warm-up (untimed): a burst of the same scenes and resolutions from
+        # other camera poses, so that the scenes' scratch and the workers'
+        # output pools are sized for the batches this mix forms (a batch that
+        # outgrows its scratch is re-run at the larger size)
+        wrng = np.random.default_rng(10)
+        for k, (s_i, cam, view) in enumerate(reqs):
+            srv.submit(s_i, scenes.random_pose(wrng), view,
+                       rgba=pool[k % len(pool)][:int(view["width"]) * int(view["height"]) * 4], tag=0)
         srv.drain()
-        srv.poll(cap=64)
+        srv.poll(cap=4096)
         t0 = time.perf_counter()
         t_next = t0
         for k, (s_i, cam, view) in enumerate(reqs):
