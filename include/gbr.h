@@ -458,25 +458,35 @@ gbr_status gbr_server_destroy(gbr_server* server);
 #define GBR_NOALLOC_MAX_RECORDS 131072u      /* visible clipped triangles per frame */
 #define GBR_NOALLOC_MAX_BIN_ENTRIES 524288u  /* triangle-tile pairs per frame */
 
+/* The entry point cannot read the device arrays without copying them, so
+ * these index preconditions are the caller's: every triangle's object_id <
+ * ndescs; every descriptor's tid (and rid, with GBR_VIEW_NORMAL_MAPPING) <
+ * mipmap_start; nums / sizes / atlas as gbr_scene_texture_layout and
+ * gbr_scene_buffer(0) describe them.  A violation reads outside the arrays:
+ * undefined behaviour.  The light count, the shadow fields of the lights and
+ * the cubemap counts are checked (the lights are read back, 64 B each). */
 typedef struct gbr_device_scene {
   const gbr_triangle* tris;               /* device, ntris; object_id < ndescs */
   uint32_t ntris;
   const gbr_obj_g_descriptor* descs;      /* device, ndescs; tid < mipmap_start */
   uint32_t ndescs;
-  const gbr_light* lights;                /* device, nlights; shadow 0 or 1 */
+  const gbr_light* lights;                /* device, nlights (<= 256); shadow 0 or 1 */
   uint32_t nlights;
   const uint8_t* atlas;                   /* device texture pages (2048^2 RGBA8 each) */
   const uint32_t* nums;                   /* device slot descriptors */
   const uint32_t* sizes;                  /* device page edge sizes */
   uint32_t mipmap_start;
-  const uint32_t* shadow_dyn;             /* device cubemaps, 6*1024^2 u32 per shadow light */
-  const uint32_t* shadow_static;          /* device cubemaps of static shadow lights */
+  const uint32_t* shadow_dyn;             /* device cubemaps, 6*1024^2 u32 per light with shadow == 1 */
+  const uint32_t* shadow_static;          /* device cubemaps, one per light with shadow && is_static */
+  uint32_t n_dyn;                         /* cubemaps at shadow_dyn */
+  uint32_t n_static;                      /* cubemaps at shadow_static */
 } gbr_device_scene;
 
 /* gbr_render_view without any device allocation: no counterpart in the
  * reference.  Renders one view of the scene described by device pointers into
  * the caller's device outputs (depth and id required; rgba and normals
- * optional), with identical results to gbr_render_view.  All scratch lives in
+ * optional; kernel3 runs only when one of them is given), with results
+ * identical to gbr_render_view's, bit for bit.  All scratch lives in
  * one fixed static device array of about 25.3 MB inside the library, held by
  * every GPU that loads it until the process exits.  Views above
  * GBR_NOALLOC_MAX_PIXELS return GBR_INVALID_ARG; frames with more visible

@@ -220,7 +220,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   }
   if (view && sh.shade) {
     CU(mark(6, st));
-    CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws.srec, st, sh.features));
+    CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws, st, sh.features));
     CU(mark(5, st));
   }
   CU(cudaMemcpyAsync(host_ctr, ws.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st));

@@ -160,9 +160,10 @@ cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,
                           uint32_t ntiles, bool with_id, int threads, cudaStream_t st,
                           uint32_t tiles_per_surface = 0);
-// features: some view has kernel3's optional switches on (gbr_view.flags)
+// features: some view has kernel3's optional switches on (gbr_view.flags).
+// Reads the pass's counters: nothing is shaded after an overflow.
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
-                         const Surface* d_surf, uint32_t ntiles, const ShadeRec* srec,
+                         const Surface* d_surf, uint32_t ntiles, const Workspace& ws,
                          cudaStream_t st, bool features = false);
 cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
                                   const uint8_t* pixels, const uint64_t* offsets,

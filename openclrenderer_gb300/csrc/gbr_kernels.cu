@@ -1167,16 +1167,19 @@ __device__ __forceinline__ f4 blend_texel(const uint8_t* __restrict__ rgba, size
 // colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
 // 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
 // FEAT: kernel3's optional switches (view flags) compiled in.
+// nrec: the records this pass wrote; the raster stores only indices below it
+// in the record map, and any other value is treated as an empty pixel, so no
+// index read from the map can leave the record arrays.
 template <bool FEAT>
 __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
-                            const ShadeRec* __restrict__ srec, const SLight* __restrict__ lights, int x, int y,
-                            const float* __restrict__ colx, const float* __restrict__ rowy) {
+                            const ShadeRec* __restrict__ srec, uint32_t nrec, const SLight* __restrict__ lights,
+                            int x, int y, const float* __restrict__ colx, const float* __restrict__ rowy) {
   const int W = S.width, H = S.height;
   const size_t p = (size_t)y * W + x;
   const uint32_t d = S.depth[p];
   const uint32_t r = S.rec[p];
   uint32_t* out = reinterpret_cast<uint32_t*>(V.rgba);
-  if (d == kDepthClear || r == kNoId) {
+  if (d == kDepthClear || r >= nrec) {
     if (out) {
       f4 c;
       c.x = V.clear[0]; c.y = V.clear[1]; c.z = V.clear[2]; c.w = V.clear[3];
@@ -1409,10 +1412,16 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
+// A pass whose setup or binning overflowed its scratch leaves the depth and
+// record map unwritten (the raster returns at once); shading returns too, and
+// the host re-runs the pass with grown scratch.
 template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
-                                               const ShadeRec* __restrict__ srec) {
+                                               const ShadeRec* __restrict__ srec, const Counters* __restrict__ ctr,
+                                               uint32_t rec_cap) {
+  if (ctr->overflow) return;
+  const uint32_t nrec = min(ctr->nrec, rec_cap);
   __shared__ uint32_t s_id;
   __shared__ SLight slights[kMaxLights];
   __shared__ float colx[kTile + 1], rowy[kTile + 1];
@@ -1450,7 +1459,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   __syncthreads();
   const int x = x0 + (threadIdx.x & (kTile - 1));
   const int y = y0 + (threadIdx.x / kTile);
-  if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, views[s_id], S, srec, slights, x, y, colx, rowy);
+  if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, views[s_id], S, srec, nrec, slights, x, y, colx, rowy);
 }
 
 // ---- texture atlas ----------------------------------------------------------------
@@ -1656,12 +1665,12 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
 }
 
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
-                         uint32_t ntiles, const ShadeRec* srec, cudaStream_t st, bool features) {
+                         uint32_t ntiles, const Workspace& ws, cudaStream_t st, bool features) {
   if (!ntiles) return cudaSuccess;
   if (features)
-    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
+    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap);
   else
-    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, srec);
+    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap);
   return cudaGetLastError();
 }
 

@@ -121,8 +121,11 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   if (P > kMaxPixels) return nfail(GBR_INVALID_ARG, "view has more pixels than GBR_NOALLOC_MAX_PIXELS");
   if (sc->ntris && (!sc->tris || !sc->descs || !sc->ndescs))
     return nfail(GBR_INVALID_ARG, "triangles need triangle and descriptor arrays");
-  if (out->rgba && sc->ntris && (!sc->atlas || !sc->nums || !sc->sizes || sc->mipmap_start == 0))
-    return nfail(GBR_INVALID_ARG, "shading needs the texture atlas, nums and sizes");
+  // kernel3 runs only when a colour or normal output is asked for (as in
+  // gbr_render_view); then every table it reads must be there
+  const bool shade = out->rgba || out->normals;
+  if (shade && sc->ntris && (!sc->atlas || !sc->nums || !sc->sizes || sc->mipmap_start == 0))
+    return nfail(GBR_INVALID_ARG, "shading (rgba or normals) needs the texture atlas, nums, sizes and mipmap_start");
   if (sc->nlights && !sc->lights) return nfail(GBR_INVALID_ARG, "null lights");
   if (sc->nlights > (uint32_t)kMaxLights) return nfail(GBR_INVALID_ARG, "more than 256 lights");
 
@@ -142,6 +145,26 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   gbr_status st = scratch_address(&base);
   if (st != GBR_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
+
+  // kernel3 reads one dynamic cubemap per light with shadow == 1 and one
+  // static cubemap per static shadow light: the lights (at most 256 x 64 B)
+  // are read back into this stack array to count them
+  if (shade && sc->ntris && sc->nlights) {
+    gbr_light hl[kMaxLights];
+    cudaError_t e = cudaMemcpyAsync(hl, sc->lights, sizeof(gbr_light) * sc->nlights, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return nfail(GBR_CUDA_ERROR, "read-back of the lights failed", e);
+    uint32_t nd = 0, ns = 0;
+    for (uint32_t i = 0; i < sc->nlights; i++) {
+      if (hl[i].shadow > 1) return nfail(GBR_INVALID_ARG, "a light's shadow field is neither 0 nor 1");
+      if (hl[i].shadow == 1) nd++;
+      if (hl[i].shadow && hl[i].is_static) ns++;
+    }
+    if (nd && (!sc->shadow_dyn || sc->n_dyn < nd))
+      return nfail(GBR_INVALID_ARG, "fewer dynamic cubemaps (n_dyn) than shadow lights");
+    if (ns && (!sc->shadow_static || sc->n_static < ns))
+      return nfail(GBR_INVALID_ARG, "fewer static cubemaps (n_static) than static shadow lights");
+  }
 
   S.depth = out->depth;
   S.id = out->id;
@@ -211,7 +234,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   NA_CU(launch_scan(ws, s), "scan launch failed");
   NA_CU(launch_fill(ws, d_surf, s), "fill launch failed");
   NA_CU(launch_raster(ws, d_surf, 1, nfine, true, kRasterThreads, s), "raster launch failed");
-  NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws.srec, s, view->flags != 0), "shade launch failed");
+  if (shade) NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws, s, view->flags != 0), "shade launch failed");
   Counters c{};
   NA_CU(cudaMemcpyAsync(&c, ws.ctr, sizeof c, cudaMemcpyDeviceToHost, s), "counter read-back failed");
   NA_CU(cudaStreamSynchronize(s), "stream synchronisation failed");
