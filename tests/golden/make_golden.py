@@ -43,6 +43,9 @@ def main(only=None):
             dyn, sta = R.shadow(sc)
             meta["cube_faces"] = [sha(dyn[l, f]) for l in range(dyn.shape[0]) for f in range(6)]
             meta["cube_written"] = int(np.count_nonzero(dyn != 0xFFFFFFFF))
+            if any(l["shadow"] and l["is_static"] for l in sc.lights):
+                meta["static_faces"] = [sha(sta[l, f]) for l in range(sta.shape[0]) for f in range(6)]
+                meta["static_written"] = int(np.count_nonzero(sta != 0xFFFFFFFF))
         arrays = {}
         for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
             fov = float(view["fov_const"]) if view["fov_const"] > 0 else O.fov_const(float(view["hfov_deg"]),

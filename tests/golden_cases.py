@@ -101,6 +101,41 @@ def features():
     return sc, {"shadows": True, "normals": True, "features": True}
 
 
+def multi_shadow_scene(seed=71, lights=None):
+    """Three dynamic shadow lights (the second also static), a plain light,
+    static objects (drawn only into the static cubemaps, the others only into
+    the dynamic ones) and objects that receive no dynamic shadows
+    (cl2.cl:4460-4464, 6126-6181; engine.cpp:1700-1783).  The cube positions
+    come from plain_cubes; seed picks the light positions."""
+    sc = scenes.plain_cubes()
+    descs = sc.descs.copy()
+    for i in range(len(descs)):
+        ff = S.FLAG_TWO_SIDED
+        if i % 3 == 0:
+            ff |= S.FLAG_IS_STATIC
+        if i % 5 == 0:
+            ff |= S.FLAG_NO_DYN_SHADOWS
+        descs[i]["feature_flag"] = ff
+    sc.descs = descs
+    if lights is None:
+        rng = np.random.default_rng(seed)
+        p = [(rng.uniform(-400, 400), rng.uniform(-300, 300), rng.uniform(300, 1500)) for _ in range(4)]
+        lights = np.stack([S.make_light(p[0], (1, 0.9, 0.8), radius=3000.0, shadow=1),
+                           S.make_light(p[1], (0.7, 0.8, 1), radius=2500.0, shadow=1, is_static=1),
+                           S.make_light(p[2], (1, 1, 1), radius=2000.0, shadow=1),
+                           S.make_light(p[3], (1, 1, 1), radius=4000.0)])
+    sc.lights = lights
+    return sc
+
+
+def multi_shadow():
+    sc = multi_shadow_scene()
+    sc.views = [S.make_view(480, 360, 90.0)]
+    sc.cameras.append(S.make_camera((-50.0, 30.0, 120.0), (-0.08, 0.18, 0.0)))
+    sc.views.append(S.make_view(400, 300, hfov_deg=80.0))
+    return sc, {"shadows": True, "normals": True}
+
+
 def blend_source(width, height, seed=61):
     """A second render context's frame for kernel3's integrated blend: depth
     (a third of it empty) spread over the scenes' depth range, RGBA8 with
@@ -170,4 +205,4 @@ POST = {"godrays": "cubes", "post": "cubes"}
 BLEND = ["cubes", "features"]
 
 CASES = {"cubes": cubes, "terrain_shadow": terrain_shadow, "soups": soups, "edges": edges,
-         "wide_boxes": wide_boxes, "features": features}
+         "wide_boxes": wide_boxes, "features": features, "multi_shadow": multi_shadow}

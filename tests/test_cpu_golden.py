@@ -38,6 +38,9 @@ def test_oracle_matches_reference_fixture(name):
         dyn, sta = O.shadow(sc)
         assert [sha(dyn[l, f]) for l in range(dyn.shape[0]) for f in range(6)] == meta["cube_faces"]
         assert int(np.count_nonzero(dyn != 0xFFFFFFFF)) == meta["cube_written"] > 0
+        if "static_faces" in meta:
+            assert [sha(sta[l, f]) for l in range(sta.shape[0]) for f in range(6)] == meta["static_faces"]
+            assert int(np.count_nonzero(sta != 0xFFFFFFFF)) == meta["static_written"] > 0
     for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
         got = O.render(sc, tex, cam, view, dyn, sta, normals=bool(opts.get("normals")))
         assert got["fragments"] == meta[f"fragments{k}"]
@@ -77,6 +80,32 @@ def test_oracle_matches_reference_kernels_random(seed):
                    O.fov_const(float(view["hfov_deg"]), w))
     got = O.render(sc, tex, sc.cameras[0], view, normals=True)
     assert got["fragments"] == ref["fragments"]
+    for key in ("depth", "id", "rgba", "normals"):
+        assert np.array_equal(got[key], ref[key]), key
+
+
+@pytest.mark.parametrize("seed", [111, 112])
+def test_oracle_multi_shadow_matches_reference_kernels_random(seed):
+    """Three dynamic shadow lights (one also static) at random positions,
+    static and no-dynamic-shadow objects: the static and dynamic cubemaps, the
+    cubemap each shadow light reads (shnum / static_num) and the shaded frame
+    against the reference kernels (cl2.cl:4460-4464, 6126-6181;
+    engine.cpp:1700-1783)."""
+    R = _ref_or_skip()
+    from openclrenderer_gb300 import structs as S
+    sc = golden_cases.multi_shadow_scene(seed)
+    rng = np.random.default_rng(seed)
+    w, h = int(rng.integers(160, 480)), int(rng.integers(120, 360))
+    sc.views = [S.make_view(w, h, float(rng.uniform(70, 100)))]
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    rdyn, rsta = R.shadow(sc)
+    dyn, sta = O.shadow(sc)
+    assert np.array_equal(dyn, rdyn) and np.array_equal(sta, rsta)
+    assert (rsta != 0xFFFFFFFF).sum() > 1000
+    view = sc.views[0]
+    ref = R.render(sc, tex.atlas, tex.nums, tex.sizes, tex.mipmap_start, sc.cameras[0], view,
+                   O.fov_const(float(view["hfov_deg"]), w), rdyn, rsta)
+    got = O.render(sc, tex, sc.cameras[0], view, dyn, sta, normals=True)
     for key in ("depth", "id", "rgba", "normals"):
         assert np.array_equal(got[key], ref[key]), key
 

@@ -109,27 +109,35 @@ def test_multiple_and_static_shadow_lights():
     """Three dynamic shadow lights (one also static), a plain light, static
     objects (drawn only into the static cubemaps, dynamic ones only into the
     dynamic cubemaps) and objects that receive no dynamic shadows
-    (cl2.cl:4460-4464, 6126-6181; engine.cpp:1700-1783)."""
-    sc = scenes.plain_cubes()
-    descs = sc.descs.copy()
-    for i in range(len(descs)):
-        ff = S.FLAG_TWO_SIDED
-        if i % 3 == 0:
-            ff |= S.FLAG_IS_STATIC
-        if i % 5 == 0:
-            ff |= S.FLAG_NO_DYN_SHADOWS
-        descs[i]["feature_flag"] = ff
-    sc.descs = descs
-    sc.lights = np.stack([S.make_light((-200, -150, 800), (1, 0.9, 0.8), radius=3000.0, shadow=1),
-                          S.make_light((250, 100, 1200), (0.7, 0.8, 1), radius=2500.0, shadow=1, is_static=1),
-                          S.make_light((0, 300, 400), (1, 1, 1), radius=2000.0, shadow=1),
-                          S.make_light((100, -100, 100), (1, 1, 1), radius=4000.0)])
-    gs, got, ref = run_both(sc, shadows=True, normals=True)
+    (cl2.cl:4460-4464, 6126-6181; engine.cpp:1700-1783): cubemaps and both
+    views against the reference kernels' fixture (tests/golden/multi_shadow.npz)
+    and the oracle."""
+    import hashlib
+    import json
+    import os
+    from tests import golden_cases
+    sc, _ = golden_cases.multi_shadow()
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "multi_shadow.npz"))
+    meta = json.loads(str(fx["meta"]))
+    gs = GpuScene(sc)
+    gs.shadow_pass()
     dyn, sta = O.shadow(sc)
-    assert np.array_equal(gs.cubemaps(), dyn[:3])
-    assert np.array_equal(gs.cubemaps(static=True), sta[:1])
-    assert (dyn[:3] != 0xFFFFFFFF).sum() > 1000 and (sta[0] != 0xFFFFFFFF).sum() > 1000
-    assert_parity(got, ref, "multi_shadow")
+    cube, scube = gs.cubemaps(), gs.cubemaps(static=True)
+    assert np.array_equal(cube, dyn[:3])
+    assert np.array_equal(scube, sta[:1])
+
+    def sha(a):
+        return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    assert [sha(cube[l, f]) for l in range(3) for f in range(6)] == meta["cube_faces"]
+    assert [sha(scube[0, f]) for f in range(6)] == meta["static_faces"]
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        got = gs.render(cam, view, normals=True).numpy()
+        torch.cuda.synchronize()
+        ref = O.render(sc, tex, cam, view, dyn, sta, normals=True)
+        assert_parity(got, ref, f"multi_shadow view {k}")
+        fixture = {key: fx[f"{key}{k}"] for key in ("depth", "id", "rgba")}
+        assert_parity(got, fixture, f"multi_shadow view {k} vs reference kernels")
 
 
 def test_optional_kernel3_features_parity():
