@@ -457,6 +457,8 @@ gbr_status gbr_server_destroy(gbr_server* server);
 #define GBR_NOALLOC_MAX_PIXELS 2097152u      /* width*height, e.g. 1920x1080 */
 #define GBR_NOALLOC_MAX_RECORDS 131072u      /* visible clipped triangles per frame */
 #define GBR_NOALLOC_MAX_BIN_ENTRIES 524288u  /* triangle-tile pairs per frame */
+#define GBR_NOALLOC_MAX_OBJECTS 65536u       /* descriptors, when rgba or normals are asked for */
+#define GBR_NOALLOC_MAX_TEXTURES 4096u       /* texture ids (mipmap_start), likewise */
 
 /* The entry point cannot read the device arrays without copying them, so
  * these index preconditions are the caller's: every triangle's object_id <
@@ -487,9 +489,11 @@ typedef struct gbr_device_scene {
  * the caller's device outputs (depth and id required; rgba and normals
  * optional; kernel3 runs only when one of them is given), with results
  * identical to gbr_render_view's, bit for bit.  All scratch lives in
- * one fixed static device array of about 25.3 MB inside the library, held by
+ * one fixed static device array of about 42.4 MB inside the library, held by
  * every GPU that loads it until the process exits.  Views above
- * GBR_NOALLOC_MAX_PIXELS return GBR_INVALID_ARG; frames with more visible
+ * GBR_NOALLOC_MAX_PIXELS, and shaded views of scenes with more descriptors or
+ * textures than GBR_NOALLOC_MAX_OBJECTS / GBR_NOALLOC_MAX_TEXTURES, return
+ * GBR_INVALID_ARG; frames with more visible
  * triangles or bin entries than the limits return GBR_BIN_OVERFLOW_RETRY (use
  * gbr_render_view).  The array is shared by all calls and keeps the previous
  * call's contents: calls that overlap on the GPU race, so serialise them.

@@ -27,7 +27,7 @@ static_assert(offsetof(gbr_obj_g_descriptor, scale) == 96, "descriptor.scale off
 static_assert(offsetof(gbr_obj_g_descriptor, feature_flag) == 132, "descriptor.feature_flag offset");
 static_assert(offsetof(gbr_light, shadow) == 32, "light.shadow offset");
 static_assert(sizeof(gbr::RasterRec) == 64, "raster record");
-static_assert(sizeof(gbr::ShadeRec) == 48, "shade record");
+static_assert(sizeof(gbr::ShadeRec) == 144, "shade record");
 
 using namespace gbr;
 
@@ -165,7 +165,7 @@ void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   if (!s->world_dirty) return GBR_OK;
   TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
-  TRY(s->objq.reserve((size_t)std::max<uint32_t>(s->ndescs, 1) * 2));
+  TRY(s->objq.reserve((size_t)std::max<uint32_t>(s->ndescs, 1) * kObjQuads));
   SceneDev sd = s->dev();
   CU(launch_world(sd, s->world.p, s->objq.p, st));
   s->stats.launches += 2;
@@ -175,7 +175,7 @@ gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
 
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
                        Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom,
-                       cudaEvent_t join) {
+                       cudaEvent_t join, const SideStream* side) {
   const bool split = geom != nullptr && geom != st;
   if (!split) geom = st;
   const SceneDev sd = s->dev();
@@ -207,6 +207,14 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
     CU(launch_setup_shadow(sd, wm.jobs.p, sh.nitems, wm.surf.p, ws, geom));
   }
   CU(mark(1, geom));
+  const bool prep = view && sh.shade;
+  const bool on_side = prep && side && side->stream;
+  if (on_side) {
+    CU(cudaEventRecord(side->fork, geom));
+    CU(cudaStreamWaitEvent(side->stream, side->fork, 0));
+    CU(launch_prep(sd, ws, side->stream));
+    CU(cudaEventRecord(side->join, side->stream));
+  }
   CU(launch_scan(ws, geom));
   CU(mark(2, geom));
   CU(launch_fill(ws, wm.surf.p, geom));
@@ -214,10 +222,12 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom, sh.tiles_per_surface));
   CU(mark(4, geom));
   if (view && s->mark_raster) CU(cudaEventRecord(s->raster_done, geom));
+  if (prep && !on_side) CU(launch_prep(sd, ws, geom));
   if (split) {
     CU(cudaEventRecord(join, geom));
     CU(cudaStreamWaitEvent(st, join, 0));
   }
+  if (on_side) CU(cudaStreamWaitEvent(st, side->join, 0));
   if (view && sh.shade) {
     CU(mark(6, st));
     CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws, st, sh.features));
@@ -261,6 +271,14 @@ Counters* counter_slot(gbr_scene* s, bool view) {
   return reinterpret_cast<Counters*>(static_cast<char*>(s->staging.p) + (view ? 0 : 256));
 }
 
+// The side stream and events of the view pass's shade constants.
+gbr_status ensure_side(gbr_scene* s) {
+  if (!s->side.stream) CU(cudaStreamCreateWithFlags(&s->side.stream, cudaStreamNonBlocking));
+  if (!s->side.fork) CU(cudaEventCreateWithFlags(&s->side.fork, cudaEventDisableTiming));
+  if (!s->side.join) CU(cudaEventCreateWithFlags(&s->side.join, cudaEventDisableTiming));
+  return GBR_OK;
+}
+
 // Launch one pass (views or shadow jobs) on the scene's own scratch and queue
 // the read-back of its counters; the caller synchronises and calls
 // check_pass.  The caller has filled the pass's surfaces / views / jobs on
@@ -271,9 +289,10 @@ gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream
   WorkMem& wm = pass_mem(s, view);
   TRY(reserve_pass(wm, sh, view));
   cudaEvent_t* ev = s->profile ? s->ev + (view ? 8 : 0) : nullptr;
+  if (view) TRY(ensure_side(s));
   TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st,
-                  geom, s->geom_done));
-  s->stats.launches += pass_kernels(view) - (view && !sh.shade ? 1u : 0u);
+                  geom, s->geom_done, view ? &s->side : nullptr));
+  s->stats.launches += pass_kernels(view, sh.shade);
   if (view) s->view_shaded = sh.shade;
   return GBR_OK;
 }
@@ -465,6 +484,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   cudaDeviceSynchronize();
   s->tris.release(); s->descs.release(); s->lights.release(); s->atlas.release();
   s->nums.release(); s->sizes.release(); s->shadow_dyn.release(); s->shadow_static.release();
+  s->texlv.release();
   s->ws_view.release();
   s->ws_shadow.release();
   s->ws_host.release();
@@ -476,6 +496,9 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->staging.release();
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
+  if (s->side.fork) cudaEventDestroy(s->side.fork);
+  if (s->side.join) cudaEventDestroy(s->side.join);
+  if (s->side.stream) cudaStreamDestroy(s->side.stream);
   if (s->pre_shadow) cudaEventDestroy(s->pre_shadow);
   if (s->geom_done) cudaEventDestroy(s->geom_done);
   if (s->aux) cudaStreamDestroy(s->aux);
@@ -626,6 +649,8 @@ gbr_status gbr_scene_set_textures(gbr_scene* s, uint32_t n, const int32_t* sizes
   s->host_sizes = pages;
   s->mipmap_start = n;
   s->npages = (uint32_t)pages.size();
+  TRY(s->texlv.reserve((size_t)std::max<uint32_t>(n, 1) * kTexLevels));
+  CU(launch_texture_levels(s->nums.p, s->sizes.p, n, s->texlv.p, 0));
   if (n) {
     std::vector<uint64_t> offs(n);
     uint64_t total = 0;

@@ -32,6 +32,7 @@ struct gbr_batch {
   cudaStream_t cap_stream = nullptr;
   cudaStream_t cap_aux = nullptr;  // the views' geometry branch of the graph
   cudaEvent_t fork = nullptr, join = nullptr;
+  SideStream side;                 // the shade constants' branch of the graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   size_t nodes = 0;
@@ -149,7 +150,7 @@ gbr_status capture(gbr_batch* b) {
                      b->cap_stream);
   if (ce == cudaSuccess && st == GBR_OK)
     st = launch_pass(s, b->wv, b->tune[GBR_PASS_VIEW], true, b->vshape, b->view_ctr(), nullptr, b->cap_stream,
-                     b->cap_aux, b->join);
+                     b->cap_aux, b->join, &b->side);
   cudaGraph_t g = nullptr;
   cudaError_t ee = cudaStreamEndCapture(b->cap_stream, &g);
   if (st != GBR_OK) {
@@ -176,8 +177,7 @@ gbr_status launch_graph(gbr_batch* b, const gbr_camera* cams, cudaStream_t st) {
   CU(cudaGraphLaunch(b->exec, st));
   CU(cudaEventRecord(b->done, st));
   b->launches++;
-  b->s->stats.launches += pass_kernels(true) - (b->vshape.shade ? 0u : 1u) +
-                          (b->sshape.nitems ? pass_kernels(false) : 0u);
+  b->s->stats.launches += pass_kernels(true, b->vshape.shade) + (b->sshape.nitems ? pass_kernels(false) : 0u);
   b->in_flight = true;
   b->last_stream = st;
   return GBR_OK;
@@ -260,6 +260,9 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side.stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gbr_batch_destroy(b);
     return fail(GBR_CUDA_ERROR, "stream / event creation failed: %s", cudaGetErrorString(e));
@@ -447,6 +450,9 @@ gbr_status gbr_batch_destroy(gbr_batch* b) {
   if (b->join) cudaEventDestroy(b->join);
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
   if (b->cap_aux) cudaStreamDestroy(b->cap_aux);
+  if (b->side.fork) cudaEventDestroy(b->side.fork);
+  if (b->side.join) cudaEventDestroy(b->side.join);
+  if (b->side.stream) cudaStreamDestroy(b->side.stream);
   delete b;
   return GBR_OK;
 }

@@ -45,12 +45,32 @@ struct __align__(16) RasterRec {
   uint32_t pad;
 };
 
-// Per view record: what kernel3 reads through the id (48 bytes).
+// Per visible clipped triangle of a view: kernel3's per-triangle constants,
+// computed once by the fill (prep_shade) instead of at every pixel the
+// triangle owns (144 bytes).  Between the setup and the fill, a / e0 / e1
+// hold what the setup knows: the projected vertices (x, y, z) with rconst
+// and the triangle index in the w lanes.
 struct __align__(16) ShadeRec {
-  float4 p0;  // projected vertex 0 (x, y, z) + rconst
-  float4 p1;  // vertex 1 + triangle index (bits)
-  float4 p2;  // vertex 2 + object id (bits)
+  float4 a;      // barycentric frame: p1 = vertex 0 * scale (xyz), d00
+  float4 e0;     // p2 - p1 (xyz), d01
+  float4 e1;     // p3 - p1 (xyz), d11
+  float4 plane;  // get_vtdiff's 1/z plane DA, DB, DC; the frame's denom
+  float4 n1;     // vertex normal 0 (xyz), vt0.x
+  float4 n2;     // vertex normal 1 (xyz), vt0.y
+  float4 n3;     // vertex normal 2 (xyz), vt1.x
+  float4 t;      // vt1.y, vt2.x, vt2.y, object id | back-facing << 31 (bits)
+  float4 col;    // vertex colours 0..2 (bits; colour 0 == 0: textured), triangle index (bits)
 };
+
+// Per object, kernel3's view of the descriptor (4 float4, rebuilt with the
+// world-space cache): rot_quat's normalised quaternion, back_rot_quat's
+// normalised inverse, (world_pos, diffuse), (spec_mult, roughness
+// clamp(1 - specular, 0.001, 10), feature_flag bits, tid bits).
+constexpr int kObjQuads = 4;
+
+// Per texture id, the atlas slot of each level (0 = the texture, 1..4 its
+// mips): (x, y) origin of the slot in its page, edge, page index (bits).
+constexpr int kTexLevels = 1 + 4;
 
 // One raster target: a view, or one face of a shadow cubemap.
 struct Surface {
@@ -104,9 +124,13 @@ struct SceneDev {
   // first half of full_rotate_quat, cl2.cl:700-710); w of vertex 0 holds the
   // object id.  3 per triangle.
   const float4* world;
-  // per object: fast_normalize4(world_rot_quat), then the normalised inverse
-  // back_rot_quat applies (cl2.cl:350-370); 2 per descriptor, or null
+  // per object, kObjQuads float4: fast_normalize4(world_rot_quat), the
+  // normalised inverse back_rot_quat applies (cl2.cl:350-370), and the
+  // material terms kernel3 reads; required by kernel3, else may be null
   const float4* objq;
+  // per texture id, kTexLevels float4 slots (texture level table); required
+  // by kernel3 and the reflections pass
+  const float4* texlv;
   const gbr_obj_g_descriptor* descs;
   uint32_t ndescs;
   const gbr_light* lights;
@@ -148,6 +172,7 @@ struct Workspace {
 };
 
 // ---- launchers (gbr_kernels.cu) ----
+// World-space cache (world may be null: objects only) and the per-object table.
 cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st);
 cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
@@ -155,6 +180,13 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
                                 const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
+// Views that shade: every record's setup output becomes its shade constants
+// (prep_shade).  Needs the setup done; kernel3 needs it done.
+cudaError_t launch_prep(const SceneDev& sc, const Workspace& ws, cudaStream_t st);
+// Texture level table (kTexLevels float4 per texture id) from the slot
+// descriptors nums / page sizes of the atlas packing.
+cudaError_t launch_texture_levels(const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start,
+                                  float4* texlv, cudaStream_t st);
 // tiles_per_surface: the common tile count when every surface has the same
 // size (cube faces), else 0.
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,

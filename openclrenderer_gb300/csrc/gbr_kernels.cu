@@ -157,11 +157,11 @@ __device__ __forceinline__ int write_rec(const Cand& c, uint32_t r, uint32_t sur
   RasterRec R;
   make_rec(c, surface, R);
   store_rec(ws.rec + r, R);
-  if (view) {
+  if (view) {  // what prep_shade needs (the fill turns it into the shade constants)
     uint32_t tri = c.key >> 1;
-    ws.srec[r].p0 = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.rc);
-    ws.srec[r].p1 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
-    ws.srec[r].p2 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
+    ws.srec[r].a = make_float4(c.p[0].x, c.p[0].y, c.p[0].z, c.rc);
+    ws.srec[r].e0 = make_float4(c.p[1].x, c.p[1].y, c.p[1].z, __uint_as_float(tri));
+    ws.srec[r].e1 = make_float4(c.p[2].x, c.p[2].y, c.p[2].z, 0.0f);
   }
   *foot = footprint(R.xr, R.yr, ws);
   return foot_count(*foot);
@@ -296,13 +296,36 @@ __device__ __forceinline__ f4 quat_inverse_n(f4 q) {
   return fast_normalize4(n);
 }
 
+// and the material terms kernel3 reads (kObjQuads float4 per object).
 __global__ void __launch_bounds__(256) k_objects(SceneDev sc, float4* __restrict__ objq) {
   const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= sc.ndescs) return;
-  const f4 q = ld4(sc.descs[o].world_rot_quat);
+  const gbr_obj_g_descriptor* G = sc.descs + o;
+  const f4 q = ld4(G->world_rot_quat);
   const f4 qn = fast_normalize4(q), qi = quat_inverse_n(q);
-  objq[2 * o] = make_float4(qn.x, qn.y, qn.z, qn.w);
-  objq[2 * o + 1] = make_float4(qi.x, qi.y, qi.z, qi.w);
+  float4* d = objq + (size_t)kObjQuads * o;
+  d[0] = make_float4(qn.x, qn.y, qn.z, qn.w);
+  d[1] = make_float4(qi.x, qi.y, qi.z, qi.w);
+  d[2] = make_float4(__ldg(&G->world_pos[0]), __ldg(&G->world_pos[1]), __ldg(&G->world_pos[2]), __ldg(&G->diffuse));
+  d[3] = make_float4(__ldg(&G->spec_mult), clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f),
+                     __int_as_float(__ldg(&G->feature_flag)), __uint_as_float(__ldg(&G->tid)));
+}
+
+// The atlas slot of level L of texture t (slot descriptor nums[...] = page <<
+// 16 | slot; pages are powers of two, 16..2048, so the slot's row and column
+// within its page are exact in integers): the texture level table entry.
+__global__ void __launch_bounds__(256) k_texture_levels(const uint32_t* __restrict__ nums,
+                                                        const uint32_t* __restrict__ sizes, uint32_t mipmap_start,
+                                                        float4* __restrict__ texlv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= mipmap_start * kTexLevels) return;
+  const uint32_t t = i / kTexLevels, L = i % kTexLevels;
+  const uint32_t nv = nums[L == 0 ? t : mipmap_start + t * kMipLevels + (L - 1)];
+  const uint32_t page = nv >> 16, which = nv & 0xFFFFu;
+  const uint32_t w = sizes[page];
+  const uint32_t hnum = (uint32_t)kTexPage / w;
+  const uint32_t row = which / hnum, col = which - row * hnum;
+  texlv[i] = make_float4((float)(col * w), (float)(row * w), (float)w, __uint_as_float(page));
 }
 
 // World-space vertices of a triangle: from the scene's cache when there is
@@ -501,6 +524,76 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Workspace ws) {
     uint64_t need = (uint64_t)ws.ctr->fine_total + ws.ctr->coarse_total;
     if (need > ws.bin_cap) ws.ctr->overflow |= 2u;
   }
+}
+
+// Barycentrics (cl2.cl:5372-5384) split into the per-triangle part and the
+// per-point part; bary_exact is barycentric() bit for bit.
+struct BaryFrame {
+  f3 a, v0, v1;
+  float d00, d01, d11, denom;
+};
+__device__ __forceinline__ BaryFrame bary_frame(f3 a, f3 b, f3 c) {
+  BaryFrame f;
+  f.a = a;
+  f.v0 = sub3(b, a);
+  f.v1 = sub3(c, a);
+  f.d00 = dot3(f.v0, f.v0);
+  f.d01 = dot3(f.v0, f.v1);
+  f.d11 = dot3(f.v1, f.v1);
+  f.denom = f.d00 * f.d11 - f.d01 * f.d01;
+  return f;
+}
+__device__ __forceinline__ void bary_exact(const BaryFrame& f, f3 p, float* u, float* v, float* w) {
+  f3 v2 = sub3(p, f.a);
+  float d20 = dot3(v2, f.v0), d21 = dot3(v2, f.v1);
+  *v = fdiv(f.d11 * d20 - f.d01 * d21, f.denom);
+  *w = fdiv(f.d00 * d21 - f.d01 * d20, f.denom);
+  *u = (1.0f - *v) - *w;
+}
+// kernel3's per-triangle arithmetic for one view record, in place: the
+// setup's projected vertices, rconst and triangle index become the
+// barycentric frame (cl2.cl:5372-5384) of the scaled object-space vertices,
+// get_vtdiff's 1/z plane through the rounded vertices (cl2.cl:5691-5760), the
+// vertex normals, UVs and colours, and the facing (cl2.cl:491-494).  Every
+// value is computed with the arithmetic kernel3 applies per pixel in the
+// reference, so the pixels read exactly what they would compute.
+__device__ __forceinline__ void prep_shade(const SceneDev& sc, ShadeRec* R) {
+  const float4 q0 = R->a, q1 = R->e0, q2 = R->e1;  // the setup's output (this thread alone touches it)
+  const f3 tp0 = mk3(q0.x, q0.y, q0.z), tp1 = mk3(q1.x, q1.y, q1.z), tp2 = mk3(q2.x, q2.y, q2.z);
+  const uint32_t tri = __float_as_uint(q1.w);
+  // the triangle as 9 float4 loads: per vertex pos, normal, (vt, object_id, vertex_col)
+  const float4* tv = reinterpret_cast<const float4*>(sc.tris + tri);
+  const float4 va0 = __ldg(tv + 0), vb0 = __ldg(tv + 1), vc0 = __ldg(tv + 2);
+  const float4 va1 = __ldg(tv + 3), vb1 = __ldg(tv + 4), vc1 = __ldg(tv + 5);
+  const float4 va2 = __ldg(tv + 6), vb2 = __ldg(tv + 7), vc2 = __ldg(tv + 8);
+  const uint32_t o_id = __float_as_uint(vc0.z);
+  const float scale = __ldg(&sc.descs[o_id].scale);
+  const BaryFrame bf = bary_frame(mul3s(mk3(va0.x, va0.y, va0.z), scale), mul3s(mk3(va1.x, va1.y, va1.z), scale),
+                                  mul3s(mk3(va2.x, va2.y, va2.z), scale));
+  const f3 xpv = mk3(roundf(tp0.x), roundf(tp1.x), roundf(tp2.x));
+  const f3 ypv = mk3(roundf(tp0.y), roundf(tp1.y), roundf(tp2.y));
+  const f3 depths = mk3(rcp(tp0.z), rcp(tp1.z), rcp(tp2.z));
+  float DA, DB, DC;
+  plane_const(depths, xpv, ypv, q0.w, &DA, &DB, &DC);
+  const uint32_t back = backface_front(tp0, tp1, tp2) ? 0u : 0x80000000u;
+  R->a = make_float4(bf.a.x, bf.a.y, bf.a.z, bf.d00);
+  R->e0 = make_float4(bf.v0.x, bf.v0.y, bf.v0.z, bf.d01);
+  R->e1 = make_float4(bf.v1.x, bf.v1.y, bf.v1.z, bf.d11);
+  R->plane = make_float4(DA, DB, DC, bf.denom);
+  R->n1 = make_float4(vb0.x, vb0.y, vb0.z, vc0.x);
+  R->n2 = make_float4(vb1.x, vb1.y, vb1.z, vc0.y);
+  R->n3 = make_float4(vb2.x, vb2.y, vb2.z, vc1.x);
+  R->t = make_float4(vc1.y, vc2.x, vc2.y, __uint_as_float(o_id | back));
+  R->col = make_float4(vc0.w, vc1.w, vc2.w, __uint_as_float(tri));
+}
+
+// The shade constants of every record of a view pass (after the setup; it
+// runs beside the scan, fill and raster, which do not read them).
+__global__ void __launch_bounds__(256, 4) k_prep(SceneDev sc, Workspace ws) {
+  if (ws.ctr->overflow) return;
+  const uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x)
+    prep_shade(sc, ws.srec + r);
 }
 
 // Scatter record indices into their tile bins (cursor atomics aggregated
@@ -831,23 +924,20 @@ __device__ __forceinline__ float depth_to_dist(uint32_t d) { return ((float)d * 
 // Exact byte -> float without a conversion instruction: 2^23 + b, minus 2^23.
 __device__ __forceinline__ float u8f(uint32_t b) { return __uint_as_float(0x4B000000u | b) - 8388608.0f; }
 
-// read_tex_array_all_precalculated (cl2.cl:823-851) with the slot origin
-// (tnumx, tnumy), which does not depend on the coordinates, computed once per
-// bilinear footprint.
+// read_tex_array_all_precalculated (cl2.cl:823-851) in one atlas slot of the
+// texture level table: (ox, oy) is the slot origin in its page, tnum * width
+// in the reference, an integer below 2048 and so exact in float, which makes
+// fma(tnum, width, c) = ox + c.
 struct TexSlot {
-  float tnumx, tnumy, width;
+  float ox, oy, width;
   const uchar4* page;
 };
-// Page edges are powers of two (16..2048), so the slot row which*w/2048 and
-// column are exact in integers: floor(which / hnum) and which mod hnum.
-__device__ __forceinline__ TexSlot tex_slot_pre(const SceneDev& sc, int which, int slice, float width) {
-  const int hnum = kTexPage / (int)width;
+__device__ __forceinline__ TexSlot level_slot(const SceneDev& sc, float4 lv) {
   TexSlot t;
-  const int row = which / hnum;
-  t.tnumy = (float)row;
-  t.tnumx = (float)(which - row * hnum);
-  t.width = width;
-  t.page = sc.atlas + (size_t)slice * kTexPage * kTexPage;
+  t.ox = lv.x;
+  t.oy = lv.y;
+  t.width = lv.z;
+  t.page = sc.atlas + (size_t)__float_as_uint(lv.w) * kTexPage * kTexPage;
   return t;
 }
 __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy) {
@@ -855,8 +945,8 @@ __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy
   cy = clampf_(cy, 0.001f, ts.width - 0.001f);
   // in [0, 2048) and never NaN (the clamp maps NaN to 0.001): plain
   // truncation equals the saturating convert_int
-  int ix = (int)fma_(ts.tnumx, ts.width, cx);
-  int iy = (int)fma_(ts.tnumy, ts.width, cy);
+  const int ix = (int)(ts.ox + cx);
+  const int iy = (int)(ts.oy + cy);
   const uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(ts.page) + ((size_t)iy * kTexPage + ix));
   f4 r; r.x = u8f(t & 0xFF); r.y = u8f((t >> 8) & 0xFF); r.z = u8f((t >> 16) & 0xFF); r.w = u8f(t >> 24);
   return r;
@@ -866,8 +956,7 @@ __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy
 // may contract; the normal map's fetch, which feeds the exact normal, keeps
 // the plain products.
 template <bool COLOUR>
-__device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, int slice, float width) {
-  const TexSlot ts = tex_slot_pre(sc, which, slice, width);
+__device__ f4 bilinear_pre(const TexSlot& ts, float mx, float my) {
   float posx = floorf(mx), posy = floorf(my);
   f4 c0 = read_tex_pre(ts, posx, posy);
   f4 c1 = read_tex_pre(ts, posx + 1, posy);
@@ -890,28 +979,24 @@ __device__ f4 bilinear_pre(const SceneDev& sc, float mx, float my, int which, in
   return r;
 }
 
-// texture_filter_diff (cl2.cl:1511-1573); COLOUR as for bilinear_pre
+// texture_filter_diff (cl2.cl:1511-1573); COLOUR as for bilinear_pre.  The
+// two mip levels come from the texture level table: level mip_lower (the
+// texture itself at 0) and level min(mip_lower, 3) + 1, the slots the
+// reference's tid_lower / tid_higher name.
 template <bool COLOUR>
 __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2) {
-  uint32_t nv = __ldg(sc.nums + tid2);
-  int slice = (int)(nv >> 16);
-  int tsize = (int)__ldg(sc.sizes + slice);
+  const float4* lv = sc.texlv + (size_t)tid2 * kTexLevels;
+  const float tsize = __ldg(&lv[0].z);
   f2 vtm = texture_mod(vt);
-  float wx = vtdiff.x * (float)tsize, wy = vtdiff.y * (float)tsize;
+  float wx = vtdiff.x * tsize, wy = vtdiff.y * tsize;
   float worst = fsqrt(wx * wx + wy * wy);
-  float wif = fmax_(log2_approx(worst), 0.0f);
+  float wif = fmax_(log2_approx(worst), 0.0f);  // finite for every input
   float mip_lower = clampf_(floorf(wif), 0.0f, (float)kMipLevels);
   float fmd = wif - mip_lower;
-  int tid_lower = mip_lower == 0.0f
-                      ? tid2
-                      : (int)(((mip_lower - 1.0f) + (float)sc.mipmap_start) + (float)(tid2 * kMipLevels));
-  int tid_higher = (int)((clampf_(mip_lower, 0.0f, kMipLevels - 1.0f) + (float)sc.mipmap_start) +
-                         (float)(tid2 * kMipLevels));
-  uint32_t lnv = __ldg(sc.nums + tid_lower), hnv = __ldg(sc.nums + tid_higher);
-  int sl = (int)(lnv >> 16), sh = (int)(hnv >> 16);
-  float szl = (float)__ldg(sc.sizes + sl), szh = (float)__ldg(sc.sizes + sh);
-  f4 c1 = bilinear_pre<COLOUR>(sc, vtm.x * szl, vtm.y * szl, (int)(lnv & 0xFFFF), sl, szl);
-  f4 c2 = bilinear_pre<COLOUR>(sc, vtm.x * szh, vtm.y * szh, (int)(hnv & 0xFFFF), sh, szh);
+  const int lo = (int)mip_lower, hi = min(lo, kMipLevels - 1) + 1;
+  const TexSlot sl = level_slot(sc, __ldg(lv + lo)), sh = level_slot(sc, __ldg(lv + hi));
+  f4 c1 = bilinear_pre<COLOUR>(sl, vtm.x * sl.width, vtm.y * sl.width);
+  f4 c2 = bilinear_pre<COLOUR>(sh, vtm.x * sh.width, vtm.y * sh.width);
   const float i255 = 1.0f / 255.0f;
   f4 r;
   if (COLOUR) {
@@ -936,9 +1021,18 @@ __device__ __forceinline__ int ssao_count(float d2, float t0, float t1, float t2
   return d2 > t2 ? (d2 > t4 ? 5 : (d2 > t3 ? 4 : 3)) : (d2 > t1 ? 2 : (d2 > t0 ? 1 : 0));
 }
 
+// A tap coordinate of generate_ssao: clamped to [1, n - 2] as the reference
+// does; for views 1 or 2 pixels wide (high), where that range is empty and the
+// reference reads outside its buffer, clamped into the view (0).
+__device__ __forceinline__ int ssao_coord(float v, int n) {
+  return max((int)clampf_(v, 1.0f, (float)n - 2.0f), 0);
+}
+
 // generate_ssao (cl2.cl:2194-2260).  The 25 taps share 5 rows and 5
-// columns, so their rounded and clamped offsets are computed once; the depth
-// thresholds dep + z are computed once; and the count (at most 125, exact in
+// columns, whose offsets round(k * world_rad), k = -2..2, are the same five
+// values: round is odd-symmetric (half away from zero) and 1 * r, 2 * r and
+// -r, -2 * r are exact, so two roundings give all of them.  The depth
+// thresholds dep + z are computed once, and the count (at most 125, exact in
 // float) is kept in an integer.  Far from the camera (world_rad < 0.25) every
 // offset rounds to 0 and all 25 taps read the same pixel; when that holds for
 // the whole warp, the pixel is read once and its count taken 25 times.
@@ -950,20 +1044,20 @@ __device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* __r
   float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
   float rad = kSsaoRad + foffset * 0.5f;  // foffset / 2, exact
   float world_rad = fdiv(rad * fov, dep);
-  int wx[5];
-#pragma unroll
-  for (int k = 0; k < 5; k++) wx[k] = (int)clampf_((float)x + roundf((float)(k - 2) * world_rad), 1.0f, (float)W - 2.0f);
   const float t0 = dep + -2.0f, t1 = dep + -1.0f, t3 = dep + 1.0f, t4 = dep + 2.0f;
   int acc = 0;
   if (__all_sync(__activemask(), world_rad < 0.25f)) {
-    const int wy = (int)clampf_((float)y, 1.0f, (float)H - 2.0f);
-    const float d2 = depth_to_dist(__ldg(depth + (size_t)wy * W + wx[2]));
+    const float d2 = depth_to_dist(__ldg(depth + (size_t)ssao_coord((float)y, H) * W + ssao_coord((float)x, W)));
     acc = 25 * ssao_count(d2, t0, t1, dep, t3, t4);
   } else {
+    const float r1 = roundf(world_rad), r2 = roundf(2.0f * world_rad), r0 = roundf(0.0f * world_rad);
+    const float off[5] = {-r2, -r1, r0, r1, r2};
+    int wx[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) wx[k] = ssao_coord((float)x + off[k], W);
 #pragma unroll 1
-    for (int yy = -2; yy <= 2; yy++) {
-      const int wy = (int)clampf_((float)y + roundf((float)yy * world_rad), 1.0f, (float)H - 2.0f);
-      const uint32_t* row = depth + (size_t)wy * W;
+    for (int k = 0; k < 5; k++) {
+      const uint32_t* row = depth + (size_t)ssao_coord((float)y + off[k], H) * W;
 #pragma unroll
       for (int xx = 0; xx < 5; xx++) {
         const float d2 = depth_to_dist(__ldg(row + wx[xx]));
@@ -1054,30 +1148,6 @@ __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a
 }
 
 
-// Barycentrics (cl2.cl:5372-5384) split into the per-triangle part and the
-// per-point part; bary_exact is barycentric() bit for bit.
-struct BaryFrame {
-  f3 a, v0, v1;
-  float d00, d01, d11, denom;
-};
-__device__ __forceinline__ BaryFrame bary_frame(f3 a, f3 b, f3 c) {
-  BaryFrame f;
-  f.a = a;
-  f.v0 = sub3(b, a);
-  f.v1 = sub3(c, a);
-  f.d00 = dot3(f.v0, f.v0);
-  f.d01 = dot3(f.v0, f.v1);
-  f.d11 = dot3(f.v1, f.v1);
-  f.denom = f.d00 * f.d11 - f.d01 * f.d01;
-  return f;
-}
-__device__ __forceinline__ void bary_exact(const BaryFrame& f, f3 p, float* u, float* v, float* w) {
-  f3 v2 = sub3(p, f.a);
-  float d20 = dot3(v2, f.v0), d21 = dot3(v2, f.v1);
-  *v = fdiv(f.d11 * d20 - f.d01 * d21, f.denom);
-  *w = fdiv(f.d00 * d21 - f.d01 * d20, f.denom);
-  *u = (1.0f - *v) - *w;
-}
 // Colour-only square root (approximate; exact IEEE result for 0, negative,
 // infinite and NaN inputs).
 __device__ __forceinline__ float csqrt(float x) {
@@ -1095,29 +1165,50 @@ __device__ __forceinline__ float c_gamma_fwd(float c) {
   return c * fma_(fma_(0.305306011f, c, 0.682171111f), c, 0.012522878f);
 }
 
-// A light as the shade loop reads it, staged once per CTA in shared memory;
-// col is already in linear space when the view renders linearly (the same
-// gamma_fwd every pixel would apply).
-struct SLight {
-  float px, py, pz, brightness;
-  float cr, cg, cb, radius;
-  float diffuse;
-  uint32_t shadow;
-  int32_t is_static;
-  float rradius;  // approximate 1 / radius, for the colour-only cutoff of unshadowed lights
-};
+// A light as the shade loop reads it, staged once per CTA in shared memory
+// as three float4: (pos, cut2), (colour, brightness), (radius, 1 / radius
+// approximated, diffuse, shadow | is_static << 1).  The colour is already in
+// linear space when the view renders linearly (the same gamma_fwd every pixel
+// would apply).  cut2 is a conservative squared distance beyond which a light
+// without shadows stays under kernel3's attenuation cutoff, so the pixel
+// skips it without computing the attenuation: brightness / (d / radius + 1)^2
+// <= 0.1 holds beyond d = radius * (sqrt(10 * brightness) - 1), and the
+// margins below cover the approximate colour-path arithmetic of that test
+// (relative errors of a few 1e-7).  -1: always under the cutoff; +inf: no
+// early test (shadow lights, whose cutoff decides the cubemap later shadow
+// lights read, and degenerate radii).
+constexpr int kLightQuads = 3;
+__device__ __forceinline__ void stage_light(const gbr_light* L, bool linear, float4* dst) {
+  f3 c = mk3(L->col[0], L->col[1], L->col[2]);
+  if (linear) c = mk3(gamma_fwd(c.x), gamma_fwd(c.y), gamma_fwd(c.z));
+  const float radius = L->radius, brightness = L->brightness;
+  const float b10 = 10.0f * brightness;
+  float cut2 = __int_as_float(0x7F800000);
+  if (!L->shadow && radius > 0.0f && b10 == b10) {
+    if (b10 <= 1.0f) {
+      cut2 = -1.0f;
+    } else {
+      const float rs = radius * ((sqrtf(b10) * 1.00001f - 1.0f) * 1.00001f);
+      cut2 = (rs * rs) * 1.00001f;
+    }
+  }
+  dst[0] = make_float4(L->pos[0], L->pos[1], L->pos[2], cut2);
+  dst[1] = make_float4(c.x, c.y, c.z, brightness);
+  dst[2] = make_float4(radius, crcp(radius), L->diffuse,
+                       __uint_as_float((L->shadow ? 1u : 0u) | (L->is_static ? 2u : 0u)));
+}
 
 // kernel3 (cl2.cl:5792-6408) for one pixel of a view.
 // ENABLE_NORMAL_MAPPING (cl2.cl:5987-6027): the tangent-space normal from the
 // object's normal map, in object space through the triangle's tangent frame,
 // then rotated into world space.  It feeds the shadow bias, so it keeps the
 // IEEE contract (normalize as fast_normalize).
-__device__ __forceinline__ f3 normal_map(const SceneDev& sc, f2 vt, f2 vtdiff, uint32_t rid, f3 p1, f3 p2, f3 p3,
+// dp1 = p2 - p1 and dp2 = p3 - p1 are the barycentric frame's edges.
+__device__ __forceinline__ f3 normal_map(const SceneDev& sc, f2 vt, f2 vtdiff, uint32_t rid, f3 dp1, f3 dp2,
                                       f2 vt1, f2 vt2, f2 vt3, f3 model_normal, f4 qn) {
   const f4 t4 = texture_filter_diff<false>(sc, vt, vtdiff, (int)rid);
   f3 tn = mk3(2.0f * t4.x - 1.0f, 2.0f * t4.y - 1.0f, 2.0f * t4.z - 1.0f);
   tn = fast_normalize3(tn);
-  const f3 dp1 = sub3(p2, p1), dp2 = sub3(p3, p1);
   const f2 duv1 = mk2(vt2.x - vt1.x, vt2.y - vt1.y), duv2 = mk2(vt3.x - vt1.x, vt3.y - vt1.y);
   const float r = fdiv(1.0f, duv1.x * duv2.y - duv1.y * duv2.x);
   f3 tangent = mk3((dp1.x * duv2.y - dp2.x * duv1.y) * r, (dp1.y * duv2.y - dp2.y * duv1.y) * r,
@@ -1166,13 +1257,13 @@ __device__ __forceinline__ f4 blend_texel(const uint8_t* __restrict__ rgba, size
 
 // colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
 // 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
-// FEAT: kernel3's optional switches (view flags) compiled in.
 // nrec: the records this pass wrote; the raster stores only indices below it
 // in the record map, and any other value is treated as an empty pixel, so no
 // index read from the map can leave the record arrays.
+// FEAT: kernel3's optional switches (view flags) compiled in.
 template <bool FEAT>
 __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
-                            const ShadeRec* __restrict__ srec, uint32_t nrec, const SLight* __restrict__ lights,
+                            const ShadeRec* __restrict__ srec, uint32_t nrec, const float4* __restrict__ lights,
                             int x, int y, const float* __restrict__ colx, const float* __restrict__ rowy) {
   const int W = S.width, H = S.height;
   const size_t p = (size_t)y * W + x;
@@ -1202,34 +1293,26 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   const f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
   const f3 cc = mk3(V.ccos[0], V.ccos[1], V.ccos[2]);
   const f3 cs = mk3(V.csin[0], V.csin[1], V.csin[2]);
-  const float4 q0 = __ldg(&srec[r].p0), q1 = __ldg(&srec[r].p1), q2 = __ldg(&srec[r].p2);
-  const f3 tp[3] = {mk3(q0.x, q0.y, q0.z), mk3(q1.x, q1.y, q1.z), mk3(q2.x, q2.y, q2.z)};
-  const float rconst = q0.w;
-  const uint32_t tri = __float_as_uint(q1.w);
-  // the triangle as 9 float4 loads: per vertex pos, normal, (vt, object_id, vertex_col)
-  const float4* tv = reinterpret_cast<const float4*>(sc.tris + tri);
-  const float4 va0 = __ldg(tv + 0), vb0 = __ldg(tv + 1), vc0v = __ldg(tv + 2);
-  const float4 va1 = __ldg(tv + 3), vb1 = __ldg(tv + 4), vc1v = __ldg(tv + 5);
-  const float4 va2 = __ldg(tv + 6), vb2 = __ldg(tv + 7), vc2v = __ldg(tv + 8);
-  const uint32_t o_id = __float_as_uint(vc0v.z);
-  const gbr_obj_g_descriptor* G = sc.descs + o_id;
-  const float scale = __ldg(&G->scale);
-  const f3 wpos = ld3(G->world_pos);
-  f4 qn, qi;  // rot_quat's and back_rot_quat's normalised quaternions
-  if (sc.objq) {
-    const float4 a = __ldg(sc.objq + 2 * o_id), b = __ldg(sc.objq + 2 * o_id + 1);
-    qn.x = a.x; qn.y = a.y; qn.z = a.z; qn.w = a.w;
-    qi.x = b.x; qi.y = b.y; qi.z = b.z; qi.w = b.w;
-  } else {
-    const f4 q = ld4(G->world_rot_quat);
-    qn = fast_normalize4(q);
-    qi = quat_inverse_n(q);
+  // the triangle's shade constants (prep_shade) and its object's terms
+  const ShadeRec* R = srec + r;
+  BaryFrame bf;
+  {
+    const float4 fa = __ldg(&R->a), f0 = __ldg(&R->e0), f1 = __ldg(&R->e1), fp = __ldg(&R->plane);
+    bf.a = mk3(fa.x, fa.y, fa.z);
+    bf.v0 = mk3(f0.x, f0.y, f0.z);
+    bf.v1 = mk3(f1.x, f1.y, f1.z);
+    bf.d00 = fa.w; bf.d01 = f0.w; bf.d11 = f1.w; bf.denom = fp.w;
   }
-  f3 p1 = mul3s(mk3(va0.x, va0.y, va0.z), scale), p2 = mul3s(mk3(va1.x, va1.y, va1.z), scale),
-     p3 = mul3s(mk3(va2.x, va2.y, va2.z), scale);
-  const BaryFrame bf = bary_frame(p1, p2, p3);
-  f2 vt1 = mk2(vc0v.x, vc0v.y), vt2 = mk2(vc1v.x, vc1v.y), vt3 = mk2(vc2v.x, vc2v.y);
-  f3 n1 = mk3(vb0.x, vb0.y, vb0.z), n2 = mk3(vb1.x, vb1.y, vb1.z), n3 = mk3(vb2.x, vb2.y, vb2.z);
+  const float4 fn1 = __ldg(&R->n1), fn2 = __ldg(&R->n2), fn3 = __ldg(&R->n3), ft = __ldg(&R->t);
+  const f2 vt1 = mk2(fn1.w, fn2.w), vt2 = mk2(fn3.w, ft.x), vt3 = mk2(ft.y, ft.z);
+  const uint32_t obits = __float_as_uint(ft.w);
+  const uint32_t o_id = obits & 0x7FFFFFFFu;
+  const float4* OQ = sc.objq + (size_t)o_id * kObjQuads;
+  const float4 oq0 = __ldg(OQ), oq1 = __ldg(OQ + 1), oq2 = __ldg(OQ + 2), oq3 = __ldg(OQ + 3);
+  f4 qn, qi;  // rot_quat's and back_rot_quat's normalised quaternions
+  qn.x = oq0.x; qn.y = oq0.y; qn.z = oq0.z; qn.w = oq0.w;
+  qi.x = oq1.x; qi.y = oq1.y; qi.z = oq1.z; qi.w = oq1.w;
+  const f3 wpos = mk3(oq2.x, oq2.y, oq2.z);
 
   const float ldepth = depth_to_dist(d);
   const float fx = (float)x, fy = (float)y;
@@ -1241,28 +1324,25 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   float l1, l2, l3;
   bary_exact(bf, olocal, &l1, &l2, &l3);
   f2 vt = mk2(fma_(vt1.x, l1, fma_(vt2.x, l2, vt3.x * l3)), fma_(vt1.y, l1, fma_(vt2.y, l2, vt3.y * l3)));
-  f3 normal = mk3(fma_(n1.x, l1, fma_(n2.x, l2, n3.x * l3)), fma_(n1.y, l1, fma_(n2.y, l2, n3.y * l3)),
-                  fma_(n1.z, l1, fma_(n2.z, l2, n3.z * l3)));
+  f3 normal = mk3(fma_(fn1.x, l1, fma_(fn2.x, l2, fn3.x * l3)), fma_(fn1.y, l1, fma_(fn2.y, l2, fn3.y * l3)),
+                  fma_(fn1.z, l1, fma_(fn2.z, l2, fn3.z * l3)));
   const f3 model_normal = normal;
   normal = rot_quat_n(normal, qn);
 
   f4 col;
-  const uint32_t vc0 = __float_as_uint(vc0v.w);
+  const float4 fcol = __ldg(&R->col);
+  const uint32_t vc0 = __float_as_uint(fcol.x);
   // normal map of the object (ENABLE_NORMAL_MAPPING), 0xFFFFFFFF if none
-  const uint32_t rid = (FEAT && (V.flags & GBR_VIEW_NORMAL_MAPPING)) ? __ldg(&G->rid) : 0xFFFFFFFFu;
+  const uint32_t rid = (FEAT && (V.flags & GBR_VIEW_NORMAL_MAPPING)) ? __ldg(&sc.descs[o_id].rid) : 0xFFFFFFFFu;
   f2 vtdiff = mk2(0.0f, 0.0f);
   if (vc0 == 0 || rid != 0xFFFFFFFFu) {
-    // get_vtdiff (cl2.cl:5691-5760).  The 1/z plane extrapolated to the
-    // neighbouring pixels is ill-conditioned for triangles seen edge-on (it
-    // can cross zero), so this stays in IEEE arithmetic: rounding differences
-    // there would pick other mip levels.
-    f3 xpv = mk3(roundf(tp[0].x), roundf(tp[1].x), roundf(tp[2].x));
-    f3 ypv = mk3(roundf(tp[0].y), roundf(tp[1].y), roundf(tp[2].y));
-    f3 depths = mk3(rcp(tp[0].z), rcp(tp[1].z), rcp(tp[2].z));
-    float DA, DB, DC;
-    plane_const(depths, xpv, ypv, rconst, &DA, &DB, &DC);
-    float dmx = fma_(DA, fx + 1.0f, fma_(DB, fy, DC));
-    float dmy = fma_(DA, fx, fma_(DB, fy + 1.0f, DC));
+    // get_vtdiff (cl2.cl:5691-5760), its 1/z plane from the shade constants.
+    // The plane extrapolated to the neighbouring pixels is ill-conditioned
+    // for triangles seen edge-on (it can cross zero), so this stays in IEEE
+    // arithmetic: rounding differences there would pick other mip levels.
+    const float4 fp = __ldg(&R->plane);
+    float dmx = fma_(fp.x, fx + 1.0f, fma_(fp.y, fy, fp.z));
+    float dmy = fma_(fp.x, fx, fma_(fp.y, fy + 1.0f, fp.z));
     const int lx = x & (kTile - 1), ly = y & (kTile - 1);
     f3 lmx = mk3(colx[lx + 1], rowy[ly], 1.0f);  // fdiv((fx + 1) - hw, fov), fdiv(fy - hh, fov)
     f3 lmy = mk3(colx[lx], rowy[ly + 1], 1.0f);  // fdiv(fx - hw, fov), fdiv((fy + 1) - hh, fov)
@@ -1282,15 +1362,15 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   // (the reference replaces the normal after its colour and jitter seeds,
   // neither of which reads it)
   if (FEAT && rid != 0xFFFFFFFFu)
-    normal = normal_map(sc, vt, vtdiff, rid, p1, p2, p3, vt1, vt2, vt3, model_normal, qn);
+    normal = normal_map(sc, vt, vtdiff, rid, bf.v0, bf.v1, vt1, vt2, vt3, model_normal, qn);
   if (vc0 != 0) {
-    f4 c0 = vertex_col(vc0), c1 = vertex_col(__float_as_uint(vc1v.w)), c2 = vertex_col(__float_as_uint(vc2v.w));
+    f4 c0 = vertex_col(vc0), c1 = vertex_col(__float_as_uint(fcol.y)), c2 = vertex_col(__float_as_uint(fcol.z));
     col.x = fma_(c0.x, l1, fma_(c1.x, l2, c2.x * l3));
     col.y = fma_(c0.y, l1, fma_(c1.y, l2, c2.y * l3));
     col.z = fma_(c0.z, l1, fma_(c1.z, l2, c2.z * l3));
     col.w = fma_(c0.w, l1, fma_(c1.w, l2, c2.w * l3));
   } else {
-    col = texture_filter_diff<true>(sc, vt, vtdiff, (int)__ldg(&G->tid));
+    col = texture_filter_diff<true>(sc, vt, vtdiff, (int)__float_as_uint(oq3.w));
   }
   if (V.use_linear) {
     col.x = c_gamma_fwd(col.x);
@@ -1303,16 +1383,16 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 rseed = mk3(((float)seed2 * kInvMulInt - 0.5f) * 2.0f, ((float)seed3 * kInvMulInt - 0.5f) * 2.0f,
                  ((float)seed4 * kInvMulInt - 0.5f) * 2.0f);
   const f3 l2p = cnormalize(sub3(cpos, gpos));
-  const int ff = __ldg(&G->feature_flag);
+  const int ff = (int)__float_as_uint(oq3.z);
   const bool two = (ff & kFlagTwoSided) > 0;
   const bool recv_dyn = !((ff & kFlagNoDynShadows) > 0);
-  if (!backface_front(tp[0], tp[1], tp[2]) && two) normal = neg3(normal);
+  if ((obits >> 31) && two) normal = neg3(normal);  // back-facing (cl2.cl:491-494)
   const float ssao = generate_ssao(x, y, seed2, S.depth, W, H, fov);
   normal = fast_normalize3(normal);
   const f3 lnormal = cnormalize(add3(normal, mk3(rseed.x * 0.01f, rseed.y * 0.01f, rseed.z * 0.01f)));
   const float ambient = V.use_linear ? gamma_fwd(kAmbient) : kAmbient;
-  const float g_diffuse = __ldg(&G->diffuse), g_spec_mult = __ldg(&G->spec_mult);
-  const float rough = clampf_(1.0f - __ldg(&G->specular), 0.001f, 10.0f);
+  const float g_diffuse = oq2.w, g_spec_mult = oq3.x;
+  const float rough = oq3.y;  // clamp(1 - specular, 0.001, 10)
   // per-pixel factors of the light loop (colour only)
   const float ndv = fmax_(0.0f, cdot3(normal, l2p));
   const float r_pndv = crcp(kPi * ndv);  // spec / (pi ndv)
@@ -1321,37 +1401,39 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   f3 dsum = mk3(0, 0, 0), ssum = mk3(0, 0, 0);
   int shnum = 0, static_num = 0;
   for (uint32_t i = 0; i < sc.nlights; i++) {
-    const SLight& L = lights[i];
-    const f3 lpos = mk3(L.px, L.py, L.pz);
-    const uint32_t lshadow = L.shadow;
-    const int lstatic = L.is_static;
+    const float4 LA = lights[kLightQuads * i];
+    const f3 lpos = mk3(LA.x, LA.y, LA.z);
     f3 ptl = sub3(lpos, gpos);
+    // The distance only feeds the colour, except through the cutoff below,
+    // which for a shadow light also decides which cubemap later shadow lights
+    // read (shnum): IEEE arithmetic for shadow lights (a warp-uniform branch),
+    // approximate otherwise, after the conservative early test.
+    const float d2 = dot3(ptl, ptl);
+    if (d2 > LA.w) continue;
+    const float4 LB = lights[kLightQuads * i + 1], LC = lights[kLightQuads * i + 2];
+    const uint32_t lflags = __float_as_uint(LC.w);
+    const bool lshadow = (lflags & 1u) != 0;
     float occlusion = 1.0f;
-    if (lshadow && lstatic) {
+    if (lflags == 3u) {  // shadow and is_static
       int face = ret_cubeface(gpos, lpos);
       occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
       static_num++;
     }
-    // The distance only feeds the colour, except through the cutoff below,
-    // which for a shadow light also decides which cubemap later shadow lights
-    // read (shnum): IEEE arithmetic for shadow lights (a warp-uniform branch),
-    // approximate otherwise.
-    const float d2 = dot3(ptl, ptl);
     const float rinv = rsqrtf(d2);
     float illum;
     if (lshadow) {
-      const float tt = fdiv(fsqrt(d2), L.radius) + 1.0f;
-      illum = fdiv(L.brightness, tt * tt);
+      const float tt = fdiv(fsqrt(d2), LC.x) + 1.0f;
+      illum = fdiv(LB.w, tt * tt);
     } else {
       const float distance = (d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
-      const float tt = fma_(distance, L.rradius, 1.0f);
-      illum = L.brightness * crcp(tt * tt);
+      const float tt = fma_(distance, LC.y, 1.0f);
+      illum = LB.w * crcp(tt * tt);
     }
     const float cutoff = 0.1f;
     illum -= cutoff;
     illum *= 1.0f / (1.0f - cutoff);
     if (illum <= 0) continue;
-    const f3 lcol = mk3(L.cr, L.cg, L.cb);
+    const f3 lcol = mk3(LB.x, LB.y, LB.z);
     if (lshadow && recv_dyn) {
       int face = ret_cubeface(gpos, lpos);
       float dyn = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_dyn, face, gpos, shnum);
@@ -1361,7 +1443,7 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
     ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
     // Lambert + ambient
     const float light = fmax_(cdot3(ptl, lnormal) * occlusion, 0.0f);
-    const float dscale = fma_(1.0f - ambient, light, ambient) * ((L.diffuse * g_diffuse) * illum);
+    const float dscale = fma_(1.0f - ambient, light, ambient) * ((LC.z * g_diffuse) * illum);
     dsum = mk3(fma_(lcol.x, dscale, dsum.x), fma_(lcol.y, dscale, dsum.y), fma_(lcol.z, dscale, dsum.z));
     // Cook-Torrance: F0 0.4, Gaussian microfacet 0.8346, geometric term
     const f3 Hv = cnormalize(add3(l2p, ptl));
@@ -1423,7 +1505,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   if (ctr->overflow) return;
   const uint32_t nrec = min(ctr->nrec, rec_cap);
   __shared__ uint32_t s_id;
-  __shared__ SLight slights[kMaxLights];
+  __shared__ float4 slights[kMaxLights * kLightQuads];
   __shared__ float colx[kTile + 1], rowy[kTile + 1];
   if (threadIdx.x < 32) {
     const uint32_t sid = find_surface_warp(surfs, nviews, blockIdx.x);
@@ -1431,21 +1513,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   }
   __syncthreads();
   const Surface& S = surfs[s_id];
-  for (uint32_t i = threadIdx.x; i < sc.nlights; i += blockDim.x) {
-    const gbr_light* L = sc.lights + i;
-    SLight l;
-    l.px = L->pos[0]; l.py = L->pos[1]; l.pz = L->pos[2];
-    l.brightness = L->brightness;
-    l.radius = L->radius;
-    l.diffuse = L->diffuse;
-    l.shadow = L->shadow;
-    l.is_static = L->is_static;
-    l.rradius = crcp(l.radius);
-    f3 c = mk3(L->col[0], L->col[1], L->col[2]);
-    if (views[s_id].use_linear) c = mk3(gamma_fwd(c.x), gamma_fwd(c.y), gamma_fwd(c.z));
-    l.cr = c.x; l.cg = c.y; l.cb = c.z;
-    slights[i] = l;
-  }
+  const bool linear = views[s_id].use_linear != 0;
+  for (uint32_t i = threadIdx.x; i < sc.nlights; i += blockDim.x)
+    stage_light(sc.lights + i, linear, slights + kLightQuads * i);
   const uint32_t lt = blockIdx.x - S.tile_base;
   const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
   if (threadIdx.x < 2 * (kTile + 1)) {
@@ -1616,7 +1686,14 @@ int num_sms() {
 
 cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st) {
   if (sc.ndescs) k_objects<<<(sc.ndescs + 255) / 256, 256, 0, st>>>(sc, objq);
-  if (sc.ntris) k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
+  if (sc.ntris && world) k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_texture_levels(const uint32_t* nums, const uint32_t* sizes, uint32_t mipmap_start, float4* texlv,
+                                  cudaStream_t st) {
+  const uint32_t n = mipmap_start * kTexLevels;
+  if (n) k_texture_levels<<<(n + 255) / 256, 256, 0, st>>>(nums, sizes, mipmap_start, texlv);
   return cudaGetLastError();
 }
 
@@ -1638,6 +1715,12 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
 
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st) {
   k_scan<<<1, kScanThreads, 0, st>>>(ws);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prep(const SceneDev& sc, const Workspace& ws, cudaStream_t st) {
+  if (!ws.srec) return cudaErrorInvalidValue;
+  k_prep<<<num_sms() * 4, 256, 0, st>>>(sc, ws);
   return cudaGetLastError();
 }
 
@@ -1667,6 +1750,7 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
                          uint32_t ntiles, const Workspace& ws, cudaStream_t st, bool features) {
   if (!ntiles) return cudaSuccess;
+  if (!sc.objq || !sc.texlv || !ws.srec) return cudaErrorInvalidValue;
   if (features)
     k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap);
   else

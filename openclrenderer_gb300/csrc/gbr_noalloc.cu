@@ -18,8 +18,10 @@
 //   view pixels   <= GBR_NOALLOC_MAX_PIXELS      (2,097,152, e.g. 1920x1080)
 //   records       <= GBR_NOALLOC_MAX_RECORDS     (131,072 visible clipped triangles)
 //   bin entries   <= GBR_NOALLOC_MAX_BIN_ENTRIES (524,288)
-// The array is about 25.3 MB (24.2 MiB) and every GPU that loads the library holds it
-// until the process exits.
+//   descriptors   <= GBR_NOALLOC_MAX_OBJECTS     (65,536; when shading)
+//   textures      <= GBR_NOALLOC_MAX_TEXTURES    (4,096 texture ids; when shading)
+// The array is about 42.4 MB (40.4 MiB) and every GPU that loads the library
+// holds it until the process exits.
 //
 // The array is shared by every call in the process on a device and keeps the
 // previous call's contents; the counters and tile counts that must start at
@@ -47,6 +49,8 @@ namespace {
 constexpr size_t kMaxPixels = GBR_NOALLOC_MAX_PIXELS;
 constexpr size_t kMaxRecords = GBR_NOALLOC_MAX_RECORDS;
 constexpr size_t kMaxBins = GBR_NOALLOC_MAX_BIN_ENTRIES;
+constexpr size_t kMaxObjects = GBR_NOALLOC_MAX_OBJECTS;
+constexpr size_t kMaxTextures = GBR_NOALLOC_MAX_TEXTURES;
 constexpr size_t kMaxFineTiles = 16384;
 constexpr size_t kMaxCoarseTiles = 1024;
 
@@ -64,7 +68,9 @@ constexpr size_t kOffRec = align256(kOffView + sizeof(ViewParams));
 constexpr size_t kOffSrec = align256(kOffRec + sizeof(RasterRec) * kMaxRecords);
 constexpr size_t kOffBins = align256(kOffSrec + sizeof(ShadeRec) * kMaxRecords);
 constexpr size_t kOffPix = align256(kOffBins + 4 * kMaxBins);
-constexpr size_t kScratchBytes = align256(kOffPix + 4 * kMaxPixels);
+constexpr size_t kOffObj = align256(kOffPix + 4 * kMaxPixels);
+constexpr size_t kOffTexLv = align256(kOffObj + sizeof(float4) * kObjQuads * kMaxObjects);
+constexpr size_t kScratchBytes = align256(kOffTexLv + sizeof(float4) * kTexLevels * kMaxTextures);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -128,6 +134,9 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
     return nfail(GBR_INVALID_ARG, "shading (rgba or normals) needs the texture atlas, nums, sizes and mipmap_start");
   if (sc->nlights && !sc->lights) return nfail(GBR_INVALID_ARG, "null lights");
   if (sc->nlights > (uint32_t)kMaxLights) return nfail(GBR_INVALID_ARG, "more than 256 lights");
+  if (shade && sc->ndescs > kMaxObjects) return nfail(GBR_INVALID_ARG, "more descriptors than GBR_NOALLOC_MAX_OBJECTS");
+  if (shade && sc->mipmap_start > kMaxTextures)
+    return nfail(GBR_INVALID_ARG, "more textures than GBR_NOALLOC_MAX_TEXTURES");
 
   Surface S{};
   S.width = view->width;
@@ -194,6 +203,9 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   d.mipmap_start = sc->mipmap_start;
   d.shadow_dyn = sc->shadow_dyn;
   d.shadow_static = sc->shadow_static;
+  // kernel3's object table and texture level table, built into the scratch
+  d.objq = reinterpret_cast<const float4*>(base + kOffObj);
+  d.texlv = reinterpret_cast<const float4*>(base + kOffTexLv);
   for (int f = 0; f < 6; f++) {
     f3 a = face_angles(f);
     float ang[3] = {a.x, a.y, a.z};
@@ -230,9 +242,18 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   NA_CU(cudaMemsetAsync(ws.ctr, 0, sizeof(Counters), s), "clear failed");
   NA_CU(cudaMemsetAsync(ws.fine_count, 0, 4 * (size_t)nfine, s), "clear failed");
   NA_CU(cudaMemsetAsync(ws.coarse_count, 0, 4 * (size_t)ncoarse, s), "clear failed");
+  if (shade) {
+    SceneDev obj = d;
+    obj.objq = nullptr;
+    obj.world = nullptr;
+    NA_CU(launch_world(obj, nullptr, reinterpret_cast<float4*>(base + kOffObj), s), "object table launch failed");
+    NA_CU(launch_texture_levels(sc->nums, sc->sizes, sc->mipmap_start, reinterpret_cast<float4*>(base + kOffTexLv), s),
+          "texture table launch failed");
+  }
   NA_CU(launch_setup_views(d, d_view, 1, d_surf, ws, s), "setup launch failed");
   NA_CU(launch_scan(ws, s), "scan launch failed");
   NA_CU(launch_fill(ws, d_surf, s), "fill launch failed");
+  if (shade) NA_CU(launch_prep(d, ws, s), "shade constants launch failed");
   NA_CU(launch_raster(ws, d_surf, 1, nfine, true, kRasterThreads, s), "raster launch failed");
   if (shade) NA_CU(launch_shade(d, d_view, 1, d_surf, nfine, ws, s, view->flags != 0), "shade launch failed");
   Counters c{};

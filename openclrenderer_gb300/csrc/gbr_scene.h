@@ -117,6 +117,13 @@ struct PassShape {
   bool features = false;            // views: some view has gbr_view.flags set
 };
 
+// A stream beside a pass's geometry stages, with the events that fork it
+// from them and join it back (launch_pass).
+struct SideStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+
 void euler_cs(const float ang[3], float c[3], float s[3]);
 
 }  // namespace gbr
@@ -129,7 +136,7 @@ struct gbr_scene {
   gbr::DevBuf<gbr_triangle> tris;
   uint32_t ntris = 0;
   gbr::DevBuf<float4> world;  // world-space vertices, 3 per triangle
-  gbr::DevBuf<float4> objq;   // per descriptor: normalised quaternion and normalised inverse
+  gbr::DevBuf<float4> objq;   // per descriptor: kernel3's object table (kObjQuads float4)
   bool world_dirty = true;    // triangles or descriptors changed since k_world ran
   gbr::DevBuf<gbr_obj_g_descriptor> descs;
   uint32_t ndescs = 0;
@@ -140,6 +147,7 @@ struct gbr_scene {
   std::vector<gbr_light> host_lights;
   gbr::DevBuf<uchar4> atlas;
   gbr::DevBuf<uint32_t> nums, sizes;
+  gbr::DevBuf<float4> texlv;  // texture level table (kTexLevels float4 per texture)
   std::vector<uint32_t> host_nums, host_sizes;
   uint32_t mipmap_start = 0;
   uint32_t npages = 0;
@@ -166,6 +174,7 @@ struct gbr_scene {
   // shadow pass), and shading waits for geom_done.
   cudaStream_t aux = nullptr;
   cudaEvent_t pre_shadow = nullptr, geom_done = nullptr;
+  gbr::SideStream side;  // the view pass's shade constants beside its raster
   bool pre_shadow_valid = false;  // pre_shadow marks the pending shadow pass's start
   bool overlap = true;
   bool view_shaded = true;  // the last view pass ran kernel3
@@ -189,6 +198,7 @@ struct gbr_scene {
     d.atlas = atlas.p;
     d.nums = nums.p;
     d.sizes = sizes.p;
+    d.texlv = texlv.p;
     d.mipmap_start = mipmap_start;
     d.shadow_dyn = shadow_dyn.p;
     d.shadow_static = shadow_static.p;
@@ -233,12 +243,18 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view);
 // Allocates nothing, so it can be captured into a graph.  ev, when not null,
 // holds the stage events (profiling): [0..4] around the geometry stages,
 // [5] after shading, [6] before shading.
+//
+// side (views that shade): the shade constants (launch_prep) run on
+// side.stream after the setup, forked by side.fork on geom, and shading
+// waits for side.join, so they overlap the scan, fill and raster; without a
+// side stream they run on geom after the raster.
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
                        Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom = nullptr,
-                       cudaEvent_t join = nullptr);
+                       cudaEvent_t join = nullptr, const SideStream* side = nullptr);
 // Kernel launches of one pass (for the launch statistics): views setup, scan,
-// fill, raster, shade; depth-only passes clear, setup, scan, fill, raster.
-inline uint32_t pass_kernels(bool view) { return view ? 5u : 5u; }
+// fill, shade constants, raster, shade (the last two only when shading);
+// depth-only passes clear, setup, scan, fill, raster.
+inline uint32_t pass_kernels(bool view, bool shade = true) { return view ? (shade ? 6u : 4u) : 5u; }
 // Timed stages of one pass (stage_ms): setup (a depth-only pass's clear
 // included), scan, fill, raster and, for views, shade.
 inline uint32_t pass_stages(bool view) { return view ? 5u : 4u; }

@@ -428,7 +428,10 @@ float generate_ssao(int x, int y, const uint32_t* depth, const ShadeView& v) {
       float wx = (float)x + ox, wy = (float)y + oy;
       wx = clampf_(wx, 1.0f, (float)v.W - 2.0f);
       wy = clampf_(wy, 1.0f, (float)v.H - 2.0f);
-      float d2 = depth_to_dist(depth[(size_t)((int)wy * v.W + (int)wx)]);
+      // views 1 or 2 pixels wide (high): [1, n - 2] is empty and the
+      // reference reads outside its buffer; pinned to the view's edge (0)
+      const int ix = std::max((int)wx, 0), iy = std::max((int)wy, 0);
+      float d2 = depth_to_dist(depth[(size_t)iy * v.W + ix]);
       for (float z = -samples; z <= samples; z += 1.0f)
         if (d2 > dep + z) acc += 1.0f;
     }
@@ -960,8 +963,8 @@ void kernel3_pixel_fp64(int x, int y, const ShadeView& v, const ShadeIn& in, con
     double acc = 0;
     for (int yy = -2; yy <= 2; yy++)
       for (int xx = -2; xx <= 2; xx++) {
-        int wx = (int)clampd(x + std::round(xx * wr), 1.0, W - 2.0);
-        int wy = (int)clampd(y + std::round(yy * wr), 1.0, H - 2.0);
+        int wx = std::max((int)clampd(x + std::round(xx * wr), 1.0, W - 2.0), 0);
+        int wy = std::max((int)clampd(y + std::round(yy * wr), 1.0, H - 2.0), 0);
         double d2 = depth_to_dist_d(depth[(size_t)wy * v.W + wx]);
         for (int z = -2; z <= 2; z++) acc += d2 > dep + z ? 1.0 : 0.0;
       }

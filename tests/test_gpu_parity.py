@@ -367,7 +367,7 @@ def test_depth_id_only_view_skips_shading():
     view = np.asarray(sc.views[0], S.VIEW).reshape(1)
     _native.check(gs.L.gbr_render_view(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(outs), _stream_ptr(None)))
     torch.cuda.synchronize()
-    assert gs.stats()["launches"] - before == 4  # setup, scan, fill, raster
+    assert gs.stats()["launches"] - before == 4  # setup, scan, fill, raster (no shade constants, no kernel3)
     got = o.numpy()
     assert np.array_equal(got["depth"], full["depth"]) and np.array_equal(got["id"], full["id"])
 
