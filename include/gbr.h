@@ -332,9 +332,26 @@ typedef struct gbr_tuning {
   int32_t coarse_tile;     /* coarse bin edge in pixels: 64, 128 or 256 */
   int32_t fine_max_tiles;  /* records touching more 16x16 tiles go to coarse bins: 1..256 */
   float scratch_headroom;  /* record / bin scratch kept, as a multiple of the need: 1.05..4 */
+  int32_t raster_shade;    /* how a view pass of several views that shade runs its raster and
+                              kernel3: GBR_RS_SEQUENTIAL, GBR_RS_FUSED or GBR_RS_PIPELINED;
+                              ignored by the shadow pass */
 } gbr_tuning;
 
-/* Defaults: 256 threads, 128-pixel coarse tiles, 16 fine tiles, 1.25. */
+/* raster_shade modes (results are the same in every mode):
+ *   SEQUENTIAL  one raster launch over every view, then one kernel3 launch;
+ *   FUSED       one persistent, cooperative launch that rasters and shades
+ *               tiles from a work queue, each view's shading once its raster
+ *               is complete (raster tiles of 128 or 256 threads; 512 runs as
+ *               256);
+ *   PIPELINED   the views in up to 8 groups of about equal tile counts: the
+ *               groups' rasters on one stream, their kernel3 launches on
+ *               another, each after its group's raster, so that one group's
+ *               shading overlaps the next groups' rasters. */
+#define GBR_RS_SEQUENTIAL 0
+#define GBR_RS_FUSED 1
+#define GBR_RS_PIPELINED 2
+
+/* Defaults: 256 threads, 128-pixel coarse tiles, 16 fine tiles, 1.25, pipelined. */
 gbr_status gbr_scene_set_tuning(gbr_scene* scene, int32_t pass, const gbr_tuning* t);
 gbr_status gbr_scene_get_tuning(gbr_scene* scene, int32_t pass, gbr_tuning* t);
 

@@ -87,6 +87,7 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view) {
   TRY(w.fine_off.reserve(sh.nfine));
   TRY(w.coarse_count.reserve(sh.ncoarse));
   TRY(w.coarse_off.reserve(sh.ncoarse));
+  TRY(w.scan_part.reserve(scan_chunks(sh.nfine)));
   TRY(w.ctr.reserve(1));
   if (view) TRY(w.pix_rec.reserve(sh.npix));
   return GBR_OK;
@@ -162,6 +163,76 @@ void shadow_layout(gbr_scene* s, bool with_static, int coarse_shift, std::vector
   sh.tiles_per_surface = surfs.empty() ? 0u : (uint32_t)(surfs[0].tiles_x * surfs[0].tiles_y);  // cube faces
 }
 
+uint32_t fused_schedule(const std::vector<Surface>& surfs, uint32_t lag, std::vector<uint32_t>& out) {
+  std::vector<uint32_t> start, info;
+  std::vector<uint64_t> after(surfs.size(), 0);
+  std::vector<uint32_t> pending;  // rasterised, not yet shaded, in order
+  size_t head = 0;
+  uint32_t item = 0;
+  auto tiles = [&](uint32_t v) { return (uint32_t)(surfs[v].tiles_x * surfs[v].tiles_y); };
+  auto shade = [&](uint32_t u) {
+    start.push_back(item);
+    info.push_back(u | 0x80000000u);
+    item += tiles(u);
+  };
+  for (uint32_t v = 0; v < (uint32_t)surfs.size(); v++) {
+    start.push_back(item);
+    info.push_back(v);
+    item += tiles(v);
+    for (size_t k = head; k < pending.size(); k++) after[pending[k]] += tiles(v);
+    pending.push_back(v);
+    while (head < pending.size() && after[pending[head]] >= lag) shade(pending[head++]);
+  }
+  while (head < pending.size()) shade(pending[head++]);
+  const uint32_t nseg = (uint32_t)info.size();
+  out.assign(start.begin(), start.end());
+  out.push_back(item);
+  out.insert(out.end(), info.begin(), info.end());
+  return nseg;
+}
+
+gbr_status plan_raster_shade(WorkMem& w, const std::vector<Surface>& surfs, const Tuning& tu, PassShape& sh,
+                             cudaStream_t st, bool sync_copy) {
+  sh.nseg = 0;
+  sh.ngroups = 0;
+  if (!sh.shade || surfs.size() < 2 || tu.raster_shade == GBR_RS_SEQUENTIAL) return GBR_OK;
+  if (tu.raster_shade == GBR_RS_PIPELINED) {
+    // consecutive views in groups of about total / G tiles each
+    uint64_t total = 0;
+    for (const Surface& S : surfs) total += (uint64_t)S.tiles_x * S.tiles_y;
+    const uint32_t G = (uint32_t)std::min<size_t>(kRsGroups, surfs.size());
+    uint64_t cum = 0;
+    uint32_t g = 0;
+    sh.group_tile[0] = 0;
+    for (size_t v = 0; v + 1 < surfs.size(); v++) {
+      cum += (uint64_t)surfs[v].tiles_x * surfs[v].tiles_y;
+      if (g + 1 < G && cum * G >= (uint64_t)(g + 1) * total) sh.group_tile[++g] = (uint32_t)cum;
+    }
+    sh.group_tile[g + 1] = (uint32_t)total;
+    sh.ngroups = g + 1 >= 2 ? g + 1 : 0;
+    return GBR_OK;
+  }
+  const int threads = tu.raster_threads == 128 ? 128 : 256;
+  const uint32_t grid = fused_blocks(threads, sh.features);
+  if (!grid) return GBR_OK;
+  std::vector<uint32_t> sched;
+  const uint32_t nseg = fused_schedule(surfs, grid, sched);
+  TRY(w.sched.reserve(sched.size()));
+  TRY(w.queue.reserve(2 + surfs.size()));
+  if (sync_copy)
+    CU(cudaMemcpy(w.sched.p, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice));
+  else
+    CU(cudaMemcpyAsync(w.sched.p, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice, st));
+  sh.nseg = nseg;
+  return GBR_OK;
+}
+
+gbr_status pass_wait_status(const Counters& c) {
+  if (c.overflow & 4u)
+    return fail(GBR_DEVICE_TIMEOUT, "a shade tile of the fused raster -> shade pass gave up waiting for its view's raster");
+  return GBR_OK;
+}
+
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   if (!s->world_dirty) return GBR_OK;
   TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
@@ -191,6 +262,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   ws.ncoarse = sh.ncoarse;
   ws.bins = wm.bins.p;
   ws.bin_cap = (uint32_t)std::min<size_t>(wm.bins.cap, 0xFFFFFFF0u);
+  ws.scan_part = wm.scan_part.p;
   ws.ctr = wm.ctr.p;
   ws.fine_max = tu.fine_max;
   ws.coarse_shift = tu.coarse_shift;
@@ -219,16 +291,45 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(mark(2, geom));
   CU(launch_fill(ws, wm.surf.p, geom));
   CU(mark(3, geom));
-  CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom, sh.tiles_per_surface));
-  CU(mark(4, geom));
-  if (view && s->mark_raster) CU(cudaEventRecord(s->raster_done, geom));
+  const bool fused = view && sh.shade && sh.nseg > 0;
+  const bool piped = !fused && view && sh.shade && sh.ngroups > 1 && split && on_side;
+  if (piped) {
+    // each group's raster, then its event: kernel3 of the group runs on st
+    // after it, beside the next groups' rasters
+    for (uint32_t g = 0; g < sh.ngroups; g++) {
+      CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.group_tile[g + 1] - sh.group_tile[g], true, tu.raster_threads,
+                       geom, 0, sh.group_tile[g]));
+      if (g + 1 == sh.ngroups) CU(mark(4, geom));
+      CU(cudaEventRecord(side->group[g], geom));
+    }
+  } else {
+    if (!fused)
+      CU(launch_raster(ws, wm.surf.p, sh.nsurf, sh.nfine, view, tu.raster_threads, geom, sh.tiles_per_surface));
+    CU(mark(4, geom));
+  }
+  if (view && s->mark_raster && !fused && !piped) CU(cudaEventRecord(s->raster_done, geom));
   if (prep && !on_side) CU(launch_prep(sd, ws, geom));
-  if (split) {
+  if (split && !piped) {
     CU(cudaEventRecord(join, geom));
     CU(cudaStreamWaitEvent(st, join, 0));
   }
   if (on_side) CU(cudaStreamWaitEvent(st, side->join, 0));
-  if (view && sh.shade) {
+  if (piped) {
+    CU(mark(6, st));
+    for (uint32_t g = 0; g < sh.ngroups; g++) {
+      CU(cudaStreamWaitEvent(st, side->group[g], 0));
+      CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.group_tile[g + 1] - sh.group_tile[g], ws, st,
+                      sh.features, sh.group_tile[g]));
+    }
+    CU(mark(5, st));
+  } else if (fused) {
+    // raster and shading in one persistent launch (its raster stage reads 0)
+    CU(cudaMemsetAsync(wm.queue.p, 0, sizeof(uint32_t) * (2 + sh.nsurf), st));
+    CU(mark(6, st));
+    CU(launch_raster_shade(sd, wm.views.p, wm.surf.p, sh.nsurf, ws, wm.sched.p, sh.nseg, wm.queue.p,
+                           tu.raster_threads, st, sh.features));
+    CU(mark(5, st));
+  } else if (view && sh.shade) {
     CU(mark(6, st));
     CU(launch_shade(sd, wm.views.p, sh.nitems, wm.surf.p, sh.nfine, ws, st, sh.features));
     CU(mark(5, st));
@@ -276,6 +377,8 @@ gbr_status ensure_side(gbr_scene* s) {
   if (!s->side.stream) CU(cudaStreamCreateWithFlags(&s->side.stream, cudaStreamNonBlocking));
   if (!s->side.fork) CU(cudaEventCreateWithFlags(&s->side.fork, cudaEventDisableTiming));
   if (!s->side.join) CU(cudaEventCreateWithFlags(&s->side.join, cudaEventDisableTiming));
+  for (cudaEvent_t& e : s->side.group)
+    if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   return GBR_OK;
 }
 
@@ -292,7 +395,7 @@ gbr_status enqueue_pass(gbr_scene* s, bool view, const PassShape& sh, cudaStream
   if (view) TRY(ensure_side(s));
   TRY(launch_pass(s, wm, s->tune[view ? GBR_PASS_VIEW : GBR_PASS_SHADOW], view, sh, counter_slot(s, view), ev, st,
                   geom, s->geom_done, view ? &s->side : nullptr));
-  s->stats.launches += pass_kernels(view, sh.shade);
+  s->stats.launches += pass_kernels(view, sh.shade, sh.nfine, &sh);
   if (view) s->view_shaded = sh.shade;
   return GBR_OK;
 }
@@ -374,10 +477,13 @@ gbr_status tuning_from_abi(const gbr_tuning* t, Tuning* out) {
     return fail(GBR_INVALID_ARG, "fine_max_tiles %d: must be in 1..256", t->fine_max_tiles);
   if (!(t->scratch_headroom >= 1.05f && t->scratch_headroom <= 4.0f))
     return fail(GBR_INVALID_ARG, "scratch_headroom %g: must be in 1.05..4", (double)t->scratch_headroom);
+  if (t->raster_shade < GBR_RS_SEQUENTIAL || t->raster_shade > GBR_RS_PIPELINED)
+    return fail(GBR_INVALID_ARG, "raster_shade %d: must be 0, 1 or 2", t->raster_shade);
   out->raster_threads = t->raster_threads;
   out->coarse_shift = shift;
   out->fine_max = t->fine_max_tiles;
   out->headroom = t->scratch_headroom;
+  out->raster_shade = t->raster_shade;
   return GBR_OK;
 }
 
@@ -386,6 +492,7 @@ void tuning_to_abi(const Tuning& t, gbr_tuning* out) {
   out->coarse_tile = kTile << t.coarse_shift;
   out->fine_max_tiles = t.fine_max;
   out->scratch_headroom = t.headroom;
+  out->raster_shade = t.raster_shade;
 }
 
 }  // namespace gbr
@@ -498,6 +605,9 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
     if (e) cudaEventDestroy(e);
   if (s->side.fork) cudaEventDestroy(s->side.fork);
   if (s->side.join) cudaEventDestroy(s->side.join);
+  for (cudaEvent_t e : s->side.group)
+    if (e) cudaEventDestroy(e);
+  if (s->pre_geom) cudaEventDestroy(s->pre_geom);
   if (s->side.stream) cudaStreamDestroy(s->side.stream);
   if (s->pre_shadow) cudaEventDestroy(s->pre_shadow);
   if (s->geom_done) cudaEventDestroy(s->geom_done);
@@ -819,10 +929,20 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   // stages run beside it on the aux stream, after the work queued before it.
   const bool overlap = s->overlap && s->shadow_pending && s->shadow_stream == st && s->pre_shadow_valid &&
                        !s->world_dirty;
+  // the pipelined raster / kernel3 mode runs the rasters on a stream of their own
+  bool any_shade = false;
+  for (uint32_t i = 0; i < n; i++) any_shade = any_shade || outs[i].rgba || outs[i].normals;
+  const bool piped = n >= 2 && any_shade && s->tune[GBR_PASS_VIEW].raster_shade == GBR_RS_PIPELINED && !s->world_dirty;
   cudaStream_t geom = st;
   if (overlap) {
     geom = s->aux;
     CU(cudaStreamWaitEvent(geom, s->pre_shadow, 0));
+  } else if (piped) {
+    TRY(ensure_aux(s));
+    if (!s->pre_geom) CU(cudaEventCreateWithFlags(&s->pre_geom, cudaEventDisableTiming));
+    CU(cudaEventRecord(s->pre_geom, st));
+    geom = s->aux;
+    CU(cudaStreamWaitEvent(geom, s->pre_geom, 0));
   }
   CU(cudaMemcpyAsync(wm.surf.p, surfs.data(), n * sizeof(Surface), cudaMemcpyHostToDevice, geom));
   CU(cudaMemcpyAsync(wm.views.p, vp.data(), n * sizeof(ViewParams), cudaMemcpyHostToDevice, geom));
@@ -836,12 +956,14 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
     if (outs[i].rgba || outs[i].normals) sh.shade = true;
     if (views[i].flags || vp[i].blend_depth) sh.features = true;
   }
+  TRY(plan_raster_shade(wm, surfs, s->tune[GBR_PASS_VIEW], sh, geom, false));
   for (int attempt = 0; attempt < 8; attempt++) {
     TRY(enqueue_pass(s, true, sh, st, attempt == 0 ? geom : st));
     if (after_enqueue) TRY((*after_enqueue)());
     CU(cudaStreamSynchronize(st));
     bool rerun = false;
     TRY(settle_shadow(s, true, &rerun));  // same stream: already complete
+    TRY(pass_wait_status(*counter_slot(s, true)));
     bool fit = check_pass(s, true);
     if (fit && !rerun) return GBR_OK;
   }

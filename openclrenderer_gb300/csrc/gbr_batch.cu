@@ -108,6 +108,7 @@ gbr_status capture(gbr_batch* b) {
   TRY(b->wv.surf.reserve(b->n));
   TRY(b->wv.views.reserve(b->n));
   CU(cudaMemcpy(b->wv.surf.p, vs.data(), b->n * sizeof(Surface), cudaMemcpyHostToDevice));
+  TRY(plan_raster_shade(b->wv, vs, b->tune[GBR_PASS_VIEW], b->vshape, b->cap_stream, true));
   // shadow faces
   bool shadow = false;
   if (b->with_shadow()) {
@@ -177,7 +178,8 @@ gbr_status launch_graph(gbr_batch* b, const gbr_camera* cams, cudaStream_t st) {
   CU(cudaGraphLaunch(b->exec, st));
   CU(cudaEventRecord(b->done, st));
   b->launches++;
-  b->s->stats.launches += pass_kernels(true, b->vshape.shade) + (b->sshape.nitems ? pass_kernels(false) : 0u);
+  b->s->stats.launches += pass_kernels(true, b->vshape.shade, b->vshape.nfine, &b->vshape) +
+                          (b->sshape.nitems ? pass_kernels(false, false, b->sshape.nfine) : 0u);
   b->in_flight = true;
   b->last_stream = st;
   return GBR_OK;
@@ -203,6 +205,7 @@ gbr_status wait_frame(gbr_batch* b) {
   for (int attempt = 0; attempt < 8; attempt++) {
     CU(cudaEventSynchronize(b->done));
     b->in_flight = false;
+    TRY(pass_wait_status(*b->view_ctr()));
     bool fit = true;
     if (b->sshape.nitems)
       fit = absorb_counters(b->s, *b->shadow_ctr(), b->wsh, b->tune[GBR_PASS_SHADOW].headroom, false) && fit;
@@ -263,6 +266,8 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side.stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming);
+  for (cudaEvent_t& ge : b->side.group)
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ge, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     gbr_batch_destroy(b);
     return fail(GBR_CUDA_ERROR, "stream / event creation failed: %s", cudaGetErrorString(e));
@@ -380,14 +385,18 @@ gbr_status gbr_batch_autotune(gbr_batch* b, const gbr_camera* cams, void* stream
     for (int pass : passes) {
       if (pass == GBR_PASS_SHADOW && !b->sshape.nitems) continue;
       Tuning& tu = b->tune[pass];
-      // coordinate descent: each axis in turn, keeping the best value
-      for (int axis = 0; axis < 3; axis++) {
-        const int cand[3][3] = {{256, 128, 512}, {3, 2, 4}, {16, 4, 64}};
-        int* field = axis == 0 ? &tu.raster_threads : axis == 1 ? &tu.coarse_shift : &tu.fine_max;
+      // coordinate descent: each axis in turn, keeping the best value; the
+      // view pass also tries the three raster / kernel3 modes
+      const int naxes = pass == GBR_PASS_VIEW ? 4 : 3;
+      for (int axis = 0; axis < naxes; axis++) {
+        const int cand[4][3] = {{256, 128, 512}, {3, 2, 4}, {16, 4, 64},
+                                {GBR_RS_PIPELINED, GBR_RS_SEQUENTIAL, GBR_RS_FUSED}};
+        int* field = axis == 0 ? &tu.raster_threads : axis == 1 ? &tu.coarse_shift : axis == 2 ? &tu.fine_max
+                                                                                                 : &tu.raster_shade;
         const int keep = *field;
         int pick = keep;
         for (int v : cand[axis]) {
-          if (v == keep) continue;
+          if (v == keep || v < 0) continue;
           *field = v;
           float ms = 0.f;
           TRY(measure(&ms));
@@ -452,6 +461,8 @@ gbr_status gbr_batch_destroy(gbr_batch* b) {
   if (b->cap_aux) cudaStreamDestroy(b->cap_aux);
   if (b->side.fork) cudaEventDestroy(b->side.fork);
   if (b->side.join) cudaEventDestroy(b->side.join);
+  for (cudaEvent_t ge : b->side.group)
+    if (ge) cudaEventDestroy(ge);
   if (b->side.stream) cudaStreamDestroy(b->side.stream);
   delete b;
   return GBR_OK;

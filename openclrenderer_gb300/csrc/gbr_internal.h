@@ -112,7 +112,7 @@ struct ShadowJob {
 struct Counters {
   unsigned long long frag_ref;  // sum of ceil(area / chunk): the reference's work items
   uint32_t nrec;                // records requested
-  uint32_t overflow;            // bit 0 records, bit 1 bins
+  uint32_t overflow;            // bit 0 records, bit 1 bins, bit 2 a bounded wait gave up (fused pass)
   uint32_t fine_total, coarse_total;
   unsigned long long samples;   // covered pixel-samples (point_in_tri passes) of the depth pass
 };
@@ -152,6 +152,7 @@ struct Tuning {
   int32_t coarse_shift = kCoarseShift;      // 2, 3 or 4 (64, 128, 256 pixels)
   int32_t fine_max = kFineMaxTiles;         // 1..256
   float headroom = 1.25f;                   // 1.05..4
+  int32_t raster_shade = GBR_RS_PIPELINED;  // views of several surfaces: GBR_RS_*
 };
 
 struct Workspace {
@@ -166,6 +167,7 @@ struct Workspace {
   uint32_t ncoarse;
   uint32_t* bins;
   uint32_t bin_cap;
+  uint32_t* scan_part;  // per chunk of fine counts (scan_chunks), or null: one-block scan
   Counters* ctr;
   int32_t fine_max;      // Tuning::fine_max
   int32_t coarse_shift;  // Tuning::coarse_shift
@@ -178,7 +180,10 @@ cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, ui
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,
                                 const Surface* d_surf, const Workspace& ws, cudaStream_t st);
+// One block when the fine counts fit one chunk (or scan_part is null), else
+// scan_chunks(nfine) blocks in two kernels.
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
+uint32_t scan_chunks(uint32_t nfine);
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
 // Views that shade: every record's setup output becomes its shade constants
 // (prep_shade).  Needs the setup done; kernel3 needs it done.
@@ -189,14 +194,24 @@ cudaError_t launch_texture_levels(const uint32_t* nums, const uint32_t* sizes, u
                                   float4* texlv, cudaStream_t st);
 // tiles_per_surface: the common tile count when every surface has the same
 // size (cube faces), else 0.
+// tile0: the first tile of the launch (ntiles tiles from there).
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf,
                           uint32_t ntiles, bool with_id, int threads, cudaStream_t st,
-                          uint32_t tiles_per_surface = 0);
+                          uint32_t tiles_per_surface = 0, uint32_t tile0 = 0);
 // features: some view has kernel3's optional switches on (gbr_view.flags).
 // Reads the pass's counters: nothing is shaded after an overflow.
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                          const Surface* d_surf, uint32_t ntiles, const Workspace& ws,
-                         cudaStream_t st, bool features = false);
+                         cudaStream_t st, bool features = false, uint32_t tile0 = 0);
+// The fused raster -> shade pass of many views: one cooperative persistent
+// launch over the work order sched (nseg segments, see k_raster_shade) with
+// the queue words (2 + views, zeroed before); raster tiles of threads (128 or
+// 256) threads.  A bounded wait that gave up sets bit 2 of the overflow word.
+cudaError_t launch_raster_shade(const SceneDev& sc, const ViewParams* d_views, const Surface* d_surf, uint32_t nsurf,
+                                const Workspace& ws, const uint32_t* sched, uint32_t nseg, uint32_t* queue,
+                                int threads, cudaStream_t st, bool features);
+// Blocks of that launch (all resident at once).
+uint32_t fused_blocks(int threads, bool features);
 cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,
                                   const uint8_t* pixels, const uint64_t* offsets,
                                   const int32_t* tsizes, uint32_t ntex, int32_t max_size,

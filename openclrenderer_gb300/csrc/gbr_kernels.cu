@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "gbr_internal.h"
 
 namespace gbr {
@@ -596,6 +598,42 @@ __global__ void __launch_bounds__(256, 4) k_prep(SceneDev sc, Workspace ws) {
     prep_shade(sc, ws.srec + r);
 }
 
+// Many tiles (batches of views): the fine counts are scanned in chunks of
+// kScanChunk, one block each, into offsets relative to the chunk, with each
+// chunk's total in scan_part; one more block scans the coarse counts whole.
+// k_scan_add then adds the totals of the chunks before each chunk.
+__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Workspace ws, uint32_t nchunks) {
+  __shared__ uint32_t sh[kScanChunk];
+  __shared__ uint32_t swarp[32];
+  __shared__ uint32_t sctot;
+  if (blockIdx.x == nchunks) {
+    block_scan_array(ws.coarse_count, ws.coarse_off, ws.ncoarse, &ws.ctr->coarse_total, sh, swarp, &sctot);
+    return;
+  }
+  const uint32_t c0 = blockIdx.x * (uint32_t)kScanChunk;
+  const uint32_t m = min((uint32_t)kScanChunk, ws.nfine - c0);
+  block_scan_array(ws.fine_count + c0, ws.fine_off + c0, m, ws.scan_part + blockIdx.x, sh, swarp, &sctot);
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_add(Workspace ws, uint32_t nchunks) {
+  __shared__ uint32_t base;
+  if (threadIdx.x < 32) {
+    uint32_t sum = 0;
+    for (uint32_t i = threadIdx.x; i < blockIdx.x; i += 32) sum += ws.scan_part[i];
+    sum = __reduce_add_sync(0xFFFFFFFFu, sum);
+    if (threadIdx.x == 0) base = sum;
+  }
+  __syncthreads();
+  const uint32_t c0 = blockIdx.x * (uint32_t)kScanChunk;
+  const uint32_t m = min((uint32_t)kScanChunk, ws.nfine - c0);
+  for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) ws.fine_off[c0 + i] += base;
+  if (blockIdx.x == nchunks - 1 && threadIdx.x == 0) {
+    const uint32_t total = base + ws.scan_part[blockIdx.x];
+    ws.ctr->fine_total = total;
+    if ((uint64_t)total + ws.ctr->coarse_total > ws.bin_cap) ws.ctr->overflow |= 2u;
+  }
+}
+
 // Scatter record indices into their tile bins (cursor atomics aggregated
 // across the warp).
 __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __restrict__ surfs) {
@@ -702,31 +740,46 @@ __device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp
 }
 
 
+// Shared memory of one tile's raster (NT threads).
+template <int NT>
+struct RasterSmem {
+  float4 srec[NT][4];
+  uint32_t sidx[NT];
+  uint32_t soff[NT + 1];
+  uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
+  uint32_t sdepth[kTilePixels];
+  unsigned long long sid[kTilePixels];
+  uint32_t swarp[NT / 32];
+  uint32_t sscan;
+  uint32_t ssamples;
+  Surface S;
+  uint32_t lists[4];
+};
+
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
-// (views) or only the depth (cube faces).
+// (views) or only the depth (cube faces).  surface: the tile's surface when
+// the caller knows it, else -1 (binary search).  Every thread of the block
+// calls it; the caller synchronises before reusing the shared memory.
 template <int NT, bool ID>
-__global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
-                                                          uint32_t nsurf) {
+__device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* __restrict__ surfs, uint32_t nsurf,
+                                            uint32_t tile, int surface, RasterSmem<NT>& sm) {
   constexpr bool with_id = ID;
   constexpr int NW = NT / 32;
   constexpr uint32_t kCountShift = 18;  // scan word: pixels (< 2^18) | records << 18
-  __shared__ float4 srec[NT][4];
-  __shared__ uint32_t sidx[NT];
-  __shared__ uint32_t soff[NT + 1];
-  __shared__ uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
-  __shared__ uint32_t sdepth[kTilePixels];
-  __shared__ unsigned long long sid[kTilePixels];
-  __shared__ uint32_t swarp[NW];
-  __shared__ uint32_t sscan;
-  __shared__ uint32_t ssamples;
-  __shared__ Surface S;
-  __shared__ uint32_t lists[4];
-  // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
-  const uint32_t tile = gridDim.y > 1 ? surfs[blockIdx.y].tile_base + blockIdx.x : blockIdx.x;
+  float4 (&srec)[NT][4] = sm.srec;
+  uint32_t* sidx = sm.sidx;
+  uint32_t* soff = sm.soff;
+  uint32_t* sgeo = sm.sgeo;
+  uint32_t* sdepth = sm.sdepth;
+  unsigned long long* sid = sm.sid;
+  uint32_t* swarp = sm.swarp;
+  uint32_t& sscan = sm.sscan;
+  uint32_t& ssamples = sm.ssamples;
+  Surface& S = sm.S;
+  uint32_t* lists = sm.lists;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (ws.ctr->overflow) return;
   if (tid == 0) {
-    const uint32_t s = gridDim.y > 1 ? blockIdx.y : find_surface(surfs, nsurf, tile);
+    const uint32_t s = surface >= 0 ? (uint32_t)surface : find_surface(surfs, nsurf, tile);
     S = surfs[s];
     uint32_t lt = tile - S.tile_base;
     int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
@@ -746,6 +799,18 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
   __syncthreads();
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
+  if (with_id && lists[1] + lists[3] == 0) {  // no records: an empty tile
+    for (int lp = tid; lp < kTilePixels; lp += NT) {
+      const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
+      if (px < S.width && py < S.height) {
+        const size_t p = (size_t)py * S.width + px;
+        S.depth[p] = kDepthClear;
+        if (S.id) S.id[p] = kNoId;
+        S.rec[p] = kNoId;
+      }
+    }
+    return;
+  }
   if (!with_id) {
     // depth-only passes: the surface was cleared and holds the small
     // triangles the setup rasterised; a tile without records keeps it as is
@@ -909,6 +974,16 @@ __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspac
   }
 }
 
+template <int NT, bool ID>
+__global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
+                                                          uint32_t nsurf, uint32_t tile0) {
+  __shared__ RasterSmem<NT> sm;
+  if (ws.ctr->overflow) return;
+  // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
+  const uint32_t tile = gridDim.y > 1 ? surfs[blockIdx.y].tile_base + blockIdx.x : tile0 + blockIdx.x;
+  raster_tile<NT, ID>(ws, surfs, nsurf, tile, gridDim.y > 1 ? (int)blockIdx.y : -1, sm);
+}
+
 // ---- kernel3 ------------------------------------------------------------------
 struct ShadeCtx {
   SceneDev sc;
@@ -1038,16 +1113,17 @@ __device__ __forceinline__ int ssao_coord(float v, int n) {
 // the whole warp, the pixel is read once and its count taken 25 times.
 // seed2 = rand_xorshift(wang_hash(x + W*H*y)), the pixel's first random
 // number, which kernel3's normal jitter also draws.
-__device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* __restrict__ depth, int W, int H,
-                               float fov) {
+// depth is read with plain (coherent) loads: in the fused pass other blocks
+// wrote it during the same launch.
+__device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* depth, int W, int H, float fov) {
   float foffset = (float)seed2 * kInvMulInt;
-  float dep = depth_to_dist(__ldg(depth + (size_t)y * W + x));
+  float dep = depth_to_dist(__ldca(depth + (size_t)y * W + x));
   float rad = kSsaoRad + foffset * 0.5f;  // foffset / 2, exact
   float world_rad = fdiv(rad * fov, dep);
   const float t0 = dep + -2.0f, t1 = dep + -1.0f, t3 = dep + 1.0f, t4 = dep + 2.0f;
   int acc = 0;
   if (__all_sync(__activemask(), world_rad < 0.25f)) {
-    const float d2 = depth_to_dist(__ldg(depth + (size_t)ssao_coord((float)y, H) * W + ssao_coord((float)x, W)));
+    const float d2 = depth_to_dist(__ldca(depth + (size_t)ssao_coord((float)y, H) * W + ssao_coord((float)x, W)));
     acc = 25 * ssao_count(d2, t0, t1, dep, t3, t4);
   } else {
     const float r1 = roundf(world_rad), r2 = roundf(2.0f * world_rad), r0 = roundf(0.0f * world_rad);
@@ -1060,7 +1136,7 @@ __device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* __r
       const uint32_t* row = depth + (size_t)ssao_coord((float)y + off[k], H) * W;
 #pragma unroll
       for (int xx = 0; xx < 5; xx++) {
-        const float d2 = depth_to_dist(__ldg(row + wx[xx]));
+        const float d2 = depth_to_dist(__ldca(row + wx[xx]));
         acc += ssao_count(d2, t0, t1, dep, t3, t4);
       }
     }
@@ -1227,19 +1303,19 @@ __device__ __forceinline__ f3 normal_map(const SceneDev& sc, f2 vt, f2 vtdiff, u
 
 // generate_outline (cl2.cl:2315-2362): the largest depth step to the four
 // neighbours, over 100, at most 1.
-__device__ __forceinline__ float generate_outline(int x, int y, const uint32_t* __restrict__ depth, int W, int H) {
-  const float d0 = depth_to_dist(__ldg(depth + (size_t)y * W + x));
+__device__ __forceinline__ float generate_outline(int x, int y, const uint32_t* depth, int W, int H) {
+  const float d0 = depth_to_dist(__ldca(depth + (size_t)y * W + x));
   float furthest = d0;
   for (int xx = -1; xx <= 1; xx++) {
     const int px = x + xx;
     if (px < 0 || px >= W) continue;
-    const float nd = depth_to_dist(__ldg(depth + (size_t)y * W + px));
+    const float nd = depth_to_dist(__ldca(depth + (size_t)y * W + px));
     if (nd > furthest) furthest = nd;
   }
   for (int yy = -1; yy <= 1; yy++) {
     const int py = y + yy;
     if (py < 0 || py >= H) continue;
-    const uint32_t d = __ldg(depth + (size_t)py * W + x);
+    const uint32_t d = __ldca(depth + (size_t)py * W + x);
     const float nd = depth_to_dist(d);
     if (fabsf(nd - d0) > fabsf(furthest - d0) && nd > kDepthCutoff && d != 0) furthest = nd;
   }
@@ -1494,6 +1570,45 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
+// Shared memory of one tile's shading.
+struct ShadeSmem {
+  float4 lights[kMaxLights * kLightQuads];
+  float colx[kTile + 1], rowy[kTile + 1];
+};
+
+// kernel3 over one 16x16 tile of view surface `sid` (NT threads, 256 / NT
+// pixels each).  Every thread of the block calls it; the caller synchronises
+// before reusing the shared memory.
+template <bool FEAT, int NT>
+__device__ __forceinline__ void shade_tile(const SceneDev& sc, const ViewParams* __restrict__ views,
+                                           const Surface* __restrict__ surfs, const ShadeRec* __restrict__ srec,
+                                           uint32_t nrec, uint32_t tile, uint32_t sid, ShadeSmem& sm) {
+  const Surface& S = surfs[sid];
+  const ViewParams& V = views[sid];
+  const uint32_t lt = tile - S.tile_base;
+  const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
+  const bool linear = V.use_linear != 0;
+  for (uint32_t i = threadIdx.x; i < sc.nlights; i += NT) stage_light(sc.lights + i, linear, sm.lights + kLightQuads * i);
+  if (threadIdx.x < 2 * (kTile + 1)) {
+    const int i = threadIdx.x % (kTile + 1);
+    if (threadIdx.x <= kTile)
+      sm.colx[i] = fdiv((float)(x0 + i) - (float)S.width / 2.0f, V.fov);
+    else
+      sm.rowy[i] = fdiv((float)(y0 + i) - (float)S.height / 2.0f, V.fov);
+  }
+  __syncthreads();
+  if (NT == kTilePixels) {  // one pixel per thread
+    const int x = x0 + (threadIdx.x & (kTile - 1)), y = y0 + threadIdx.x / kTile;
+    if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, V, S, srec, nrec, sm.lights, x, y, sm.colx, sm.rowy);
+    return;
+  }
+#pragma unroll 1
+  for (int lp = threadIdx.x; lp < kTilePixels; lp += NT) {
+    const int x = x0 + (lp & (kTile - 1)), y = y0 + lp / kTile;
+    if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, V, S, srec, nrec, sm.lights, x, y, sm.colx, sm.rowy);
+  }
+}
+
 // A pass whose setup or binning overflowed its scratch leaves the depth and
 // record map unwritten (the raster returns at once); shading returns too, and
 // the host re-runs the pass with grown scratch.
@@ -1501,35 +1616,101 @@ template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec, const Counters* __restrict__ ctr,
-                                               uint32_t rec_cap) {
+                                               uint32_t rec_cap, uint32_t tile0) {
+  __shared__ ShadeSmem sm;
+  __shared__ uint32_t s_id;
   if (ctr->overflow) return;
   const uint32_t nrec = min(ctr->nrec, rec_cap);
-  __shared__ uint32_t s_id;
-  __shared__ float4 slights[kMaxLights * kLightQuads];
-  __shared__ float colx[kTile + 1], rowy[kTile + 1];
+  const uint32_t tile = tile0 + blockIdx.x;
   if (threadIdx.x < 32) {
-    const uint32_t sid = find_surface_warp(surfs, nviews, blockIdx.x);
+    const uint32_t sid = find_surface_warp(surfs, nviews, tile);
     if (threadIdx.x == 0) s_id = sid;
   }
   __syncthreads();
-  const Surface& S = surfs[s_id];
-  const bool linear = views[s_id].use_linear != 0;
-  for (uint32_t i = threadIdx.x; i < sc.nlights; i += blockDim.x)
-    stage_light(sc.lights + i, linear, slights + kLightQuads * i);
-  const uint32_t lt = blockIdx.x - S.tile_base;
-  const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
-  if (threadIdx.x < 2 * (kTile + 1)) {
-    const int i = threadIdx.x % (kTile + 1);
-    const float fov = views[s_id].fov;
-    if (threadIdx.x <= kTile)
-      colx[i] = fdiv((float)(x0 + i) - (float)S.width / 2.0f, fov);
-    else
-      rowy[i] = fdiv((float)(y0 + i) - (float)S.height / 2.0f, fov);
-  }
+  shade_tile<FEAT, 256>(sc, views, surfs, srec, nrec, tile, s_id, sm);
+}
+
+// ---- the fused raster -> shade pass of many views ------------------------------
+// One persistent, cooperative launch (every block resident) takes the pass's
+// tiles from a work queue: each view's raster tiles (kernel1 + kernel2), and
+// each view's shade tiles (kernel3), which the host orders after at least a
+// grid's worth of later views' raster tiles.  kernel3's SSAO reads depth
+// anywhere in its view (its tap offsets grow as the depth shrinks), so a
+// shade tile waits until every raster tile of its view is done: a per-view
+// counter, polled with a bounded wait.  Every item depends only on items
+// taken before it, so the waits always end; a wait that reaches its limit
+// anyway sets bit 2 of the pass's overflow word and leaves that tile
+// unshaded (the host reports GBR_DEVICE_TIMEOUT).  One view's shading thus
+// overlaps later views' rasters: the raster waits on block barriers, the
+// shading is bound by instruction issue.
+//
+// queue: [0] next item, [1] unused, [2 + v] raster tiles done of view v
+// (zeroed by the host before the launch).  sched: seg_start[nseg + 1] (first
+// item of each segment; seg_start[nseg] = item count), then seg_view[nseg]
+// (view | 1 << 31 for shade segments).
+constexpr uint32_t kWaitPolls = 1u << 22;  // with ~0.25 us sleeps: about a second
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+template <int NT, bool FEAT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_raster_shade(Workspace ws, const Surface* __restrict__ surfs,
+                                                                uint32_t nsurf, SceneDev sc,
+                                                                const ViewParams* __restrict__ views,
+                                                                const uint32_t* __restrict__ sched, uint32_t nseg,
+                                                                uint32_t* __restrict__ queue) {
+  union Smem {
+    RasterSmem<NT> r;
+    ShadeSmem s;
+  };
+  __shared__ Smem sm;
+  __shared__ uint32_t s_item[2];
+  __shared__ int s_ok;
+  if (ws.ctr->overflow) return;
+  const uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
+  const uint32_t total = __ldg(sched + nseg);
+  if (threadIdx.x == 0) s_item[0] = atomicAdd(&queue[0], 1u);
   __syncthreads();
-  const int x = x0 + (threadIdx.x & (kTile - 1));
-  const int y = y0 + (threadIdx.x / kTile);
-  if (x < S.width && y < S.height) shade_pixel<FEAT>(sc, views[s_id], S, srec, nrec, slights, x, y, colx, rowy);
+#pragma unroll 1
+  for (int cur = 0;; cur ^= 1) {
+    const uint32_t item = s_item[cur];
+    if (item >= total) break;
+    if (threadIdx.x == 0) s_item[cur ^ 1] = atomicAdd(&queue[0], 1u);  // the next item, taken early
+    int seg = 0, hi = (int)nseg - 1;
+    while (seg < hi) {
+      const int mid = (seg + hi + 1) >> 1;
+      if (__ldg(sched + mid) <= item) seg = mid; else hi = mid - 1;
+    }
+    const uint32_t info = __ldg(sched + nseg + 1 + seg);
+    const uint32_t v = info & 0x7FFFFFFFu;
+    const uint32_t tile = surfs[v].tile_base + (item - __ldg(sched + seg));
+    if (!(info >> 31)) {
+      raster_tile<NT, true>(ws, surfs, nsurf, tile, (int)v, sm.r);
+      __threadfence();  // this thread's depth / id / record-map writes, before the count
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(&queue[2 + v], 1u);
+    } else {
+      if (threadIdx.x == 0) {
+        const uint32_t need = (uint32_t)(surfs[v].tiles_x * surfs[v].tiles_y);
+        int ok = 1;
+        for (uint32_t polls = 0; ld_acquire_gpu(&queue[2 + v]) < need; polls++) {
+          if (polls >= kWaitPolls) {
+            ok = 0;
+            atomicOr(&ws.ctr->overflow, 4u);
+            break;
+          }
+          __nanosleep(256);
+        }
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (s_ok) shade_tile<FEAT, NT>(sc, views, surfs, ws.srec, nrec, tile, v, sm.s);
+    }
+    __syncthreads();
+  }
 }
 
 // ---- texture atlas ----------------------------------------------------------------
@@ -1714,9 +1895,17 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
 }
 
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st) {
-  k_scan<<<1, kScanThreads, 0, st>>>(ws);
+  const uint32_t nchunks = (ws.nfine + kScanChunk - 1) / kScanChunk;
+  if (nchunks <= 1 || !ws.scan_part) {
+    k_scan<<<1, kScanThreads, 0, st>>>(ws);
+  } else {
+    k_scan_chunks<<<nchunks + 1, kScanThreads, 0, st>>>(ws, nchunks);
+    k_scan_add<<<nchunks, kScanThreads, 0, st>>>(ws, nchunks);
+  }
   return cudaGetLastError();
 }
+
+uint32_t scan_chunks(uint32_t nfine) { return (nfine + kScanChunk - 1) / kScanChunk; }
 
 cudaError_t launch_prep(const SceneDev& sc, const Workspace& ws, cudaStream_t st) {
   if (!ws.srec) return cudaErrorInvalidValue;
@@ -1730,32 +1919,83 @@ cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t
 }
 
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, uint32_t ntiles,
-                          bool with_id, int threads, cudaStream_t st, uint32_t tiles_per_surface) {
+                          bool with_id, int threads, cudaStream_t st, uint32_t tiles_per_surface, uint32_t tile0) {
   if (!ntiles) return cudaSuccess;
   const int wid = with_id ? 1 : 0;
   // surfaces of equal size: one grid row per surface, no search for the owner
-  const dim3 grid = (tiles_per_surface && nsurf > 1 && nsurf <= 65535 && tiles_per_surface * nsurf == ntiles)
-                        ? dim3(tiles_per_surface, nsurf) : dim3(ntiles);
+  const dim3 grid = (tile0 == 0 && tiles_per_surface && nsurf > 1 && nsurf <= 65535 &&
+                     tiles_per_surface * nsurf == ntiles) ? dim3(tiles_per_surface, nsurf) : dim3(ntiles);
   switch (threads * 2 + wid) {
-    case 256: k_raster<128, false><<<grid, 128, 0, st>>>(ws, d_surf, nsurf); break;
-    case 257: k_raster<128, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf); break;
-    case 1024: k_raster<512, false><<<grid, 512, 0, st>>>(ws, d_surf, nsurf); break;
-    case 1025: k_raster<512, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf); break;
-    case 513: k_raster<256, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf); break;
-    default: k_raster<256, false><<<grid, 256, 0, st>>>(ws, d_surf, nsurf); break;
+    case 256: k_raster<128, false><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 257: k_raster<128, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 1024: k_raster<512, false><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 1025: k_raster<512, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 513: k_raster<256, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    default: k_raster<256, false><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
   }
   return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
-                         uint32_t ntiles, const Workspace& ws, cudaStream_t st, bool features) {
+                         uint32_t ntiles, const Workspace& ws, cudaStream_t st, bool features, uint32_t tile0) {
   if (!ntiles) return cudaSuccess;
   if (!sc.objq || !sc.texlv || !ws.srec) return cudaErrorInvalidValue;
   if (features)
-    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap);
+    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0);
   else
-    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap);
+    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0);
   return cudaGetLastError();
+}
+
+// Blocks of the fused pass that fit on the device at once (cooperative grid).
+template <int NT, bool FEAT>
+uint32_t fused_grid() {
+  static uint32_t cached[2] = {0, 0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  uint32_t& g = cached[dev > 0 ? 1 : 0];
+  if (!g || dev > 1) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_shade<NT, FEAT>, NT, 0) != cudaSuccess)
+      per_sm = 0;
+    g = (uint32_t)std::max(per_sm, 0) * (uint32_t)num_sms();
+  }
+  return g;
+}
+
+template <int NT, bool FEAT>
+cudaError_t launch_fused_t(const SceneDev& sc, const ViewParams* d_views, const Surface* d_surf, uint32_t nsurf,
+                           const Workspace& ws, const uint32_t* sched, uint32_t nseg, uint32_t* queue,
+                           cudaStream_t st) {
+  const uint32_t grid = fused_grid<NT, FEAT>();
+  if (!grid) return cudaErrorInvalidConfiguration;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_raster_shade<NT, FEAT>, ws, d_surf, nsurf, sc, d_views, sched, nseg, queue);
+}
+
+cudaError_t launch_raster_shade(const SceneDev& sc, const ViewParams* d_views, const Surface* d_surf, uint32_t nsurf,
+                                const Workspace& ws, const uint32_t* sched, uint32_t nseg, uint32_t* queue,
+                                int threads, cudaStream_t st, bool features) {
+  if (!sc.objq || !sc.texlv || !ws.srec || !sched || !queue || !nseg) return cudaErrorInvalidValue;
+  if (threads == 128)
+    return features ? launch_fused_t<128, true>(sc, d_views, d_surf, nsurf, ws, sched, nseg, queue, st)
+                    : launch_fused_t<128, false>(sc, d_views, d_surf, nsurf, ws, sched, nseg, queue, st);
+  return features ? launch_fused_t<256, true>(sc, d_views, d_surf, nsurf, ws, sched, nseg, queue, st)
+                  : launch_fused_t<256, false>(sc, d_views, d_surf, nsurf, ws, sched, nseg, queue, st);
+}
+
+uint32_t fused_blocks(int threads, bool features) {
+  if (threads == 128) return features ? fused_grid<128, true>() : fused_grid<128, false>();
+  return features ? fused_grid<256, true>() : fused_grid<256, false>();
 }
 
 cudaError_t launch_texture_upload(uchar4* atlas, const uint32_t* nums, const uint32_t* sizes,

@@ -93,21 +93,25 @@ struct HostBuf {
 struct WorkMem {
   DevBuf<RasterRec> rec;
   DevBuf<ShadeRec> srec;
-  DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins;
+  DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins, scan_part;
   DevBuf<Counters> ctr;
   DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
   DevBuf<uint8_t> pix_rgba;
   DevBuf<Surface> surf;
   DevBuf<ViewParams> views;
   DevBuf<ShadowJob> jobs;
+  DevBuf<uint32_t> sched, queue;  // fused raster -> shade pass: work order and queue words
   uint32_t rec_target = 0, bin_target = 0;
   void release() {
     rec.release(); srec.release(); fine_count.release(); fine_off.release();
-    coarse_count.release(); coarse_off.release(); bins.release(); ctr.release();
+    coarse_count.release(); coarse_off.release(); bins.release(); scan_part.release(); ctr.release();
     pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
-    surf.release(); views.release(); jobs.release();
+    surf.release(); views.release(); jobs.release(); sched.release(); queue.release();
   }
 };
+
+// Groups of views of the pipelined raster / kernel3 mode (GBR_RS_PIPELINED).
+constexpr int kRsGroups = 8;
 
 struct PassShape {
   uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
@@ -115,13 +119,32 @@ struct PassShape {
   bool shade = true;  // views: some view wants RGBA or normals (else depth / id only)
   uint32_t tiles_per_surface = 0;  // every surface has this many fine tiles (cube faces), else 0
   bool features = false;            // views: some view has gbr_view.flags set
+  uint32_t nseg = 0;                // views: segments of the fused raster -> shade pass (GBR_RS_FUSED)
+  uint32_t ngroups = 0;             // views: pipelined groups (GBR_RS_PIPELINED), 0 or >= 2
+  uint32_t group_tile[kRsGroups + 1] = {};  // first tile of each group; [ngroups] = all tiles
 };
 
+// The fused pass's work order over view surfaces (k_raster_shade): each
+// view's raster tiles, and each view's shade tiles once at least `lag' raster
+// tiles of later views come between; returns the segment count.  out holds
+// seg_start[nseg + 1], then seg_view[nseg].
+uint32_t fused_schedule(const std::vector<Surface>& surfs, uint32_t lag, std::vector<uint32_t>& out);
+// Lay out how a view pass of several views that shade runs its raster and
+// kernel3 (tu.raster_shade): the fused pass (sh.nseg, the work order in
+// w.sched, copied on st or synchronously) or the pipelined groups
+// (sh.ngroups, sh.group_tile).  Otherwise both stay 0: one launch each.
+gbr_status plan_raster_shade(WorkMem& w, const std::vector<Surface>& surfs, const Tuning& tu, PassShape& sh,
+                             cudaStream_t st, bool sync_copy);
+// GBR_DEVICE_TIMEOUT when a pass's bounded wait gave up (overflow bit 2).
+gbr_status pass_wait_status(const Counters& c);
+
 // A stream beside a pass's geometry stages, with the events that fork it
-// from them and join it back (launch_pass).
+// from them and join it back, and one event per pipelined group's raster
+// (launch_pass).
 struct SideStream {
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t group[kRsGroups] = {};
 };
 
 void euler_cs(const float ang[3], float c[3], float s[3]);
@@ -174,6 +197,7 @@ struct gbr_scene {
   // shadow pass), and shading waits for geom_done.
   cudaStream_t aux = nullptr;
   cudaEvent_t pre_shadow = nullptr, geom_done = nullptr;
+  cudaEvent_t pre_geom = nullptr;  // the stream's work before a pipelined view pass moves to aux
   gbr::SideStream side;  // the view pass's shade constants beside its raster
   bool pre_shadow_valid = false;  // pre_shadow marks the pending shadow pass's start
   bool overlap = true;
@@ -254,7 +278,15 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
 // Kernel launches of one pass (for the launch statistics): views setup, scan,
 // fill, shade constants, raster, shade (the last two only when shading);
 // depth-only passes clear, setup, scan, fill, raster.
-inline uint32_t pass_kernels(bool view, bool shade = true) { return view ? (shade ? 6u : 4u) : 5u; }
+// A scan over more than one chunk of fine tiles is two kernels.
+// The fused raster -> shade pass is one kernel for two; pipelined groups are
+// two kernels per group.
+inline uint32_t pass_kernels(bool view, bool shade, uint32_t nfine, const PassShape* sh = nullptr) {
+  uint32_t k = (view ? (shade ? 6u : 4u) : 5u) + (scan_chunks(nfine) > 1 ? 1u : 0u);
+  if (sh && sh->nseg) k -= 1;
+  if (sh && sh->ngroups > 1) k += 2 * (sh->ngroups - 1);
+  return k;
+}
 // Timed stages of one pass (stage_ms): setup (a depth-only pass's clear
 // included), scan, fill, raster and, for views, shade.
 inline uint32_t pass_stages(bool view) { return view ? 5u : 4u; }

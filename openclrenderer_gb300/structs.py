@@ -59,20 +59,23 @@ SERVER_STATS = np.dtype([
 
 # gbr_tuning / gbr_batch_info (include/gbr.h)
 TUNING = np.dtype([("raster_threads", "<i4"), ("coarse_tile", "<i4"), ("fine_max_tiles", "<i4"),
-                   ("scratch_headroom", "<f4")])
+                   ("scratch_headroom", "<f4"), ("raster_shade", "<i4")])
+RS_SEQUENTIAL, RS_FUSED, RS_PIPELINED = 0, 1, 2
 BATCH_INFO = np.dtype([("views", "<u4"), ("graph_nodes", "<u4"), ("captures", "<u8"), ("launches", "<u8"),
                        ("reruns", "<u8"), ("scratch_bytes", "<u8")])
 PASS_SHADOW, PASS_VIEW = 0, 1
 BATCH_WITH_SHADOW = 1
-DEFAULT_TUNING = {"raster_threads": 256, "coarse_tile": 128, "fine_max_tiles": 16, "scratch_headroom": 1.25}
+DEFAULT_TUNING = {"raster_threads": 256, "coarse_tile": 128, "fine_max_tiles": 16, "scratch_headroom": 1.25,
+                  "raster_shade": 2}
 
 
-def make_tuning(raster_threads=256, coarse_tile=128, fine_max_tiles=16, scratch_headroom=1.25):
+def make_tuning(raster_threads=256, coarse_tile=128, fine_max_tiles=16, scratch_headroom=1.25, raster_shade=2):
     t = np.zeros((), TUNING)
     t["raster_threads"] = raster_threads
     t["coarse_tile"] = coarse_tile
     t["fine_max_tiles"] = fine_max_tiles
     t["scratch_headroom"] = scratch_headroom
+    t["raster_shade"] = raster_shade
     return t
 
 

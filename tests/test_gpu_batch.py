@@ -63,11 +63,47 @@ def test_shapes_on_binning_stress():
 
 def test_invalid_tuning_rejected():
     gs = GpuScene(scenes.plain_cubes())
-    for bad in ({"raster_threads": 100}, {"coarse_tile": 96}, {"fine_max_tiles": 0}, {"scratch_headroom": 0.5}):
+    for bad in ({"raster_threads": 100}, {"coarse_tile": 96}, {"fine_max_tiles": 0}, {"scratch_headroom": 0.5},
+                {"raster_shade": 3}):
         with pytest.raises(_native.GbrError) as e:
             gs.set_tuning(S.PASS_VIEW, **bad)
         assert e.value.status == "GBR_INVALID_ARG"
     assert gs.tuning(S.PASS_VIEW) == S.DEFAULT_TUNING
+
+
+def test_raster_shade_modes_match():
+    """The three ways a pass of several views runs its raster and kernel3
+    (tuning raster_shade: one launch each, the persistent fused launch, and
+    pipelined groups of views on two streams) give the same results bit for
+    bit, for every raster block size, uncaptured and in captured graphs, with
+    kernel3's optional switches on one view."""
+    sc = scenes.spheres_batch(n_spheres=60, n_views=10)
+    sc.views[1] = S.make_view(int(sc.views[1]["width"]), int(sc.views[1]["height"]), 90.0,
+                              flags=S.VIEW_OUTLINE)
+    gs = GpuScene(sc)
+    gs.shadow_pass()
+    gs.set_tuning(S.PASS_VIEW, raster_shade=S.RS_SEQUENTIAL)
+    ref = [o.numpy() for o in gs.render_batch(sc.cameras, sc.views)]
+    launches = gs.stats()["launches"]
+    gs.render_batch(sc.cameras, sc.views)
+    seq = gs.stats()["launches"] - launches
+    for mode in (S.RS_FUSED, S.RS_PIPELINED):
+        for threads in (256, 128, 512):
+            gs.set_tuning(S.PASS_VIEW, raster_shade=mode, raster_threads=threads)
+            launches = gs.stats()["launches"]
+            got = [o.numpy() for o in gs.render_batch(sc.cameras, sc.views)]
+            n = gs.stats()["launches"] - launches
+            if mode == S.RS_FUSED:
+                assert n == seq - 1  # one launch for raster and kernel3
+            else:
+                assert n > seq  # two launches per group of views
+            for i, (g, r) in enumerate(zip(got, ref)):
+                same(r, g, f"mode {mode}, {threads} threads, view {i}")
+        b = Batch(gs, sc.views)
+        assert b.tuning(S.PASS_VIEW)["raster_shade"] == mode
+        for i, (g, r) in enumerate(zip([o.numpy() for o in b.render(sc.cameras)], ref)):
+            same(r, g, f"mode {mode} graph, view {i}")
+        b.close()
 
 
 def _perturb(cams, rng, scale=20.0):
@@ -149,6 +185,7 @@ def test_autotune_picks_a_valid_shape():
         assert t["raster_threads"] in (128, 256, 512)
         assert t["coarse_tile"] in (64, 128, 256)
         assert t["fine_max_tiles"] in (4, 16, 64)
+        assert t["raster_shade"] in (S.RS_SEQUENTIAL, S.RS_FUSED, S.RS_PIPELINED)
     assert pick["best_ms"] > 0
     assert b.tuning(S.PASS_VIEW) == pick["view"]
     got = [o.numpy() for o in b.render(sc.cameras)]
