@@ -90,6 +90,7 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view) {
   TRY(w.scan_part.reserve(scan_chunks(sh.nfine)));
   TRY(w.ctr.reserve(1));
   if (view) TRY(w.pix_rec.reserve(sh.npix));
+  if (view) TRY(w.vis.reserve((size_t)std::max<uint32_t>(sh.nitems, 1) * std::max<uint32_t>((sh.nobjects + 31) / 32, 1)));
   return GBR_OK;
 }
 
@@ -237,8 +238,9 @@ gbr_status ensure_world(gbr_scene* s, cudaStream_t st) {
   if (!s->world_dirty) return GBR_OK;
   TRY(s->world.reserve((size_t)std::max<uint32_t>(s->ntris, 1) * 3));
   TRY(s->objq.reserve((size_t)std::max<uint32_t>(s->ndescs, 1) * kObjQuads));
+  TRY(s->objr.reserve(std::max<uint32_t>(s->ndescs, 1)));
   SceneDev sd = s->dev();
-  CU(launch_world(sd, s->world.p, s->objq.p, st));
+  CU(launch_world(sd, s->world.p, s->objq.p, s->objr.p, st));
   s->stats.launches += 2;
   s->world_dirty = false;
   return GBR_OK;
@@ -263,6 +265,10 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   ws.bins = wm.bins.p;
   ws.bin_cap = (uint32_t)std::min<size_t>(wm.bins.cap, 0xFFFFFFF0u);
   ws.scan_part = wm.scan_part.p;
+  // views: the object cull needs the world cache (and with it the radii)
+  const bool cull = view && sd.world && s->objr.p && sd.ndescs && sh.nobjects == sd.ndescs && sh.nitems <= 65535;
+  ws.vis = cull ? wm.vis.p : nullptr;
+  ws.vis_words = cull ? (sd.ndescs + 31) / 32 : 0;
   ws.ctr = wm.ctr.p;
   ws.fine_max = tu.fine_max;
   ws.coarse_shift = tu.coarse_shift;
@@ -272,6 +278,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   auto mark = [&](int k, cudaStream_t on) -> cudaError_t { return ev ? cudaEventRecord(ev[k], on) : cudaSuccess; };
   CU(mark(0, geom));
   if (view) {
+    if (cull) CU(launch_object_cull(sd, wm.views.p, wm.surf.p, sh.nitems, s->objr.p, ws.vis_words, wm.vis.p, geom));
     CU(launch_setup_views(sd, wm.views.p, sh.nitems, wm.surf.p, ws, geom));
   } else {
     // the setup writes small triangles straight into the faces
@@ -600,6 +607,7 @@ gbr_status gbr_scene_destroy(gbr_scene* s) {
   s->flush_buf.release();
   s->world.release();
   s->objq.release();
+  s->objr.release();
   s->staging.release();
   for (auto& e : s->ev)
     if (e) cudaEventDestroy(e);
@@ -951,6 +959,7 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   sh.nfine = tb;
   sh.ncoarse = cb;
   sh.npix = npix;
+  sh.nobjects = s->ndescs;
   sh.shade = false;
   for (uint32_t i = 0; i < n; i++) {
     if (outs[i].rgba || outs[i].normals) sh.shade = true;

@@ -95,6 +95,7 @@ gbr_status capture(gbr_batch* b) {
   b->vshape.nfine = tb;
   b->vshape.ncoarse = cb;
   b->vshape.npix = npix;
+  b->vshape.nobjects = s->ndescs;
   b->vshape.shade = false;
   for (uint32_t i = 0; i < b->n; i++) {
     if (b->outs[i].rgba || b->outs[i].normals) b->vshape.shade = true;

@@ -152,7 +152,7 @@ struct Tuning {
   int32_t coarse_shift = kCoarseShift;      // 2, 3 or 4 (64, 128, 256 pixels)
   int32_t fine_max = kFineMaxTiles;         // 1..256
   float headroom = 1.25f;                   // 1.05..4
-  int32_t raster_shade = GBR_RS_PIPELINED;  // views of several surfaces: GBR_RS_*
+  int32_t raster_shade = GBR_RS_SEQUENTIAL;  // views of several surfaces: GBR_RS_*
 };
 
 struct Workspace {
@@ -168,6 +168,8 @@ struct Workspace {
   uint32_t* bins;
   uint32_t bin_cap;
   uint32_t* scan_part;  // per chunk of fine counts (scan_chunks), or null: one-block scan
+  const uint32_t* vis;  // views: object cull bits (k_object_cull), vis_words per view, or null
+  uint32_t vis_words;
   Counters* ctr;
   int32_t fine_max;      // Tuning::fine_max
   int32_t coarse_shift;  // Tuning::coarse_shift
@@ -175,7 +177,11 @@ struct Workspace {
 
 // ---- launchers (gbr_kernels.cu) ----
 // World-space cache (world may be null: objects only) and the per-object table.
-cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st);
+cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, uint32_t* objr, cudaStream_t st);
+// Object cull bits of a view pass (words = ceil(ndescs / 32) per view); needs
+// the per-object table and the radii of the world-space cache.
+cudaError_t launch_object_cull(const SceneDev& sc, const ViewParams* d_views, const Surface* d_surf, uint32_t nviews,
+                               const uint32_t* objr, uint32_t words, uint32_t* vis, cudaStream_t st);
 cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews,
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st);
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,

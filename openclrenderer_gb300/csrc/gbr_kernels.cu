@@ -269,22 +269,83 @@ __device__ __forceinline__ void load_tri_pos(const gbr_triangle* T, f3 v[3], uin
 // the object half of full_rotate_quat (cl2.cl:700-710).  It does not depend on
 // the camera, so one pass serves the view and all cube faces until the
 // triangles or descriptors change.
-__global__ void __launch_bounds__(256) k_world(SceneDev sc, float4* __restrict__ world) {
+// Also the radius of each object's world-space vertices around its
+// world_pos (objr, float bits, zeroed before): the bounding sphere of the
+// object cull.
+__global__ void __launch_bounds__(256) k_world(SceneDev sc, float4* __restrict__ world, uint32_t* __restrict__ objr) {
   const uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tri >= sc.ntris) return;
-  f3 v[3];
-  uint32_t o_id;
-  load_tri_pos(sc.tris + tri, v, &o_id);
-  const gbr_obj_g_descriptor* G = sc.descs + o_id;
-  const f4 qn = fast_normalize4(ld4(G->world_rot_quat));
-  const f3 wp = ld3(G->world_pos);
-  const float scale = __ldg(&G->scale);
-  float4* out = world + (size_t)tri * 3;
+  const bool valid = tri < sc.ntris;
+  uint32_t o_id = 0;
+  float rmax = 0.0f;
+  if (valid) {
+    f3 v[3];
+    load_tri_pos(sc.tris + tri, v, &o_id);
+    const gbr_obj_g_descriptor* G = sc.descs + o_id;
+    const f4 qn = fast_normalize4(ld4(G->world_rot_quat));
+    const f3 wp = ld3(G->world_pos);
+    const float scale = __ldg(&G->scale);
+    float4* out = world + (size_t)tri * 3;
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    f3 r = add3(rot_quat_n(mul3s(v[k], scale), qn), wp);
-    out[k] = make_float4(r.x, r.y, r.z, k == 0 ? __uint_as_float(o_id) : 0.0f);
+    for (int k = 0; k < 3; k++) {
+      f3 r = add3(rot_quat_n(mul3s(v[k], scale), qn), wp);
+      out[k] = make_float4(r.x, r.y, r.z, k == 0 ? __uint_as_float(o_id) : 0.0f);
+      const float d = fast_length3(sub3(r, wp));
+      rmax = d == d ? fmax_(rmax, d) : __int_as_float(0x7F800000);  // a NaN vertex disables the cull
+    }
   }
+  // the largest radius per object, aggregated over the warp's lanes of that object
+  const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
+  if (valid) {
+    const unsigned grp = __match_any_sync(act, o_id);
+    const uint32_t m = __reduce_max_sync(grp, __float_as_uint(rmax));  // non-negative floats order as integers
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(grp) - 1)) atomicMax(objr + o_id, m);
+  }
+}
+
+// Object cull of a view pass: bit o of row v is 0 when every triangle of
+// object o is culled by prearrange's own tests in view v, so its setup
+// threads stop after reading the object id.  Object o lies within radius
+// objr[o] of its world_pos.  It is culled when it is farther than depth_far
+// (the reference's object test, exactly), or when its bounding sphere lies
+// entirely behind the near clip (z <= 20) or beyond the far clip (z >
+// 350000) -- every vertex is then clipped away -- or, lying entirely nearer
+// than the far clip, beyond one side plane of the view.  In that last case a
+// clipped vertex lies on an edge between a vertex behind the near clip and
+// one in front of it, inside the same half-space, so every projected vertex
+// is off-screen on that side and the off-screen cull removes the triangle
+// (cl2.cl:4352-4377).  (A vertex beyond the far clip is also clipped against
+// z = 20, by extrapolation along its edge, which can leave the half-space:
+// hence the far-clip condition.)  The margins (a relative 1e-3 of the radius
+// and of the distance, plus one unit) are orders of magnitude above the
+// float rounding of the per-triangle transform.
+__global__ void __launch_bounds__(256) k_object_cull(SceneDev sc, const ViewParams* __restrict__ views,
+                                                     const Surface* __restrict__ surfs, const uint32_t* __restrict__ objr,
+                                                     uint32_t words, uint32_t* __restrict__ vis) {
+  const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t v = blockIdx.y;
+  bool keep = false;
+  if (o < sc.ndescs) {
+    const ViewParams& V = views[v];
+    const Surface& S = surfs[V.surface];
+    const f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
+    const float4 q2 = __ldg(sc.objq + (size_t)o * kObjQuads + 2);
+    const f3 wp = mk3(q2.x, q2.y, q2.z);
+    const float dist = fast_length3(sub3(wp, cpos));
+    if (!(dist > kDepthFar)) {
+      const float r = __uint_as_float(__ldg(objr + o));
+      const float m = r * 1.001f + dist * 1e-3f + 1.0f;
+      const f3 q = rot_cs(wp, cpos, mk3(V.ccos[0], V.ccos[1], V.ccos[2]), mk3(V.csin[0], V.csin[1], V.csin[2]));
+      // side planes through the camera: x * fov = -+ z * W/2, y * fov = -+ z * H/2
+      const float hw = (float)S.width * 0.5f, hh = (float)S.height * 0.5f;
+      const float nx = rsqrtf(V.fov * V.fov + hw * hw), ny = rsqrtf(V.fov * V.fov + hh * hh);
+      const bool side = (q.x * V.fov + q.z * hw) * nx < -m || (q.x * V.fov - q.z * hw) * nx > m ||
+                        (q.y * V.fov + q.z * hh) * ny < -m || (q.y * V.fov - q.z * hh) * ny > m;
+      const bool out = q.z + m < kDepthCutoff || q.z - m > kDepthFar || (q.z + m < kDepthFar && side);
+      keep = !out || !(m < 1e30f);  // an infinite or NaN radius culls nothing
+    }
+  }
+  const unsigned bits = __ballot_sync(0xFFFFFFFFu, keep);
+  if ((threadIdx.x & 31) == 0 && (o >> 5) < words) vis[(size_t)v * words + (o >> 5)] = bits;
 }
 
 // Per object: the normalised rotation quaternion rot_quat applies, and the
@@ -398,7 +459,17 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
   const Surface& S = surfs[V.surface];
   Cand c0, c1;
   int n = 0;
-  if (tri < sc.ntris) {
+  // the object cull (k_object_cull), when the pass has one: the object id
+  // alone decides
+  bool live = tri < sc.ntris;
+  if (live && ws.vis) {
+    const uint32_t o_id = __float_as_uint(__ldg(&sc.world[(size_t)tri * 3].w));
+    live = (__ldg(ws.vis + (size_t)blockIdx.y * ws.vis_words + (o_id >> 5)) >> (o_id & 31)) & 1u;
+  }
+  // a warp with nothing to set up (objects are mostly contiguous runs of
+  // triangles) leaves before emit's warp-wide work
+  if (!__any_sync(0xFFFFFFFFu, live)) return;
+  if (live) {
     f3 wv[3];
     uint32_t o_id;
     load_world(sc, tri, wv, &o_id);
@@ -1865,9 +1936,22 @@ int num_sms() {
 
 }  // namespace
 
-cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, cudaStream_t st) {
+cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, uint32_t* objr, cudaStream_t st) {
   if (sc.ndescs) k_objects<<<(sc.ndescs + 255) / 256, 256, 0, st>>>(sc, objq);
-  if (sc.ntris && world) k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world);
+  if (sc.ntris && world) {
+    if (!objr) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(objr, 0, sizeof(uint32_t) * sc.ndescs, st);
+    if (e != cudaSuccess) return e;
+    k_world<<<(sc.ntris + 255) / 256, 256, 0, st>>>(sc, world, objr);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_object_cull(const SceneDev& sc, const ViewParams* d_views, const Surface* d_surf, uint32_t nviews,
+                               const uint32_t* objr, uint32_t words, uint32_t* vis, cudaStream_t st) {
+  if (!nviews || !words) return cudaSuccess;
+  if (!sc.objq || !objr || !vis || nviews > 65535) return cudaErrorInvalidValue;
+  k_object_cull<<<dim3((words * 32 + 255) / 256, nviews), 256, 0, st>>>(sc, d_views, d_surf, objr, words, vis);
   return cudaGetLastError();
 }
 

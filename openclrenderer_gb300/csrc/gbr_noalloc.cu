@@ -246,7 +246,8 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
     SceneDev obj = d;
     obj.objq = nullptr;
     obj.world = nullptr;
-    NA_CU(launch_world(obj, nullptr, reinterpret_cast<float4*>(base + kOffObj), s), "object table launch failed");
+    NA_CU(launch_world(obj, nullptr, reinterpret_cast<float4*>(base + kOffObj), nullptr, s),
+          "object table launch failed");
     NA_CU(launch_texture_levels(sc->nums, sc->sizes, sc->mipmap_start, reinterpret_cast<float4*>(base + kOffTexLv), s),
           "texture table launch failed");
   }

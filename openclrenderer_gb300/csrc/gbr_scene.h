@@ -101,12 +101,13 @@ struct WorkMem {
   DevBuf<ViewParams> views;
   DevBuf<ShadowJob> jobs;
   DevBuf<uint32_t> sched, queue;  // fused raster -> shade pass: work order and queue words
+  DevBuf<uint32_t> vis;           // views: object cull bits
   uint32_t rec_target = 0, bin_target = 0;
   void release() {
     rec.release(); srec.release(); fine_count.release(); fine_off.release();
     coarse_count.release(); coarse_off.release(); bins.release(); scan_part.release(); ctr.release();
     pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
-    surf.release(); views.release(); jobs.release(); sched.release(); queue.release();
+    surf.release(); views.release(); jobs.release(); sched.release(); queue.release(); vis.release();
   }
 };
 
@@ -115,6 +116,7 @@ constexpr int kRsGroups = 8;
 
 struct PassShape {
   uint32_t nitems = 0, nsurf = 0, nfine = 0, ncoarse = 0;
+  uint32_t nobjects = 0;  // views: descriptors of the scene (object cull bits)
   size_t npix = 0;
   bool shade = true;  // views: some view wants RGBA or normals (else depth / id only)
   uint32_t tiles_per_surface = 0;  // every surface has this many fine tiles (cube faces), else 0
@@ -160,6 +162,7 @@ struct gbr_scene {
   uint32_t ntris = 0;
   gbr::DevBuf<float4> world;  // world-space vertices, 3 per triangle
   gbr::DevBuf<float4> objq;   // per descriptor: kernel3's object table (kObjQuads float4)
+  gbr::DevBuf<uint32_t> objr; // per descriptor: radius of its world-space vertices (float bits)
   bool world_dirty = true;    // triangles or descriptors changed since k_world ran
   gbr::DevBuf<gbr_obj_g_descriptor> descs;
   uint32_t ndescs = 0;
@@ -282,7 +285,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
 // The fused raster -> shade pass is one kernel for two; pipelined groups are
 // two kernels per group.
 inline uint32_t pass_kernels(bool view, bool shade, uint32_t nfine, const PassShape* sh = nullptr) {
-  uint32_t k = (view ? (shade ? 6u : 4u) : 5u) + (scan_chunks(nfine) > 1 ? 1u : 0u);
+  uint32_t k = (view ? (shade ? 7u : 5u) : 5u) + (scan_chunks(nfine) > 1 ? 1u : 0u);  // views: + the object cull
   if (sh && sh->nseg) k -= 1;
   if (sh && sh->ngroups > 1) k += 2 * (sh->ngroups - 1);
   return k;

@@ -140,6 +140,38 @@ def test_multiple_and_static_shadow_lights():
         assert_parity(got, fixture, f"multi_shadow view {k} vs reference kernels")
 
 
+def test_object_cull_edges_parity():
+    """Objects all around the camera: in front, behind, straddling the near
+    clip, across every side plane of the view, and out to and past the far
+    clip (350,000), where prearrange's clip extrapolates along the edges.  The
+    object cull of the view setup may skip only triangles the reference's own
+    tests cull: depth, id and the reference fragment count equal the oracle's,
+    which has no object cull."""
+    rng = np.random.default_rng(77)
+    n = 400
+    dirs = rng.normal(size=(n, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    dist = np.exp(rng.uniform(np.log(30.0), np.log(420000.0), n))
+    scale = rng.uniform(20.0, 400.0, n) * np.maximum(dist / 3000.0, 1.0)
+    pos = (dirs * dist[:, None]).astype(np.float32)
+    tris = np.concatenate([scenes.cube_triangles(i) for i in range(n)])
+    descs = np.stack([S.make_descriptor(world_pos=pos[i] - 0.5 * scale[i], scale=float(scale[i]), tid=0,
+                                        feature_flag=S.FLAG_TWO_SIDED if i % 2 else 0) for i in range(n)])
+    lights = np.stack([S.make_light((0, -200, 500), (1, 1, 1), radius=50000.0)])
+    sc = scenes.Scene(tris, descs, lights, [64], scenes.random_textures(1, 64, 3), name="cull_edges")
+    sc.cameras = [S.make_camera((0, 0, 0), (0.1, 0.3, 0.0)), S.make_camera((10, -5, 3), (-0.4, 2.5, 0.2))]
+    sc.views = [S.make_view(640, 360, 90.0), S.make_view(320, 480, 60.0)]
+    gs = GpuScene(sc)
+    tex = O.build_textures(sc.tex_sizes, sc.tex_pixels)
+    for k, (cam, view) in enumerate(zip(sc.cameras, sc.views)):
+        got = gs.render(cam, view).numpy()
+        torch.cuda.synchronize()
+        ref = O.render(sc, tex, cam, view)
+        assert (ref["depth"] != 0xFFFFFFFF).sum() > 2000
+        assert_parity(got, ref, f"cull edges view {k}")
+        assert gs.stats()["fragments_ref"] == ref["fragments"]
+
+
 def test_optional_kernel3_features_parity():
     """Normal maps and the per-object outline (ENABLE_NORMAL_MAPPING,
     CAN_OUTLINE; gbr_view.flags) against the oracle, which the reference's
@@ -367,7 +399,7 @@ def test_depth_id_only_view_skips_shading():
     view = np.asarray(sc.views[0], S.VIEW).reshape(1)
     _native.check(gs.L.gbr_render_view(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.byref(outs), _stream_ptr(None)))
     torch.cuda.synchronize()
-    assert gs.stats()["launches"] - before == 4  # setup, scan, fill, raster (no shade constants, no kernel3)
+    assert gs.stats()["launches"] - before == 5  # object cull, setup, scan, fill, raster (no shade constants, no kernel3)
     got = o.numpy()
     assert np.array_equal(got["depth"], full["depth"]) and np.array_equal(got["id"], full["id"])
 
