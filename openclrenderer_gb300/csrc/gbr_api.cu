@@ -269,6 +269,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   const bool cull = view && sd.world && s->objr.p && sd.ndescs && sh.nobjects == sd.ndescs && sh.nitems <= 65535;
   ws.vis = cull ? wm.vis.p : nullptr;
   ws.vis_words = cull ? (sd.ndescs + 31) / 32 : 0;
+  ws.pack_keys = view && sd.ntris < (1u << 22) - 1;
   ws.ctr = wm.ctr.p;
   ws.fine_max = tu.fine_max;
   ws.coarse_shift = tu.coarse_shift;

@@ -170,6 +170,7 @@ struct Workspace {
   uint32_t* scan_part;  // per chunk of fine counts (scan_chunks), or null: one-block scan
   const uint32_t* vis;  // views: object cull bits (k_object_cull), vis_words per view, or null
   uint32_t vis_words;
+  uint32_t pack_keys;   // views: every key (2 * triangle + 1) is below 2^23 - 1 (32-bit id resolve)
   Counters* ctr;
   int32_t fine_max;      // Tuning::fine_max
   int32_t coarse_shift;  // Tuning::coarse_shift

@@ -784,6 +784,7 @@ __device__ __forceinline__ uint32_t find_surface_warp(const Surface* surfs, uint
 // at most kRasterCache windows, pass 1 reuses the covered tests of pass 0
 // kept in registers.
 constexpr int kRasterCache = 8;
+constexpr uint32_t kSlotBits = 9;  // staged slots of a one-chunk tile: below 512
 
 // Exclusive block scan with a single barrier: each warp scans its lanes,
 // publishes its total, and after the barrier every thread adds up the totals
@@ -814,7 +815,7 @@ __device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp
 // Shared memory of one tile's raster (NT threads).
 template <int NT>
 struct RasterSmem {
-  float4 srec[NT][4];
+  float4 srec[4][NT];  // the staged records' four float4, one array each (conflict-free stores)
   uint32_t sidx[NT];
   uint32_t soff[NT + 1];
   uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
@@ -837,7 +838,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   constexpr bool with_id = ID;
   constexpr int NW = NT / 32;
   constexpr uint32_t kCountShift = 18;  // scan word: pixels (< 2^18) | records << 18
-  float4 (&srec)[NT][4] = sm.srec;
+  float4 (&srec)[4][NT] = sm.srec;
   uint32_t* sidx = sm.sidx;
   uint32_t* soff = sm.soff;
   uint32_t* sgeo = sm.sgeo;
@@ -895,6 +896,12 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
   const bool resident = ntotal <= (uint32_t)NT;
+  // A tile resolved in one chunk keeps the canonical id as 32 bits, key <<
+  // kSlotBits | staged slot (keys of the scene below ws.pack_keys): a record
+  // has one key, so the minimum of these picks the same record as the
+  // minimum of (key << 32 | record), with half the shared-memory traffic.
+  const bool packed = with_id && resident && ws.pack_keys;
+  uint32_t* sid32 = reinterpret_cast<uint32_t*>(sid);
   // the covered tests of pass 0 (resident tiles), up to kRasterCache per
   // thread: depth, and pixel | staged record << 8 | 1 << 31; nh counts them
   uint32_t cache_d[kRasterCache], cache_m[kRasterCache];
@@ -929,10 +936,10 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
         const uint32_t off = block_excl_scan1<NT>(word, swarp, &tot);
         if (area) {
           const uint32_t slot = off >> kCountShift;
-          srec[slot][0] = q0;
-          srec[slot][1] = q1;
-          srec[slot][2] = q2;
-          srec[slot][3] = q3;
+          srec[0][slot] = q0;
+          srec[1][slot] = q1;
+          srec[2][slot] = q2;
+          srec[3][slot] = q3;
           sidx[slot] = r;
           sgeo[slot] = geo;
           soff[slot] = off & ((1u << kCountShift) - 1);
@@ -953,8 +960,13 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
           const int p = (int)(cache_m[g] & 0xFF);
           const uint32_t lo = (cache_m[g] >> 8) & 0x3FF;
           const uint32_t d = cache_d[g], fd = sdepth[p];
-          if (d > fd - kBufError && d < fd + kBufError)
-            atomicMin(&sid[p], ((unsigned long long)__float_as_uint(srec[lo][2].w) << 32) | sidx[lo]);
+          if (d > fd - kBufError && d < fd + kBufError) {
+            const uint32_t key = __float_as_uint(srec[2][lo].w);
+            if (packed)
+              atomicMin(sid32 + p, (key << kSlotBits) | lo);
+            else
+              atomicMin(&sid[p], ((unsigned long long)key << 32) | sidx[lo]);
+          }
         }
         continue;
       }
@@ -989,7 +1001,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
             const uint32_t bw = (geo >> 8) & 0x1F;
             const uint32_t ry = (local * (geo >> 13)) >> 16, rx = local - ry * bw;
             const int lx = (int)(geo & 0xF) + (int)rx, ly = (int)((geo >> 4) & 0xF) + (int)ry;
-            const float4 q[4] = {srec[lo][0], srec[lo][1], srec[lo][2], srec[lo][3]};
+            const float4 q[4] = {srec[0][lo], srec[1][lo], srec[2][lo], srec[3][lo]};
             const int x = tx0 + lx, y = ty0 + ly;
             hit = covers_in_bbox(q, x, y, chunk);
             if (hit) {
@@ -1008,8 +1020,12 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
                 }
               } else {
                 const uint32_t fd = sdepth[p];
-                if (d > fd - kBufError && d < fd + kBufError)
-                  atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
+                if (d > fd - kBufError && d < fd + kBufError) {
+                  if (packed)
+                    atomicMin(sid32 + p, (__float_as_uint(q[2].w) << kSlotBits) | lo);
+                  else
+                    atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
+                }
               }
             }
           }
@@ -1036,7 +1052,11 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
     if (px < S.width && py < S.height) {
       const size_t p = (size_t)py * S.width + px;
       S.depth[p] = sdepth[lp];
-      if (with_id) {
+      if (with_id && packed) {
+        const uint32_t v = sid32[lp];
+        if (S.id) S.id[p] = v == ~0u ? kNoId : v >> kSlotBits;
+        S.rec[p] = v == ~0u ? kNoId : sidx[v & ((1u << kSlotBits) - 1)];
+      } else if (with_id) {
         const unsigned long long v = sid[lp];
         if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
         S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;

@@ -227,6 +227,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   ws.bin_cap = (uint32_t)kMaxBins;
   ws.fine_max = kFineMaxTiles;
   ws.coarse_shift = kCoarseShift;
+  ws.pack_keys = sc->ntris < (1u << 22) - 1;
   Surface* d_surf = reinterpret_cast<Surface*>(base + kOffSurface);
   ViewParams* d_view = reinterpret_cast<ViewParams*>(base + kOffView);
 

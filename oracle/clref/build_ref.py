@@ -19,7 +19,10 @@ LIB = os.path.join(REF_DIR, "libclref.so")
 # the same kernels with kernel3's optional switches on (normal mapping, outline)
 KERNELS_F3 = os.path.join(REF_DIR, "cl2_hot_f3.cpp")
 LIB_F3 = os.path.join(REF_DIR, "libclref_f3.so")
-REFERENCE_CL = os.environ.get("GBR_REFERENCE_CL", "/root/reference/cl2.cl")
+# the reference checkout's cl2.cl: GBR_REFERENCE_CL, else a checkout named
+# "reference" beside this repository's root
+REFERENCE_CL = os.environ.get("GBR_REFERENCE_CL") or os.path.normpath(
+    os.path.join(ORACLE, "..", "..", "reference", "cl2.cl"))
 
 
 def _build_one(kernels, lib, extra, force):
