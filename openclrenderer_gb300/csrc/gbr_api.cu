@@ -289,16 +289,16 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(mark(1, geom));
   const bool prep = view && sh.shade;
   const bool on_side = prep && side && side->stream;
-  if (on_side) {
+  CU(launch_scan(ws, geom));
+  CU(mark(2, geom));
+  CU(launch_fill(ws, wm.surf.p, geom));
+  CU(mark(3, geom));
+  if (on_side) {  // the shade constants beside the raster
     CU(cudaEventRecord(side->fork, geom));
     CU(cudaStreamWaitEvent(side->stream, side->fork, 0));
     CU(launch_prep(sd, ws, side->stream));
     CU(cudaEventRecord(side->join, side->stream));
   }
-  CU(launch_scan(ws, geom));
-  CU(mark(2, geom));
-  CU(launch_fill(ws, wm.surf.p, geom));
-  CU(mark(3, geom));
   const bool fused = view && sh.shade && sh.nseg > 0;
   const bool piped = !fused && view && sh.shade && sh.ngroups > 1 && split && on_side;
   if (piped) {

@@ -1106,16 +1106,22 @@ __device__ __forceinline__ TexSlot level_slot(const SceneDev& sc, float4 lv) {
   t.page = sc.atlas + (size_t)__float_as_uint(lv.w) * kTexPage * kTexPage;
   return t;
 }
-__device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy) {
-  cx = clampf_(cx, 0.001f, ts.width - 0.001f);
-  cy = clampf_(cy, 0.001f, ts.width - 0.001f);
-  // in [0, 2048) and never NaN (the clamp maps NaN to 0.001): plain
-  // truncation equals the saturating convert_int
-  const int ix = (int)(ts.ox + cx);
-  const int iy = (int)(ts.oy + cy);
+__device__ __forceinline__ f4 texel(const TexSlot& ts, int ix, int iy) {
   const uint32_t t = __ldg(reinterpret_cast<const uint32_t*>(ts.page) + ((size_t)iy * kTexPage + ix));
   f4 r; r.x = u8f(t & 0xFF); r.y = u8f((t >> 8) & 0xFF); r.z = u8f((t >> 16) & 0xFF); r.w = u8f(t >> 24);
   return r;
+}
+
+// The column (row) of a texel of the bilinear footprint at pos (+ 1 for the
+// second): the reference clamps the float coordinate to [0.001, w - 0.001]
+// and truncates o + c, o the slot origin.  pos is an integer-valued float
+// (floor), so that is o + clamp(pos, 0, w - 1) in integers: 0.001 truncates
+// to 0, w - 0.001 to w - 1 (o + w <= 2048 keeps o + w - 0.001 below o + w in
+// float), and a NaN coordinate clamps to 0.001, for both texels.
+__device__ __forceinline__ int texel_coord(float pos, int plus, int w) {
+  if (pos != pos) return 0;
+  const int p = min((int)pos, w) + plus;  // saturating conversion; below INT_MAX after the min
+  return min(max(p, 0), w - 1);
 }
 
 // COLOUR: the result only scales the colour (the texel colour), so the blend
@@ -1124,10 +1130,13 @@ __device__ __forceinline__ f4 read_tex_pre(const TexSlot& ts, float cx, float cy
 template <bool COLOUR>
 __device__ f4 bilinear_pre(const TexSlot& ts, float mx, float my) {
   float posx = floorf(mx), posy = floorf(my);
-  f4 c0 = read_tex_pre(ts, posx, posy);
-  f4 c1 = read_tex_pre(ts, posx + 1, posy);
-  f4 c2 = read_tex_pre(ts, posx, posy + 1);
-  f4 c3 = read_tex_pre(ts, posx + 1, posy + 1);
+  const int w = (int)ts.width, ox = (int)ts.ox, oy = (int)ts.oy;
+  const int x0 = ox + texel_coord(posx, 0, w), x1 = ox + texel_coord(posx, 1, w);
+  const int y0 = oy + texel_coord(posy, 0, w), y1 = oy + texel_coord(posy, 1, w);
+  f4 c0 = texel(ts, x0, y0);
+  f4 c1 = texel(ts, x1, y0);
+  f4 c2 = texel(ts, x0, y1);
+  f4 c3 = texel(ts, x1, y1);
   float ux = mx - posx, uy = my - posy;
   float bx = 1.0f - ux, by = 1.0f - uy;
   f4 r;
@@ -1179,6 +1188,13 @@ __device__ f4 texture_filter_diff(const SceneDev& sc, f2 vt, f2 vtdiff, int tid2
   return r;
 }
 
+// depth_to_dist(d) compared with a threshold t: (float)d * 2^-32 is exact and
+// a scaling by a power of two commutes with rounding (every value here is a
+// normal float), so depth_to_dist(d) = RN((float)d * 350000) * 2^-32, and
+// depth_to_dist(d) > t exactly when RN((float)d * 350000) > t * 2^32.
+constexpr float kTwo32 = 4294967296.0f;
+__device__ __forceinline__ float depth_scaled(uint32_t d) { return (float)d * kDepthFar; }
+
 // How many of the thresholds t0 < t1 < t2 < t3 < t4 lie below d2, i.e.
 // (d2 > t0) + ... + (d2 > t4): the thresholds dep + z (z = -2..2, dep <=
 // 350000) are strictly increasing in float, so the predicates are monotone and
@@ -1211,11 +1227,13 @@ __device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* dep
   float dep = depth_to_dist(__ldca(depth + (size_t)y * W + x));
   float rad = kSsaoRad + foffset * 0.5f;  // foffset / 2, exact
   float world_rad = fdiv(rad * fov, dep);
-  const float t0 = dep + -2.0f, t1 = dep + -1.0f, t3 = dep + 1.0f, t4 = dep + 2.0f;
+  // the thresholds dep + z, z = -2..2, scaled by 2^32 (depth_scaled)
+  const float t0 = (dep + -2.0f) * kTwo32, t1 = (dep + -1.0f) * kTwo32, t2 = dep * kTwo32,
+              t3 = (dep + 1.0f) * kTwo32, t4 = (dep + 2.0f) * kTwo32;
   int acc = 0;
   if (__all_sync(__activemask(), world_rad < 0.25f)) {
-    const float d2 = depth_to_dist(__ldca(depth + (size_t)ssao_coord((float)y, H) * W + ssao_coord((float)x, W)));
-    acc = 25 * ssao_count(d2, t0, t1, dep, t3, t4);
+    const float d2 = depth_scaled(__ldca(depth + (size_t)ssao_coord((float)y, H) * W + ssao_coord((float)x, W)));
+    acc = 25 * ssao_count(d2, t0, t1, t2, t3, t4);
   } else {
     const float r1 = roundf(world_rad), r2 = roundf(2.0f * world_rad), r0 = roundf(0.0f * world_rad);
     const float off[5] = {-r2, -r1, r0, r1, r2};
@@ -1227,8 +1245,8 @@ __device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* dep
       const uint32_t* row = depth + (size_t)ssao_coord((float)y + off[k], H) * W;
 #pragma unroll
       for (int xx = 0; xx < 5; xx++) {
-        const float d2 = depth_to_dist(__ldca(row + wx[xx]));
-        acc += ssao_count(d2, t0, t1, dep, t3, t4);
+        const float d2 = depth_scaled(__ldca(row + wx[xx]));
+        acc += ssao_count(d2, t0, t1, t2, t3, t4);
       }
     }
   }
