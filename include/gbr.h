@@ -419,6 +419,11 @@ typedef struct gbr_server_config {
   uint64_t hbm_budget_bytes; /* device bytes admitted requests may hold at once */
   uint32_t max_batch_views;  /* views per batch (0 = 64) */
   uint32_t max_batch_pixels; /* pixels per batch (0 = 33177600, four 4K views) */
+  uint32_t max_inflight;     /* batches on the GPU at once, over all scenes (0 = one per scene): a
+                                worker whose scene has requests waits for a slot, and requests
+                                that arrive meanwhile join its batch */
+  uint32_t batch_window_us;  /* a worker holds a batch open this long after its first request
+                                (0 = launch at once), unless the batch limits fill it first */
 } gbr_server_config;
 
 typedef struct gbr_request {

@@ -36,7 +36,7 @@ struct Req {
   gbr_request r;
   uint64_t id;
   uint64_t bytes;
-  Clock::time_point t_submit, t_launch;
+  Clock::time_point t_submit, t_launch, t_admit;
 };
 
 // Device outputs of one batch; two per worker so that a batch renders while
@@ -84,6 +84,7 @@ struct gbr_server {
   uint64_t next_id = 1, submitted = 0, completed = 0, rejected = 0, batches = 0, batch_views = 0;
   uint64_t pixels_completed = 0;
   uint64_t in_system = 0;  // submitted, not completed
+  uint32_t inflight = 0;   // batches launched, not completed
   bool stop = false;
   bool started = false;
   Clock::time_point t_first, t_last;
@@ -97,6 +98,7 @@ void admit_locked(gbr_server* s) {
   while (!s->waiting.empty()) {
     Req& q = s->waiting.front();
     if (s->admitted_bytes + q.bytes > s->cfg.hbm_budget_bytes) break;
+    q.t_admit = Clock::now();
     s->admitted_bytes += q.bytes;
     s->peak_bytes = std::max(s->peak_bytes, s->admitted_bytes);
     s->workers[q.r.scene]->pending.push_back(q);
@@ -139,6 +141,21 @@ void worker_loop(gbr_server* s, Worker* w) {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_work.wait(lk, [&] { return s->stop || !w->pending.empty(); });
       if (s->stop && w->pending.empty()) return;
+      // a batching window from the oldest pending request, cut short when
+      // the batch limits are reached or the server stops
+      if (s->cfg.batch_window_us) {
+        const Clock::time_point until = w->pending.front().t_admit + std::chrono::microseconds(s->cfg.batch_window_us);
+        s->cv_work.wait_until(lk, until, [&] {
+          if (s->stop) return true;
+          uint64_t pix = 0;
+          for (const Req& q : w->pending) pix += (uint64_t)q.r.view.width * q.r.view.height;
+          return w->pending.size() >= max_views || pix >= max_pix;
+        });
+      }
+      // a slot on the GPU: requests arriving meanwhile join this batch
+      if (s->cfg.max_inflight)
+        s->cv_work.wait(lk, [&] { return s->stop || s->inflight < s->cfg.max_inflight; });
+      s->inflight++;
       uint64_t pix = 0;
       while (!w->pending.empty() && batch.size() < max_views) {
         const Req& q = w->pending.front();
@@ -228,10 +245,12 @@ void complete(gbr_server* s, std::vector<Req>& batch, gbr_status st, Clock::time
     }
     s->batches++;
     s->batch_views += batch.size();
+    s->inflight--;
     s->t_last = t_done;
     admit_locked(s);
   }
   s->cv_done.notify_all();
+  s->cv_work.notify_all();  // a GPU slot is free
 }
 
 }  // namespace

@@ -363,7 +363,8 @@ class Server:
     """Serving loop over resident GpuScenes (gbr_server_*): HBM-budgeted
     admission and continuous batching per scene, results in host memory."""
 
-    def __init__(self, scenes, hbm_budget_bytes=8 << 30, max_batch_views=0, max_batch_pixels=0):
+    def __init__(self, scenes, hbm_budget_bytes=8 << 30, max_batch_views=0, max_batch_pixels=0, max_inflight=0,
+                 batch_window_us=0):
         self.L = _native.load()
         self.scenes = list(scenes)
         arr = (_P * len(self.scenes))(*[g.h.value for g in self.scenes])
@@ -371,6 +372,8 @@ class Server:
         cfg["hbm_budget_bytes"] = hbm_budget_bytes
         cfg["max_batch_views"] = max_batch_views
         cfg["max_batch_pixels"] = max_batch_pixels
+        cfg["max_inflight"] = max_inflight
+        cfg["batch_window_us"] = batch_window_us
         h = _P()
         _native.check(self.L.gbr_server_create(arr, len(self.scenes), _np_ptr(cfg), ctypes.byref(h)))
         self.h = h

@@ -42,7 +42,8 @@ STATS = np.dtype([
 STAGES = ("shadow_setup", "shadow_scan", "shadow_fill", "shadow_raster",
           "view_setup", "view_scan", "view_fill", "view_raster", "view_shade")
 
-SERVER_CONFIG = np.dtype([("hbm_budget_bytes", "<u8"), ("max_batch_views", "<u4"), ("max_batch_pixels", "<u4")])
+SERVER_CONFIG = np.dtype([("hbm_budget_bytes", "<u8"), ("max_batch_views", "<u4"), ("max_batch_pixels", "<u4"),
+                          ("max_inflight", "<u4"), ("batch_window_us", "<u4")])
 REQUEST = np.dtype([
     ("scene", "<u4"), ("reserved", "<u4"), ("cam", CAMERA), ("view", VIEW),
     ("depth", "<u8"), ("id", "<u8"), ("rgba", "<u8"), ("user_tag", "<u8"),

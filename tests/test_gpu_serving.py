@@ -125,3 +125,39 @@ def test_bounded_drain():
     done = srv.poll(cap=1024)
     assert len(done) == len(reqs) and all(c["status"] == 0 for c in done)
     srv.close()
+
+
+def test_serving_inflight_cap_and_window_batch_more():
+    """One GPU slot over all scenes and a batching window: requests that
+    arrive while a batch is on the GPU join the next one, so batches grow
+    over the same paced arrivals; every result equals the request rendered
+    alone."""
+    scs = _scenes()
+    gss = [GpuScene(sc) for sc in scs]
+    for g in gss:
+        g.shadow_pass()
+    rng = np.random.default_rng(31)
+    reqs = _requests(48, rng)
+    alone = [gss[s].render_host(cam, view) for s, cam, view in reqs]
+    torch.cuda.synchronize()
+    means = []
+    for cfg in ({}, {"max_inflight": 1, "batch_window_us": 2000}):
+        srv = Server(gss, hbm_budget_bytes=8 << 30, **cfg)
+        outs = []
+        for k, (s, cam, view) in enumerate(reqs):
+            W, H = int(view["width"]), int(view["height"])
+            o = {"depth": np.zeros((H, W), np.uint32), "id": np.zeros((H, W), np.uint32),
+                 "rgba": np.zeros((H, W, 4), np.uint8)}
+            outs.append(o)
+            srv.submit(s, cam, view, o["depth"], o["id"], o["rgba"], tag=k)
+            time.sleep(0.0003)
+        srv.drain()
+        done = srv.poll(cap=1024)
+        st = srv.stats()
+        srv.close()
+        assert len(done) == len(reqs) and np.all(done["status"] == 0)
+        means.append(st["mean_batch_views"])
+        for k, (a, b) in enumerate(zip(alone, outs)):
+            for key in ("depth", "id", "rgba"):
+                assert np.array_equal(a[key], b[key]), f"{cfg}: request {k} {key} differs"
+    assert means[1] > means[0] and means[1] >= 2.0, means
