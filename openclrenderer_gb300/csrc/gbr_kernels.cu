@@ -812,6 +812,14 @@ __device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp
 }
 
 
+// Shared-memory slot of tile pixel p = ly * 16 + lx in the per-pixel depth
+// (32-bit words) and id (64-bit words) arrays: a row of 16 pixels fills 16
+// of the 32 banks, so rows y and y + 2 (64-bit: y and y + 1) would share
+// banks and a narrow triangle's tests collide; XOR-ing the column with the
+// row pair (row) spreads them.  A permutation within each row.
+__device__ __forceinline__ int swz32(int p) { return p ^ ((p >> 5) & 15); }
+__device__ __forceinline__ int swz64(int p) { return p ^ ((p >> 4) & 15); }
+
 // Shared memory of one tile's raster (NT threads).
 template <int NT>
 struct RasterSmem {
@@ -889,7 +897,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
     if (lists[1] + lists[3] == 0) return;
     for (int p = tid; p < kTilePixels; p += NT) {
       const int px = tx0 + (p & (kTile - 1)), py = ty0 + p / kTile;
-      sdepth[p] = (px < S.width && py < S.height) ? S.depth[(size_t)py * S.width + px] : kDepthClear;
+      sdepth[swz32(p)] = (px < S.width && py < S.height) ? S.depth[(size_t)py * S.width + px] : kDepthClear;
     }
   }
   const int chunk = S.chunk;
@@ -959,13 +967,13 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
           if (!(cache_m[g] >> 31)) continue;
           const int p = (int)(cache_m[g] & 0xFF);
           const uint32_t lo = (cache_m[g] >> 8) & 0x3FF;
-          const uint32_t d = cache_d[g], fd = sdepth[p];
+          const uint32_t d = cache_d[g], fd = sdepth[swz32(p)];
           if (d > fd - kBufError && d < fd + kBufError) {
             const uint32_t key = __float_as_uint(srec[2][lo].w);
             if (packed)
-              atomicMin(sid32 + p, (key << kSlotBits) | lo);
+              atomicMin(sid32 + swz32(p), (key << kSlotBits) | lo);
             else
-              atomicMin(&sid[p], ((unsigned long long)key << 32) | sidx[lo]);
+              atomicMin(&sid[swz64(p)], ((unsigned long long)key << 32) | sidx[lo]);
           }
         }
         continue;
@@ -1008,7 +1016,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
               const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
               const int p = ly * kTile + lx;
               if (pass == 0) {
-                atomicMin(&sdepth[p], d);
+                atomicMin(&sdepth[swz32(p)], d);
                 if (keep) {
 #pragma unroll
                   for (int k = 0; k < kRasterCache; k++)
@@ -1019,12 +1027,12 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
                   nh++;
                 }
               } else {
-                const uint32_t fd = sdepth[p];
+                const uint32_t fd = sdepth[swz32(p)];
                 if (d > fd - kBufError && d < fd + kBufError) {
                   if (packed)
-                    atomicMin(sid32 + p, (__float_as_uint(q[2].w) << kSlotBits) | lo);
+                    atomicMin(sid32 + swz32(p), (__float_as_uint(q[2].w) << kSlotBits) | lo);
                   else
-                    atomicMin(&sid[p], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
+                    atomicMin(&sid[swz64(p)], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
                 }
               }
             }
@@ -1051,13 +1059,13 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
     const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
     if (px < S.width && py < S.height) {
       const size_t p = (size_t)py * S.width + px;
-      S.depth[p] = sdepth[lp];
+      S.depth[p] = sdepth[swz32(lp)];
       if (with_id && packed) {
-        const uint32_t v = sid32[lp];
+        const uint32_t v = sid32[swz32(lp)];
         if (S.id) S.id[p] = v == ~0u ? kNoId : v >> kSlotBits;
         S.rec[p] = v == ~0u ? kNoId : sidx[v & ((1u << kSlotBits) - 1)];
       } else if (with_id) {
-        const unsigned long long v = sid[lp];
+        const unsigned long long v = sid[swz64(lp)];
         if (S.id) S.id[p] = v == ~0ull ? kNoId : (uint32_t)(v >> 32);
         S.rec[p] = v == ~0ull ? kNoId : (uint32_t)v;
       }
