@@ -55,6 +55,10 @@ struct texture {
   int id = -1;                 // position in the gpu texture order
   int size = 0;                // square edge, power of two 16..2048
   std::vector<uint8_t> rgba;   // size*size*4
+  std::string location;        // texture::set_location: the file (or cache name) it came from
+  bool is_unique = false;      // texture::set_unique: never returned by make_new_cached
+  void set_location(const std::string& loc) { location = loc; }
+  void set_unique() { is_unique = true; }
   // texture::set_create_colour: a uniform square texture
   void set_create_colour(uint8_t r, uint8_t g, uint8_t b, uint8_t a, int edge) {
     size = edge;
@@ -77,6 +81,20 @@ struct texture_context {
     textures.back()->id = (int)textures.size() - 1;
     return textures.back().get();
   }
+  // texture_context::make_new_cached (texture_context.cpp:27-49): the first
+  // texture of the context at location loc that is not unique, else a new one
+  // at loc (*fresh tells which).
+  texture* make_new_cached(const std::string& loc, bool* fresh = nullptr) {
+    for (const auto& t : textures)
+      if (!t->is_unique && t->location == loc) {
+        if (fresh) *fresh = false;
+        return t.get();
+      }
+    texture* t = make_new();
+    t->location = loc;
+    if (fresh) *fresh = true;
+    return t;
+  }
   void destroy(texture* t) {
     textures.erase(std::remove_if(textures.begin(), textures.end(),
                                   [&](const std::unique_ptr<texture>& u) { return u.get() == t; }),
@@ -97,6 +115,9 @@ struct object {
   float specular = 0.9f, spec_mult = 1.f, diffuse = 1.f;  // object.cpp:72-74
   int32_t feature_flag = 0;
   texture* normal_map = nullptr;  // descriptor rid (obj.rid / normal_map, obj_load.cpp:544-556)
+  texture* bump = nullptr;        // obj.bid: the material's map_Bump (obj_load.cpp:520-532)
+  uint32_t has_bump = 0;          // descriptor has_bump
+  std::string object_name;        // the OBJ group of its usemtl section (obj_load.cpp:414-415, 538)
   texture* ss_map = nullptr;      // descriptor ssid: the screen-space reflection map (object.cpp:106-109)
 };
 
@@ -106,6 +127,9 @@ struct objects_container {
   bool isloaded = false;
   std::string file;             // set_file: loaded by object_context::load_active
   float requested_scale = 1.f;  // applied to positions at load (obj_load.cpp:437)
+  float current_scale = 1.f;    // the scale the loaded positions carry (obj_load.cpp:563-564)
+  bool textures_are_unique = false;  // set_unique_textures: loads skip the texture cache
+  std::string normal_map_file;  // set_normal: every loaded object's normal map (obj_load.cpp:544-556)
   float4 pos;
   float4 rot_quat{0, 0, 0, 1};
   float dynamic_scale = 1.f;
@@ -142,6 +166,8 @@ struct objects_container {
   }
   void set_file(const std::string& f) { file = f; isloaded = false; }
   void request_scale(float s) { requested_scale = s; }
+  void set_unique_textures(bool u) { textures_are_unique = u; }  // objects_container.cpp:342-345
+  void set_normal(const std::string& f) { normal_map_file = f; }  // objects_container.cpp:538-541
   void set_pos(float4 p) { pos = p; for (auto& o : objs) o.pos = p; }
   void offset_pos(float4 d) { set_pos(float4{pos.x + d.x, pos.y + d.y, pos.z + d.z, pos.w}); }
   void set_rot_quat(float4 q) { rot_quat = q; for (auto& o : objs) o.rot_quat = q; }
@@ -265,6 +291,7 @@ struct object_context {
         g.tid = (uint32_t)tex_ctx.get_gpu_position_id(o.tex);
         g.rid = o.normal_map ? (uint32_t)tex_ctx.get_gpu_position_id(o.normal_map) : 0xFFFFFFFFu;
         g.ssid = o.ss_map ? (uint32_t)tex_ctx.get_gpu_position_id(o.ss_map) : 0xFFFFFFFFu;
+        g.has_bump = o.has_bump;
         g.specular = o.specular;
         g.spec_mult = o.spec_mult;
         g.diffuse = o.diffuse;

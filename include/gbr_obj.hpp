@@ -4,15 +4,12 @@
 // (PNG through zlib, binary PPM, uncompressed TGA) in place of the
 // reference's SFML image loader (texture.cpp:323-358).
 //
-// As in the reference: one object per `usemtl` section, with the material's
-// map_Kd texture, or a 32x32 texture of its Kd colour, or magenta when the
-// material has neither; positions scaled by the container's requested scale;
-// vt and vn taken as written (the atlas upload flips rows as the reference).
-// Beyond the reference, which requires triangulated v/vt/vn faces: polygons
-// are split into fans, faces without vt get (0, 0) and faces without vn get
-// the face normal, and negative (relative) indices are resolved.  Textures must
-// be square powers of two from 16 to 2048 in the atlas; other images are
-// resampled (nearest texel) to the next power of two in that range.
+// obj_load follows the reference's parsing and material rules as they are
+// written (the comment above it lists them), so that on the files the
+// reference accepts it yields the same objects, triangles and texture choices;
+// it also reads polygons, relative indices and faces without vt or vn.
+// Textures must be square powers of two from 16 to 2048 in the atlas; other
+// images are resampled (nearest texel) to the next power of two in that range.
 //
 // Header-only; PNG decoding needs zlib (link -lz).
 #ifndef GBR_OBJ_HPP
@@ -26,7 +23,6 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
-#include <map>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -204,103 +200,189 @@ inline std::vector<uint8_t> resample_square(const std::vector<uint8_t>& rgba, in
   return out;
 }
 
-// texture::set_location + load: decode a file into a texture (cached by path
-// in the context, as make_new_cached).
-inline texture* texture_from_file(texture_context& ctx, std::map<std::string, texture*>& cache,
-                                  const std::string& path, std::string* error) {
-  auto it = cache.find(path);
-  if (it != cache.end()) return it->second;
+// texture::set_location + load: decode the image file at path into t, made
+// square for the atlas.
+inline bool texture_load_file(texture* t, const std::string& path, std::string* error) {
   int w = 0, h = 0;
   std::vector<uint8_t> px;
-  if (!load_image_rgba(path, w, h, px, error)) return nullptr;
+  if (!load_image_rgba(path, w, h, px, error)) return false;
   const int edge = atlas_edge(w, h);
-  texture* t = ctx.make_new();
   t->set_pixels(edge, resample_square(px, w, h, edge).data());
-  cache[path] = t;
+  t->set_location(path);
+  return true;
+}
+
+// The context's texture for an image file: make_new_cached(cache_name) (a new
+// texture when unique), located at path and decoded unless it already holds
+// that file's pixels (obj_load.cpp:452-460).  A new texture that cannot be
+// decoded is removed again and nullptr returned.
+inline texture* texture_file(texture_context& ctx, const std::string& cache_name, const std::string& path, bool unique,
+                             std::string* error) {
+  bool fresh = true;
+  texture* t = unique ? ctx.make_new() : ctx.make_new_cached(cache_name, &fresh);
+  if (fresh || t->rgba.empty() || t->location != path) {
+    if (!texture_load_file(t, path, error)) {
+      if (fresh) ctx.destroy(t);
+      return nullptr;
+    }
+  }
   return t;
 }
 
 // ---- OBJ / MTL -----------------------------------------------------------------
-struct obj_material {
-  std::string map_kd;
-  float kd[3] = {0, 0, 0};
-  bool has_kd = false;
-};
+// The rules of the reference's loader, stated on their own (obj_load.cpp:18-168).
+namespace obj_detail {
 
-inline std::map<std::string, obj_material> parse_mtl(const std::string& path) {
-  std::map<std::string, obj_material> mats;
+inline bool read_lines(const std::string& path, std::vector<std::string>& out) {
   std::ifstream f(path);
-  std::string line, cur;
-  while (std::getline(f, line)) {
-    std::istringstream in(line);
-    std::string key;
-    in >> key;
-    if (key == "newmtl") {
-      in >> cur;
-      mats[cur];
-    } else if (key == "map_Kd" && !cur.empty()) {
-      std::string rest;
-      std::getline(in, rest);
-      const size_t a = rest.find_first_not_of(" \t"), b = rest.find_last_not_of(" \t\r");
-      mats[cur].map_kd = a == std::string::npos ? "" : rest.substr(a, b - a + 1);
-    } else if (key == "Kd" && !cur.empty()) {
-      obj_material& m = mats[cur];
-      in >> m.kd[0] >> m.kd[1] >> m.kd[2];
-      m.has_kd = true;
-    }
-  }
-  return mats;
+  if (!f.is_open()) return false;
+  std::string line;
+  while (std::getline(f, line)) out.push_back(line);
+  return true;
 }
 
-// obj_load (obj_load.cpp:181-568): appends one object per usemtl section to c.
-// Returns false (with *error set) when the file cannot be read or is malformed.
+inline bool file_exists(const std::string& path) { return std::ifstream(path).good(); }
+
+// get_file_name (util.hpp:23-28): the text after the last '/' or '\'
+inline std::string file_name(const std::string& path) { return path.substr(path.find_last_of("/\\") + 1); }
+
+// is_samemtl (obj_load.cpp:26-29): a "newmtl " line whose text after its last
+// space begins with name
+inline bool is_samemtl(const std::string& line, const std::string& name) {
+  return line.compare(0, 7, "newmtl ") == 0 && line.compare(line.find_last_of(' ') + 1, name.size(), name) == 0;
+}
+
+// retrieve_diffuse_new (obj_load.cpp:32-50): the text after the last space of
+// the first "map_Kd " line at or after the material's newmtl line (the search
+// runs on into later materials), else ""
+inline std::string diffuse_name(const std::vector<std::string>& mtl, const std::string& name) {
+  bool found = false;
+  for (const std::string& l : mtl) {
+    found = found || is_samemtl(l, name);
+    if (found && l.compare(0, 7, "map_Kd ") == 0) return l.substr(l.find_last_of(' ') + 1);
+  }
+  return "";
+}
+
+// retrieve_bumpmap (obj_load.cpp:53-79): the material's own "map_Bump " file,
+// else "None"
+inline std::string bumpmap_name(const std::vector<std::string>& mtl, const std::string& name) {
+  bool found = false;
+  for (const std::string& l : mtl) {
+    if (is_samemtl(l, name)) {
+      found = true;
+      continue;
+    }
+    if (found && l.compare(0, 9, "map_Bump ") == 0) return l.substr(l.find_last_of(' ') + 1);
+    if (found && l.compare(0, 7, "newmtl ") == 0) return "None";
+  }
+  return "None";
+}
+
+// split (util.hpp:4-20): fields between single spaces, a trailing empty field dropped
+inline std::vector<std::string> split_spaces(const std::string& s) {
+  std::vector<std::string> out;
+  size_t a = 0;
+  while (a < s.size()) {
+    const size_t b = s.find(' ', a);
+    out.push_back(s.substr(a, b == std::string::npos ? std::string::npos : b - a));
+    if (b == std::string::npos) break;
+    a = b + 1;
+  }
+  return out;
+}
+
+// get_Kd (obj_load.cpp:83-116): the first line beginning "Kd" at or after the
+// material's newmtl line, its fields 1-3 read as doubles rounded to float
+inline bool get_kd(const std::vector<std::string>& mtl, const std::string& name, float kd[3]) {
+  bool found = false;
+  for (const std::string& l : mtl) {
+    if (is_samemtl(l, name)) {
+      found = true;
+      continue;
+    }
+    if (!found || l.compare(0, 2, "Kd") != 0) continue;
+    const std::vector<std::string> f = split_spaces(l);
+    if (f.size() < 4) return false;
+    for (int k = 0; k < 3; k++) kd[k] = (float)std::strtod(f[k + 1].c_str(), nullptr);
+    return true;
+  }
+  return false;
+}
+
+// decompose_attribute (obj_load.cpp:121-141): n values, each read from just
+// after the line's next space; the whole line as integers when it has no '.',
+// else as doubles rounded to float.  (A missing space wraps the position to
+// the start of the line, as the reference's int arithmetic does.)
+inline void attributes(const std::string& s, float* out, int n) {
+  const bool real = s.find('.') != std::string::npos;
+  size_t p = s.find(' ');
+  for (int i = 0; i < n; i++) {
+    const char* t = s.c_str() + (p + 1);
+    out[i] = real ? (float)std::strtod(t, nullptr) : (float)std::atoi(t);
+    p = s.find(' ', p + 1);
+  }
+}
+
+// col2cachename (texture.cpp:9-12): the cache name of a colour texture
+inline std::string colour_cache_name(float r, float g, float b, float a) {
+  return "CACHE" + std::to_string(r) + std::to_string(g) + std::to_string(b) + std::to_string(a);
+}
+
+// float to sf::Uint8 as the reference's sf::Color(float, ...) converts it
+inline uint8_t colour_byte(float x) { return (uint8_t)(int32_t)x; }
+
+}  // namespace obj_detail
+
+// obj_load (obj_load.cpp:181-568): appends one object per usemtl section to c
+// and returns true; false (with *error set) when the file cannot be opened, a
+// face index is out of range or an image cannot be decoded.
+//
+// The reference's rules, as it states them (on the files it accepts, with
+// triangulated v/vt/vn faces and positive indices, the result is the same):
+// lines classified by their first characters ("f ", "v ", "vt ", "vn ", "use",
+// "g "); attribute values as decompose_attribute reads them; face indices
+// resolved after the whole file is read; objects only for usemtl sections
+// (faces before the first usemtl belong to none), empty ones included, named
+// by the section's group when there are as many "g " lines as usemtl lines;
+// the diffuse texture is the material's map_Kd file (dir/name, else
+// dir/basename), else a 32x32 texture of Kd*255 (cached by colour), else a new
+// magenta 32x32 texture; a map_Bump file becomes the object's bump texture
+// (descriptor has_bump) and the container's set_normal file its normal map,
+// both cached by path; positions x requested_scale, vt and vn as written.
+// Beyond the reference: polygons become fans, relative (negative) indices
+// resolve against the counts so far, faces without vt get (0, 0) and faces
+// without vn the face normal.
 inline bool obj_load(objects_container* c, texture_context& tex_ctx, const std::string& filename, float scale,
                      std::string* error = nullptr) {
-  std::ifstream f(filename);
-  if (!f) {
+  std::vector<std::string> lines, mtl;
+  if (!obj_detail::read_lines(filename, lines)) {
     if (error) *error = filename + " could not be opened";
     return false;
   }
+  obj_detail::read_lines(filename.substr(0, filename.find_last_of('.')) + ".mtl", mtl);  // none: no materials
   const size_t slash = filename.find_last_of('/');
   const std::string dir = slash == std::string::npos ? "." : filename.substr(0, slash);
-  const size_t dot = filename.find_last_of('.');
-  std::map<std::string, obj_material> mats = parse_mtl(filename.substr(0, dot) + ".mtl");
-  std::vector<float> v, vt, vn;
-  struct Section {
-    std::string mtl;
-    std::vector<gbr_triangle> tris;
+
+  struct Corner {
+    long v, t, n;  // 0-based; -1 = absent (t, n)
   };
-  std::vector<Section> sections(1);
-  std::string line;
-  auto resolve = [](long i, size_t n) -> long { return i > 0 ? i - 1 : (i < 0 ? (long)n + i : -1); };
-  while (std::getline(f, line)) {
-    if (line.size() < 2) continue;
-    std::istringstream in(line);
-    std::string key;
-    in >> key;
-    if (key == "v") {
-      float a = 0, b = 0, cc = 0;
-      in >> a >> b >> cc;
-      v.insert(v.end(), {a, b, cc});
-    } else if (key == "vt") {
-      float a = 0, b = 0;
-      in >> a >> b;
-      vt.insert(vt.end(), {a, b});
-    } else if (key == "vn") {
-      float a = 0, b = 0, cc = 0;
-      in >> a >> b >> cc;
-      vn.insert(vn.end(), {a, b, cc});
-    } else if (key == "usemtl") {
-      std::string name;
-      in >> name;
-      if (!sections.back().tris.empty() || !sections.back().mtl.empty()) sections.push_back(Section());
-      sections.back().mtl = name;
-    } else if (key == "f") {
-      struct Corner { long v, t, n; };
+  struct Tri {
+    Corner k[3];
+  };
+  std::vector<float> v, vt, vn;
+  std::vector<Tri> faces;
+  std::vector<size_t> use_pos;
+  std::vector<std::string> use_name, group_name;
+  for (const std::string& ln : lines) {
+    const auto at = [&](size_t i) { return i < ln.size() ? ln[i] : '\0'; };
+    if (at(0) == 'f' && at(1) == ' ') {
+      std::istringstream in(ln.substr(2));
       std::vector<Corner> poly;
       std::string tok;
+      // 1-based, or negative = relative to the elements read so far, 0 = absent
+      const auto idx = [](long i, size_t n) -> long { return i > 0 ? i - 1 : (i < 0 ? (long)n + i : -1); };
       while (in >> tok) {
-        Corner k{-1, -1, -1};
         long parts[3] = {0, 0, 0};
         int np = 0;
         size_t s = 0;
@@ -311,65 +393,108 @@ inline bool obj_load(objects_container* c, texture_context& tex_ctx, const std::
           if (e == std::string::npos) break;
           s = e + 1;
         }
-        k.v = resolve(parts[0], v.size() / 3);
-        k.t = np > 1 ? resolve(parts[1], vt.size() / 2) : -1;
-        k.n = np > 2 ? resolve(parts[2], vn.size() / 3) : -1;
-        if (k.v < 0 || (size_t)k.v >= v.size() / 3 || (size_t)(k.t + 1) > vt.size() / 2 + 1 ||
-            (size_t)(k.n + 1) > vn.size() / 3 + 1) {
-          if (error) *error = filename + ": face index out of range: " + line;
-          return false;
-        }
+        Corner k;
+        k.v = parts[0] ? idx(parts[0], v.size() / 3) : -2;
+        k.t = np > 1 ? idx(parts[1], vt.size() / 2) : -1;
+        k.n = np > 2 ? idx(parts[2], vn.size() / 3) : -1;
         poly.push_back(k);
       }
-      for (size_t i = 1; i + 1 < poly.size(); i++) {  // fan
-        const Corner cs[3] = {poly[0], poly[i], poly[i + 1]};
-        gbr_triangle t;
-        std::memset(&t, 0, sizeof t);
-        float p[3][3];
-        for (int k = 0; k < 3; k++)
-          for (int a = 0; a < 3; a++) p[k][a] = v[cs[k].v * 3 + a];
-        const float e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
-        const float e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
-        float fnrm[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-        const float fl = std::sqrt(fnrm[0] * fnrm[0] + fnrm[1] * fnrm[1] + fnrm[2] * fnrm[2]);
-        for (float& x : fnrm) x = fl > 0 ? x / fl : 0.f;
-        for (int k = 0; k < 3; k++) {
-          gbr_vertex& vx = t.vertices[k];
-          for (int a = 0; a < 3; a++) vx.pos[a] = p[k][a] * scale;  // implement scale here (obj_load.cpp:437)
-          if (cs[k].t >= 0) { vx.vt[0] = vt[cs[k].t * 2]; vx.vt[1] = vt[cs[k].t * 2 + 1]; }
-          for (int a = 0; a < 3; a++) vx.normal[a] = cs[k].n >= 0 ? vn[cs[k].n * 3 + a] : fnrm[a];
-        }
-        sections.back().tris.push_back(t);
-      }
+      for (size_t i = 1; i + 1 < poly.size(); i++) faces.push_back(Tri{{poly[0], poly[i], poly[i + 1]}});
+    } else if (at(0) == 'v' && at(1) == ' ') {
+      float a[3];
+      obj_detail::attributes(ln, a, 3);
+      v.insert(v.end(), a, a + 3);
+    } else if (at(0) == 'v' && at(1) == 't' && at(2) == ' ') {
+      float a[2];
+      obj_detail::attributes(ln, a, 2);
+      vt.insert(vt.end(), a, a + 2);
+    } else if (at(0) == 'v' && at(1) == 'n' && at(2) == ' ') {
+      float a[3];
+      obj_detail::attributes(ln, a, 3);
+      vn.insert(vn.end(), a, a + 3);
+    } else if (at(0) == 'u' && at(1) == 's' && at(2) == 'e') {
+      use_pos.push_back(faces.size());
+      use_name.push_back(ln.substr(ln.find_last_of(' ') + 1));
+    } else if (at(0) == 'g' && at(1) == ' ') {
+      group_name.push_back(ln.substr(ln.find_last_of(' ') + 1));
     }
   }
-  std::map<std::string, texture*> cache;
-  for (const Section& sec : sections) {
-    if (sec.tris.empty()) continue;
+
+  // resolve: positions x scale (w = 0 x scale, as mult), vt and vn as written
+  const size_t nv = v.size() / 3, nvt = vt.size() / 2, nvn = vn.size() / 3;
+  std::vector<gbr_triangle> tris(faces.size());
+  for (size_t f = 0; f < faces.size(); f++) {
+    const Corner* cs = faces[f].k;
+    for (int k = 0; k < 3; k++)
+      if (cs[k].v < 0 || (size_t)cs[k].v >= nv || cs[k].t < -1 || cs[k].t >= (long)nvt || cs[k].n < -1 ||
+          cs[k].n >= (long)nvn) {
+        if (error) *error = filename + ": face index out of range in face " + std::to_string(f + 1);
+        return false;
+      }
+    gbr_triangle& t = tris[f];
+    std::memset(&t, 0, sizeof t);
+    float p[3][3];
+    for (int k = 0; k < 3; k++)
+      for (int a = 0; a < 3; a++) p[k][a] = v[cs[k].v * 3 + a];
+    const float e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+    const float e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+    float fnrm[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const float fl = std::sqrt(fnrm[0] * fnrm[0] + fnrm[1] * fnrm[1] + fnrm[2] * fnrm[2]);
+    for (float& x : fnrm) x = fl > 0 ? x / fl : 0.f;
+    for (int k = 0; k < 3; k++) {
+      gbr_vertex& vx = t.vertices[k];
+      for (int a = 0; a < 3; a++) vx.pos[a] = p[k][a] * scale;  // implement scale here (obj_load.cpp:437)
+      vx.pos[3] = 0.f * scale;
+      if (cs[k].t >= 0) { vx.vt[0] = vt[cs[k].t * 2]; vx.vt[1] = vt[cs[k].t * 2 + 1]; }
+      for (int a = 0; a < 3; a++) vx.normal[a] = cs[k].n >= 0 ? vn[cs[k].n * 3 + a] : fnrm[a];
+    }
+  }
+
+  // one object per usemtl section, with its textures
+  use_pos.push_back(tris.size());
+  const bool using_groups = use_name.size() == group_name.size();
+  const bool unique = c->textures_are_unique;
+  for (size_t i = 0; i + 1 < use_pos.size(); i++) {
+    const std::string tex_name = obj_detail::diffuse_name(mtl, use_name[i]);
+    const std::string bump_name = obj_detail::bumpmap_name(mtl, use_name[i]);
+    std::string full = dir + "/" + tex_name;
+    const std::string cache_name = full;
+    bool exists = obj_detail::file_exists(full);
+    if (!exists && !tex_name.empty()) {
+      full = dir + "/" + obj_detail::file_name(tex_name);
+      exists = obj_detail::file_exists(full);
+    }
     texture* tex = nullptr;
-    const auto m = mats.find(sec.mtl);
-    if (m != mats.end() && !m->second.map_kd.empty()) tex = texture_from_file(tex_ctx, cache, dir + "/" + m->second.map_kd, error);
-    if (!tex) {
-      // the material's Kd as a 32x32 texture, else magenta (obj_load.cpp:508-540)
-      const bool kd = m != mats.end() && m->second.has_kd;
-      const std::string key = kd ? "kd:" + std::to_string(m->second.kd[0]) + "," + std::to_string(m->second.kd[1]) +
-                                       "," + std::to_string(m->second.kd[2])
-                                 : "kd:magenta";
-      auto it = cache.find(key);
-      if (it != cache.end()) {
-        tex = it->second;
-      } else {
-        tex = tex_ctx.make_new();
-        if (kd)
-          tex->set_create_colour((uint8_t)(m->second.kd[0] * 255.f), (uint8_t)(m->second.kd[1] * 255.f),
-                                 (uint8_t)(m->second.kd[2] * 255.f), 255, 32);
-        else
-          tex->set_create_colour(255, 0, 255, 255, 32);
-        cache[key] = tex;
-      }
+    float kd[3];
+    if (!tex_name.empty() && exists) {
+      if (!(tex = texture_file(tex_ctx, cache_name, full, unique, error))) return false;
+    } else if (obj_detail::get_kd(mtl, use_name[i], kd)) {
+      const float r = kd[0] * 255.f, g = kd[1] * 255.f, b = kd[2] * 255.f;
+      tex = unique ? tex_ctx.make_new() : tex_ctx.make_new_cached(obj_detail::colour_cache_name(r, g, b, 255.f));
+      tex->set_create_colour(obj_detail::colour_byte(r), obj_detail::colour_byte(g), obj_detail::colour_byte(b), 255,
+                             32);
+    } else {
+      tex = tex_ctx.make_new();
+      tex->set_create_colour(255, 0, 255, 255, 32);
     }
-    c->add_object(sec.tris, tex);
+    texture* bump = nullptr;
+    if (bump_name != "None") {
+      const std::string bump_full = dir + "/" + bump_name;
+      if (!(bump = texture_file(tex_ctx, bump_full, bump_full, false, error))) return false;
+    }
+    texture* normal = nullptr;
+    if (!c->normal_map_file.empty() &&
+        !(normal = texture_file(tex_ctx, c->normal_map_file, c->normal_map_file, false, error)))
+      return false;
+    c->add_object(std::vector<gbr_triangle>(tris.begin() + use_pos[i], tris.begin() + use_pos[i + 1]), tex);
+    object& o = c->objs.back();
+    o.object_name = using_groups ? group_name[i] : "";
+    o.bump = bump;
+    o.has_bump = bump != nullptr;
+    o.normal_map = normal;
   }
+  c->current_scale = scale;
+  c->requested_scale = 1.f;
   return true;
 }
 

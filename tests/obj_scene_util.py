@@ -43,6 +43,64 @@ def write_png(path, rgba):
         f.write(chunk(b"IEND", b""))
 
 
+def read_png(path):
+    """RGBA8 texels of an 8-bit, non-interlaced PNG (grey, RGB, palette, grey +
+    alpha or RGBA), decoded here independently of the loader's decoder."""
+    d = open(path, "rb").read()
+    assert d[:8] == b"\x89PNG\r\n\x1a\n", path
+    pos, idat, plte, trns = 8, b"", None, b""
+    while pos < len(d):
+        n, t = struct.unpack(">I", d[pos:pos + 4])[0], d[pos + 4:pos + 8]
+        c = d[pos + 8:pos + 8 + n]
+        if t == b"IHDR":
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", c)
+        elif t == b"PLTE":
+            plte = np.frombuffer(c, np.uint8).reshape(-1, 3)
+        elif t == b"tRNS":
+            trns = c
+        elif t == b"IDAT":
+            idat += c
+        pos += 12 + n
+    assert depth == 8 and interlace == 0, path
+    bpp = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, w * bpp + 1)
+    img = np.zeros((h, w * bpp), np.uint8)
+    prev = np.zeros(w * bpp, np.int64)
+    for y in range(h):
+        ft, row = int(raw[y, 0]), raw[y, 1:].astype(np.int64)
+        if ft == 0:
+            cur = row
+        elif ft == 1:  # sub: a running sum per channel
+            cur = np.cumsum(row.reshape(w, bpp), axis=0).reshape(-1) & 0xFF
+        elif ft == 2:
+            cur = (row + prev) & 0xFF
+        else:
+            cur = np.zeros_like(row)
+            for i in range(len(row)):
+                a = int(cur[i - bpp]) if i >= bpp else 0
+                b = int(prev[i])
+                cc = int(prev[i - bpp]) if i >= bpp else 0
+                cur[i] = (int(row[i]) + ((a + b) // 2 if ft == 3 else _paeth(a, b, cc))) & 0xFF
+        img[y] = cur
+        prev = cur
+    px = img.reshape(h, w, bpp)
+    out = np.full((h, w, 4), 255, np.uint8)
+    if ctype in (0, 4):
+        out[..., :3] = px[..., :1]
+        if ctype == 4:
+            out[..., 3] = px[..., 1]
+    elif ctype == 2:
+        out[..., :3] = px
+    elif ctype == 6:
+        out[:] = px
+    else:
+        out[..., :3] = plte[px[..., 0]]
+        alpha = np.full(256, 255, np.uint8)
+        alpha[:len(trns)] = np.frombuffer(trns, np.uint8)
+        out[..., 3] = alpha[px[..., 0]]
+    return out
+
+
 def write_ppm(path, rgb):
     h, w, _ = rgb.shape
     with open(path, "wb") as f:
