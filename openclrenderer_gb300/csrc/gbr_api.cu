@@ -90,6 +90,7 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view) {
   TRY(w.scan_part.reserve(scan_chunks(sh.nfine)));
   TRY(w.ctr.reserve(1));
   if (view) TRY(w.pix_rec.reserve(sh.npix));
+  if (view) TRY(w.tile_empty.reserve(sh.nfine));
   if (view) TRY(w.vis.reserve((size_t)std::max<uint32_t>(sh.nitems, 1) * std::max<uint32_t>((sh.nobjects + 31) / 32, 1)));
   return GBR_OK;
 }
@@ -301,6 +302,10 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   }
   const bool fused = view && sh.shade && sh.nseg > 0;
   const bool piped = !fused && view && sh.shade && sh.ngroups > 1 && split && on_side;
+  if (view && sh.shade && !fused) {  // the raster finishes tiles without records
+    ws.views = wm.views.p;
+    ws.tile_empty = wm.tile_empty.p;
+  }
   if (piped) {
     // each group's raster, then its event: kernel3 of the group runs on st
     // after it, beside the next groups' rasters

@@ -440,7 +440,7 @@ gbr_status gbr_batch_get_info(gbr_batch* b, gbr_batch_info* out) {
   for (const WorkMem* w : {&b->wv, &b->wsh}) {
     bytes += w->rec.cap * sizeof(RasterRec) + w->srec.cap * sizeof(ShadeRec) + w->bins.cap * 4;
     bytes += (w->fine_count.cap + w->fine_off.cap + w->coarse_count.cap + w->coarse_off.cap) * 4;
-    bytes += (w->pix_rec.cap + w->pix_depth.cap) * 4;
+    bytes += (w->pix_rec.cap + w->pix_depth.cap) * 4 + w->tile_empty.cap;
   }
   out->scratch_bytes = bytes;
   return GBR_OK;

@@ -171,6 +171,13 @@ struct Workspace {
   const uint32_t* vis;  // views: object cull bits (k_object_cull), vis_words per view, or null
   uint32_t vis_words;
   uint32_t pack_keys;   // views: every key (2 * triangle + 1) is below 2^23 - 1 (32-bit id resolve)
+  // Views that shade, raster and kernel3 in separate launches: the raster
+  // writes kernel3's output for a tile without records (the clear colour, zero
+  // normals) unless its view blends in another context, and sets
+  // tile_empty[tile] to 1 for such a tile, else 0; kernel3 then leaves the
+  // tile alone.  Null otherwise.
+  const ViewParams* views;
+  uint8_t* tile_empty;
   Counters* ctr;
   int32_t fine_max;      // Tuning::fine_max
   int32_t coarse_shift;  // Tuning::coarse_shift

@@ -739,16 +739,6 @@ __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __res
   }
 }
 
-// The surface owning a tile (binary search over tile_base, one thread).
-__device__ __forceinline__ uint32_t find_surface(const Surface* surfs, uint32_t nsurf, uint32_t tile) {
-  uint32_t lo = 0, hi = nsurf - 1;
-  while (lo < hi) {
-    uint32_t mid = (lo + hi + 1) >> 1;
-    if (surfs[mid].tile_base <= tile) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 // The surface owning a tile, found by one warp: surfaces are sorted by
 // tile_base, so one ballot over 32 of them finds the last one starting at or
 // before the tile.  Every lane of the warp must call it; all get the result.
@@ -820,6 +810,11 @@ __device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp
 __device__ __forceinline__ int swz32(int p) { return p ^ ((p >> 5) & 15); }
 __device__ __forceinline__ int swz64(int p) { return p ^ ((p >> 4) & 15); }
 
+// kernel3's RGBA8 output word
+__device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
+  return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
+}
+
 // Shared memory of one tile's raster (NT threads).
 template <int NT>
 struct RasterSmem {
@@ -833,12 +828,13 @@ struct RasterSmem {
   uint32_t sscan;
   uint32_t ssamples;
   Surface S;
+  uint32_t s;  // the tile's surface
   uint32_t lists[4];
 };
 
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
 // (views) or only the depth (cube faces).  surface: the tile's surface when
-// the caller knows it, else -1 (binary search).  Every thread of the block
+// the caller knows it, else -1 (found by warp 0).  Every thread of the block
 // calls it; the caller synchronises before reusing the shared memory.
 template <int NT, bool ID>
 __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* __restrict__ surfs, uint32_t nsurf,
@@ -858,17 +854,21 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   Surface& S = sm.S;
   uint32_t* lists = sm.lists;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) {
-    const uint32_t s = surface >= 0 ? (uint32_t)surface : find_surface(surfs, nsurf, tile);
-    S = surfs[s];
-    uint32_t lt = tile - S.tile_base;
-    int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
-    uint32_t ct = S.ctile_base + (ty >> ws.coarse_shift) * S.ctiles_x + (tx >> ws.coarse_shift);
-    lists[0] = ws.fine_off[tile];
-    lists[1] = ws.fine_count[tile];
-    lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
-    lists[3] = ws.coarse_count[ct];
-    ssamples = 0;
+  if (tid < 32) {  // warp 0: the tile's surface (one ballot search) and its bins
+    const uint32_t foff = tid == 0 ? ws.fine_off[tile] : 0u, fcnt = tid == 0 ? ws.fine_count[tile] : 0u;
+    const uint32_t s = surface >= 0 ? (uint32_t)surface : (nsurf > 1 ? find_surface_warp(surfs, nsurf, tile) : 0u);
+    if (tid == 0) {
+      S = surfs[s];
+      sm.s = s;
+      uint32_t lt = tile - S.tile_base;
+      int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
+      uint32_t ct = S.ctile_base + (ty >> ws.coarse_shift) * S.ctiles_x + (tx >> ws.coarse_shift);
+      lists[0] = foff;
+      lists[1] = fcnt;
+      lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
+      lists[3] = ws.coarse_count[ct];
+      ssamples = 0;
+    }
   }
   if (with_id) {
     for (int p = tid; p < kTilePixels; p += NT) {
@@ -880,6 +880,21 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
   if (with_id && lists[1] + lists[3] == 0) {  // no records: an empty tile
+    // kernel3's output here is the clear colour and zero normals, unless the
+    // view blends in another context's colour: write it, and mark the tile
+    uint32_t* rgba = nullptr;
+    uint32_t* nrm = nullptr;
+    uint32_t clear = 0;
+    if (ws.tile_empty) {
+      const ViewParams& V = ws.views[sm.s];
+      const bool direct = V.blend_depth == nullptr;
+      if (direct) {
+        rgba = reinterpret_cast<uint32_t*>(V.rgba);
+        nrm = reinterpret_cast<uint32_t*>(V.normals);
+        clear = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
+      }
+      if (tid == 0) ws.tile_empty[tile] = direct ? 1 : 0;
+    }
     for (int lp = tid; lp < kTilePixels; lp += NT) {
       const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
       if (px < S.width && py < S.height) {
@@ -887,10 +902,13 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
         S.depth[p] = kDepthClear;
         if (S.id) S.id[p] = kNoId;
         S.rec[p] = kNoId;
+        if (rgba) rgba[p] = clear;
+        if (nrm) nrm[p] = 0;
       }
     }
     return;
   }
+  if (with_id && ws.tile_empty && tid == 0) ws.tile_empty[tile] = 0;
   if (!with_id) {
     // depth-only passes: the surface was cleared and holds the small
     // triangles the setup rasterised; a tile without records keeps it as is
@@ -1336,10 +1354,6 @@ __device__ __forceinline__ float c_rational_acos(float x) {
   return fma_(x * fma_(b, x2, a), crcp(fma_(x2, fma_(d, x2, c), 1.0f)), kPi / 2.0f);
 }
 
-__device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a) {
-  return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
-}
-
 
 // Colour-only square root (approximate; exact IEEE result for 0, negative,
 // infinite and NaN inputs).
@@ -1448,40 +1462,41 @@ __device__ __forceinline__ f4 blend_texel(const uint8_t* __restrict__ rgba, size
   return o;
 }
 
+// kernel3's output for a pixel with nothing to shade (depth d): the clear
+// colour and zero normals.  FEAT: kernel3's optional switches (view flags)
+// compiled in.
+template <bool FEAT>
+__device__ __forceinline__ void shade_clear(const ViewParams& V, size_t p, uint32_t d) {
+  uint32_t* out = reinterpret_cast<uint32_t*>(V.rgba);
+  if (out) {
+    f4 c;
+    c.x = V.clear[0]; c.y = V.clear[1]; c.z = V.clear[2]; c.w = V.clear[3];
+    // CAN_INTEGRATED_BLEND (cl2.cl:5839-5851): the other context's colour
+    // over the clear colour where it has depth; its .xyzz swizzle gives
+    // alpha = blue
+    if (FEAT && V.blend_depth && V.blend_depth[p] < d) {
+      const f4 o = blend_texel(V.blend_rgba, p);
+      c.x = fma_(o.x, o.w, c.x * (1.0f - o.w));
+      c.y = fma_(o.y, o.w, c.y * (1.0f - o.w));
+      c.z = fma_(o.z, o.w, c.z * (1.0f - o.w));
+      c.w = c.z;
+    }
+    out[p] = pack_rgba(c.x, c.y, c.z, c.w);
+  }
+  if (V.normals) reinterpret_cast<uint32_t*>(V.normals)[p] = 0;
+}
+
+// kernel3 for a covered pixel: depth d, record r (< the pass's record count).
 // colx[i] = ((float)(x0 + i) - W/2) / fov and rowy[j] likewise for the tile's
 // 17 columns and rows: the per-column / per-row divisions of get_vtdiff.
-// nrec: the records this pass wrote; the raster stores only indices below it
-// in the record map, and any other value is treated as an empty pixel, so no
-// index read from the map can leave the record arrays.
-// FEAT: kernel3's optional switches (view flags) compiled in.
 template <bool FEAT>
-__device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
-                            const ShadeRec* __restrict__ srec, uint32_t nrec, const float4* __restrict__ lights,
-                            int x, int y, const float* __restrict__ colx, const float* __restrict__ rowy) {
+__device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Surface& S,
+                              const ShadeRec* __restrict__ srec, const float4* __restrict__ lights, int x, int y,
+                              uint32_t d, uint32_t r, const float* __restrict__ colx,
+                              const float* __restrict__ rowy) {
   const int W = S.width, H = S.height;
   const size_t p = (size_t)y * W + x;
-  const uint32_t d = S.depth[p];
-  const uint32_t r = S.rec[p];
   uint32_t* out = reinterpret_cast<uint32_t*>(V.rgba);
-  if (d == kDepthClear || r >= nrec) {
-    if (out) {
-      f4 c;
-      c.x = V.clear[0]; c.y = V.clear[1]; c.z = V.clear[2]; c.w = V.clear[3];
-      // CAN_INTEGRATED_BLEND (cl2.cl:5839-5851): the other context's colour
-      // over the clear colour where it has depth; its .xyzz swizzle gives
-      // alpha = blue
-      if (FEAT && V.blend_depth && V.blend_depth[p] < d) {
-        const f4 o = blend_texel(V.blend_rgba, p);
-        c.x = fma_(o.x, o.w, c.x * (1.0f - o.w));
-        c.y = fma_(o.y, o.w, c.y * (1.0f - o.w));
-        c.z = fma_(o.z, o.w, c.z * (1.0f - o.w));
-        c.w = c.z;
-      }
-      out[p] = pack_rgba(c.x, c.y, c.z, c.w);
-    }
-    if (V.normals) reinterpret_cast<uint32_t*>(V.normals)[p] = 0;
-    return;
-  }
   const float fov = V.fov;
   const f3 cpos = mk3(V.cpos[0], V.cpos[1], V.cpos[2]);
   const f3 cc = mk3(V.ccos[0], V.ccos[1], V.ccos[2]);
@@ -1687,6 +1702,24 @@ __device__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surfa
   }
 }
 
+// kernel3 for one pixel.  nrec: the records this pass wrote; the raster
+// stores only indices below it in the record map, and any other value is
+// treated as an empty pixel, so no index read from the map can leave the
+// record arrays.
+template <bool FEAT>
+__device__ __forceinline__ void shade_pixel(const SceneDev& sc, const ViewParams& V, const Surface& S,
+                                            const ShadeRec* __restrict__ srec, uint32_t nrec,
+                                            const float4* __restrict__ lights, int x, int y,
+                                            const float* __restrict__ colx, const float* __restrict__ rowy) {
+  const size_t p = (size_t)y * S.width + x;
+  const uint32_t d = S.depth[p];
+  const uint32_t r = S.rec[p];
+  if (d == kDepthClear || r >= nrec)
+    shade_clear<FEAT>(V, p, d);
+  else
+    shade_covered<FEAT>(sc, V, S, srec, lights, x, y, d, r, colx, rowy);
+}
+
 // Shared memory of one tile's shading.
 struct ShadeSmem {
   float4 lights[kMaxLights * kLightQuads];
@@ -1729,22 +1762,80 @@ __device__ __forceinline__ void shade_tile(const SceneDev& sc, const ViewParams*
 // A pass whose setup or binning overflowed its scratch leaves the depth and
 // record map unwritten (the raster returns at once); shading returns too, and
 // the host re-runs the pass with grown scratch.
+// tile_empty (or null): tiles whose output the raster wrote (Workspace).
 template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec, const Counters* __restrict__ ctr,
-                                               uint32_t rec_cap, uint32_t tile0) {
+                                               uint32_t rec_cap, uint32_t tile0,
+                                               const uint8_t* __restrict__ tile_empty) {
+  constexpr int NW = kTilePixels / 32;
   __shared__ ShadeSmem sm;
-  __shared__ uint32_t s_id;
+  __shared__ uint32_t s_id, s_done;
+  __shared__ uint32_t s_warp[NW];
+  __shared__ uint32_t s_px[kTilePixels], s_d[kTilePixels], s_r[kTilePixels];
   if (ctr->overflow) return;
   const uint32_t nrec = min(ctr->nrec, rec_cap);
   const uint32_t tile = tile0 + blockIdx.x;
   if (threadIdx.x < 32) {
+    const uint32_t done = (tile_empty && threadIdx.x == 0) ? tile_empty[tile] : 0u;
     const uint32_t sid = find_surface_warp(surfs, nviews, tile);
-    if (threadIdx.x == 0) s_id = sid;
+    if (threadIdx.x == 0) {
+      s_id = sid;
+      s_done = done;
+    }
   }
   __syncthreads();
-  shade_tile<FEAT, 256>(sc, views, surfs, srec, nrec, tile, s_id, sm);
+  if (s_done) return;
+  const Surface& S = surfs[s_id];
+  const ViewParams& V = views[s_id];
+  const uint32_t lt = tile - S.tile_base;
+  const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
+  // the thread's own pixel: empty pixels are written at once; covered ones
+  // are compacted (in pixel order) so that whole warps shade them
+  const int lp = threadIdx.x, lane = lp & 31, warp = lp >> 5;
+  const int x = x0 + (lp & (kTile - 1)), y = y0 + lp / kTile;
+  const bool inside = x < S.width && y < S.height;
+  const size_t p = (size_t)y * S.width + x;
+  uint32_t d = kDepthClear, r = kNoId;
+  if (inside) {
+    d = S.depth[p];
+    r = S.rec[p];
+  }
+  const bool cov = inside && d != kDepthClear && r < nrec;
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, cov);
+  if (lane == 0) s_warp[warp] = __popc(m);
+  if (inside && !cov) shade_clear<FEAT>(V, p, d);
+  const bool linear = V.use_linear != 0;
+  for (uint32_t i = threadIdx.x; i < sc.nlights; i += kTilePixels)
+    stage_light(sc.lights + i, linear, sm.lights + kLightQuads * i);
+  if (threadIdx.x < 2 * (kTile + 1)) {
+    const int i = threadIdx.x % (kTile + 1);
+    if (threadIdx.x <= kTile)
+      sm.colx[i] = fdiv((float)(x0 + i) - (float)S.width / 2.0f, V.fov);
+    else
+      sm.rowy[i] = fdiv((float)(y0 + i) - (float)S.height / 2.0f, V.fov);
+  }
+  __syncthreads();
+  uint32_t base = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < NW; w++) {
+    const uint32_t c = s_warp[w];
+    base += w < warp ? c : 0u;
+    total += c;
+  }
+  if (cov) {
+    const uint32_t k = base + __popc(m & ((1u << lane) - 1u));
+    s_px[k] = (uint32_t)lp;
+    s_d[k] = d;
+    s_r[k] = r;
+  }
+  __syncthreads();
+  if (threadIdx.x < total) {
+    const uint32_t q = s_px[threadIdx.x];
+    shade_covered<FEAT>(sc, V, S, srec, sm.lights, x0 + (int)(q & (kTile - 1)), y0 + (int)(q / kTile),
+                        s_d[threadIdx.x], s_r[threadIdx.x], sm.colx, sm.rowy);
+  }
 }
 
 // ---- the fused raster -> shade pass of many views ------------------------------
@@ -2071,9 +2162,11 @@ cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t
   if (!ntiles) return cudaSuccess;
   if (!sc.objq || !sc.texlv || !ws.srec) return cudaErrorInvalidValue;
   if (features)
-    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0);
+    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
+                                          ws.tile_empty);
   else
-    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0);
+    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
+                                           ws.tile_empty);
   return cudaGetLastError();
 }
 

@@ -70,7 +70,8 @@ constexpr size_t kOffBins = align256(kOffSrec + sizeof(ShadeRec) * kMaxRecords);
 constexpr size_t kOffPix = align256(kOffBins + 4 * kMaxBins);
 constexpr size_t kOffObj = align256(kOffPix + 4 * kMaxPixels);
 constexpr size_t kOffTexLv = align256(kOffObj + sizeof(float4) * kObjQuads * kMaxObjects);
-constexpr size_t kScratchBytes = align256(kOffTexLv + sizeof(float4) * kTexLevels * kMaxTextures);
+constexpr size_t kOffTileEmpty = align256(kOffTexLv + sizeof(float4) * kTexLevels * kMaxTextures);
+constexpr size_t kScratchBytes = align256(kOffTileEmpty + kMaxFineTiles);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -230,6 +231,10 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   ws.pack_keys = sc->ntris < (1u << 22) - 1;
   Surface* d_surf = reinterpret_cast<Surface*>(base + kOffSurface);
   ViewParams* d_view = reinterpret_cast<ViewParams*>(base + kOffView);
+  if (shade) {  // the raster finishes tiles without records
+    ws.views = d_view;
+    ws.tile_empty = reinterpret_cast<uint8_t*>(base + kOffTileEmpty);
+  }
 
   cudaError_t e;
 #define NA_CU(call, what)                                    \

@@ -94,6 +94,7 @@ struct WorkMem {
   DevBuf<RasterRec> rec;
   DevBuf<ShadeRec> srec;
   DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins, scan_part;
+  DevBuf<uint8_t> tile_empty;  // views that shade: per fine tile, whether the raster wrote kernel3's output
   DevBuf<Counters> ctr;
   DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
   DevBuf<uint8_t> pix_rgba;
@@ -104,7 +105,7 @@ struct WorkMem {
   DevBuf<uint32_t> vis;           // views: object cull bits
   uint32_t rec_target = 0, bin_target = 0;
   void release() {
-    rec.release(); srec.release(); fine_count.release(); fine_off.release();
+    rec.release(); srec.release(); fine_count.release(); fine_off.release(); tile_empty.release();
     coarse_count.release(); coarse_off.release(); bins.release(); scan_part.release(); ctr.release();
     pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
     surf.release(); views.release(); jobs.release(); sched.release(); queue.release(); vis.release();
