@@ -1372,9 +1372,13 @@ __device__ __forceinline__ float c_gamma_fwd(float c) {
   return c * fma_(fma_(0.305306011f, c, 0.682171111f), c, 0.012522878f);
 }
 
+// kernel3's attenuation cutoff: a light adds (illum - 0.1) / 0.9 where that is positive
+constexpr float kLightCutoff = 0.1f;
+
 // A light as the shade loop reads it, staged once per CTA in shared memory
-// as three float4: (pos, cut2), (colour, brightness), (radius, 1 / radius
-// approximated, diffuse, shadow | is_static << 1).  The colour is already in
+// as three float4: (pos, cut2), (colour, brightness, divided by 1 - cutoff
+// for lights without shadows), (radius, 1 / radius approximated, diffuse,
+// shadow | is_static << 1).  The colour is already in
 // linear space when the view renders linearly (the same gamma_fwd every pixel
 // would apply).  cut2 is a conservative squared distance beyond which a light
 // without shadows stays under kernel3's attenuation cutoff, so the pixel
@@ -1399,8 +1403,11 @@ __device__ __forceinline__ void stage_light(const gbr_light* L, bool linear, flo
       cut2 = (rs * rs) * 1.00001f;
     }
   }
+  // lights without shadows fold kernel3's cutoff into the brightness:
+  // (b / tt^2 - 0.1) / 0.9 = (b / 0.9) / tt^2 - 0.1 / 0.9 (colour only)
+  const float bw = L->shadow ? brightness : brightness * (1.0f / (1.0f - kLightCutoff));
   dst[0] = make_float4(L->pos[0], L->pos[1], L->pos[2], cut2);
-  dst[1] = make_float4(c.x, c.y, c.z, brightness);
+  dst[1] = make_float4(c.x, c.y, c.z, bw);
   dst[2] = make_float4(radius, crcp(radius), L->diffuse,
                        __uint_as_float((L->shadow ? 1u : 0u) | (L->is_static ? 2u : 0u)));
 }
@@ -1602,10 +1609,12 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
   const float g_diffuse = oq2.w, g_spec_mult = oq3.x;
   const float rough = oq3.y;  // clamp(1 - specular, 0.001, 10)
   // per-pixel factors of the light loop (colour only)
-  const float ndv = fmax_(0.0f, cdot3(normal, l2p));
+  const float ndv_raw = cdot3(normal, l2p);
+  const float ndv = fmax_(0.0f, ndv_raw);
   const float r_pndv = crcp(kPi * ndv);  // spec / (pi ndv)
   const float nr2 = -crcp(rough * rough);  // Gaussian exponent -alpha^2 / rough^2
   const float spec_k = 0.4f * g_spec_mult;
+  const float amb1 = 1.0f - ambient;
   f3 dsum = mk3(0, 0, 0), ssum = mk3(0, 0, 0);
   int shnum = 0, static_num = 0;
   for (uint32_t i = 0; i < sc.nlights; i++) {
@@ -1620,44 +1629,66 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
     if (d2 > LA.w) continue;
     const float4 LB = lights[kLightQuads * i + 1], LC = lights[kLightQuads * i + 2];
     const uint32_t lflags = __float_as_uint(LC.w);
-    const bool lshadow = (lflags & 1u) != 0;
-    float occlusion = 1.0f;
-    if (lflags == 3u) {  // shadow and is_static
-      int face = ret_cubeface(gpos, lpos);
-      occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
-      static_num++;
-    }
-    const float rinv = rsqrtf(d2);
-    float illum;
-    if (lshadow) {
-      const float tt = fdiv(fsqrt(d2), LC.x) + 1.0f;
-      illum = fdiv(LB.w, tt * tt);
-    } else {
-      const float distance = (d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
-      const float tt = fma_(distance, LC.y, 1.0f);
-      illum = LB.w * crcp(tt * tt);
-    }
-    const float cutoff = 0.1f;
-    illum -= cutoff;
-    illum *= 1.0f / (1.0f - cutoff);
-    if (illum <= 0) continue;
     const f3 lcol = mk3(LB.x, LB.y, LB.z);
-    if (lshadow && recv_dyn) {
-      int face = ret_cubeface(gpos, lpos);
-      float dyn = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_dyn, face, gpos, shnum);
-      occlusion = fmin_(occlusion, dyn);
-      shnum++;
+    const float rinv = rsqrtf(d2);
+    if (lflags & 1u) {  // a shadow light
+      float occlusion = 1.0f;
+      if (lflags & 2u) {  // is_static
+        int face = ret_cubeface(gpos, lpos);
+        occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
+        static_num++;
+      }
+      const float tt = fdiv(fsqrt(d2), LC.x) + 1.0f;
+      float illum = fdiv(LB.w, tt * tt);
+      illum -= kLightCutoff;
+      illum *= 1.0f / (1.0f - kLightCutoff);
+      if (illum <= 0) continue;
+      if (recv_dyn) {
+        int face = ret_cubeface(gpos, lpos);
+        float dyn = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_dyn, face, gpos, shnum);
+        occlusion = fmin_(occlusion, dyn);
+        shnum++;
+      }
+      ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
+      // Lambert + ambient
+      const float light = fmax_(cdot3(ptl, lnormal) * occlusion, 0.0f);
+      const float dscale = fma_(amb1, light, ambient) * ((LC.z * g_diffuse) * illum);
+      dsum = mk3(fma_(lcol.x, dscale, dsum.x), fma_(lcol.y, dscale, dsum.y), fma_(lcol.z, dscale, dsum.z));
+      // Cook-Torrance: F0 0.4, Gaussian microfacet 0.8346, geometric term
+      const f3 Hv = cnormalize(add3(l2p, ptl));
+      const float ndh = fmax_(0.0f, cdot3(normal, Hv));
+      const float vdh = fmax_(0.0f, cdot3(l2p, Hv));
+      const float ndl = fmax_(0.0f, cdot3(normal, ptl));
+      const float omv = 1.0f - vdh, omv2 = omv * omv;
+      const float fresnel = fma_(0.6f, (omv2 * omv2) * omv, 0.4f);
+      const float alpha = c_rational_acos(ndh);
+      const float microfacet = 0.8346f * __expf((alpha * alpha) * nr2);
+      const float sv = (2.0f * ndh) * crcp(vdh);
+      const float geometric = min3f(1.0f, sv * ndv, sv * ndl);
+      const float spec = ((fresnel * microfacet) * geometric) * r_pndv;
+      const float sscale = spec * (spec_k * illum);
+      ssum = mk3(fmax_(fma_(lcol.x, sscale, ssum.x), 0.0f) * occlusion,
+                 fmax_(fma_(lcol.y, sscale, ssum.y), 0.0f) * occlusion,
+                 fmax_(fma_(lcol.z, sscale, ssum.z), 0.0f) * occlusion);
+      continue;
     }
-    ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
-    // Lambert + ambient
-    const float light = fmax_(cdot3(ptl, lnormal) * occlusion, 0.0f);
-    const float dscale = fma_(1.0f - ambient, light, ambient) * ((LC.z * g_diffuse) * illum);
+    // a light without shadows: its occlusion is 1
+    const float distance = (d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
+    const float tt = fma_(distance, LC.y, 1.0f);
+    const float illum = fma_(LB.w, crcp(tt * tt), -kLightCutoff / (1.0f - kLightCutoff));
+    if (illum <= 0) continue;
+    ptl = mul3s(ptl, rinv);
+    const float light = fmax_(cdot3(ptl, lnormal), 0.0f);
+    const float dscale = fma_(amb1, light, ambient) * ((LC.z * g_diffuse) * illum);
     dsum = mk3(fma_(lcol.x, dscale, dsum.x), fma_(lcol.y, dscale, dsum.y), fma_(lcol.z, dscale, dsum.z));
-    // Cook-Torrance: F0 0.4, Gaussian microfacet 0.8346, geometric term
-    const f3 Hv = cnormalize(add3(l2p, ptl));
-    const float ndh = fmax_(0.0f, cdot3(normal, Hv));
-    const float vdh = fmax_(0.0f, cdot3(l2p, Hv));
-    const float ndl = fmax_(0.0f, cdot3(normal, ptl));
+    // the half vector H = (v + l) / |v + l| of the unit vectors v (l2p) and l
+    // (ptl) through dot products: |v + l|^2 = 2 + 2 v.l, n.H = (n.v + n.l) /
+    // |v + l|, v.H = (1 + v.l) / |v + l|
+    const float nl = cdot3(normal, ptl), vl = cdot3(l2p, ptl);
+    const float rh = rsqrtf(fma_(2.0f, vl, 2.0f));
+    const float vdh = fmax_(0.0f, (1.0f + vl) * rh);
+    const float ndh = fmax_(0.0f, (ndv_raw + nl) * rh);
+    const float ndl = fmax_(0.0f, nl);
     const float omv = 1.0f - vdh, omv2 = omv * omv;
     const float fresnel = fma_(0.6f, (omv2 * omv2) * omv, 0.4f);
     const float alpha = c_rational_acos(ndh);
@@ -1666,9 +1697,8 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
     const float geometric = min3f(1.0f, sv * ndv, sv * ndl);
     const float spec = ((fresnel * microfacet) * geometric) * r_pndv;
     const float sscale = spec * (spec_k * illum);
-    ssum = mk3(fmax_(fma_(lcol.x, sscale, ssum.x), 0.0f) * occlusion,
-               fmax_(fma_(lcol.y, sscale, ssum.y), 0.0f) * occlusion,
-               fmax_(fma_(lcol.z, sscale, ssum.z), 0.0f) * occlusion);
+    ssum = mk3(fmax_(fma_(lcol.x, sscale, ssum.x), 0.0f), fmax_(fma_(lcol.y, sscale, ssum.y), 0.0f),
+               fmax_(fma_(lcol.z, sscale, ssum.z), 0.0f));
   }
   ssum = mul3s(ssum, ssao);
   dsum = mul3s(dsum, ssao);
