@@ -882,8 +882,10 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   if (with_id && lists[1] + lists[3] == 0) {  // no records: an empty tile
     // kernel3's output here is the clear colour and zero normals, unless the
     // view blends in another context's colour: write it, and mark the tile
+    // (kernel3 then reads nothing of it, the record map included)
     uint32_t* rgba = nullptr;
     uint32_t* nrm = nullptr;
+    uint32_t* rmap = S.rec;
     uint32_t clear = 0;
     if (ws.tile_empty) {
       const ViewParams& V = ws.views[sm.s];
@@ -891,6 +893,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
       if (direct) {
         rgba = reinterpret_cast<uint32_t*>(V.rgba);
         nrm = reinterpret_cast<uint32_t*>(V.normals);
+        rmap = nullptr;
         clear = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
       }
       if (tid == 0) ws.tile_empty[tile] = direct ? 1 : 0;
@@ -901,7 +904,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
         const size_t p = (size_t)py * S.width + px;
         S.depth[p] = kDepthClear;
         if (S.id) S.id[p] = kNoId;
-        S.rec[p] = kNoId;
+        if (rmap) rmap[p] = kNoId;
         if (rgba) rgba[p] = clear;
         if (nrm) nrm[p] = 0;
       }
