@@ -138,19 +138,57 @@ __device__ __forceinline__ Foot footprint(uint32_t xr, uint32_t yr, const Worksp
   return f;
 }
 
-// Coverage of a pixel known to lie inside the record's bbox: the reference
-// walk's skipped left-column pixels, then point_in_tri.
-__device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py, int chunk) {
-  const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
-  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
-  if (px == minx && py > miny &&
-      !walk_visits(0, py - miny, (int)(xr >> 16) - minx, (int)(yr >> 16) - miny, (float)miny, chunk))
-    return false;
+// point_in_tri of a record at pixel (px, py).
+__device__ __forceinline__ bool rec_in_tri(const float4 q[4], int px, int py) {
   float fx = (float)px, fy = (float)py;
   float sgn = q[1].w;
   float s = ((q[1].x + q[1].y * fx) + q[1].z * fy) * sgn;
   float t = ((q[2].x + q[2].y * fx) + q[2].z * fy) * sgn;
   return s > -0.0001f && t > -0.0001f && (s + t) < q[0].w;
+}
+
+// Is the left-column pixel (minx, py) of a record's bbox skipped by the
+// reference walk (py > miny)?
+__device__ __forceinline__ bool walk_skips(uint32_t xr, uint32_t yr, int py, int chunk) {
+  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
+  return py > miny && !walk_visits(0, py - miny, (int)(xr >> 16) - minx, (int)(yr >> 16) - miny, (float)miny, chunk);
+}
+
+// walk_skips for the rows [y0, y1) of a record's bbox at once: bit py - ty
+// set where the left-column pixel is skipped.  The same arithmetic as
+// walk_visits (walk_row_late's 1 / w computed once, (r + 1) * w % chunk
+// stepped row by row).
+__device__ __forceinline__ uint32_t walk_skip_rows(uint32_t xr, uint32_t yr, int y0, int y1, int ty, int chunk) {
+  const int minx = xr & 0xFFFF, miny = yr & 0xFFFF;
+  const int w = (int)(xr >> 16) - minx, h = (int)(yr >> 16) - miny;
+  const float iw = fdiv(1.0f, (float)w), fminy = (float)miny;
+  const int first = max(y0, miny + 1) - miny;  // r of the first row with r > 0
+  const int last = y1 - miny;                  // one past
+  if (first >= last) return 0u;
+  auto late = [&](int r) { return floorf(fma_((float)(r * w), iw, fminy)) != fminy + (float)r; };
+  const int wm = w % chunk;
+  int m = ((first + 1) * w) % chunk;  // (r + 1) * w % chunk
+  bool late_r = late(first);
+  uint32_t bits = 0;
+  for (int r = first; r < last; r++) {
+    const int r1 = r + 1;
+    const bool late_r1 = r1 < h ? late(r1) : false;
+    // walk_visits: not late, or the next row is late and a fragment starts at (r + 1) * w
+    const bool visits = !late_r || (r1 < h && m == 0 && late_r1);
+    if (!visits) bits |= 1u << (miny + r - ty);
+    late_r = late_r1;
+    m += wm;
+    if (m >= chunk) m -= chunk;
+  }
+  return bits;
+}
+
+// Coverage of a pixel known to lie inside the record's bbox: the reference
+// walk's skipped left-column pixels, then point_in_tri.
+__device__ __forceinline__ bool covers_in_bbox(const float4 q[4], int px, int py, int chunk) {
+  const uint32_t xr = __float_as_uint(q[3].x), yr = __float_as_uint(q[3].y);
+  if (px == (int)(xr & 0xFFFF) && walk_skips(xr, yr, py, chunk)) return false;
+  return rec_in_tri(q, px, py);
 }
 
 // One candidate as a record (and shade record for views); returns its tile footprint.
@@ -774,6 +812,10 @@ __device__ __forceinline__ uint32_t find_surface_warp(const Surface* surfs, uint
 // at most kRasterCache windows, pass 1 reuses the covered tests of pass 0
 // kept in registers.
 constexpr int kRasterCache = 8;
+// Cache slots of an NT-thread view raster: 512-thread CTAs keep none (their
+// static shared memory stays under 48 KB) and re-test in the id pass.
+template <int NT>
+__host__ __device__ constexpr int raster_cache_slots() { return NT <= 256 ? kRasterCache : 0; }
 constexpr uint32_t kSlotBits = 9;  // staged slots of a one-chunk tile: below 512
 
 // Exclusive block scan with a single barrier: each warp scans its lanes,
@@ -815,13 +857,18 @@ __device__ __forceinline__ uint32_t pack_rgba(float r, float g, float b, float a
   return quant8(r) | (quant8(g) << 8) | (quant8(b) << 16) | (quant8(a) << 24);
 }
 
-// Shared memory of one tile's raster (NT threads).
-template <int NT>
+// Shared memory of one tile's raster (NT threads; ID: views).
+template <int NT, bool ID>
 struct RasterSmem {
   float4 srec[4][NT];  // the staged records' four float4, one array each (conflict-free stores)
   uint32_t sidx[NT];
   uint32_t soff[NT + 1];
   uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
+  uint16_t sskip[NT];  // bit ly: the walk skips the record's left-column pixel in tile row ly
+  // the covered tests of pass 0 kept for the id pass: depth, and pixel |
+  // staged record << 8; slot k of thread t at k * NT + t
+  uint32_t scd[ID && raster_cache_slots<NT>() ? raster_cache_slots<NT>() * NT : 1];
+  uint32_t scm[ID && raster_cache_slots<NT>() ? raster_cache_slots<NT>() * NT : 1];
   uint32_t sdepth[kTilePixels];
   unsigned long long sid[kTilePixels];
   uint32_t swarp[NT / 32];
@@ -838,7 +885,7 @@ struct RasterSmem {
 // calls it; the caller synchronises before reusing the shared memory.
 template <int NT, bool ID>
 __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* __restrict__ surfs, uint32_t nsurf,
-                                            uint32_t tile, int surface, RasterSmem<NT>& sm) {
+                                            uint32_t tile, int surface, RasterSmem<NT, ID>& sm) {
   constexpr bool with_id = ID;
   constexpr int NW = NT / 32;
   constexpr uint32_t kCountShift = 18;  // scan word: pixels (< 2^18) | records << 18
@@ -846,6 +893,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   uint32_t* sidx = sm.sidx;
   uint32_t* soff = sm.soff;
   uint32_t* sgeo = sm.sgeo;
+  uint16_t* sskip = sm.sskip;
   uint32_t* sdepth = sm.sdepth;
   unsigned long long* sid = sm.sid;
   uint32_t* swarp = sm.swarp;
@@ -932,16 +980,16 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   const bool packed = with_id && resident && ws.pack_keys;
   uint32_t* sid32 = reinterpret_cast<uint32_t*>(sid);
   // the covered tests of pass 0 (resident tiles), up to kRasterCache per
-  // thread: depth, and pixel | staged record << 8 | 1 << 31; nh counts them
-  uint32_t cache_d[kRasterCache], cache_m[kRasterCache];
+  // thread, kept in sm.scd / sm.scm; nh counts them
   uint32_t nh = 0;
+  uint32_t wsamples = 0;  // covered tests of pass 0 seen by this warp
   bool cached = false;
   for (int pass = 0; pass < passes; pass++) {
     for (uint32_t c0 = 0; c0 < ntotal; c0 += NT) {
       const uint32_t m = min((uint32_t)NT, ntotal - c0);
       if (!(resident && pass == 1)) {
         if (pass != 0 || c0 != 0) __syncthreads();  // the previous chunk's readers are done
-        uint32_t area = 0, r = 0, geo = 0;
+        uint32_t area = 0, r = 0, geo = 0, skip = 0;
         float4 q0, q1, q2, q3;
         if ((uint32_t)tid < m) {
           const uint32_t e = c0 + tid;
@@ -958,6 +1006,8 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
             const uint32_t bw = (uint32_t)(bx1 - bx0);
             area = bw * (uint32_t)(by1 - by0);
             geo = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 4) | (bw << 8) | (((65536u + bw - 1) / bw) << 13);
+            // the walk rule of the bbox's left column, once per row of this tile
+            if ((int)(xr & 0xFFFF) >= tx0) skip = walk_skip_rows(xr, yr, by0, by1, ty0, chunk);
           }
         }
         const uint32_t word = area ? (area | (1u << kCountShift)) : 0u;
@@ -971,6 +1021,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
           srec[3][slot] = q3;
           sidx[slot] = r;
           sgeo[slot] = geo;
+          sskip[slot] = (uint16_t)skip;
           soff[slot] = off & ((1u << kCountShift) - 1);
         }
         if (tid == 0) {
@@ -983,12 +1034,11 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
       const uint32_t total = soff[nstaged];
       if (resident && pass == 1 && cached) {
         // pass 1 from the tests pass 0 kept
-#pragma unroll
-        for (int g = 0; g < kRasterCache; g++) {
-          if (!(cache_m[g] >> 31)) continue;
-          const int p = (int)(cache_m[g] & 0xFF);
-          const uint32_t lo = (cache_m[g] >> 8) & 0x3FF;
-          const uint32_t d = cache_d[g], fd = sdepth[swz32(p)];
+        for (uint32_t g = 0; g < nh; g++) {
+          const uint32_t cm = sm.scm[g * NT + tid];
+          const int p = (int)(cm & 0xFF);
+          const uint32_t lo = (cm >> 8) & 0x3FF;
+          const uint32_t d = sm.scd[g * NT + tid], fd = sdepth[swz32(p)];
           if (d > fd - kBufError && d < fd + kBufError) {
             const uint32_t key = __float_as_uint(srec[2][lo].w);
             if (packed)
@@ -1002,11 +1052,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
       // this warp's contiguous range of the test list, in windows of 32
       const uint32_t per = ((total + NW * 32 - 1) / (NW * 32)) * 32;
       const uint32_t start = min(total, (uint32_t)warp * per), end = min(total, start + per);
-      const bool keep = resident && pass == 0 && with_id;
-      if (keep) {
-#pragma unroll
-        for (int g = 0; g < kRasterCache; g++) cache_m[g] = 0;
-      }
+      const bool keep = resident && pass == 0 && with_id && raster_cache_slots<NT>() > 0;
       if (start < end) {
         // first record: the last staged record with soff <= start (warp-uniform)
         int rec = 0, hi = (int)nstaged - 1;
@@ -1032,19 +1078,18 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
             const int lx = (int)(geo & 0xF) + (int)rx, ly = (int)((geo >> 4) & 0xF) + (int)ry;
             const float4 q[4] = {srec[0][lo], srec[1][lo], srec[2][lo], srec[3][lo]};
             const int x = tx0 + lx, y = ty0 + ly;
-            hit = covers_in_bbox(q, x, y, chunk);
+            // covers_in_bbox, the walk rule from the staged mask
+            hit = !(x == (int)(__float_as_uint(q[3].x) & 0xFFFF) && ((sskip[lo] >> ly) & 1)) && rec_in_tri(q, x, y);
             if (hit) {
               const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
               const int p = ly * kTile + lx;
               if (pass == 0) {
                 atomicMin(&sdepth[swz32(p)], d);
                 if (keep) {
-#pragma unroll
-                  for (int k = 0; k < kRasterCache; k++)
-                    if (k == (int)nh) {
-                      cache_d[k] = d;
-                      cache_m[k] = (uint32_t)p | (lo << 8) | (1u << 31);
-                    }
+                  if (nh < (uint32_t)raster_cache_slots<NT>()) {
+                    sm.scd[nh * NT + tid] = d;
+                    sm.scm[nh * NT + tid] = (uint32_t)p | (lo << 8);
+                  }
                   nh++;
                 }
               } else {
@@ -1058,22 +1103,22 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
               }
             }
           }
-          if (pass == 0) {
-            const uint32_t hits = __ballot_sync(0xFFFFFFFFu, hit);
-            if (lane == 0 && hits) atomicAdd(&ssamples, (uint32_t)__popc(hits));
-          }
+          if (pass == 0) wsamples += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, hit));
           // the record of test base + 32: lane 31's, or the next one if it starts there
           rec = (int)((uint32_t)rec + __popc(starts));
           if ((uint32_t)rec + 1 < nstaged && soff[rec + 1] == base + 32) rec++;
         }
       }
     }
+    if (pass == 0 && lane == 0 && wsamples) atomicAdd(&ssamples, wsamples);
     // a resident tile's id pass reads pass 0's kept tests when every thread's
     // fit (block-uniform)
-    if (resident && with_id && pass == 0)
-      cached = __syncthreads_or(nh > (uint32_t)kRasterCache) == 0;
-    else
+    if (resident && with_id && pass == 0) {
+      const bool over = __syncthreads_or(nh > (uint32_t)raster_cache_slots<NT>()) != 0;
+      cached = raster_cache_slots<NT>() > 0 && !over;
+    } else {
       __syncthreads();
+    }
   }
   if (tid == 0 && ssamples) atomicAdd(&ws.ctr->samples, (unsigned long long)ssamples);
   for (int lp = tid; lp < kTilePixels; lp += NT) {
@@ -1097,7 +1142,7 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
 template <int NT, bool ID>
 __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
                                                           uint32_t nsurf, uint32_t tile0) {
-  __shared__ RasterSmem<NT> sm;
+  __shared__ RasterSmem<NT, ID> sm;
   if (ws.ctr->overflow) return;
   // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
   const uint32_t tile = gridDim.y > 1 ? surfs[blockIdx.y].tile_base + blockIdx.x : tile0 + blockIdx.x;
@@ -1904,7 +1949,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_raster_shade(Workspace ws, co
                                                                 const uint32_t* __restrict__ sched, uint32_t nseg,
                                                                 uint32_t* __restrict__ queue) {
   union Smem {
-    RasterSmem<NT> r;
+    RasterSmem<NT, true> r;
     ShadeSmem s;
   };
   __shared__ Smem sm;
