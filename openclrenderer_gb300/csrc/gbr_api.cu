@@ -85,6 +85,7 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view) {
   TRY(w.bins.reserve(w.bin_target));
   TRY(w.fine_count.reserve(sh.nfine));
   TRY(w.fine_off.reserve(sh.nfine));
+  TRY(w.tiles.reserve(sh.nfine));
   TRY(w.coarse_count.reserve(sh.ncoarse));
   TRY(w.coarse_off.reserve(sh.ncoarse));
   TRY(w.scan_part.reserve(scan_chunks(sh.nfine)));
@@ -266,6 +267,8 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   ws.bins = wm.bins.p;
   ws.bin_cap = (uint32_t)std::min<size_t>(wm.bins.cap, 0xFFFFFFF0u);
   ws.scan_part = wm.scan_part.p;
+  const bool table = pass_tile_table(view, sh);
+  ws.tiles = table ? wm.tiles.p : nullptr;
   // views: the object cull needs the world cache (and with it the radii)
   const bool cull = view && sd.world && s->objr.p && sd.ndescs && sh.nobjects == sd.ndescs && sh.nitems <= 65535;
   ws.vis = cull ? wm.vis.p : nullptr;
@@ -290,6 +293,7 @@ gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, c
   CU(mark(1, geom));
   const bool prep = view && sh.shade;
   const bool on_side = prep && side && side->stream;
+  if (table) CU(launch_tile_table(ws, wm.surf.p, sh.nsurf, geom));
   CU(launch_scan(ws, geom));
   CU(mark(2, geom));
   CU(launch_fill(ws, wm.surf.p, geom));

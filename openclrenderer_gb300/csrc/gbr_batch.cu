@@ -180,7 +180,7 @@ gbr_status launch_graph(gbr_batch* b, const gbr_camera* cams, cudaStream_t st) {
   CU(cudaEventRecord(b->done, st));
   b->launches++;
   b->s->stats.launches += pass_kernels(true, b->vshape.shade, b->vshape.nfine, &b->vshape) +
-                          (b->sshape.nitems ? pass_kernels(false, false, b->sshape.nfine) : 0u);
+                          (b->sshape.nitems ? pass_kernels(false, false, b->sshape.nfine, &b->sshape) : 0u);
   b->in_flight = true;
   b->last_stream = st;
   return GBR_OK;

@@ -167,6 +167,8 @@ struct Workspace {
   uint32_t ncoarse;
   uint32_t* bins;
   uint32_t bin_cap;
+  // per fine tile: its surface and its global coarse tile (launch_tile_table)
+  const uint2* tiles;
   uint32_t* scan_part;  // per chunk of fine counts (scan_chunks), or null: one-block scan
   const uint32_t* vis;  // views: object cull bits (k_object_cull), vis_words per view, or null
   uint32_t vis_words;
@@ -197,6 +199,8 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
 // One block when the fine counts fit one chunk (or scan_part is null), else
 // scan_chunks(nfine) blocks in two kernels.
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st);
+// ws.tiles for the pass's nsurf surfaces (ws.nfine fine tiles, ws.coarse_shift).
+cudaError_t launch_tile_table(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, cudaStream_t st);
 uint32_t scan_chunks(uint32_t nfine);
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st);
 // Views that shade: every record's setup output becomes its shade constants

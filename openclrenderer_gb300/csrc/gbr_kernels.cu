@@ -560,6 +560,23 @@ __global__ void __launch_bounds__(256, 3) k_setup_shadow(SceneDev sc, const Shad
   add_frags(ws, frags);
 }
 
+// Each fine tile's surface (binary search over tile_base) and global coarse
+// tile: the raster's and kernel3's first loads.
+__global__ void __launch_bounds__(256) k_tile_table(const Surface* __restrict__ surfs, uint32_t nsurf,
+                                                    uint32_t nfine, int coarse_shift, uint2* __restrict__ tiles) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nfine) return;
+  uint32_t lo = 0, hi = nsurf - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (surfs[mid].tile_base <= t) lo = mid; else hi = mid - 1;
+  }
+  const Surface& S = surfs[lo];
+  const uint32_t lt = t - S.tile_base;
+  const int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
+  tiles[t] = make_uint2(lo, S.ctile_base + (ty >> coarse_shift) * S.ctiles_x + (tx >> coarse_shift));
+}
+
 // Exclusive scan of fine and coarse tile counts (one block of 1024 threads);
 // counts are reset to zero to serve as fill cursors.  Rounds of 8192 counts
 // are staged in shared memory with coalesced loads, each thread scans 8
@@ -777,20 +794,6 @@ __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __res
   }
 }
 
-// The surface owning a tile, found by one warp: surfaces are sorted by
-// tile_base, so one ballot over 32 of them finds the last one starting at or
-// before the tile.  Every lane of the warp must call it; all get the result.
-__device__ __forceinline__ uint32_t find_surface_warp(const Surface* surfs, uint32_t nsurf, uint32_t tile) {
-  const int lane = threadIdx.x & 31;
-  uint32_t owner = 0;
-  for (uint32_t b = 0; b < nsurf; b += 32) {
-    const uint32_t i = b + lane;
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, i < nsurf && __ldg(&surfs[i].tile_base) <= tile);
-    if (m) owner = b + 31 - __clz(m);
-    if (m != 0xFFFFFFFFu) break;
-  }
-  return owner;
-}
 
 
 
@@ -881,8 +884,9 @@ struct RasterSmem {
 
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
 // (views) or only the depth (cube faces).  surface: the tile's surface when
-// the caller knows it, else -1 (found by warp 0).  Every thread of the block
-// calls it; the caller synchronises before reusing the shared memory.
+// the caller knows it, else -1 (ws.tiles, or the pass's only surface).
+// Every thread of the block calls it; the caller synchronises before reusing
+// the shared memory.
 template <int NT, bool ID>
 __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* __restrict__ surfs, uint32_t nsurf,
                                             uint32_t tile, int surface, RasterSmem<NT, ID>& sm) {
@@ -902,21 +906,27 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   Surface& S = sm.S;
   uint32_t* lists = sm.lists;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid < 32) {  // warp 0: the tile's surface (one ballot search) and its bins
-    const uint32_t foff = tid == 0 ? ws.fine_off[tile] : 0u, fcnt = tid == 0 ? ws.fine_count[tile] : 0u;
-    const uint32_t s = surface >= 0 ? (uint32_t)surface : (nsurf > 1 ? find_surface_warp(surfs, nsurf, tile) : 0u);
-    if (tid == 0) {
+  if (tid == 0) {  // the tile's surface and bins
+    const uint32_t foff = ws.fine_off[tile], fcnt = ws.fine_count[tile], ftot = ws.ctr->fine_total;
+    uint32_t s, ct;
+    if (ws.tiles) {  // two rounds of loads
+      const uint2 tt = ws.tiles[tile];
+      s = surface >= 0 ? (uint32_t)surface : tt.x;
+      ct = tt.y;
       S = surfs[s];
-      sm.s = s;
-      uint32_t lt = tile - S.tile_base;
-      int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
-      uint32_t ct = S.ctile_base + (ty >> ws.coarse_shift) * S.ctiles_x + (tx >> ws.coarse_shift);
-      lists[0] = foff;
-      lists[1] = fcnt;
-      lists[2] = ws.ctr->fine_total + ws.coarse_off[ct];
-      lists[3] = ws.coarse_count[ct];
-      ssamples = 0;
+    } else {  // the surface is known (grid row, or the pass's only one)
+      s = surface >= 0 ? (uint32_t)surface : 0u;
+      S = surfs[s];
+      const uint32_t lt = tile - S.tile_base;
+      const int tx = lt % S.tiles_x, ty = lt / S.tiles_x;
+      ct = S.ctile_base + (ty >> ws.coarse_shift) * S.ctiles_x + (tx >> ws.coarse_shift);
     }
+    sm.s = s;
+    lists[0] = foff;
+    lists[1] = fcnt;
+    lists[2] = ftot + ws.coarse_off[ct];
+    lists[3] = ws.coarse_count[ct];
+    ssamples = 0;
   }
   if (with_id) {
     for (int p = tid; p < kTilePixels; p += NT) {
@@ -1840,13 +1850,15 @@ __device__ __forceinline__ void shade_tile(const SceneDev& sc, const ViewParams*
 // A pass whose setup or binning overflowed its scratch leaves the depth and
 // record map unwritten (the raster returns at once); shading returns too, and
 // the host re-runs the pass with grown scratch.
-// tile_empty (or null): tiles whose output the raster wrote (Workspace).
+// tile_empty (or null): tiles whose output the raster wrote; tiles (null for
+// one view): each tile's surface (Workspace).
 template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
                                                const ShadeRec* __restrict__ srec, const Counters* __restrict__ ctr,
                                                uint32_t rec_cap, uint32_t tile0,
-                                               const uint8_t* __restrict__ tile_empty) {
+                                               const uint8_t* __restrict__ tile_empty,
+                                               const uint2* __restrict__ tiles) {
   constexpr int NW = kTilePixels / 32;
   __shared__ ShadeSmem sm;
   __shared__ uint32_t s_id, s_done;
@@ -1855,13 +1867,9 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
   if (ctr->overflow) return;
   const uint32_t nrec = min(ctr->nrec, rec_cap);
   const uint32_t tile = tile0 + blockIdx.x;
-  if (threadIdx.x < 32) {
-    const uint32_t done = (tile_empty && threadIdx.x == 0) ? tile_empty[tile] : 0u;
-    const uint32_t sid = find_surface_warp(surfs, nviews, tile);
-    if (threadIdx.x == 0) {
-      s_id = sid;
-      s_done = done;
-    }
+  if (threadIdx.x == 0) {
+    s_done = tile_empty ? tile_empty[tile] : 0u;
+    s_id = tiles ? tiles[tile].x : 0u;  // null: one view
   }
   __syncthreads();
   if (s_done) return;
@@ -2193,6 +2201,14 @@ cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uin
   return cudaGetLastError();
 }
 
+cudaError_t launch_tile_table(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, cudaStream_t st) {
+  if (!ws.nfine) return cudaSuccess;
+  if (!ws.tiles || !nsurf) return cudaErrorInvalidValue;
+  k_tile_table<<<(ws.nfine + 255) / 256, 256, 0, st>>>(d_surf, nsurf, ws.nfine, ws.coarse_shift,
+                                                       const_cast<uint2*>(ws.tiles));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st) {
   const uint32_t nchunks = (ws.nfine + kScanChunk - 1) / kScanChunk;
   if (nchunks <= 1 || !ws.scan_part) {
@@ -2238,13 +2254,13 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
                          uint32_t ntiles, const Workspace& ws, cudaStream_t st, bool features, uint32_t tile0) {
   if (!ntiles) return cudaSuccess;
-  if (!sc.objq || !sc.texlv || !ws.srec) return cudaErrorInvalidValue;
+  if (!sc.objq || !sc.texlv || !ws.srec || (nviews > 1 && !ws.tiles)) return cudaErrorInvalidValue;
   if (features)
     k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
-                                          ws.tile_empty);
+                                          ws.tile_empty, ws.tiles);
   else
     k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
-                                           ws.tile_empty);
+                                           ws.tile_empty, ws.tiles);
   return cudaGetLastError();
 }
 

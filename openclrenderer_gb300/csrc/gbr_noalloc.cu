@@ -225,6 +225,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   ws.srec = reinterpret_cast<ShadeRec*>(base + kOffSrec);
   ws.rec_cap = (uint32_t)kMaxRecords;
   ws.bins = reinterpret_cast<uint32_t*>(base + kOffBins);
+
   ws.bin_cap = (uint32_t)kMaxBins;
   ws.fine_max = kFineMaxTiles;
   ws.coarse_shift = kCoarseShift;

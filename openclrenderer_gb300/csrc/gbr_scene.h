@@ -95,6 +95,7 @@ struct WorkMem {
   DevBuf<ShadeRec> srec;
   DevBuf<uint32_t> fine_count, fine_off, coarse_count, coarse_off, bins, scan_part;
   DevBuf<uint8_t> tile_empty;  // views that shade: per fine tile, whether the raster wrote kernel3's output
+  DevBuf<uint2> tiles;         // per fine tile: surface, global coarse tile (Workspace::tiles)
   DevBuf<Counters> ctr;
   DevBuf<uint32_t> pix_rec, pix_depth, pix_id;  // per view pixel
   DevBuf<uint8_t> pix_rgba;
@@ -105,7 +106,7 @@ struct WorkMem {
   DevBuf<uint32_t> vis;           // views: object cull bits
   uint32_t rec_target = 0, bin_target = 0;
   void release() {
-    rec.release(); srec.release(); fine_count.release(); fine_off.release(); tile_empty.release();
+    rec.release(); srec.release(); fine_count.release(); fine_off.release(); tile_empty.release(); tiles.release();
     coarse_count.release(); coarse_off.release(); bins.release(); scan_part.release(); ctr.release();
     pix_rec.release(); pix_depth.release(); pix_id.release(); pix_rgba.release();
     surf.release(); views.release(); jobs.release(); sched.release(); queue.release(); vis.release();
@@ -279,14 +280,23 @@ gbr_status reserve_pass(WorkMem& w, const PassShape& sh, bool view);
 gbr_status launch_pass(gbr_scene* s, WorkMem& wm, const Tuning& tu, bool view, const PassShape& sh,
                        Counters* host_ctr, cudaEvent_t* ev, cudaStream_t st, cudaStream_t geom = nullptr,
                        cudaEvent_t join = nullptr, const SideStream* side = nullptr);
-// Kernel launches of one pass (for the launch statistics): views setup, scan,
-// fill, shade constants, raster, shade (the last two only when shading);
-// depth-only passes clear, setup, scan, fill, raster.
-// A scan over more than one chunk of fine tiles is two kernels.
+// Does a pass need the per-tile table (Workspace::tiles)?  Passes of several
+// surfaces whose raster cannot take the surface from its grid row (views;
+// cube faces of more than 65535 surfaces).
+inline bool pass_tile_table(bool view, const PassShape& sh) {
+  return sh.nsurf > 1 && (view || !(sh.tiles_per_surface && sh.nsurf <= 65535 &&
+                                    (uint64_t)sh.tiles_per_surface * sh.nsurf == sh.nfine));
+}
+// Kernel launches of one pass (for the launch statistics): views object
+// cull, setup, scan, fill, raster, and when shading the shade constants and
+// kernel3; depth-only passes clear, setup, scan, fill, raster; the tile
+// table when the pass needs it.  A scan over more than one chunk of fine
+// tiles is two kernels.
 // The fused raster -> shade pass is one kernel for two; pipelined groups are
 // two kernels per group.
 inline uint32_t pass_kernels(bool view, bool shade, uint32_t nfine, const PassShape* sh = nullptr) {
-  uint32_t k = (view ? (shade ? 7u : 5u) : 5u) + (scan_chunks(nfine) > 1 ? 1u : 0u);  // views: + the object cull
+  uint32_t k = (view ? (shade ? 7u : 5u) : 5u) + (scan_chunks(nfine) > 1 ? 1u : 0u);
+  if (sh && pass_tile_table(view, *sh)) k += 1;
   if (sh && sh->nseg) k -= 1;
   if (sh && sh->ngroups > 1) k += 2 * (sh->ngroups - 1);
   return k;
