@@ -1731,7 +1731,8 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
       continue;
     }
     // a light without shadows: its occlusion is 1
-    const float distance = (d2 > 0.0f && d2 < 3.0e38f) ? d2 * rinv : fsqrt(d2);
+    // the approximate square root; 0, +inf and NaN are their own square roots
+    const float distance = (d2 > 0.0f && d2 <= 3.4028235e38f) ? d2 * rinv : d2;
     const float tt = fma_(distance, LC.y, 1.0f);
     const float illum = fma_(LB.w, crcp(tt * tt), -kLightCutoff / (1.0f - kLightCutoff));
     if (illum <= 0) continue;
