@@ -227,12 +227,31 @@ __device__ __noinline__ uint32_t direct_raster(const Cand& c, uint32_t surface, 
                        make_float4(__uint_as_float(R.xr), __uint_as_float(R.yr), 0.0f, 0.0f)};
   const int x0 = (int)(R.xr & 0xFFFF), x1 = (int)(R.xr >> 16), y0 = (int)(R.yr & 0xFFFF), y1 = (int)(R.yr >> 16);
   uint32_t hits = 0;
-  for (int y = y0; y < y1; y++)
-    for (int x = x0; x < x1; x++)
-      if (covers_in_bbox(q, x, y, S.chunk)) {
+  // covers_in_bbox row by row: the walk rule of each row's left-column pixel
+  // (walk_visits) with 1 / w and (r + 1) * w % chunk computed incrementally
+  const int w = x1 - x0, h = y1 - y0, chunk = S.chunk;
+  const float iw = fdiv(1.0f, (float)w), fminy = (float)y0;
+  auto late = [&](int r) { return floorf(fma_((float)(r * w), iw, fminy)) != fminy + (float)r; };
+  const int wm = w % chunk;
+  int m = (2 * w) % chunk;  // (r + 1) * w % chunk for row r = 1
+  bool late_r = h > 1 ? late(1) : false;
+  for (int y = y0; y < y1; y++) {
+    const int r = y - y0;
+    bool skip_left = false;
+    if (r > 0) {
+      const int r1 = r + 1;
+      const bool late_r1 = r1 < h ? late(r1) : false;
+      skip_left = late_r && !(r1 < h && m == 0 && late_r1);
+      late_r = late_r1;
+      m += wm;
+      if (m >= chunk) m -= chunk;
+    }
+    for (int x = skip_left ? x0 + 1 : x0; x < x1; x++)
+      if (rec_in_tri(q, x, y)) {
         atomicMin(S.depth + (size_t)y * S.width + x, depth_at(R.A, R.B, R.C, (float)x, (float)y));
         hits++;
       }
+  }
   return hits;
 }
 
