@@ -56,6 +56,10 @@ def parse():
                     help="one launch of every kernel inside cudaProfilerStart/Stop (for ncu --profile-from-start off), "
                          "then exit: scene build, a 1080p terrain frame, the four post passes, an 8-view sphere batch "
                          "in each raster / kernel3 mode")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="the 64-view sphere batch (the mixed-resolution batched workload) rendered once inside "
+                         "cudaProfilerStart/Stop after a warm-up batch, with the tuning its captured graph uses "
+                         "(128-thread rasters), then exit")
     return ap.parse_args()
 
 
@@ -96,6 +100,23 @@ def profile_pass():
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
     print("profile pass done")
+
+
+def profile_batch():
+    """The batched workload's pass once, between cudaProfilerStart and
+    cudaProfilerStop, after an untimed warm-up batch."""
+    import torch
+    from openclrenderer_gb300.pipeline import GpuScene
+    mb = scenes.spheres_batch()
+    g = GpuScene(mb)
+    g.set_tuning(S.PASS_VIEW, raster_threads=128)
+    outs = g.render_batch(mb.cameras, mb.views)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    g.render_batch(mb.cameras, mb.views, outs=outs)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print("profile batch done")
 
 
 def dist_env():
@@ -456,6 +477,9 @@ def main():
     world, rank, local = dist_env()
     if args.profile_pass:
         profile_pass()
+        return
+    if args.profile_batch:
+        profile_batch()
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
