@@ -869,9 +869,14 @@ __device__ __forceinline__ uint32_t block_excl_scan1(uint32_t v, uint32_t* swarp
 // Shared-memory slot of tile pixel p = ly * 16 + lx in the per-pixel depth
 // (32-bit words) and id (64-bit words) arrays: a row of 16 pixels fills 16
 // of the 32 banks, so rows y and y + 2 (64-bit: y and y + 1) would share
-// banks and a narrow triangle's tests collide; XOR-ing the column with the
-// row pair (row) spreads them.  A permutation within each row.
-__device__ __forceinline__ int swz32(int p) { return p ^ ((p >> 5) & 15); }
+// banks and a narrow triangle's tests collide.  32-bit: each 32-word line
+// (a row pair) is rotated by 4 banks per line, so that a footprint up to 4
+// pixels wide and 8 rows tall falls on distinct banks; 64-bit: the column is
+// XOR-ed with the row.  Permutations within each line (row).
+__device__ __forceinline__ int swz32(int p) {
+  const int line = p >> 5;
+  return (line << 5) | ((p + 4 * line) & 31);
+}
 __device__ __forceinline__ int swz64(int p) { return p ^ ((p >> 4) & 15); }
 
 // kernel3's RGBA8 output word
