@@ -351,7 +351,7 @@ typedef struct gbr_tuning {
 #define GBR_RS_FUSED 1
 #define GBR_RS_PIPELINED 2
 
-/* Defaults: 256 threads, 128-pixel coarse tiles, 16 fine tiles, 1.25, sequential. */
+/* Defaults: 128 threads, 128-pixel coarse tiles, 16 fine tiles, 1.25, sequential. */
 gbr_status gbr_scene_set_tuning(gbr_scene* scene, int32_t pass, const gbr_tuning* t);
 gbr_status gbr_scene_get_tuning(gbr_scene* scene, int32_t pass, gbr_tuning* t);
 

@@ -29,7 +29,7 @@ constexpr int kTilePixels = kTile * kTile;
 constexpr int kCoarseShift = 3;              // coarse tile edge = kTile << shift = 128 pixels
 constexpr int kCoarse = kTile << kCoarseShift;
 constexpr int kFineMaxTiles = 16;            // more fine tiles than this -> coarse bins
-constexpr int kRasterThreads = kTilePixels;  // threads of one raster CTA
+constexpr int kRasterThreads = 128;  // threads of one raster CTA (default tuning)
 constexpr int kMaxLights = 256;              // lights a scene may hold (staged in shared memory)
 
 // Per visible clipped triangle on one surface: everything kernel1/kernel2

@@ -66,11 +66,11 @@ BATCH_INFO = np.dtype([("views", "<u4"), ("graph_nodes", "<u4"), ("captures", "<
                        ("reruns", "<u8"), ("scratch_bytes", "<u8")])
 PASS_SHADOW, PASS_VIEW = 0, 1
 BATCH_WITH_SHADOW = 1
-DEFAULT_TUNING = {"raster_threads": 256, "coarse_tile": 128, "fine_max_tiles": 16, "scratch_headroom": 1.25,
+DEFAULT_TUNING = {"raster_threads": 128, "coarse_tile": 128, "fine_max_tiles": 16, "scratch_headroom": 1.25,
                   "raster_shade": 0}
 
 
-def make_tuning(raster_threads=256, coarse_tile=128, fine_max_tiles=16, scratch_headroom=1.25, raster_shade=0):
+def make_tuning(raster_threads=128, coarse_tile=128, fine_max_tiles=16, scratch_headroom=1.25, raster_shade=0):
     t = np.zeros((), TUNING)
     t["raster_threads"] = raster_threads
     t["coarse_tile"] = coarse_tile

@@ -19,7 +19,7 @@ from openclrenderer_gb300 import structs as S  # noqa: E402
 from openclrenderer_gb300.pipeline import Batch, GpuScene  # noqa: E402
 
 SHAPES = [
-    {"raster_threads": 128},
+    {"raster_threads": 256},
     {"raster_threads": 512},
     {"coarse_tile": 64},
     {"coarse_tile": 256},

@@ -46,9 +46,10 @@ def test_serving_results_identical_alone_and_in_mix():
     # alone: one request at a time through the single-view host path
     alone = [gss[s].render_host(cam, view) for s, cam, view in reqs]
     torch.cuda.synchronize()
-    # in the mix: all submitted at once; a budget that holds only a few views
+    # in the mix: all submitted at once (the output buffers made first); a
+    # budget that holds only a few views; one batch on the GPU at a time, so
+    # that requests arriving meanwhile queue and join the next batch
     budget = 4 * 1280 * 720 * 46
-    srv = Server(gss, hbm_budget_bytes=budget)
     outs, keep = [], []
     for k, (s, cam, view) in enumerate(reqs):
         W, H = int(view["width"]), int(view["height"])
@@ -62,6 +63,8 @@ def test_serving_results_identical_alone_and_in_mix():
             keep.append(t)
             o["rgba"] = t.numpy()[off:off + W * H * 4].reshape(H, W, 4)
         outs.append(o)
+    srv = Server(gss, hbm_budget_bytes=budget, max_inflight=1)
+    for k, ((s, cam, view), o) in enumerate(zip(reqs, outs)):
         srv.submit(s, cam, view, o["depth"], o["id"], o["rgba"], tag=k)
     srv.drain()
     done = srv.poll(cap=1024)
