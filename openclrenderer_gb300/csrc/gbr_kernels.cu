@@ -1886,20 +1886,17 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
                                                const uint2* __restrict__ tiles) {
   constexpr int NW = kTilePixels / 32;
   __shared__ ShadeSmem sm;
-  __shared__ uint32_t s_id, s_done;
   __shared__ uint32_t s_warp[NW];
   __shared__ uint32_t s_px[kTilePixels], s_d[kTilePixels], s_r[kTilePixels];
   if (ctr->overflow) return;
   const uint32_t nrec = min(ctr->nrec, rec_cap);
   const uint32_t tile = tile0 + blockIdx.x;
-  if (threadIdx.x == 0) {
-    s_done = tile_empty ? tile_empty[tile] : 0u;
-    s_id = tiles ? tiles[tile].x : 0u;  // null: one view
-  }
-  __syncthreads();
-  if (s_done) return;
-  const Surface& S = surfs[s_id];
-  const ViewParams& V = views[s_id];
+  // every thread reads the tile's flag and surface (the same words): the
+  // return is block-uniform and needs no barrier
+  if (tile_empty && tile_empty[tile]) return;
+  const uint32_t sid = tiles ? tiles[tile].x : 0u;  // null: one view
+  const Surface& S = surfs[sid];
+  const ViewParams& V = views[sid];
   const uint32_t lt = tile - S.tile_base;
   const int x0 = (lt % S.tiles_x) * kTile, y0 = (lt / S.tiles_x) * kTile;
   // the thread's own pixel: empty pixels are written at once; covered ones
