@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
 }
 
 // prearrange_realtime_shadowing (cl2.cl:4419-4636), one thread per (triangle, light job).
-__global__ void __launch_bounds__(256, 3) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
+__global__ void __launch_bounds__(128, 6) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
                                                       const Surface* __restrict__ surfs, Workspace ws) {
   uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
   const ShadowJob& J = jobs[blockIdx.y];
@@ -2218,8 +2218,8 @@ cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, ui
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,
                                 const Surface* d_surf, const Workspace& ws, cudaStream_t st) {
   if (!sc.ntris || !njobs) return cudaSuccess;
-  dim3 grid((sc.ntris + 255) / 256, njobs);
-  k_setup_shadow<<<grid, 256, 0, st>>>(sc, d_jobs, d_surf, ws);
+  dim3 grid((sc.ntris + 127) / 128, njobs);  // small blocks: lanes' direct rasters differ in length
+  k_setup_shadow<<<grid, 128, 0, st>>>(sc, d_jobs, d_surf, ws);
   return cudaGetLastError();
 }
 
