@@ -820,19 +820,20 @@ __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __res
 //
 // The tile's records (its fine bin, then its coarse tile's bin) are staged NT
 // at a time in shared memory, keeping those whose bbox meets the tile.  Each
-// contributes the pixels of its bbox clipped to the tile; one block scan
-// (packing the record count and the pixel count) compacts them and lays all
-// (record, pixel) tests of the chunk end to end.  Each warp takes one
+// contributes the horizontal pixel pairs of its bbox clipped to the tile (a
+// test covers one pair: the record's loads and decode serve two pixels); one
+// block scan (packing the record count and the pair count) compacts them and
+// lays all (record, pair) tests of the chunk end to end.  Each warp takes one
 // contiguous range of that list, finds its first record by binary search,
 // and then maps 32 tests at a time to records with one ballot of the record
-// starts inside the window (every staged record has at least one pixel, so
+// starts inside the window (every staged record has at least one pair, so
 // at most 32 start there), so small and large triangles are load-balanced
 // alike.  Pass 0 resolves the minimum depth with shared-memory atomicMin;
 // pass 1 the minimum packed (key << 32 | record) among tests within +-20 of
 // the final depth.  Both are minima, so neither bin order nor thread order
 // changes the result.  When the whole list fits one chunk and each lane has
-// at most kRasterCache windows, pass 1 reuses the covered tests of pass 0
-// kept in registers.
+// at most kRasterCache covered pixels, pass 1 reuses the covered pixels of
+// pass 0 kept in shared memory.
 constexpr int kRasterCache = 8;
 // Cache slots of an NT-thread view raster: 512-thread CTAs keep none (their
 // static shared memory stays under 48 KB) and re-test in the id pass.
@@ -1037,9 +1038,10 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
           const int bx0 = max((int)(xr & 0xFFFF), tx0), bx1 = min((int)(xr >> 16), tx0 + kTile);
           const int by0 = max((int)(yr & 0xFFFF), ty0), by1 = min((int)(yr >> 16), ty0 + kTile);
           if (bx1 > bx0 && by1 > by0) {
-            const uint32_t bw = (uint32_t)(bx1 - bx0);
-            area = bw * (uint32_t)(by1 - by0);
-            geo = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 4) | (bw << 8) | (((65536u + bw - 1) / bw) << 13);
+            // the tests are horizontal pixel pairs: ceil(bw / 2) per row
+            const uint32_t bw = (uint32_t)(bx1 - bx0), pw = (bw + 1) >> 1;
+            area = pw * (uint32_t)(by1 - by0);
+            geo = (uint32_t)(bx0 - tx0) | ((uint32_t)(by0 - ty0) << 4) | (bw << 8) | (((65536u + pw - 1) / pw) << 13);
             // the walk rule of the bbox's left column, once per row of this tile
             if ((int)(xr & 0xFFFF) >= tx0) skip = walk_skip_rows(xr, yr, by0, by1, ty0, chunk);
           }
@@ -1103,20 +1105,24 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
           const uint32_t upto = lane == 31 ? starts : starts & ((2u << lane) - 1u);
           const uint32_t lo = (uint32_t)rec + __popc(upto);
           const uint32_t t = base + lane;
-          bool hit = false;
+          uint32_t nhit = 0;
           if (t < end) {
+            // test t of the record: the pixel pair (lx, ly), (lx + 1, ly)
             const uint32_t geo = sgeo[lo];
             const uint32_t local = t - soff[lo];
-            const uint32_t bw = (geo >> 8) & 0x1F;
-            const uint32_t ry = (local * (geo >> 13)) >> 16, rx = local - ry * bw;
-            const int lx = (int)(geo & 0xF) + (int)rx, ly = (int)((geo >> 4) & 0xF) + (int)ry;
+            const uint32_t bw = (geo >> 8) & 0x1F, pw = (bw + 1) >> 1;
+            const uint32_t ry = (local * (geo >> 13)) >> 16, rp = local - ry * pw;
+            const int lx = (int)(geo & 0xF) + 2 * (int)rp, ly = (int)((geo >> 4) & 0xF) + (int)ry;
             const float4 q[4] = {srec[0][lo], srec[1][lo], srec[2][lo], srec[3][lo]};
             const int x = tx0 + lx, y = ty0 + ly;
-            // covers_in_bbox, the walk rule from the staged mask
-            hit = !(x == (int)(__float_as_uint(q[3].x) & 0xFFFF) && ((sskip[lo] >> ly) & 1)) && rec_in_tri(q, x, y);
-            if (hit) {
-              const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)x, (float)y);
-              const int p = ly * kTile + lx;
+            // covers_in_bbox, the walk rule from the staged mask (only the
+            // first pixel of a pair can be the bbox's left column)
+            const bool h0 = !(x == (int)(__float_as_uint(q[3].x) & 0xFFFF) && ((sskip[lo] >> ly) & 1)) &&
+                            rec_in_tri(q, x, y);
+            const bool h1 = 2 * rp + 1 < bw && rec_in_tri(q, x + 1, y);
+            auto resolve = [&](int px, int plx) {
+              const uint32_t d = depth_at(q[0].x, q[0].y, q[0].z, (float)px, (float)y);
+              const int p = ly * kTile + plx;
               if (pass == 0) {
                 atomicMin(&sdepth[swz32(p)], d);
                 if (keep) {
@@ -1135,9 +1141,12 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
                     atomicMin(&sid[swz64(p)], ((unsigned long long)__float_as_uint(q[2].w) << 32) | sidx[lo]);
                 }
               }
-            }
+            };
+            if (h0) resolve(x, lx);
+            if (h1) resolve(x + 1, lx + 1);
+            nhit = (uint32_t)h0 + (uint32_t)h1;
           }
-          if (pass == 0) wsamples += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, hit));
+          if (pass == 0) wsamples += __reduce_add_sync(0xFFFFFFFFu, nhit);
           // the record of test base + 32: lane 31's, or the next one if it starts there
           rec = (int)((uint32_t)rec + __popc(starts));
           if ((uint32_t)rec + 1 < nstaged && soff[rec + 1] == base + 32) rec++;
