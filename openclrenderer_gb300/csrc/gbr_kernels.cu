@@ -1715,21 +1715,23 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
     // The distance only feeds the colour, except through the cutoff below,
     // which for a shadow light also decides which cubemap later shadow lights
     // read (shnum): IEEE arithmetic for shadow lights (a warp-uniform branch),
-    // approximate otherwise, after the conservative early test.
-    const float d2 = dot3(ptl, ptl);
+    // approximate otherwise, after the conservative early test (whose margins
+    // cover the contracted dot product).
+    const float d2 = cdot3(ptl, ptl);
     if (d2 > LA.w) continue;
     const float4 LB = lights[kLightQuads * i + 1], LC = lights[kLightQuads * i + 2];
     const uint32_t lflags = __float_as_uint(LC.w);
     const f3 lcol = mk3(LB.x, LB.y, LB.z);
     const float rinv = rsqrtf(d2);
-    if (lflags & 1u) {  // a shadow light
+    if (lflags & 1u) {  // a shadow light: its distance in IEEE arithmetic
+      const float d2s = dot3(ptl, ptl);
       float occlusion = 1.0f;
       if (lflags & 2u) {  // is_static
         int face = ret_cubeface(gpos, lpos);
         occlusion = 1.0f - hard_occlusion(sc, lpos, normal, ptl, sc.shadow_static, face, gpos, static_num);
         static_num++;
       }
-      const float tt = fdiv(fsqrt(d2), LC.x) + 1.0f;
+      const float tt = fdiv(fsqrt(d2s), LC.x) + 1.0f;
       float illum = fdiv(LB.w, tt * tt);
       illum -= kLightCutoff;
       illum *= 1.0f / (1.0f - kLightCutoff);
@@ -1740,7 +1742,7 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
         occlusion = fmin_(occlusion, dyn);
         shnum++;
       }
-      ptl = mul3s(ptl, rinv);  // cnormalize(ptl): the same rsqrtf of the same dot
+      ptl = mul3s(ptl, rinv);  // cnormalize(ptl), the dot contracted (colour only)
       // Lambert + ambient
       const float light = fmax_(cdot3(ptl, lnormal) * occlusion, 0.0f);
       const float dscale = fma_(amb1, light, ambient) * ((LC.z * g_diffuse) * illum);
