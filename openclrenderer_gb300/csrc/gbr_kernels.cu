@@ -891,9 +891,9 @@ struct RasterSmem {
   float4 srec[4][NT];  // the staged records' four float4, one array each (conflict-free stores)
   uint32_t sidx[NT];
   uint32_t soff[NT + 1];
-  uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / bw) << 13
+  uint32_t sgeo[NT];  // lx0 | ly0 << 4 | bw << 8 | ceil(65536 / pairs per row) << 13
   uint16_t sskip[NT];  // bit ly: the walk skips the record's left-column pixel in tile row ly
-  // the covered tests of pass 0 kept for the id pass: depth, and pixel |
+  // the covered pixels of pass 0 kept for the id pass: depth, and pixel |
   // staged record << 8; slot k of thread t at k * NT + t
   uint32_t scd[ID && raster_cache_slots<NT>() ? raster_cache_slots<NT>() * NT : 1];
   uint32_t scm[ID && raster_cache_slots<NT>() ? raster_cache_slots<NT>() * NT : 1];
@@ -1886,8 +1886,11 @@ __device__ __forceinline__ void shade_tile(const SceneDev& sc, const ViewParams*
 // A pass whose setup or binning overflowed its scratch leaves the depth and
 // record map unwritten (the raster returns at once); shading returns too, and
 // the host re-runs the pass with grown scratch.
-// tile_empty (or null): tiles whose output the raster wrote; tiles (null for
-// one view): each tile's surface (Workspace).
+// kernel3 over the tiles of a pass, one 256-thread CTA per 16x16 tile.
+// tile_empty (or null): tiles whose output the raster wrote, which return at
+// once; tiles (null for one view): each tile's surface (Workspace).  Each
+// thread reads its pixel; empty pixels get the clear colour, covered ones are
+// compacted in pixel order into the first threads, which shade them.
 template <bool FEAT>
 __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams* __restrict__ views,
                                                const Surface* __restrict__ surfs, uint32_t nviews,
