@@ -110,7 +110,9 @@ typedef struct gbr_view {
  * outline of generate_outline (cl2.cl:2315-2362) added to their colour. */
 #define GBR_VIEW_OUTLINE 2u
 
-/* Device output buffers of one view, row-major W*H.  Any may be NULL. */
+/* Device output buffers of one view, row-major W*H.  Any may be NULL.  The
+ * kernels access every one as 32-bit words (RGBA8 pixels, normal pairs):
+ * each must be 4-byte aligned (GBR_INVALID_ARG otherwise). */
 typedef struct gbr_outputs {
   uint32_t* depth;   /* u32 depth, UINT_MAX where empty (kernel1) */
   uint32_t* id;      /* canonical id 2*triangle+clip_sub, 0xFFFFFFFF where empty (kernel2) */

@@ -118,6 +118,11 @@ gbr_status validate_view(const gbr_view* v) {
   return GBR_OK;
 }
 
+gbr_status validate_outputs(const gbr_outputs& o) {
+  if (const char* b = misaligned_output(o)) return fail(GBR_INVALID_ARG, "%s output is not 4-byte aligned", b);
+  return GBR_OK;
+}
+
 void fill_view_params(const gbr_camera& cam, const gbr_view& v, const gbr_outputs& o, uint32_t surface,
                       ViewParams& V) {
   memcpy(V.cpos, cam.pos, 12);
@@ -906,6 +911,8 @@ static gbr_status render_views(gbr_scene* s, uint32_t n, const gbr_camera* cams,
   size_t npix = 0;
   for (uint32_t i = 0; i < n; i++) {
     TRY(validate_view(&views[i]));
+    TRY(validate_outputs(outs[i]));
+    if (blend) TRY(validate_outputs(blend[i]));
     npix += (size_t)views[i].width * views[i].height;
   }
   std::vector<Surface> surfs(n);

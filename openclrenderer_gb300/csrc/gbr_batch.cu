@@ -250,7 +250,10 @@ gbr_status gbr_batch_create(gbr_scene* s, uint32_t n, const gbr_view* views, con
   TRY(check_scene(s));
   if (!n || !views || !outs) return fail(GBR_INVALID_ARG, "a batch needs n > 0 views and outputs");
   if (flags & ~GBR_BATCH_WITH_SHADOW) return fail(GBR_INVALID_ARG, "unknown batch flags %d", flags);
-  for (uint32_t i = 0; i < n; i++) TRY(validate_view(&views[i]));
+  for (uint32_t i = 0; i < n; i++) {
+    TRY(validate_view(&views[i]));
+    TRY(validate_outputs(outs[i]));
+  }
   gbr_batch* b = new gbr_batch();
   b->s = s;
   b->n = n;

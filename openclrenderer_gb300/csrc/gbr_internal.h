@@ -267,4 +267,16 @@ void set_last_error(const char* msg);
 // while it is rendered (outputs, record map, scratch estimate), for admission.
 uint64_t view_device_bytes(int32_t width, int32_t height);
 
+// The kernels read and write depth, id, RGBA8 pixels and normal pairs as
+// 32-bit words: the name of the first buffer that is not 4-byte aligned, or
+// null.
+inline const char* misaligned_output(const gbr_outputs& o) {
+  auto bad = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 3u) != 0; };
+  if (bad(o.depth)) return "depth";
+  if (bad(o.id)) return "id";
+  if (bad(o.rgba)) return "rgba";
+  if (bad(o.normals)) return "normals";
+  return nullptr;
+}
+
 }  // namespace gbr

@@ -1555,8 +1555,8 @@ __device__ __forceinline__ float generate_outline(int x, int y, const uint32_t* 
 __device__ __forceinline__ f4 blend_texel(const uint8_t* __restrict__ rgba, size_t p) {
   const uchar4 t = reinterpret_cast<const uchar4*>(rgba)[p];
   f4 o;
-  o.x = fdiv((float)t.x, 255.0f); o.y = fdiv((float)t.y, 255.0f);
-  o.z = fdiv((float)t.z, 255.0f); o.w = fdiv((float)t.w, 255.0f);
+  o.x = u8_over_255(t.x); o.y = u8_over_255(t.y);  // fdiv(t, 255.0f)
+  o.z = u8_over_255(t.z); o.w = u8_over_255(t.w);
   return o;
 }
 
@@ -1819,8 +1819,9 @@ __device__ void shade_covered(const SceneDev& sc, const ViewParams& V, const Sur
     if (nx * nx + ny * ny < 0.0001f) nx = 0.01f;
     float l = fsqrt(nx * nx + ny * ny);
     float sq = fsqrt(fmax_(nz * 0.5f + 0.5f, 0.0f));
-    float ex = fdiv(fdiv(nx, l) * sq + 1.0f, 2.0f) * 65536.0f - 1.0f;
-    float ey = fdiv(fdiv(ny, l) * sq + 1.0f, 2.0f) * 65536.0f - 1.0f;
+    // (v / 2 = v * 0.5 exactly: both are the correctly rounded v / 2)
+    float ex = ((fdiv(nx, l) * sq + 1.0f) * 0.5f) * 65536.0f - 1.0f;
+    float ey = ((fdiv(ny, l) * sq + 1.0f) * 0.5f) * 65536.0f - 1.0f;
     uint32_t ux = min(f2u_sat(ex), 65535u), uy = min(f2u_sat(ey), 65535u);
     reinterpret_cast<uint32_t*>(V.normals)[p] = ux | (uy << 16);
   }

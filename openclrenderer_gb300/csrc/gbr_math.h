@@ -489,6 +489,36 @@ GBR_HD uint32_t quant8(float v) {
 }
 
 // ---- post passes -----------------------------------------------------------
+// fdiv(t, 255.0f) and fdiv(t, 65535.0f) for the integers t of a byte and of a
+// 16-bit word, without a division: the product q = t * r with r = RN(1 / d),
+// corrected once by its exact residual, q + (t - d q) r (Markstein's
+// correction step, P. Markstein, "Computation of elementary functions on the
+// IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  Equal to
+// the correctly rounded quotient for every t of the range, checked
+// exhaustively against the IEEE division (tests/cpp/div_const_check.cpp);
+// the post passes' GPU parity tests compare their outputs bit for bit.
+GBR_HD float u8_over_255(uint32_t t) {
+  const float x = (float)t, r = 0x1.010102p-8f;  // RN(1 / 255)
+  const float q = x * r;
+  return fma_(fma_(-255.0f, q, x), r, q);
+}
+GBR_HD float u16_over_65535(uint32_t t) {
+  const float x = (float)t, r = 0x1.0001p-16f;  // RN(1 / 65535)
+  const float q = x * r;
+  return fma_(fma_(-65535.0f, q, x), r, q);
+}
+
+// Pixel p of an RGBA8 image as one word, R in bits 0-7 (the image is 4-byte
+// aligned: the entry points check it; on the device one 32-bit load).
+GBR_HD uint32_t rgba8_word(const uint8_t* img, size_t p) {
+#if defined(__CUDA_ARCH__)
+  return __ldg(reinterpret_cast<const uint32_t*>(img) + p);
+#else
+  const uint8_t* q = img + 4 * p;
+  return (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
+#endif
+}
+
 // Bilinear read of an RGBA8 image at unnormalised float coordinates with
 // clamp-to-edge: OpenCL 1.2 section 8.2's linear filter (i0 = floor(x - 0.5),
 // a = frac(x - 0.5)) with float weights, the device precision pinned.
@@ -501,8 +531,8 @@ GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy
   const int ys[2] = {j0 < 0 ? 0 : (j0 >= H ? H - 1 : j0), j0 + 1 < 0 ? 0 : (j0 + 1 >= H ? H - 1 : j0 + 1)};
   float t[4][4];
   for (int k = 0; k < 4; k++) {
-    const uint8_t* p = img + ((size_t)ys[k >> 1] * W + xs[k & 1]) * 4;
-    for (int c = 0; c < 4; c++) t[k][c] = fdiv((float)p[c], 255.0f);
+    const uint32_t w = rgba8_word(img, (size_t)ys[k >> 1] * W + xs[k & 1]);
+    for (int c = 0; c < 4; c++) t[k][c] = u8_over_255((w >> (8 * c)) & 0xFFu);  // fdiv(channel, 255.0f)
   }
   f4 r;
   float* rc = &r.x;
@@ -516,8 +546,8 @@ GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy
 // normals buffer back to a unit vector; xy carry the direction, their length
 // the z component.
 GBR_HD f3 decode_normal(uint32_t sx, uint32_t sy) {
-  const float vx = fdiv((float)sx, 65535.0f) * 2.0f - 1.0f;
-  const float vy = fdiv((float)sy, 65535.0f) * 2.0f - 1.0f;
+  const float vx = u16_over_65535(sx) * 2.0f - 1.0f;  // fdiv(sx, 65535.0f)
+  const float vy = u16_over_65535(sy) * 2.0f - 1.0f;
   const float z = (vx * vx + vy * vy) * 2.0f - 1.0f;
   const float l = fsqrt(vx * vx + vy * vy);
   const float g = fsqrt(fmax_(1.0f - z * z, 0.0f));

@@ -122,6 +122,7 @@ extern "C" gbr_status gbr_render_view_noalloc(const gbr_device_scene* sc, const 
   set_last_error("");
   if (!sc || !cam || !view || !out) return nfail(GBR_INVALID_ARG, "null argument");
   if (!out->depth || !out->id) return nfail(GBR_INVALID_ARG, "depth and id outputs are required");
+  if (misaligned_output(*out)) return nfail(GBR_INVALID_ARG, "an output buffer is not 4-byte aligned");
   if (view->width < 1 || view->height < 1 || view->width > kMaxWalkWidth || view->height > kMaxWalkHeight)
     return nfail(GBR_INVALID_ARG, "view size outside 1..3840 x 1..2160");
   const size_t P = (size_t)view->width * view->height;

@@ -24,6 +24,11 @@ float view_fov(const gbr_view* v) {
 // The image a pass writes: rgba_out, or the scratch image when in place.
 gbr_status post_target(gbr_scene* s, const gbr_view* view, const uint8_t* in, uint8_t* out, uint8_t** dst) {
   const size_t P = (size_t)view->width * view->height * 4;
+  gbr_outputs io{};
+  io.rgba = const_cast<uint8_t*>(in);
+  TRY(validate_outputs(io));
+  io.rgba = out;
+  TRY(validate_outputs(io));
   if (out == in) {
     TRY(s->post_scratch.reserve(P));
     *dst = s->post_scratch.p;
@@ -48,6 +53,7 @@ gbr_status gbr_post_godrays(gbr_scene* s, const gbr_camera* cam, const gbr_view*
   TRY(check_scene(s));
   TRY(validate_view(view));
   if (!cam || !depth || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  TRY(validate_outputs(gbr_outputs{const_cast<uint32_t*>(depth), nullptr, nullptr, nullptr}));
   uint8_t* dst = nullptr;
   TRY(post_target(s, view, rgba_in, rgba_out, &dst));
   float cc[3], cs[3];
@@ -65,6 +71,7 @@ gbr_status gbr_post_reflections(gbr_scene* s, const gbr_camera* cam, const gbr_v
   TRY(check_scene(s));
   TRY(validate_view(view));
   if (!cam || !depth || !id || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  TRY(validate_outputs(gbr_outputs{const_cast<uint32_t*>(depth), const_cast<uint32_t*>(id), nullptr, nullptr}));
   if (s->ntris && s->max_object_id >= s->ndescs)
     return fail(GBR_INVALID_ARG, "object id %u has no descriptor (%u)", s->max_object_id, s->ndescs);
   if (s->has_ssid && s->max_ssid >= s->mipmap_start)
@@ -86,6 +93,8 @@ gbr_status gbr_post_pseudo_aa(gbr_scene* s, const gbr_view* view, const uint32_t
   TRY(check_scene(s));
   TRY(validate_view(view));
   if (!depth || !id || !normals || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  TRY(validate_outputs(gbr_outputs{const_cast<uint32_t*>(depth), const_cast<uint32_t*>(id), nullptr,
+                                   const_cast<uint16_t*>(normals)}));
   uint8_t* dst = nullptr;
   TRY(post_target(s, view, rgba_in, rgba_out, &dst));
   const cudaStream_t st = (cudaStream_t)stream;
@@ -101,6 +110,7 @@ gbr_status gbr_post_motion_blur(gbr_scene* s, const gbr_camera* cam, const gbr_c
   TRY(check_scene(s));
   TRY(validate_view(view));
   if (!cam || !cam_old || !depth || !id || !rgba_in || !rgba_out) return fail(GBR_INVALID_ARG, "null argument");
+  TRY(validate_outputs(gbr_outputs{const_cast<uint32_t*>(depth), const_cast<uint32_t*>(id), nullptr, nullptr}));
   if (s->ntris && s->max_object_id >= s->ndescs)
     return fail(GBR_INVALID_ARG, "object id %u has no descriptor (%u)", s->max_object_id, s->ndescs);
   uint8_t* dst = nullptr;

@@ -40,6 +40,9 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
     dir = mul3s(dir, step);
     const f3 cval = mul3s(mk3(L.col[0], L.col[1], L.col[2]), ray_intensity);
     const float thr = original.z - 5.0f;
+    // depth_to_dist(d) < thr exactly when depth_scaled(d) < thr * 2^32 (the
+    // scaling by 2^-32 commutes with rounding): one multiplication per step
+    const float thr_scaled = thr * kTwo32;
     const float xmax = (float)W - 1.0f, ymax = (float)H - 1.0f;
     // steps j with (float)j < mnum and j < samples
     const int n = mnum > 0.0f ? (int)fminf(ceilf(mnum), samples) : 0;
@@ -80,7 +83,7 @@ __device__ f4 godrays_pixel(int x, int y, const uint32_t* depth, const uint8_t* 
         if (k < m) {
           // (the reference also requires cdepth != UINT_MAX; an empty pixel is at
           // 350000, never below thr = the pixel's own distance - 5 <= 349995)
-          if (depth_to_dist(dv[k]) < thr) {
+          if (depth_scaled(dv[k]) < thr_scaled) {
             idecay *= 0.9f;
             iter_col = add3(iter_col, mul3s(mul3s(cval, idecay), weight));
           }
@@ -126,65 +129,103 @@ cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* ou
 // units (test 0), or by more than 20 degrees of normal (test 1).  The first
 // test that finds an edge replaces the colour with 0.65 x the mean of the
 // similar neighbours + 0.35 x the mean of the differing ones.
-__device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int H, const uint32_t* __restrict__ depth,
-                                                const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
-                                                f3* out) {
-  const size_t p = (size_t)y * W + x;
-  const float here = depth_to_dist(depth[p]);
-  const ushort2 np = nrm[p];
-  const f3 n0 = fast_normalize3(decode_normal(np.x, np.y));
-  int horiz[2] = {0, 0}, vert[2] = {0, 0}, diag[2] = {0, 0};
-  f3 same[2] = {mk3(0, 0, 0), mk3(0, 0, 0)}, other[2] = {mk3(0, 0, 0), mk3(0, 0, 0)};
-  float nsame[2] = {0, 0}, nother[2] = {0, 0};
+// The 8 neighbours in the reference's order (dy = -1..1, then dx = -1..1),
+// bit j of an edge mask: diagonals j = 0, 2, 5, 7; horizontal 3, 4; vertical
+// 1, 6.
+constexpr uint32_t kAADiag = 0xA5u, kAAHoriz = 0x18u, kAAVert = 0x42u;
+// A 16x16 block's pixels and their neighbours: an 18x18 halo.
+constexpr int kAAHalo = 18;
+
+// The pixel at halo index h (distances and decoded normals staged in shared
+// memory): the edge masks of both tests, then, for the first test that
+// finds an edge, the colour means in the reference's accumulation order.
+// The colours are read only for edge pixels: the other test's sums never
+// reach the output.
+__device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int h, const float* sd, const float* snx,
+                                                const float* sny, const float* snz,
+                                                const uchar4* __restrict__ in, f3* out) {
+  const float here = sd[h];
+  const f3 n0 = fast_normalize3(mk3(snx[h], sny[h], snz[h]));
+  uint32_t e0 = 0, e1 = 0;
+  int j = 0;
 #pragma unroll
   for (int dy = -1; dy <= 1; dy++) {
 #pragma unroll
     for (int dx = -1; dx <= 1; dx++) {
       if (dx == 0 && dy == 0) continue;
-      const size_t q = (size_t)(y + dy) * W + (x + dx);
-      const float d = depth_to_dist(depth[q]);
-      const ushort2 nq = nrm[q];
-      const f3 n = decode_normal(nq.x, nq.y);
-      const uchar4 t = in[q];
-      const f3 c = mk3(fdiv((float)t.x, 255.0f), fdiv((float)t.y, 255.0f), fdiv((float)t.z, 255.0f));
-      const bool edge[2] = {fabsf(d - here) > 100.0f, dot3(n0, n) < kAACos};
+      const int hq = h + dy * kAAHalo + dx;
+      if (fabsf(sd[hq] - here) > 100.0f) e0 |= 1u << j;
+      if (dot3(n0, mk3(snx[hq], sny[hq], snz[hq])) < kAACos) e1 |= 1u << j;
+      j++;
+    }
+  }
+  auto is_edge = [](uint32_t e) {
+    return __popc(e & kAAHoriz) == 1 && __popc(e & kAAVert) == 1 && (e & kAADiag) != 0;
+  };
+  uint32_t e;
+  if (is_edge(e0)) e = e0;
+  else if (is_edge(e1)) e = e1;
+  else return false;
+  f3 same = mk3(0, 0, 0), other = mk3(0, 0, 0);
+  float nsame = 0, nother = 0;
+  j = 0;
 #pragma unroll
-      for (int k = 0; k < 2; k++) {
-        if (edge[k]) {
-          if (dx == dy || dx == -dy) diag[k]++;
-          else if (dx != 0) horiz[k]++;
-          else vert[k]++;
-          other[k] = add3(other[k], c);
-          nother[k] += 1.0f;
-        } else {
-          same[k] = add3(same[k], c);
-          nsame[k] += 1.0f;
-        }
+  for (int dy = -1; dy <= 1; dy++) {
+#pragma unroll
+    for (int dx = -1; dx <= 1; dx++) {
+      if (dx == 0 && dy == 0) continue;
+      const uchar4 t = in[(size_t)(y + dy) * W + (x + dx)];
+      const f3 c = mk3(u8_over_255(t.x), u8_over_255(t.y), u8_over_255(t.z));  // fdiv(t, 255.0f)
+      if ((e >> j) & 1u) {
+        other = add3(other, c);
+        nother += 1.0f;
+      } else {
+        same = add3(same, c);
+        nsame += 1.0f;
       }
+      j++;
     }
   }
-#pragma unroll
-  for (int k = 0; k < 2; k++) {
-    if (horiz[k] == 1 && vert[k] == 1 && diag[k] >= 1) {
-      const f3 m = mk3(fdiv(same[k].x, nsame[k]), fdiv(same[k].y, nsame[k]), fdiv(same[k].z, nsame[k]));
-      const f3 o = mk3(fdiv(other[k].x, nother[k]), fdiv(other[k].y, nother[k]), fdiv(other[k].z, nother[k]));
-      *out = add3(mul3s(m, 0.65f), mul3s(o, 0.35f));
-      return true;
-    }
-  }
-  return false;
+  const f3 m = mk3(fdiv(same.x, nsame), fdiv(same.y, nsame), fdiv(same.z, nsame));
+  const f3 o = mk3(fdiv(other.x, nother), fdiv(other.y, nother), fdiv(other.z, nother));
+  *out = add3(mul3s(m, 0.65f), mul3s(o, 0.35f));
+  return true;
 }
 
-// engine::do_pseudo_aa (engine.cpp:1513-1516): one thread per pixel.
+// engine::do_pseudo_aa (engine.cpp:1513-1516): one thread per pixel, 16x16
+// pixels per block.  The block's 18x18 neighbourhood of distances and
+// decoded normals is staged in shared memory first: each is decoded once
+// instead of by each of its nine readers.
 __global__ void __launch_bounds__(256) k_pseudo_aa(const uint32_t* __restrict__ depth, const uint32_t* __restrict__ ids,
                                                    const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
                                                    uchar4* __restrict__ out, int W, int H) {
-  const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
+  constexpr int E = kAAHalo;
+  __shared__ float sd[E * E], snx[E * E], sny[E * E], snz[E * E];
+  const int bx = blockIdx.x * 16, by = blockIdx.y * 16;
+  for (int i = threadIdx.x; i < E * E; i += blockDim.x) {
+    const int hx = bx - 1 + i % E, hy = by - 1 + i / E;
+    float d = 0.0f;
+    f3 n = mk3(0, 0, 0);
+    if (hx >= 0 && hy >= 0 && hx < W && hy < H) {
+      const size_t q = (size_t)hy * W + hx;
+      d = depth_to_dist(depth[q]);
+      const ushort2 nq = nrm[q];
+      n = decode_normal(nq.x, nq.y);
+    }
+    sd[i] = d;
+    snx[i] = n.x;
+    sny[i] = n.y;
+    snz[i] = n.z;
+  }
+  __syncthreads();
+  const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+  const int x = bx + lx, y = by + ly;
   if (x >= W || y >= H) return;
   const size_t p = (size_t)y * W + x;
   f3 c;
   const bool inner = x >= 1 && y >= 1 && x < W - 1 && y < H - 1;
-  if (inner && depth[p] != kDepthClear && ids[p] != kNoId && pseudo_aa_pixel(x, y, W, H, depth, nrm, in, &c)) {
+  if (inner && depth[p] != kDepthClear && ids[p] != kNoId &&
+      pseudo_aa_pixel(x, y, W, (ly + 1) * E + lx + 1, sd, snx, sny, snz, in, &c)) {
     reinterpret_cast<uint32_t*>(out)[p] = pack_rgba(c.x, c.y, c.z, 1.0f);
   } else {
     out[p] = in[p];
@@ -263,7 +304,7 @@ __global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restr
       sx = fdiv(mx, (float)n);
       sy = fdiv(my, (float)n);
     }
-    float cx = (float)x - fdiv(mx, 2.0f), cy = (float)y - fdiv(my, 2.0f);
+    float cx = (float)x - mx * 0.5f, cy = (float)y - my * 0.5f;  // mx / 2 exactly
     acc.x = acc.y = acc.z = acc.w = 0.0f;
     float cnt = 0.0f;
     for (int i = 0; i < n; i++, cx += sx, cy += sy) {
@@ -506,9 +547,9 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
   const f4 fc = read_linear_rgba8(in, W, H, hit.x, hit.y);
   const uchar4 t = reinterpret_cast<const uchar4*>(in)[p];
   const float den = 1.0f + fade;
-  out->x = fdiv(fdiv((float)t.x, 255.0f) + fc.x * fade, den);
-  out->y = fdiv(fdiv((float)t.y, 255.0f) + fc.y * fade, den);
-  out->z = fdiv(fdiv((float)t.z, 255.0f) + fc.z * fade, den);
+  out->x = fdiv(u8_over_255(t.x) + fc.x * fade, den);  // u8_over_255(t) = fdiv(t, 255.0f)
+  out->y = fdiv(u8_over_255(t.y) + fc.y * fade, den);
+  out->z = fdiv(u8_over_255(t.z) + fc.z * fade, den);
   out->w = 1.0f;
   return 1;
 }

@@ -251,6 +251,7 @@ gbr_status check_scene(gbr_scene* s);
 // Every index the kernels follow must stay inside its table.
 gbr_status check_indices(gbr_scene* s, bool shading);
 gbr_status validate_view(const gbr_view* v);
+gbr_status validate_outputs(const gbr_outputs& o);
 // World-space vertex cache (k_world), rebuilt when triangles or descriptors change.
 gbr_status ensure_world(gbr_scene* s, cudaStream_t st);
 // Fine and coarse tile numbering of a surface; advances the running bases.

@@ -164,6 +164,17 @@ def test_walk_boundaries_are_at_most_one_late(tmp_path):
     assert "early=0" in r.stdout and "late2=0" in r.stdout
 
 
+def test_constant_divisions_match_ieee_division(tmp_path):
+    """u8_over_255 / u16_over_65535 (the post passes' byte and normal decodes)
+    equal the correctly rounded division for every input, bit for bit."""
+    exe = tmp_path / "dcc"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "cpp", "div_const_check.cpp")], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "mismatches_255=0 mismatches_65535=0" in r.stdout
+
+
 def test_oracle_literal_walk_fragment():
     # one fragment of a 10x4 box: 501 steps cover all 40 pixels, in row-major order
     tp = [1, 11, 100, 10, 11, 100, 1, 14, 100]

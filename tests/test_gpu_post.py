@@ -234,6 +234,13 @@ def test_post_and_new_entry_points_reject_bad_arguments():
     o = (ctypes.c_void_p * 4)(d, i, c, None)
     assert status(L.gbr_render_view_blend(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.cast(o, ctypes.c_void_p), None,
                                           None)) == INVALID
+    # buffers the kernels access as 32-bit words must be 4-byte aligned
+    assert status(L.gbr_post_pseudo_aa(gs.h, _np_ptr(view), d, i, n, c + 1, dst, None)) == INVALID
+    assert status(L.gbr_post_godrays(gs.h, _np_ptr(cam), _np_ptr(view), d, c, dst + 2, None)) == INVALID
+    for k, ptrs in enumerate([(d + 2, i, c, n), (d, i + 1, c, n), (d, i, c + 3, n), (d, i, c, n + 2)]):
+        o = (ctypes.c_void_p * 4)(*ptrs)
+        assert status(L.gbr_render_view(gs.h, _np_ptr(cam), _np_ptr(view), ctypes.cast(o, ctypes.c_void_p),
+                                        None)) == INVALID, f"misaligned output {k} accepted"
     buf = np.zeros(len(sc.descs) + 1, S.OBJ_DESC)
     assert status(L.gbr_scene_get_descriptors(gs.h, _np_ptr(buf), len(buf))) == INVALID
     assert status(L.gbr_batch_wait_for(None, 10)) == INVALID
