@@ -502,9 +502,14 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
 #pragma unroll
     for (int k = 3; k >= 0; k--)
       if (pt[k].x < 0 || pt[k].y < 0 || pt[k].x >= fw || pt[k].y >= fh) m = k;
+    // a step on screen has 0 <= x < W and 0 <= y < H, or a NaN coordinate
+    // (every comparison above fails on NaN): f2i_sat is then a truncation,
+    // or 0 for NaN
+    auto on_screen_int = [](float c) { return c == c ? (int)c : 0; };
     uint32_t dv[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) dv[k] = k < m ? __ldg(depth + (size_t)f2i_sat(pt[k].y) * W + f2i_sat(pt[k].x)) : 0u;
+    for (int k = 0; k < 4; k++)
+      dv[k] = k < m ? __ldg(depth + (size_t)on_screen_int(pt[k].y) * W + on_screen_int(pt[k].x)) : 0u;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (found) break;
@@ -523,12 +528,14 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
   f3 hit = cur;
   bool ok = false;
   for (int i = 0; i < 10; i++) {
-    hit = line_depth_point(vprev, vstart, ta);
+    // line_depth_point(vprev, vstart, ta) with its two reciprocals hoisted
+    const float tb = 1.0f - ta;
+    hit = mk3(fma_(vprev.x, tb, vstart.x * ta), fma_(vprev.y, tb, vstart.y * ta), rcp(fma_(ipz, tb, isz * ta)));
     if (stop < hit.z + 1.0f && stop > hit.z - 20.0f) {
       ok = true;
       break;
     }
-    ta += fdiv(1.0f, 10.0f);
+    ta += 0.1f;  // fdiv(1.0f, 10.0f) = RN(0.1)
   }
   if (!ok) return 0;
   const f3 te = line_depth_point(vstart, hit, 1.35f);
