@@ -521,8 +521,13 @@ GBR_HD uint32_t rgba8_word(const uint8_t* img, size_t p) {
 
 // Bilinear read of an RGBA8 image at unnormalised float coordinates with
 // clamp-to-edge: OpenCL 1.2 section 8.2's linear filter (i0 = floor(x - 0.5),
-// a = frac(x - 0.5)) with float weights, the device precision pinned.
-GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy) {
+// a = frac(x - 0.5)) with float weights, the device precision pinned.  conv
+// maps a channel byte c to fdiv(c, 255.0f).
+struct ByteOver255 {
+  GBR_HD float operator()(uint32_t c) const { return u8_over_255(c); }
+};
+template <typename Conv>
+GBR_HD f4 read_linear_rgba8_with(const uint8_t* img, int W, int H, float cx, float cy, Conv conv) {
   const float u = cx - 0.5f, v = cy - 0.5f;
   const float fi = floorf(u), fj = floorf(v);
   const float a = u - fi, b = v - fj;
@@ -532,7 +537,7 @@ GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy
   float t[4][4];
   for (int k = 0; k < 4; k++) {
     const uint32_t w = rgba8_word(img, (size_t)ys[k >> 1] * W + xs[k & 1]);
-    for (int c = 0; c < 4; c++) t[k][c] = u8_over_255((w >> (8 * c)) & 0xFFu);  // fdiv(channel, 255.0f)
+    for (int c = 0; c < 4; c++) t[k][c] = conv((w >> (8 * c)) & 0xFFu);
   }
   f4 r;
   float* rc = &r.x;
@@ -540,6 +545,9 @@ GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy
     rc[c] = ((((1.0f - a) * (1.0f - b)) * t[0][c] + (a * (1.0f - b)) * t[1][c]) + ((1.0f - a) * b) * t[2][c]) +
             (a * b) * t[3][c];
   return r;
+}
+GBR_HD f4 read_linear_rgba8(const uint8_t* img, int W, int H, float cx, float cy) {
+  return read_linear_rgba8_with(img, W, H, cx, cy, ByteOver255());
 }
 
 // short_to_float + decode_normal (cl2.cl:5597-5642): the ushort2 of the

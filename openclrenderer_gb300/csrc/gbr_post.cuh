@@ -133,8 +133,11 @@ cudaError_t launch_godrays(const uint32_t* depth, const uint8_t* in, uint8_t* ou
 // bit j of an edge mask: diagonals j = 0, 2, 5, 7; horizontal 3, 4; vertical
 // 1, 6.
 constexpr uint32_t kAADiag = 0xA5u, kAAHoriz = 0x18u, kAAVert = 0x42u;
-// A 16x16 block's pixels and their neighbours: an 18x18 halo.
-constexpr int kAAHalo = 18;
+// A block covers 32x8 pixels, one row per warp (so that a warp's halo reads
+// are 32 consecutive words, free of bank conflicts); with their neighbours,
+// a 34x10 halo.
+constexpr int kAABlockW = 32, kAABlockH = 8;
+constexpr int kAAHalo = kAABlockW + 2, kAAHaloH = kAABlockH + 2;
 
 // The pixel at halo index h (distances and decoded normals staged in shared
 // memory): the edge masks of both tests, then, for the first test that
@@ -192,17 +195,17 @@ __device__ __forceinline__ bool pseudo_aa_pixel(int x, int y, int W, int h, cons
   return true;
 }
 
-// engine::do_pseudo_aa (engine.cpp:1513-1516): one thread per pixel, 16x16
-// pixels per block.  The block's 18x18 neighbourhood of distances and
+// engine::do_pseudo_aa (engine.cpp:1513-1516): one thread per pixel, 32x8
+// pixels per block.  The block's 34x10 neighbourhood of distances and
 // decoded normals is staged in shared memory first: each is decoded once
 // instead of by each of its nine readers.
 __global__ void __launch_bounds__(256) k_pseudo_aa(const uint32_t* __restrict__ depth, const uint32_t* __restrict__ ids,
                                                    const ushort2* __restrict__ nrm, const uchar4* __restrict__ in,
                                                    uchar4* __restrict__ out, int W, int H) {
-  constexpr int E = kAAHalo;
-  __shared__ float sd[E * E], snx[E * E], sny[E * E], snz[E * E];
-  const int bx = blockIdx.x * 16, by = blockIdx.y * 16;
-  for (int i = threadIdx.x; i < E * E; i += blockDim.x) {
+  constexpr int E = kAAHalo, N = kAAHalo * kAAHaloH;
+  __shared__ float sd[N], snx[N], sny[N], snz[N];
+  const int bx = blockIdx.x * kAABlockW, by = blockIdx.y * kAABlockH;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const int hx = bx - 1 + i % E, hy = by - 1 + i / E;
     float d = 0.0f;
     f3 n = mk3(0, 0, 0);
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(256) k_pseudo_aa(const uint32_t* __restrict__ 
     snz[i] = n.z;
   }
   __syncthreads();
-  const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+  const int lx = threadIdx.x % kAABlockW, ly = threadIdx.x / kAABlockW;
   const int x = bx + lx, y = by + ly;
   if (x >= W || y >= H) return;
   const size_t p = (size_t)y * W + x;
@@ -234,8 +237,8 @@ __global__ void __launch_bounds__(256) k_pseudo_aa(const uint32_t* __restrict__ 
 
 cudaError_t launch_pseudo_aa(const uint32_t* depth, const uint32_t* ids, const uint16_t* normals, const uint8_t* in,
                              uint8_t* out, int W, int H, cudaStream_t st) {
-  dim3 grid((W + 15) / 16, (H + 15) / 16);
-  k_pseudo_aa<<<grid, 256, 0, st>>>(depth, ids, reinterpret_cast<const ushort2*>(normals),
+  dim3 grid((W + kAABlockW - 1) / kAABlockW, (H + kAABlockH - 1) / kAABlockH);
+  k_pseudo_aa<<<grid, kAABlockW * kAABlockH, 0, st>>>(depth, ids, reinterpret_cast<const ushort2*>(normals),
                                     reinterpret_cast<const uchar4*>(in), reinterpret_cast<uchar4*>(out), W, H);
   return cudaGetLastError();
 }
@@ -260,6 +263,16 @@ __global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restr
                                                      const uint32_t* __restrict__ ids, const uint8_t* __restrict__ in,
                                                      uint8_t* __restrict__ out, int W, int H, MotionCam a,
                                                      uint32_t* __restrict__ seen, uint32_t ntris) {
+  // the 256 quotients c / 255 of a channel byte (u8_over_255), read by every
+  // bilinear tap from shared memory
+  __shared__ float s255[256];
+  s255[threadIdx.x] = u8_over_255(threadIdx.x);
+  __syncthreads();
+  struct Tab {
+    const float* t;
+    __device__ float operator()(uint32_t c) const { return t[c]; }
+  };
+  const Tab tab{s255};
   const int x = blockIdx.x * 16 + (threadIdx.x & 15), y = blockIdx.y * 16 + (threadIdx.x >> 4);
   if (x >= W || y >= H) return;
   const size_t p = (size_t)y * W + x;
@@ -285,7 +298,7 @@ __global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restr
   const f3 prev = depth_project1(rot_cs(last, a.opos, a.oc, a.os), (float)W, (float)H, a.fov);
   f4 acc;
   if (prev.z < 20.0f) {
-    acc = read_linear_rgba8(in, W, H, (float)x + 0.5f, (float)y + 0.5f);
+    acc = read_linear_rgba8_with(in, W, H, (float)x + 0.5f, (float)y + 0.5f, tab);
   } else {
     float mx = (float)x - prev.x, my = (float)y - prev.y;
     const float nx = (float)x - nocam.x, ny = (float)y - nocam.y;
@@ -309,7 +322,7 @@ __global__ void __launch_bounds__(256) k_motion_blur(const gbr_triangle* __restr
     float cnt = 0.0f;
     for (int i = 0; i < n; i++, cx += sx, cy += sy) {
       if (cx < 0 || cx >= (float)W || cy < 0 || cy >= (float)H) continue;
-      const f4 c = read_linear_rgba8(in, W, H, cx + 0.5f, cy + 0.5f);
+      const f4 c = read_linear_rgba8_with(in, W, H, cx + 0.5f, cy + 0.5f, tab);
       acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
       cnt += 1.0f;
     }
@@ -478,34 +491,37 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
   const float fw = (float)W, fh = (float)H;
   if (sj.x < 0 || sj.y < 0 || sj.x >= fw || sj.y >= fh) return 0;
   // The march: step i at sj (i = 0) or line_depth_point(vprev, vstart, 1 + i),
-  // until the depth buffer is more than 1 unit in front of the ray.  Four
-  // steps at a time: positions first (they do not depend on the loads), then
-  // their depth loads in flight together, then the tests in order.
+  // i < 200, until the depth buffer is more than 1 unit in front of the ray;
+  // a step off screen ends it unmet.  Step 0 first, then four steps at a
+  // time: positions first (they do not depend on the loads), then their
+  // depth loads in flight together, then the tests in order.
   const float ipz = rcp(vprev.z), isz = rcp(vstart.z);  // line_depth_point's reciprocals, loop-invariant
-  f3 cur = sj;
+  // a step on screen has 0 <= x < W and 0 <= y < H, or a NaN coordinate
+  // (every comparison of the test fails on NaN): f2i_sat is then a
+  // truncation, or 0 for NaN
+  auto on_screen_int = [](float c) { return c == c ? (int)c : 0; };
   float a = 1.0f, stop = 0.0f;
   bool found = false;
-  for (int i0 = 0; i0 < 200 && !found; i0 += 4) {
+  {
+    const float dd = depth_to_dist(__ldg(depth + (size_t)on_screen_int(sj.y) * W + on_screen_int(sj.x)));
+    if (dd < sj.z - 1.0f) {
+      found = true;
+      stop = dd;  // the refinement reads the depth where the march stopped on every try
+    }
+  }
+  for (int i0 = 1; i0 < 200 && !found; i0 += 4) {
     f3 pt[4];
-    int m = 4;  // the first step off screen
+    int m = min(4, 200 - i0);  // the first step off screen, or past the last
+    const float fi0 = (float)i0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      const int i = i0 + k;
-      if (i == 0) {
-        pt[k] = sj;
-      } else {
-        const float ai = 1.0f + (float)i, b = 1.0f - ai;
-        pt[k] = mk3(fma_(vprev.x, b, vstart.x * ai), fma_(vprev.y, b, vstart.y * ai),
-                    rcp(fma_(ipz, b, isz * ai)));
-      }
+      // ai = 1 + i and b = 1 - ai = -i, both exact (integers below 2^24)
+      const float fi = fi0 + (float)k, ai = fi + 1.0f;
+      pt[k] = mk3(fma_(vprev.x, -fi, vstart.x * ai), fma_(vprev.y, -fi, vstart.y * ai), rcp(fma_(ipz, -fi, isz * ai)));
     }
 #pragma unroll
     for (int k = 3; k >= 0; k--)
-      if (pt[k].x < 0 || pt[k].y < 0 || pt[k].x >= fw || pt[k].y >= fh) m = k;
-    // a step on screen has 0 <= x < W and 0 <= y < H, or a NaN coordinate
-    // (every comparison above fails on NaN): f2i_sat is then a truncation,
-    // or 0 for NaN
-    auto on_screen_int = [](float c) { return c == c ? (int)c : 0; };
+      if (pt[k].x < 0 || pt[k].y < 0 || pt[k].x >= fw || pt[k].y >= fh) m = min(m, k);
     uint32_t dv[4];
 #pragma unroll
     for (int k = 0; k < 4; k++)
@@ -513,19 +529,18 @@ __device__ int reflection_pixel(const SceneDev& sc, const ReflectCam& v, int x, 
 #pragma unroll
     for (int k = 0; k < 4; k++) {
       if (found) break;
-      if (k >= m) return 0;  // off screen before the ray met anything
+      if (k >= m) return 0;  // off screen (or past step 199) before the ray met anything
       const float dd = depth_to_dist(dv[k]);
       if (dd < pt[k].z - 1.0f) {
         found = true;
-        cur = pt[k];
-        a = 1.0f + (float)(i0 + k);
-        stop = dd;  // the refinement reads the depth where the march stopped on every try
+        a = fi0 + (float)(k + 1);  // 1 + i
+        stop = dd;
       }
     }
   }
   if (!found) return 0;
   float ta = a;
-  f3 hit = cur;
+  f3 hit = sj;
   bool ok = false;
   for (int i = 0; i < 10; i++) {
     // line_depth_point(vprev, vstart, ta) with its two reciprocals hoisted
