@@ -908,11 +908,11 @@ struct RasterSmem {
 };
 
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
-// (views) or only the depth (cube faces).  surface: the tile's surface when
-// the caller knows it, else -1 (ws.tiles, or the pass's only surface).
-// Every thread of the block calls it; the caller synchronises before reusing
-// the shared memory.
-template <int NT, bool ID>
+// (views) or only the depth (cube faces); CC: see chunk below.  surface: the
+// tile's surface when the caller knows it, else -1 (ws.tiles, or the pass's
+// only surface).  Every thread of the block calls it; the caller synchronises
+// before reusing the shared memory.
+template <int NT, bool ID, bool CC = false>
 __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* __restrict__ surfs, uint32_t nsurf,
                                             uint32_t tile, int surface, RasterSmem<NT, ID>& sm) {
   constexpr bool with_id = ID;
@@ -1004,7 +1004,12 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
       sdepth[swz32(p)] = (px < S.width && py < S.height) ? S.depth[(size_t)py * S.width + px] : kDepthClear;
     }
   }
-  const int chunk = S.chunk;
+  // the walk's fragment size (Surface.chunk: op_size for views, op_size_light
+  // for cube faces).  CC (passes of several view surfaces) takes it as the
+  // constant op_size, so that the walk rule's modulos are multiplications:
+  // 1.8 % faster batches; the one-view raster measured faster with the
+  // runtime value
+  const int chunk = CC ? kOpSize : S.chunk;
   const uint32_t nfine = lists[1], ntotal = lists[1] + lists[3];
   const int passes = ntotal == 0 ? 0 : (with_id ? 2 : 1);
   const bool resident = ntotal <= (uint32_t)NT;
@@ -1182,14 +1187,14 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   }
 }
 
-template <int NT, bool ID>
+template <int NT, bool ID, bool CC = false>
 __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
                                                           uint32_t nsurf, uint32_t tile0) {
   __shared__ RasterSmem<NT, ID> sm;
   if (ws.ctr->overflow) return;
   // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
   const uint32_t tile = gridDim.y > 1 ? surfs[blockIdx.y].tile_base + blockIdx.x : tile0 + blockIdx.x;
-  raster_tile<NT, ID>(ws, surfs, nsurf, tile, gridDim.y > 1 ? (int)blockIdx.y : -1, sm);
+  raster_tile<NT, ID, CC>(ws, surfs, nsurf, tile, gridDim.y > 1 ? (int)blockIdx.y : -1, sm);
 }
 
 // ---- kernel3 ------------------------------------------------------------------
@@ -2277,6 +2282,14 @@ cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t n
   // surfaces of equal size: one grid row per surface, no search for the owner
   const dim3 grid = (tile0 == 0 && tiles_per_surface && nsurf > 1 && nsurf <= 65535 &&
                      tiles_per_surface * nsurf == ntiles) ? dim3(tiles_per_surface, nsurf) : dim3(ntiles);
+  if (with_id && ws.tiles) {
+    switch (threads) {
+      case 128: k_raster<128, true, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+      case 512: k_raster<512, true, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+      default: k_raster<256, true, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    }
+    return cudaGetLastError();
+  }
   switch (threads * 2 + wid) {
     case 256: k_raster<128, false><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
     case 257: k_raster<128, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
