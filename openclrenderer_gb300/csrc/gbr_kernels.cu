@@ -322,15 +322,6 @@ __device__ __forceinline__ void load_tri_pos(const gbr_triangle* T, f3 v[3], uin
 }
 
 
-// Programmatic dependent launch.  The pass kernels launched with
-// launch_dep may be scheduled while the previous kernel of their stream
-// drains: pdl_wait() holds every thread until that kernel has completed and
-// its writes are visible (it returns at once for a kernel launched the usual
-// way), and pdl_trigger() lets the next kernel be scheduled once every block
-// of this one has started.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-
 // World-space vertices of every triangle: rot_quat(v * scale, q) + world_pos,
 // the object half of full_rotate_quat (cl2.cl:700-710).  It does not depend on
 // the camera, so one pass serves the view and all cube faces until the
@@ -387,8 +378,6 @@ __global__ void __launch_bounds__(256) k_world(SceneDev sc, float4* __restrict__
 __global__ void __launch_bounds__(256) k_object_cull(SceneDev sc, const ViewParams* __restrict__ views,
                                                      const Surface* __restrict__ surfs, const uint32_t* __restrict__ objr,
                                                      uint32_t words, uint32_t* __restrict__ vis) {
-  pdl_wait();
-  pdl_trigger();
   const uint32_t o = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t v = blockIdx.y;
   bool keep = false;
@@ -522,8 +511,6 @@ __device__ __forceinline__ int make_cands(const f3 w[3], f3 cpos, f3 c, f3 s, fl
 // prearrange (cl2.cl:4271-4409), one thread per (triangle, view).
 __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewParams* __restrict__ views,
                                                      const Surface* __restrict__ surfs, Workspace ws) {
-  pdl_wait();
-  pdl_trigger();
   uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
   const ViewParams& V = views[blockIdx.y];
   const Surface& S = surfs[V.surface];
@@ -558,8 +545,6 @@ __global__ void __launch_bounds__(256) k_setup_views(SceneDev sc, const ViewPara
 // prearrange_realtime_shadowing (cl2.cl:4419-4636), one thread per (triangle, light job).
 __global__ void __launch_bounds__(128, 6) k_setup_shadow(SceneDev sc, const ShadowJob* __restrict__ jobs,
                                                       const Surface* __restrict__ surfs, Workspace ws) {
-  pdl_wait();
-  pdl_trigger();
   uint32_t tri = blockIdx.x * blockDim.x + threadIdx.x;
   const ShadowJob& J = jobs[blockIdx.y];
   const float L = (float)kLightBufferDim;
@@ -598,8 +583,6 @@ __global__ void __launch_bounds__(128, 6) k_setup_shadow(SceneDev sc, const Shad
 // tile: the raster's and kernel3's first loads.
 __global__ void __launch_bounds__(256) k_tile_table(const Surface* __restrict__ surfs, uint32_t nsurf,
                                                     uint32_t nfine, int coarse_shift, uint2* __restrict__ tiles) {
-  pdl_wait();
-  pdl_trigger();
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nfine) return;
   uint32_t lo = 0, hi = nsurf - 1;
@@ -678,8 +661,6 @@ __device__ void block_scan_array(uint32_t* count, uint32_t* off, uint32_t n, uin
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan(Workspace ws) {
-  pdl_wait();
-  pdl_trigger();
   __shared__ uint32_t sh[kScanChunk];
   __shared__ uint32_t swarp[32];
   __shared__ uint32_t sctot;
@@ -767,8 +748,6 @@ __global__ void __launch_bounds__(256, 4) k_prep(SceneDev sc, Workspace ws) {
 // chunk's total in scan_part; one more block scans the coarse counts whole.
 // k_scan_add then adds the totals of the chunks before each chunk.
 __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Workspace ws, uint32_t nchunks) {
-  pdl_wait();
-  pdl_trigger();
   __shared__ uint32_t sh[kScanChunk];
   __shared__ uint32_t swarp[32];
   __shared__ uint32_t sctot;
@@ -782,8 +761,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(Workspace ws, uint
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_add(Workspace ws, uint32_t nchunks) {
-  pdl_wait();
-  pdl_trigger();
   __shared__ uint32_t base;
   if (threadIdx.x < 32) {
     uint32_t sum = 0;
@@ -805,8 +782,6 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(Workspace ws, uint32_
 // Scatter record indices into their tile bins (cursor atomics aggregated
 // across the warp).
 __global__ void __launch_bounds__(256) k_fill(Workspace ws, const Surface* __restrict__ surfs) {
-  pdl_wait();
-  pdl_trigger();
   const uint32_t nrec = min(ws.ctr->nrec, ws.rec_cap);
   if (ws.ctr->overflow) return;
   const uint32_t coarse_base = ws.ctr->fine_total;
@@ -932,44 +907,6 @@ struct RasterSmem {
   uint32_t lists[4];
 };
 
-// A view tile without records: depth, id and record map cleared; where the
-// raster finishes kernel3's output too (views that do not blend in another
-// context), the clear RGBA8 and zero normals, and the tile is flagged so that
-// kernel3 reads nothing of it.  Every thread of the block calls it.
-template <int NT>
-__device__ __forceinline__ void empty_view_tile(const Workspace& ws, const Surface& S, uint32_t s, uint32_t tile,
-                                                int tx0, int ty0, int tid) {
-  uint32_t* rgba = nullptr;
-  uint32_t* nrm = nullptr;
-  uint32_t* rmap = S.rec;
-  uint32_t clear = 0;
-  if (ws.tile_empty) {
-    const ViewParams& V = ws.views[s];
-    const bool direct = V.blend_depth == nullptr;
-    if (direct) {
-      rgba = reinterpret_cast<uint32_t*>(V.rgba);
-      nrm = reinterpret_cast<uint32_t*>(V.normals);
-      rmap = nullptr;
-      clear = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
-    }
-    if (tid == 0) ws.tile_empty[tile] = direct ? 1 : 0;
-  }
-  const int W = S.width, H = S.height;
-  uint32_t* depth = S.depth;
-  uint32_t* id = S.id;
-  for (int lp = tid; lp < kTilePixels; lp += NT) {
-    const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
-    if (px < W && py < H) {
-      const size_t p = (size_t)py * W + px;
-      depth[p] = kDepthClear;
-      if (id) id[p] = kNoId;
-      if (rmap) rmap[p] = kNoId;
-      if (rgba) rgba[p] = clear;
-      if (nrm) nrm[p] = 0;
-    }
-  }
-}
-
 // NT threads per CTA (128, 256 or 512); ID: resolve the canonical id too
 // (views) or only the depth (cube faces); CC: see chunk below.  surface: the
 // tile's surface when the caller knows it, else -1 (ws.tiles, or the pass's
@@ -1026,7 +963,35 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
   const uint32_t lt = tile - S.tile_base;
   const int tx0 = (lt % S.tiles_x) * kTile, ty0 = (lt / S.tiles_x) * kTile;
   if (with_id && lists[1] + lists[3] == 0) {  // no records: an empty tile
-    empty_view_tile<NT>(ws, S, sm.s, tile, tx0, ty0, tid);
+    // kernel3's output here is the clear colour and zero normals, unless the
+    // view blends in another context's colour: write it, and mark the tile
+    // (kernel3 then reads nothing of it, the record map included)
+    uint32_t* rgba = nullptr;
+    uint32_t* nrm = nullptr;
+    uint32_t* rmap = S.rec;
+    uint32_t clear = 0;
+    if (ws.tile_empty) {
+      const ViewParams& V = ws.views[sm.s];
+      const bool direct = V.blend_depth == nullptr;
+      if (direct) {
+        rgba = reinterpret_cast<uint32_t*>(V.rgba);
+        nrm = reinterpret_cast<uint32_t*>(V.normals);
+        rmap = nullptr;
+        clear = pack_rgba(V.clear[0], V.clear[1], V.clear[2], V.clear[3]);
+      }
+      if (tid == 0) ws.tile_empty[tile] = direct ? 1 : 0;
+    }
+    for (int lp = tid; lp < kTilePixels; lp += NT) {
+      const int px = tx0 + (lp & (kTile - 1)), py = ty0 + (lp / kTile);
+      if (px < S.width && py < S.height) {
+        const size_t p = (size_t)py * S.width + px;
+        S.depth[p] = kDepthClear;
+        if (S.id) S.id[p] = kNoId;
+        if (rmap) rmap[p] = kNoId;
+        if (rgba) rgba[p] = clear;
+        if (nrm) nrm[p] = 0;
+      }
+    }
     return;
   }
   if (with_id && ws.tile_empty && tid == 0) ws.tile_empty[tile] = 0;
@@ -1225,8 +1190,6 @@ __device__ __forceinline__ void raster_tile(const Workspace& ws, const Surface* 
 template <int NT, bool ID, bool CC = false>
 __global__ void __launch_bounds__(NT, (ID ? 1024 : 1280) / NT) k_raster(Workspace ws, const Surface* __restrict__ surfs,
                                                           uint32_t nsurf, uint32_t tile0) {
-  pdl_wait();
-  pdl_trigger();
   __shared__ RasterSmem<NT, ID> sm;
   if (ws.ctr->overflow) return;
   // surfaces of one size (cube faces) come as grid rows: surface = blockIdx.y
@@ -1941,8 +1904,6 @@ __global__ void __launch_bounds__(256, 4) k_shade(SceneDev sc, const ViewParams*
                                                uint32_t rec_cap, uint32_t tile0,
                                                const uint8_t* __restrict__ tile_empty,
                                                const uint2* __restrict__ tiles) {
-  pdl_wait();
-  pdl_trigger();
   constexpr int NW = kTilePixels / 32;
   __shared__ ShadeSmem sm;
   __shared__ uint32_t s_warp[NW];
@@ -2194,8 +2155,6 @@ __global__ void k_flush_objects(gbr_obj_g_descriptor* descs, const gbr_object_fl
 // Clear every surface of a depth-only pass to UINT_MAX before its setup
 // rasterises small candidates into them (blockIdx.y = surface).
 __global__ void __launch_bounds__(256) k_clear_surfaces(const Surface* __restrict__ surfs) {
-  pdl_wait();
-  pdl_trigger();
   const Surface& S = surfs[blockIdx.y];
   const size_t n = (size_t)S.width * S.height;
   uint4* d4 = reinterpret_cast<uint4*>(S.depth);
@@ -2242,28 +2201,6 @@ int num_sms() {
 
 }  // namespace
 
-// A pass kernel launched so that it may be scheduled while the previous
-// kernel of the stream drains (its pdl_wait() orders it after that kernel):
-// a 1080p frame 1.2 % and a small view's call 6 % faster.  A stream being
-// captured into a graph gets the usual launch: captured batches measured 1 %
-// slower with programmatic edges.
-template <typename... P, typename... A>
-cudaError_t launch_dep(void (*k)(P...), dim3 grid, dim3 block, cudaStream_t st, A... args) {
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return cudaGetLastError();
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = 0;
-  cfg.stream = st;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = cap == cudaStreamCaptureStatusNone ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, k, args...);
-}
-
 cudaError_t launch_world(const SceneDev& sc, float4* world, float4* objq, uint32_t* objr, cudaStream_t st) {
   if (sc.ndescs) k_objects<<<(sc.ndescs + 255) / 256, 256, 0, st>>>(sc, objq);
   if (sc.ntris && world) {
@@ -2294,29 +2231,35 @@ cudaError_t launch_setup_views(const SceneDev& sc, const ViewParams* d_views, ui
                                const Surface* d_surf, const Workspace& ws, cudaStream_t st) {
   if (!sc.ntris || !nviews) return cudaSuccess;
   dim3 grid((sc.ntris + 255) / 256, nviews);
-  return launch_dep(k_setup_views, grid, dim3(256), st, sc, d_views, d_surf, ws);
+  k_setup_views<<<grid, 256, 0, st>>>(sc, d_views, d_surf, ws);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_setup_shadow(const SceneDev& sc, const ShadowJob* d_jobs, uint32_t njobs,
                                 const Surface* d_surf, const Workspace& ws, cudaStream_t st) {
   if (!sc.ntris || !njobs) return cudaSuccess;
   dim3 grid((sc.ntris + 127) / 128, njobs);  // small blocks: lanes' direct rasters differ in length
-  return launch_dep(k_setup_shadow, grid, dim3(128), st, sc, d_jobs, d_surf, ws);
+  k_setup_shadow<<<grid, 128, 0, st>>>(sc, d_jobs, d_surf, ws);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_tile_table(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, cudaStream_t st) {
   if (!ws.nfine) return cudaSuccess;
   if (!ws.tiles || !nsurf) return cudaErrorInvalidValue;
-  return launch_dep(k_tile_table, dim3((ws.nfine + 255) / 256), dim3(256), st, d_surf, nsurf, ws.nfine,
-                    ws.coarse_shift, const_cast<uint2*>(ws.tiles));
+  k_tile_table<<<(ws.nfine + 255) / 256, 256, 0, st>>>(d_surf, nsurf, ws.nfine, ws.coarse_shift,
+                                                       const_cast<uint2*>(ws.tiles));
+  return cudaGetLastError();
 }
 
 cudaError_t launch_scan(const Workspace& ws, cudaStream_t st) {
   const uint32_t nchunks = (ws.nfine + kScanChunk - 1) / kScanChunk;
-  if (nchunks <= 1 || !ws.scan_part) return launch_dep(k_scan, dim3(1), dim3(kScanThreads), st, ws);
-  cudaError_t e = launch_dep(k_scan_chunks, dim3(nchunks + 1), dim3(kScanThreads), st, ws, nchunks);
-  if (e != cudaSuccess) return e;
-  return launch_dep(k_scan_add, dim3(nchunks), dim3(kScanThreads), st, ws, nchunks);
+  if (nchunks <= 1 || !ws.scan_part) {
+    k_scan<<<1, kScanThreads, 0, st>>>(ws);
+  } else {
+    k_scan_chunks<<<nchunks + 1, kScanThreads, 0, st>>>(ws, nchunks);
+    k_scan_add<<<nchunks, kScanThreads, 0, st>>>(ws, nchunks);
+  }
+  return cudaGetLastError();
 }
 
 uint32_t scan_chunks(uint32_t nfine) { return (nfine + kScanChunk - 1) / kScanChunk; }
@@ -2328,34 +2271,34 @@ cudaError_t launch_prep(const SceneDev& sc, const Workspace& ws, cudaStream_t st
 }
 
 cudaError_t launch_fill(const Workspace& ws, const Surface* d_surf, cudaStream_t st) {
-  return launch_dep(k_fill, dim3(num_sms() * 8), dim3(256), st, ws, d_surf);
+  k_fill<<<num_sms() * 8, 256, 0, st>>>(ws, d_surf);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_raster(const Workspace& ws, const Surface* d_surf, uint32_t nsurf, uint32_t ntiles,
                           bool with_id, int threads, cudaStream_t st, uint32_t tiles_per_surface, uint32_t tile0) {
   if (!ntiles) return cudaSuccess;
   const int wid = with_id ? 1 : 0;
-  cudaError_t e = cudaSuccess;
   // surfaces of equal size: one grid row per surface, no search for the owner
   const dim3 grid = (tile0 == 0 && tiles_per_surface && nsurf > 1 && nsurf <= 65535 &&
                      tiles_per_surface * nsurf == ntiles) ? dim3(tiles_per_surface, nsurf) : dim3(ntiles);
   if (with_id && ws.tiles) {
     switch (threads) {
-      case 128: e = launch_dep(k_raster<128, true, true>, grid, dim3(128), st, ws, d_surf, nsurf, tile0); break;
-      case 512: e = launch_dep(k_raster<512, true, true>, grid, dim3(512), st, ws, d_surf, nsurf, tile0); break;
-      default: e = launch_dep(k_raster<256, true, true>, grid, dim3(256), st, ws, d_surf, nsurf, tile0); break;
+      case 128: k_raster<128, true, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+      case 512: k_raster<512, true, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+      default: k_raster<256, true, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
     }
-    return e;
+    return cudaGetLastError();
   }
   switch (threads * 2 + wid) {
-    case 256: e = launch_dep(k_raster<128, false>, grid, dim3(128), st, ws, d_surf, nsurf, tile0); break;
-    case 257: e = launch_dep(k_raster<128, true>, grid, dim3(128), st, ws, d_surf, nsurf, tile0); break;
-    case 1024: e = launch_dep(k_raster<512, false>, grid, dim3(512), st, ws, d_surf, nsurf, tile0); break;
-    case 1025: e = launch_dep(k_raster<512, true>, grid, dim3(512), st, ws, d_surf, nsurf, tile0); break;
-    case 513: e = launch_dep(k_raster<256, true>, grid, dim3(256), st, ws, d_surf, nsurf, tile0); break;
-    default: e = launch_dep(k_raster<256, false>, grid, dim3(256), st, ws, d_surf, nsurf, tile0); break;
+    case 256: k_raster<128, false><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 257: k_raster<128, true><<<grid, 128, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 1024: k_raster<512, false><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 1025: k_raster<512, true><<<grid, 512, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    case 513: k_raster<256, true><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
+    default: k_raster<256, false><<<grid, 256, 0, st>>>(ws, d_surf, nsurf, tile0); break;
   }
-  return e;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t nviews, const Surface* d_surf,
@@ -2363,10 +2306,12 @@ cudaError_t launch_shade(const SceneDev& sc, const ViewParams* d_views, uint32_t
   if (!ntiles) return cudaSuccess;
   if (!sc.objq || !sc.texlv || !ws.srec || (nviews > 1 && !ws.tiles)) return cudaErrorInvalidValue;
   if (features)
-    return launch_dep(k_shade<true>, dim3(ntiles), dim3(256), st, sc, d_views, d_surf, nviews, ws.srec,
-                      (const Counters*)ws.ctr, ws.rec_cap, tile0, (const uint8_t*)ws.tile_empty, (const uint2*)ws.tiles);
-  return launch_dep(k_shade<false>, dim3(ntiles), dim3(256), st, sc, d_views, d_surf, nviews, ws.srec,
-                    (const Counters*)ws.ctr, ws.rec_cap, tile0, (const uint8_t*)ws.tile_empty, (const uint2*)ws.tiles);
+    k_shade<true><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
+                                          ws.tile_empty, ws.tiles);
+  else
+    k_shade<false><<<ntiles, 256, 0, st>>>(sc, d_views, d_surf, nviews, ws.srec, ws.ctr, ws.rec_cap, tile0,
+                                           ws.tile_empty, ws.tiles);
+  return cudaGetLastError();
 }
 
 // Blocks of the fused pass that fit on the device at once (cooperative grid).
