@@ -71,6 +71,24 @@ def test_invalid_tuning_rejected():
     assert gs.tuning(S.PASS_VIEW) == S.DEFAULT_TUNING
 
 
+def test_batch_rejects_misaligned_outputs():
+    """A batch whose output buffers are not 4-byte aligned is refused at creation."""
+    import ctypes
+
+    sc = scenes.plain_cubes()
+    gs = GpuScene(sc)
+    views = np.ascontiguousarray(np.stack([np.asarray(sc.views[0], S.VIEW)]))
+    W, H = int(views["width"][0]), int(views["height"][0])
+    d = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    i = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    c = torch.zeros(H * W * 4 + 4, dtype=torch.uint8, device="cuda")
+    outs = (ctypes.c_void_p * 4)(d.data_ptr(), i.data_ptr(), c.data_ptr() + 2, None)
+    h = ctypes.c_void_p()
+    st = gs.L.gbr_batch_create(gs.h, 1, views.ctypes.data, ctypes.cast(outs, ctypes.c_void_p), 0, ctypes.byref(h))
+    assert _native.STATUS[st] == "GBR_INVALID_ARG"
+    assert not h.value
+
+
 def test_raster_shade_modes_match():
     """The three ways a pass of several views runs its raster and kernel3
     (tuning raster_shade: one launch each, the persistent fused launch, and

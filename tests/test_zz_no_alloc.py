@@ -205,3 +205,23 @@ def test_noalloc_rejects_oversized_view():
     st, got = _noalloc(L, ds, sc.cameras[0], sc.views[0])
     assert st == 0
     _compare(got, gs.render(sc.cameras[0], sc.views[0]).numpy(), "cubes after rejection")
+
+
+def test_noalloc_rejects_misaligned_outputs():
+    """Outputs the kernels access as 32-bit words must be 4-byte aligned: a
+    misaligned RGBA8 pointer comes back as GBR_INVALID_ARG before any launch."""
+    L = _native.load()
+    sc = scenes.plain_cubes()
+    gs = GpuScene(sc)
+    ds, keep = _device_scene(sc, gs)
+    view = np.asarray(sc.views[0], S.VIEW).reshape(1)
+    cam = np.asarray(sc.cameras[0], S.CAMERA).reshape(1)
+    W, H = int(view["width"][0]), int(view["height"][0])
+    d = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    i = torch.zeros((H, W), dtype=torch.int32, device="cuda")
+    c = torch.zeros(H * W * 4 + 4, dtype=torch.uint8, device="cuda")
+    o = Outs(d.data_ptr(), i.data_ptr(), c.data_ptr() + 1, None)
+    st = L.gbr_render_view_noalloc(ctypes.byref(ds), _P(cam.ctypes.data), _P(view.ctypes.data), ctypes.byref(o),
+                                   _P(torch.cuda.current_stream().cuda_stream))
+    assert _native.STATUS[st] == "GBR_INVALID_ARG"
+    assert b"aligned" in L.gbr_last_error_string()
