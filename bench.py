@@ -60,7 +60,53 @@ def parse():
                     help="the 64-view sphere batch (the mixed-resolution batched workload) rendered once inside "
                          "cudaProfilerStart/Stop after a warm-up batch, with the tuning its captured graph uses "
                          "(128-thread rasters), then exit")
+    ap.add_argument("--tile-stats", action="store_true",
+                    help="CPU only: the 1080p terrain frame's records and bins for fine tiles of 8, 16 and 32 "
+                         "pixels, from a numpy model of the view setup's culls, bounding boxes and footprints, then "
+                         "exit (at 16 pixels it reproduces the GPU's record and bin-entry counts)")
     return ap.parse_args()
+
+
+def tile_stats():
+    """Records per fine tile and bin entries of the 1080p terrain frame for
+    8x8, 16x16 and 32x32 tiles.  The view setup modelled in float64: the
+    camera rotation, the near clip (whole triangles), projection, rounded
+    bounding boxes (min - 1 .. max, clamped, empty boxes dropped), back-face
+    cull, then footprints with records over 16 fine tiles in 128-pixel coarse
+    bins, as the fill does."""
+    sc = scenes.terrain()
+    view = sc.views[0]
+    W, H, fov = int(view["width"]), int(view["height"]), 960.0
+    rot = np.array(sc.cameras[0]["rot"][:3], np.float64)
+    c, s = np.cos(rot), np.sin(rot)
+    rel = sc.tris["vertices"]["pos"][:, :, :3].astype(np.float64)  # identity descriptors: world = object space
+    a = s[2] * rel[..., 1] + c[2] * rel[..., 0]
+    b = c[1] * rel[..., 2] + s[1] * a
+    d = c[2] * rel[..., 1] - s[2] * rel[..., 0]
+    X, Y, Z = c[1] * a - s[1] * rel[..., 2], s[0] * b + c[0] * d, c[0] * b - s[0] * d
+    x, y = X / Z * fov + W / 2, Y / Z * fov + H / 2
+    cross = (x[:, 1] - x[:, 0]) * (y[:, 2] - y[:, 0]) - (y[:, 1] - y[:, 0]) * (x[:, 2] - x[:, 0])
+    xr, yr = np.round(x), np.round(y)
+    x0, x1 = np.clip(xr.min(1) - 1, 0, W - 1), np.clip(xr.max(1), 0, W - 1)
+    y0, y1 = np.clip(yr.min(1) - 1, 0, H - 1), np.clip(yr.max(1), 0, H - 1)
+    keep = np.all(Z > 20, axis=1) & (x1 > x0) & (y1 > y0) & (cross <= 0)
+    X0, X1, Y0, Y1 = (v[keep].astype(np.int64) for v in (x0, x1, y0, y1))
+    out = {"workload": "terrain_1080p_1M", "records": int(keep.sum()), "tiles": {}}
+    for T in (8, 16, 32):
+        tx0, tx1, ty0, ty1 = X0 // T, (X1 - 1) // T, Y0 // T, (Y1 - 1) // T
+        n = (tx1 - tx0 + 1) * (ty1 - ty0 + 1)
+        coarse = n > 16
+        cn = ((X1 - 1) // 128 - X0 // 128 + 1) * ((Y1 - 1) // 128 - Y0 // 128 + 1)
+        cnt = np.zeros(((H + T - 1) // T, (W + T - 1) // T), np.int64)
+        for i in np.nonzero(~coarse)[0]:
+            cnt[ty0[i]:ty1[i] + 1, tx0[i]:tx1[i] + 1] += 1
+        nz = cnt[cnt > 0]
+        out["tiles"][f"{T}x{T}"] = {
+            "tiles": int(cnt.size), "bin_entries": int(np.where(coarse, cn, n).sum()),
+            "records_per_tile_mean": round(float(nz.mean()), 1), "records_per_tile_p99": round(float(np.percentile(nz, 99))),
+            "records_per_tile_max": int(nz.max()), "tiles_over_128_records": round(float(np.mean(cnt > 128)), 4),
+            "tiles_over_512_records": round(float(np.mean(cnt > 512)), 4)}
+    print(json.dumps(out))
 
 
 def profile_pass():
@@ -480,6 +526,9 @@ def main():
         return
     if args.profile_batch:
         profile_batch()
+        return
+    if args.tile_stats:
+        tile_stats()
         return
     if args.impl == "reference":
         run_reference(args, world, rank)
