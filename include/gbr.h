@@ -272,7 +272,9 @@ gbr_status gbr_framebuffer_destroy(gbr_framebuffer* fb);
  * rgba_out == rgba_in works in place, as the reference's call does, but every
  * pixel reads the unmodified input (through a scene-owned scratch image); a
  * partial overlap is rejected.  The input is read with the bilinear filter the
- * reference's image sampler applies, pinned to float weights. */
+ * reference's image sampler applies, pinned to float weights.  As for
+ * gbr_outputs, every buffer of a post pass is 4-byte aligned (GBR_INVALID_ARG
+ * otherwise). */
 gbr_status gbr_post_godrays(gbr_scene* scene, const gbr_camera* cam, const gbr_view* view, const uint32_t* depth,
                             const uint8_t* rgba_in, uint8_t* rgba_out, void* stream);
 
