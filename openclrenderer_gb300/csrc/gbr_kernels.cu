@@ -1362,7 +1362,7 @@ __device__ float generate_ssao(int x, int y, uint32_t seed2, const uint32_t* dep
     int wx[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) wx[k] = ssao_coord((float)x + off[k], W);
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < 5; k++) {
       const uint32_t* row = depth + (size_t)ssao_coord((float)y + off[k], H) * W;
 #pragma unroll
